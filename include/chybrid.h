@@ -1,0 +1,198 @@
+/*
+ * chybrid.h -- C ABI of the GB300 (sm_103a) hybrid-PIC hot path.
+ *
+ * One step of the collisional hybrid particle-in-cell method on one GPU:
+ *   UpdateVelocities   Boris push with E = -grad(phi) + ion-neutral collisions
+ *   UpdatePositions    x += v dt with periodic wrap
+ *   CollectVlasovQuantities  cloud-in-cell deposit of n and Gamma = n v
+ *   ComputePotential   19-point quasineutral potential solve (matrix free)
+ *
+ * Every entry point returns ch_status (0 = CH_OK, negative = error); the
+ * message of the last error on the calling thread is ch_last_error().
+ * Host buffers are owned by the caller and copied in or out; device buffers
+ * are owned by the ch_ctx.  Calls are synchronous at return.  One host
+ * thread drives one ch_ctx at a time.
+ *
+ * Layouts follow the reference so that a PETSc host can pass its borrowed
+ * arrays straight through:
+ *   ch_real_vector == RealVector {x, y, z, r}  (src/hybrid.h:40-45), the
+ *                     DMSwarm "position"/"velocity" field (src/setup.c:130-132)
+ *   ch_grid_node   == GridNode {n, flux[3]}     (src/hybrid.h:140-143), the
+ *                     dof-4 DMDA "vlasov" vector (src/setup.c:15-16)
+ *   grid vectors are in DMDA natural order idx = (k*Ny + j)*Nx + i.
+ */
+#ifndef CHYBRID_H
+#define CHYBRID_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CH_ABI_VERSION 1
+
+typedef int32_t ch_status;
+enum {
+  CH_OK = 0,
+  CH_ERR_ARG = -1,            /* bad argument or option value            */
+  CH_ERR_CUDA = -2,           /* CUDA runtime error                      */
+  CH_ERR_NOMEM = -3,          /* device or host allocation failed        */
+  CH_ERR_NOT_CONVERGED = -4,  /* Krylov solve missed rtol within max_it  */
+  CH_ERR_COLLISION_LIMIT = -5,/* >= 10 collisions refused in one step
+                                 (src/particles.c:597-606)               */
+  CH_ERR_NAN = -6,            /* non-finite value in a moment or phi     */
+  CH_ERR_RANGE = -7,          /* fixed-point deposit range exceeded      */
+  CH_ERR_TIMEOUT = -8,        /* a bounded device wait ran out           */
+  CH_ERR_STATE = -9,          /* call out of order (e.g. no particles)   */
+  CH_ERR_UNSUPPORTED = -10    /* option combination not implemented      */
+};
+
+/* RealVector (src/hybrid.h:40-45): the r slot is carried, never read. */
+typedef struct ch_real_vector { double x, y, z, r; } ch_real_vector;
+/* GridNode (src/hybrid.h:140-143). */
+typedef struct ch_grid_node { double n, flux[3]; } ch_grid_node;
+
+/* --lhs-type (src/lhs.h:8-12) */
+enum { CH_LHS_IDENTITY = 0, CH_LHS_LAPLACIAN = 1, CH_LHS_FULL = 2 };
+/* --rhs-type (src/rhs.h:8-12) */
+enum { CH_RHS_CONSTANT = 0, CH_RHS_SINUSOIDAL = 1, CH_RHS_FULL = 2 };
+/* -ksp_type / -pc_type subset */
+enum { CH_KSP_CG = 0, CH_KSP_BCGS = 1 };
+enum { CH_PC_NONE = 0, CH_PC_JACOBI = 1, CH_PC_MG = 2 };
+/* -ch_precision */
+enum { CH_FP64 = 0, CH_MIXED = 1 };
+/* neutral-density profile (scales the local collision rate) */
+enum { CH_NN_UNIFORM = 0, CH_NN_GAUSSIAN_X = 1 };
+
+/* Reference-faithful switches, one bit per documented defect of the
+ * reference's as-written code.  All off = the corrected algorithm. */
+enum {
+  CH_FAITHFUL_D2 = 1u << 2,  /* CrossProduct returns 0 (src/vectors.c:157-159) */
+  CH_FAITHFUL_D3 = 1u << 3,  /* degenerate z lerp in DifferenceVector (src/vectors.c:61-67) */
+  CH_FAITHFUL_D4 = 1u << 4,  /* one-sided difference at ixh==N (src/vectors.c:48-60) */
+  CH_FAITHFUL_D5 = 1u << 5,  /* UpdatePositions discards x (src/particles.c:677-706) */
+  CH_FAITHFUL_D6 = 1u << 6,  /* moments accumulate across steps (src/particles.c:242) */
+  CH_FAITHFUL_D7 = 1u << 7,  /* operator A(n) frozen at the first solve */
+  CH_FAITHFUL_D8 = 1u << 8   /* d2Fdyz uses the x-z stencil (src/calculus.c:464) */
+};
+
+/* Run parameters: the Context fields that the hot path reads
+ * (src/hybrid.h:106-138) after ProcessOptions (src/parameters.c:28-562)
+ * has derived them.  Option names in the comments are the reference's. */
+typedef struct ch_params {
+  int32_t Nx, Ny, Nz;        /* -Nx -Ny -Nz                                   */
+  int32_t precision;         /* CH_FP64 | CH_MIXED  (-ch_precision)           */
+  double x0, y0, z0;         /* -x0 -y0 -z0                                   */
+  double x1, y1, z1;         /* -x1 -y1 -z1   (L = x1-x0, d = L/N, src/setup.c:47-49) */
+  double qi, mi;             /* -qi -mi                                       */
+  double nui;                /* -nui  ion-neutral collision frequency         */
+  double dt;                 /* -dt                                           */
+  double vi0[3];             /* -vi0x -vi0y -vi0z  ion drift (enters vrm)     */
+  double viT[3];             /* -viTx -viTy -viTz  ion per-component thermal speed */
+  double mn;                 /* -mn   neutral mass; <= 0 disables collisions  */
+  double vnT;                /* neutral thermal speed (std of each component) */
+  double vn0[3];             /* -vn0x -vn0y -vn0z neutral drift               */
+  double B0[3];              /* -B0x -B0y -B0z                                */
+  double E0[3];              /* -E0x -E0y -E0z  (enters the RHS only)         */
+  double kappa_e[3];         /* electron magnetization Omega_e/nu_e           */
+  double cth;                /* gamma kB Te / e  (src/rhs.c:190)              */
+  double cG;                 /* me nue / e       (src/rhs.c:191)              */
+  int32_t lhs_type;          /* --lhs-type  CH_LHS_*                          */
+  int32_t rhs_type;          /* --rhs-type  CH_RHS_*                          */
+  int32_t ksp_type;          /* -ksp_type cg|bcgs                             */
+  int32_t pc_type;           /* -ch_pc none|jacobi|mg                         */
+  double ksp_rtol;           /* -ksp_rtol                                     */
+  double ksp_atol;           /* -ksp_atol                                     */
+  int32_t ksp_max_it;        /* -ksp_max_it                                   */
+  int32_t nn_profile;        /* CH_NN_*                                       */
+  double nn_center, nn_sigma, nn_floor;  /* Gaussian neutral-density profile  */
+  uint64_t seed;             /* -ch_seed  Philox key                          */
+  uint32_t run;              /* ensemble member index (Philox counter word 3) */
+  uint32_t faithful;         /* CH_FAITHFUL_* bits                            */
+  int32_t push_E0;           /* -ch_push_E0: add E0 to the ion push           */
+  int32_t sort_period;       /* steps between counting sorts (0 = never)      */
+  double deposit_scale_log2; /* fixed-point deposit scale 2^s (0 = default)   */
+} ch_params;
+
+/* Fills *p with the reference defaults (src/parameters.c:28-562) in
+ * normalised units: e = kB = 1.  Grid, species and solver fields that the
+ * reference derives are set for a 7^3 unit box, periodic. */
+ch_status ch_params_default(ch_params* p);
+
+/* Per-solve report (KSPGetIterationNumber / KSPGetResidualNorm). */
+typedef struct ch_solve_info {
+  int32_t iterations;        /* Krylov iterations (outer + inner for mixed)   */
+  int32_t refinements;       /* FP64 refinement passes (mixed form)           */
+  double rnorm;              /* ||b - A phi||_2, FP64, unpreconditioned       */
+  double bnorm;              /* ||b||_2                                       */
+} ch_solve_info;
+
+/* Per-step counters. */
+typedef struct ch_step_info {
+  int64_t Nc;                /* collisions the reference would attempt (src/particles.c:514) */
+  int64_t collisions;        /* accepted ion-neutral collisions               */
+  int64_t refused;           /* collisions refused for |v_f| > 10 vT          */
+  double expected;           /* sum of per-ion collision probabilities        */
+  double moment_sum[4];      /* FP64 global sums of n, Gx, Gy, Gz             */
+  ch_solve_info solve;       /* last potential solve of the call              */
+} ch_step_info;
+
+/* Opaque per-run state: device particles, grid fields, solver workspace. */
+typedef struct ch_ctx ch_ctx;
+
+const char* ch_last_error(void);
+int32_t ch_abi_version(void);
+
+/* Creates the device state for one run (SetUpVlasovDM, SetUpPotentialDM,
+ * SetUpIonsDM; src/setup.c:6,71,105).  Selects device `device` (-1: current). */
+ch_status ch_create(const ch_params* p, int32_t device, ch_ctx** out);
+ch_status ch_destroy(ch_ctx* c);
+
+/* Copies np ions in (DMSwarm "position"/"velocity", AoS 32 B each).  Ion id
+ * = array index; ids key the Philox streams. */
+ch_status ch_particles_upload(ch_ctx* c, const ch_real_vector* pos,
+                              const ch_real_vector* vel, int64_t np);
+/* Copies the ions out in id order (the order they were uploaded). */
+ch_status ch_particles_download(ch_ctx* c, ch_real_vector* pos, ch_real_vector* vel);
+
+/* Seeded synthetic plasma on the device (replaces InitializePositions /
+ * InitializeVelocities, src/particles.c:9-132): x by inverse CDF of
+ * n(x) = 1 + sum_m amp[m] sin(2 pi m x/Lx + phase[m]), m = 1..3; y, z uniform;
+ * v = v0 + vT * N(0,1) per component, Philox-keyed by (id, seed). */
+typedef struct ch_loader {
+  double amp[3];
+  double phase[3];
+  double v0[3];
+  double vT[3];
+} ch_loader;
+ch_status ch_particles_load(ch_ctx* c, int64_t np, const ch_loader* L);
+
+/* UpdateVelocities (src/particles.c:628-643): BorisMover (:348-464) with E
+ * gathered from the current phi, then ComputeCollisions (:471-624) if mn > 0.
+ * `step` keys the Philox streams of this step. */
+ch_status ch_update_velocities(ch_ctx* c, int64_t step, ch_step_info* info);
+/* UpdatePositions (src/particles.c:647-718). */
+ch_status ch_update_positions(ch_ctx* c);
+/* CollectVlasovQuantities (src/particles.c:136-255).  host_out (nullable)
+ * receives Nx*Ny*Nz GridNode in natural order. */
+ch_status ch_collect_moments(ch_ctx* c, ch_grid_node* host_out, ch_step_info* info);
+/* ComputePotential (src/potential.c:6-15): RHS (rhs.c), operator (lhs.c),
+ * Krylov solve warm-started from the previous phi.  phi_out nullable. */
+ch_status ch_compute_potential(ch_ctx* c, double* phi_out, ch_solve_info* info);
+/* The reference time-loop body (src/hybrid.c:101-123) without output,
+ * nsteps times, steps numbered first_step, first_step+1, ... */
+ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_step_info* info);
+
+/* Grid-vector access for hosts and tests (natural order, FP64). */
+ch_status ch_set_moments(ch_ctx* c, const ch_grid_node* host_in);  /* LoadVlasovQuantities, src/fileio.c:6-70 */
+ch_status ch_get_phi(ch_ctx* c, double* out);
+ch_status ch_set_phi(ch_ctx* c, const double* in);
+ch_status ch_get_rhs(ch_ctx* c, double* out);   /* ctx->rhs after the last RHS build */
+/* y = A(n) x with the current operator (matrix-free ComputeFullLHS). */
+ch_status ch_apply_operator(ch_ctx* c, const double* x, double* y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CHYBRID_H */
