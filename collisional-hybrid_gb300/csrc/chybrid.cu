@@ -1,0 +1,573 @@
+// chybrid.cu -- the C ABI (include/chybrid.h) over the sm_103a kernels.
+//
+// Mirrors the reference's per-step entry points (src/particles.h:11-21,
+// src/potential.h:7-13): one ch_ctx holds what Context + the DMDA/DMSwarm/KSP
+// objects hold in the reference, all resident in HBM.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <new>
+
+#include "particles.cuh"
+#include "solver.cuh"
+
+using namespace ch;
+
+static thread_local char g_err[512] = "";
+
+ch_status ch_fail(ch_status code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+ch_status ch_cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+  return ch_fail(e == cudaErrorMemoryAllocation ? CH_ERR_NOMEM : CH_ERR_CUDA, "%s failed: %s (%s:%d)", what,
+                 cudaGetErrorString(e), file, line);
+}
+
+struct ch_ctx {
+  ch_params p;
+  GridDesc g;
+  int device = 0;
+  int sms = 1;
+  bool mixed = false;
+  cudaStream_t stream = nullptr;
+  int64_t np = 0;
+  // ions (ping-pong buffers for the counting sort)
+  F64Particles P{}, Q{};
+  MixParticles M{}, MQ{};
+  uint32_t* keys = nullptr;
+  // grid
+  uint32_t *counts = nullptr, *starts = nullptr, *cursor = nullptr, *block_sums = nullptr;
+  double *phi = nullptr, *E64 = nullptr, *mom = nullptr, *rhs = nullptr, *nfz = nullptr;
+  float4* E32 = nullptr;
+  unsigned long long* acc = nullptr;
+  // reductions
+  DevCounters* cnt = nullptr;
+  DevCounters* hcnt = nullptr;
+  double* part = nullptr;
+  int part_cap = 0;
+  double* red = nullptr;
+  double* hred = nullptr;
+  // staging for AoS transfers
+  double4_32a *stage_pos = nullptr, *stage_vel = nullptr;
+  // state
+  double sbar = 0.0;
+  double dep_scale = 0.0;
+  bool solved_once = false;
+  bool moments_valid = false;
+  int64_t since_sort = 0;
+  PotentialSolver solver;
+};
+
+extern "C" const char* ch_last_error(void) { return g_err; }
+extern "C" int32_t ch_abi_version(void) { return CH_ABI_VERSION; }
+
+extern "C" ch_status ch_params_default(ch_params* p) {
+  if (!p) return ch_fail(CH_ERR_ARG, "ch_params_default: null");
+  memset(p, 0, sizeof(*p));
+  // src/parameters.c:28-562 defaults in normalised units (e = kB = 1, mi = 1)
+  p->Nx = p->Ny = p->Nz = 7;  // src/setup.c:10-12
+  p->x1 = p->y1 = p->z1 = 1.0;
+  p->qi = 1.0;
+  p->mi = 1.0;
+  p->nui = 1.0;
+  p->dt = 1.0 / p->nui;  // src/parameters.c:417
+  p->mn = p->mi;         // src/parameters.c:337
+  p->vnT = 0.0;          // sqrt(2 kB Tn/mn) with Tn = Ti = 0
+  p->cth = 0.0;          // Te = 0
+  p->cG = 1.0 / 1836.15267343;  // me nue / e with nue = 1, me/mi
+  p->lhs_type = CH_LHS_FULL;
+  p->rhs_type = CH_RHS_FULL;
+  p->ksp_type = CH_KSP_CG;
+  p->pc_type = CH_PC_JACOBI;
+  p->ksp_rtol = 1e-5;  // PETSc KSP defaults
+  p->ksp_atol = 1e-50;
+  p->ksp_max_it = 10000;
+  p->precision = CH_FP64;
+  p->seed = 12345;     // |-(rank+1)*12345| for rank 0 (src/hybrid.c:49)
+  p->nn_profile = CH_NN_UNIFORM;
+  p->nn_sigma = 1.0;
+  p->sort_period = 8;
+  return CH_OK;
+}
+
+static ch_status validate(const ch_params* p) {
+  if (p->Nx < 3 || p->Ny < 3 || p->Nz < 3)
+    return ch_fail(CH_ERR_ARG, "grid %dx%dx%d: each axis needs at least 3 nodes for the 19-point stencil", p->Nx,
+                   p->Ny, p->Nz);
+  if (p->Nx > CH_MAX_NX || p->Ny > CH_MAX_NY || p->Nz > CH_MAX_NZ)
+    return ch_fail(CH_ERR_ARG, "grid %dx%dx%d exceeds %dx%dx%d", p->Nx, p->Ny, p->Nz, CH_MAX_NX, CH_MAX_NY,
+                   CH_MAX_NZ);
+  if (!(p->x1 > p->x0) || !(p->y1 > p->y0) || !(p->z1 > p->z0)) return ch_fail(CH_ERR_ARG, "empty domain");
+  if (!(p->mi > 0.0)) return ch_fail(CH_ERR_ARG, "ion mass must be positive");
+  if (!(p->dt > 0.0) || !isfinite(p->dt)) return ch_fail(CH_ERR_ARG, "dt must be positive");
+  if (p->precision != CH_FP64 && p->precision != CH_MIXED) return ch_fail(CH_ERR_ARG, "unknown precision");
+  if (p->ksp_type != CH_KSP_CG && p->ksp_type != CH_KSP_BCGS) return ch_fail(CH_ERR_ARG, "unknown ksp_type");
+  if (p->pc_type != CH_PC_NONE && p->pc_type != CH_PC_JACOBI && p->pc_type != CH_PC_MG)
+    return ch_fail(CH_ERR_ARG, "unknown pc_type");
+  if (p->lhs_type < 0 || p->lhs_type > 2 || p->rhs_type < 0 || p->rhs_type > 2)
+    return ch_fail(CH_ERR_ARG, "unknown lhs/rhs type");
+  if (p->precision == CH_MIXED && (p->faithful & (CH_FAITHFUL_D3 | CH_FAITHFUL_D4)))
+    return ch_fail(CH_ERR_UNSUPPORTED, "the as-written DifferenceVector (D3/D4) runs in the FP64 form only");
+  if (!(p->ksp_rtol > 0.0) || p->ksp_max_it < 1) return ch_fail(CH_ERR_ARG, "bad ksp tolerance / max_it");
+  if (p->mn > 0.0 && !(p->viT[0] > 0.0 || p->viT[1] > 0.0 || p->viT[2] > 0.0))
+    return ch_fail(CH_ERR_ARG, "collisions need a positive ion thermal speed (vrm, src/particles.c:511)");
+  return CH_OK;
+}
+
+static GridDesc make_grid(const ch_params& p) {
+  GridDesc g;
+  g.Nx = p.Nx; g.Ny = p.Ny; g.Nz = p.Nz;
+  g.N = (int64_t)p.Nx * p.Ny * p.Nz;
+  g.x0 = p.x0; g.y0 = p.y0; g.z0 = p.z0;
+  g.Lx = p.x1 - p.x0; g.Ly = p.y1 - p.y0; g.Lz = p.z1 - p.z0;
+  g.dx = g.Lx / p.Nx; g.dy = g.Ly / p.Ny; g.dz = g.Lz / p.Nz;
+  return g;
+}
+
+static void free_particles(ch_ctx* c) {
+  void* v[] = {c->P.x, c->P.y, c->P.z, c->P.vx, c->P.vy, c->P.vz, c->P.id, c->Q.x, c->Q.y, c->Q.z, c->Q.vx,
+               c->Q.vy, c->Q.vz, c->Q.id, c->M.pos, c->M.vel, c->MQ.pos, c->MQ.vel, c->keys, c->stage_pos,
+               c->stage_vel, c->part};
+  for (void* q : v)
+    if (q) cudaFree(q);
+  c->P = F64Particles{};
+  c->Q = F64Particles{};
+  c->M = MixParticles{};
+  c->MQ = MixParticles{};
+  c->keys = nullptr;
+  c->stage_pos = c->stage_vel = nullptr;
+  c->part = nullptr;
+  c->part_cap = 0;
+  c->np = 0;
+}
+
+extern "C" ch_status ch_destroy(ch_ctx* c) {
+  if (!c) return CH_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_particles(c);
+  void* v[] = {c->counts, c->starts, c->cursor, c->block_sums, c->phi, c->E64, c->mom, c->rhs, c->nfz,
+               c->E32, c->acc, c->cnt, c->red};
+  for (void* q : v)
+    if (q) cudaFree(q);
+  if (c->hcnt) cudaFreeHost(c->hcnt);
+  if (c->hred) cudaFreeHost(c->hred);
+  c->solver.release();
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return CH_OK;
+}
+
+extern "C" ch_status ch_create(const ch_params* p, int32_t device, ch_ctx** out) {
+  if (!p || !out) return ch_fail(CH_ERR_ARG, "ch_create: null argument");
+  *out = nullptr;
+  ch_status rc = validate(p);
+  if (rc) return rc;
+  int ndev = 0;
+  CH_CUDA_OK(cudaGetDeviceCount(&ndev));
+  if (ndev < 1) return ch_fail(CH_ERR_CUDA, "no CUDA device");
+  if (device >= 0) CH_CUDA_OK(cudaSetDevice(device));
+  ch_ctx* c = new (std::nothrow) ch_ctx();
+  if (!c) return ch_fail(CH_ERR_NOMEM, "ch_create: host allocation");
+  c->p = *p;
+  c->g = make_grid(*p);
+  c->mixed = p->precision == CH_MIXED;
+  CH_CUDA_OK(cudaGetDevice(&c->device));
+  CH_CUDA_OK(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device));
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { ch_destroy(c); return ch_cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__); }
+  const int64_t N = c->g.N;
+  const int nsb = (int)((N + 1023) / 1024) + 1;
+  struct { void** p; size_t b; } allocs[] = {
+      {(void**)&c->counts, sizeof(uint32_t) * N},       {(void**)&c->starts, sizeof(uint32_t) * (N + 1)},
+      {(void**)&c->cursor, sizeof(uint32_t) * N},       {(void**)&c->block_sums, sizeof(uint32_t) * nsb},
+      {(void**)&c->phi, sizeof(double) * N},            {(void**)&c->mom, sizeof(double) * 4 * N},
+      {(void**)&c->rhs, sizeof(double) * N},            {(void**)&c->nfz, sizeof(double) * N},
+      {(void**)&c->acc, sizeof(unsigned long long) * 4 * N}, {(void**)&c->cnt, sizeof(DevCounters)},
+      {(void**)&c->red, sizeof(double) * 8}};
+  for (auto& a : allocs) {
+    e = cudaMalloc(a.p, a.b);
+    if (e != cudaSuccess) { ch_destroy(c); return ch_cuda_fail(e, "cudaMalloc(grid)", __FILE__, __LINE__); }
+  }
+  e = c->mixed ? cudaMalloc(&c->E32, sizeof(float4) * N) : cudaMalloc(&c->E64, sizeof(double) * 3 * N);
+  if (e != cudaSuccess) { ch_destroy(c); return ch_cuda_fail(e, "cudaMalloc(E)", __FILE__, __LINE__); }
+  if (cudaMallocHost(&c->hcnt, sizeof(DevCounters)) != cudaSuccess ||
+      cudaMallocHost(&c->hred, sizeof(double) * 8) != cudaSuccess) {
+    ch_destroy(c);
+    return ch_fail(CH_ERR_NOMEM, "pinned host allocation");
+  }
+  cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream);
+  cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * N, c->stream);
+  cudaMemsetAsync(c->mom, 0, sizeof(double) * 4 * N, c->stream);
+  rc = c->solver.init(*p, c->g, c->sms);
+  if (rc) { ch_destroy(c); return rc; }
+  // fixed-point deposit scale 2^s
+  c->dep_scale = ldexp(1.0, (int)(p->deposit_scale_log2 > 0.0 ? p->deposit_scale_log2 : 40.0));
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) { ch_destroy(c); return ch_cuda_fail(e, "ch_create", __FILE__, __LINE__); }
+  *out = c;
+  return CH_OK;
+}
+
+static StepConsts consts(const ch_ctx* c, int64_t step) {
+  const ch_params& p = c->p;
+  StepConsts k;
+  memset(&k, 0, sizeof(k));
+  k.g = c->g;
+  k.tscale = 0.5 * (p.qi / p.mi) * p.dt;
+  double tt = 0.0;
+  for (int d = 0; d < 3; ++d) { k.t[d] = k.tscale * p.B0[d]; tt += k.t[d] * k.t[d]; }
+  for (int d = 0; d < 3; ++d) k.s[d] = 2.0 * k.t[d] / (1.0 + tt);
+  for (int d = 0; d < 3; ++d) k.E0[d] = p.E0[d];
+  k.push_E0 = p.push_E0;
+  k.faithful = p.faithful;
+  k.dt = p.dt;
+  k.collide = p.mn > 0.0;
+  k.vnT = p.vnT;
+  for (int d = 0; d < 3; ++d) k.vn0[d] = p.vn0[d];
+  k.mi = p.mi;
+  k.mn = p.mn;
+  k.viTr = sqrt(p.viT[0] * p.viT[0] + p.viT[1] * p.viT[1] + p.viT[2] * p.viT[2]);
+  k.m1 = 2.0 * p.vnT * sqrt(2.0 / CH_PI);
+  k.nn_profile = p.nn_profile;
+  k.nn_center = p.nn_center;
+  k.nn_sigma = p.nn_sigma;
+  k.nn_floor = p.nn_floor;
+  k.seed_lo = (uint32_t)p.seed;
+  k.seed_hi = (uint32_t)(p.seed >> 32);
+  k.run = p.run;
+  k.step = (uint32_t)step;
+  k.dep_scale = c->dep_scale;
+  return k;
+}
+
+// src/particles.c:510-519
+static int64_t collision_count(const ch_params& p, int64_t np) {
+  const double viTr = sqrt(p.viT[0] * p.viT[0] + p.viT[1] * p.viT[1] + p.viT[2] * p.viT[2]);
+  const double dvx = p.vi0[0] - p.vn0[0], dvy = p.vi0[1] - p.vn0[1], dvz = p.vi0[2] - p.vn0[2];
+  const double vrm = 4.0 * viTr + sqrt(dvx * dvx + dvy * dvy + dvz * dvz);
+  const double vn0r = sqrt(p.vn0[0] * p.vn0[0] + p.vn0[1] * p.vn0[1] + p.vn0[2] * p.vn0[2]);
+  const double den = (p.vnT + vn0r) * sqrt(p.mn / p.mi);
+  const double fc = p.nui * p.dt;
+  if (!(den > 0.0)) return np;
+  const double v = ((double)np * fc * vrm) / den;
+  if (v >= (double)np) return np;
+  if (v < 0.0) return 0;
+  return (int64_t)v;
+}
+
+static ch_status ensure_particles(ch_ctx* c, int64_t np) {
+  if (np <= 0) return ch_fail(CH_ERR_ARG, "number of ions must be positive");
+  if (np > 0xFFFFFFFFll) return ch_fail(CH_ERR_ARG, "at most 2^32-1 ions (32-bit ids)");
+  if (c->np == np) return CH_OK;
+  free_particles(c);
+  cudaError_t e = cudaSuccess;
+  if (c->mixed) {
+    e = cudaMalloc(&c->M.pos, sizeof(float4) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&c->M.vel, sizeof(float4) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&c->MQ.pos, sizeof(float4) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&c->MQ.vel, sizeof(float4) * np);
+    c->M.np = c->MQ.np = np;
+  } else {
+    double** a[] = {&c->P.x, &c->P.y, &c->P.z, &c->P.vx, &c->P.vy, &c->P.vz,
+                    &c->Q.x, &c->Q.y, &c->Q.z, &c->Q.vx, &c->Q.vy, &c->Q.vz};
+    for (double** q : a)
+      if (e == cudaSuccess) e = cudaMalloc(q, sizeof(double) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&c->P.id, sizeof(uint32_t) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&c->Q.id, sizeof(uint32_t) * np);
+    c->P.np = c->Q.np = np;
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&c->keys, sizeof(uint32_t) * np);
+  const int cap = grid_for(np > c->g.N ? np : c->g.N, 256, c->sms, 8);
+  if (e == cudaSuccess) e = cudaMalloc(&c->part, sizeof(double) * 4 * cap);
+  if (e != cudaSuccess) {
+    free_particles(c);
+    return ch_cuda_fail(e, "cudaMalloc(ions)", __FILE__, __LINE__);
+  }
+  c->part_cap = cap;
+  c->np = np;
+  return CH_OK;
+}
+
+static ch_status ensure_staging(ch_ctx* c) {
+  if (c->stage_pos) return CH_OK;
+  cudaError_t e = cudaMalloc(&c->stage_pos, sizeof(double4_32a) * c->np);
+  if (e == cudaSuccess) e = cudaMalloc(&c->stage_vel, sizeof(double4_32a) * c->np);
+  if (e != cudaSuccess) return ch_cuda_fail(e, "cudaMalloc(staging)", __FILE__, __LINE__);
+  return CH_OK;
+}
+
+static void do_sort(ch_ctx* c) {
+  launch_sort(c->mixed, c->g, c->P, c->Q, c->M, c->MQ, c->counts, c->starts, c->cursor, c->keys, c->block_sums,
+              c->sms, c->stream);
+  std::swap(c->P, c->Q);
+  std::swap(c->M, c->MQ);
+  c->since_sort = 0;
+}
+
+static ch_status after_load(ch_ctx* c) {
+  do_sort(c);
+  if (c->p.mn > 0.0) {
+    StepConsts k = consts(c, 0);
+    const int nb = launch_sbar(c->mixed, k, c->P, c->M, c->part, c->sms, c->stream);
+    launch_reduce_partials(c->part, nb, 1, c->red, c->stream);
+    CH_CUDA_OK(cudaMemcpyAsync(c->hred, c->red, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  }
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  c->sbar = c->p.mn > 0.0 ? c->hred[0] : 0.0;
+  c->moments_valid = false;  // phi stays: a host that re-uploads its ions keeps the warm start
+  return CH_OK;
+}
+
+extern "C" ch_status ch_particles_upload(ch_ctx* c, const ch_real_vector* pos, const ch_real_vector* vel,
+                                         int64_t np) {
+  if (!c || !pos || !vel) return ch_fail(CH_ERR_ARG, "ch_particles_upload: null argument");
+  ch_status rc = ensure_particles(c, np);
+  if (rc) return rc;
+  rc = ensure_staging(c);
+  if (rc) return rc;
+  CH_CUDA_OK(cudaMemcpyAsync(c->stage_pos, pos, sizeof(double4_32a) * np, cudaMemcpyHostToDevice, c->stream));
+  CH_CUDA_OK(cudaMemcpyAsync(c->stage_vel, vel, sizeof(double4_32a) * np, cudaMemcpyHostToDevice, c->stream));
+  launch_aos_in(c->mixed, c->g, c->stage_pos, c->stage_vel, c->P, c->M, c->sms, c->stream);
+  return after_load(c);
+}
+
+extern "C" ch_status ch_particles_load(ch_ctx* c, int64_t np, const ch_loader* L) {
+  if (!c || !L) return ch_fail(CH_ERR_ARG, "ch_particles_load: null argument");
+  double s = fabs(L->amp[0]) + fabs(L->amp[1]) + fabs(L->amp[2]);
+  if (!(s < 1.0)) return ch_fail(CH_ERR_ARG, "density perturbation amplitudes must sum below 1");
+  ch_status rc = ensure_particles(c, np);
+  if (rc) return rc;
+  launch_load(c->mixed, c->g, *L, c->p.seed, c->p.run, c->P, c->M, c->sms, c->stream);
+  return after_load(c);
+}
+
+extern "C" ch_status ch_particles_download(ch_ctx* c, ch_real_vector* pos, ch_real_vector* vel) {
+  if (!c || !pos || !vel) return ch_fail(CH_ERR_ARG, "ch_particles_download: null argument");
+  if (c->np == 0) return ch_fail(CH_ERR_STATE, "no ions");
+  ch_status rc = ensure_staging(c);
+  if (rc) return rc;
+  launch_aos_out(c->mixed, c->g, c->P, c->M, c->stage_pos, c->stage_vel, c->sms, c->stream);
+  CH_CUDA_OK(cudaMemcpyAsync(pos, c->stage_pos, sizeof(double4_32a) * c->np, cudaMemcpyDeviceToHost, c->stream));
+  CH_CUDA_OK(cudaMemcpyAsync(vel, c->stage_vel, sizeof(double4_32a) * c->np, cudaMemcpyDeviceToHost, c->stream));
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  return CH_OK;
+}
+
+// ------------------------------------------------------------------ phases
+static ch_status run_pass(ch_ctx* c, int phases, int64_t step, ch_step_info* info) {
+  StepConsts k = consts(c, step);
+  const bool push = (phases & PH_PUSH) != 0;
+  int64_t Nc = 0;
+  if (push) {
+    launch_node_efield(c->mixed, c->g, k.tscale, c->phi, c->E64, c->E32, c->sms, c->stream);
+    CH_CUDA_OK(cudaMemsetAsync(c->cnt, 0, sizeof(DevCounters), c->stream));
+    if (k.collide) Nc = collision_count(c->p, c->np);
+  }
+  const int nb = launch_pass(c->mixed, phases, k, c->P, c->M, c->E64, c->E32, c->phi, c->acc, (double)Nc, c->sbar,
+                             c->cnt, c->part, c->sms, c->stream);
+  if (push) {
+    launch_reduce_partials(c->part, nb, 2, c->red, c->stream);
+    CH_CUDA_OK(cudaMemcpyAsync(c->hred, c->red, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
+    CH_CUDA_OK(cudaMemcpyAsync(c->hcnt, c->cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, c->stream));
+    CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+    if (k.collide) c->sbar = c->hred[1];
+    if (info) {
+      info->Nc = Nc;
+      info->collisions = (int64_t)c->hcnt->collisions;
+      info->refused = (int64_t)c->hcnt->refused;
+      info->expected = c->hred[0];
+    }
+    if (c->hcnt->refused >= 10)
+      return ch_fail(CH_ERR_COLLISION_LIMIT, "%llu collisions refused in step %lld (src/particles.c:603-605)",
+                     (unsigned long long)c->hcnt->refused, (long long)step);
+  }
+  if (phases & PH_MOVE) c->since_sort++;
+  return CH_OK;
+}
+
+static ch_status finalize_moments(ch_ctx* c, ch_step_info* info) {
+  CH_CUDA_OK(cudaMemsetAsync(&c->cnt->range_error, 0, sizeof(int), c->stream));
+  const int reset = (c->p.faithful & CH_FAITHFUL_D6) ? 0 : 1;
+  const int nb = launch_finalize(c->g.N, c->acc, 1.0 / c->dep_scale, reset, c->mom, c->part, c->cnt, c->sms,
+                                 c->stream);
+  launch_reduce_partials(c->part, nb, 4, c->red + 4, c->stream);
+  CH_CUDA_OK(cudaMemcpyAsync(c->hred + 4, c->red + 4, sizeof(double) * 4, cudaMemcpyDeviceToHost, c->stream));
+  CH_CUDA_OK(cudaMemcpyAsync(&c->hcnt->range_error, &c->cnt->range_error, sizeof(int), cudaMemcpyDeviceToHost,
+                             c->stream));
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  c->moments_valid = true;
+  if (info)
+    for (int q = 0; q < 4; ++q) info->moment_sum[q] = c->hred[4 + q];
+  if (c->hcnt->range_error)
+    return ch_fail(CH_ERR_RANGE, "deposit exceeded the fixed-point range 2^%d; lower deposit_scale_log2",
+                   63 - (int)log2(c->dep_scale));
+  for (int q = 0; q < 4; ++q)
+    if (!isfinite(c->hred[4 + q])) return ch_fail(CH_ERR_NAN, "non-finite moment sum");
+  return CH_OK;
+}
+
+extern "C" ch_status ch_update_velocities(ch_ctx* c, int64_t step, ch_step_info* info) {
+  if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
+  if (c->np == 0) return ch_fail(CH_ERR_STATE, "no ions");
+  return run_pass(c, PH_PUSH, step, info);
+}
+
+extern "C" ch_status ch_update_positions(ch_ctx* c) {
+  if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
+  if (c->np == 0) return ch_fail(CH_ERR_STATE, "no ions");
+  ch_status rc = run_pass(c, PH_MOVE, 0, nullptr);
+  if (rc) return rc;
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  return CH_OK;
+}
+
+static ch_status copy_moments_out(ch_ctx* c, ch_grid_node* host_out) {
+  // SoA device -> interleaved GridNode on the host
+  const int64_t N = c->g.N;
+  CH_CUDA_OK(cudaMemcpy2DAsync(host_out, sizeof(ch_grid_node), c->mom, sizeof(double), sizeof(double), N,
+                               cudaMemcpyDeviceToHost, c->stream));
+  for (int q = 1; q < 4; ++q)
+    CH_CUDA_OK(cudaMemcpy2DAsync((char*)host_out + q * sizeof(double), sizeof(ch_grid_node), c->mom + q * N,
+                                 sizeof(double), sizeof(double), N, cudaMemcpyDeviceToHost, c->stream));
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  return CH_OK;
+}
+
+extern "C" ch_status ch_collect_moments(ch_ctx* c, ch_grid_node* host_out, ch_step_info* info) {
+  if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
+  if (c->np == 0) return ch_fail(CH_ERR_STATE, "no ions");
+  ch_status rc = run_pass(c, PH_DEPOSIT, 0, nullptr);
+  if (rc) return rc;
+  rc = finalize_moments(c, info);
+  if (rc) return rc;
+  if (host_out) return copy_moments_out(c, host_out);
+  return CH_OK;
+}
+
+static ch_status potential(ch_ctx* c, ch_solve_info* info) {
+  if (!c->moments_valid) return ch_fail(CH_ERR_STATE, "no moments: call ch_collect_moments first");
+  const int64_t N = c->g.N;
+  c->solver.build_rhs(c->mom, c->rhs, c->stream);
+  const double* n = c->mom;
+  if (c->p.faithful & CH_FAITHFUL_D7) {
+    if (!c->solved_once) CH_CUDA_OK(cudaMemcpyAsync(c->nfz, c->mom, sizeof(double) * N, cudaMemcpyDeviceToDevice,
+                                                    c->stream));
+    n = c->nfz;
+  }
+  if (!c->solved_once) CH_CUDA_OK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));  // ComputeInitialPhi
+  SolveStats st{};
+  ch_status rc = c->solver.solve(n, c->rhs, c->phi, &st, c->stream);
+  c->solved_once = true;
+  if (info) {
+    info->iterations = st.iterations;
+    info->refinements = st.refinements;
+    info->rnorm = st.rnorm;
+    info->bnorm = st.bnorm;
+  }
+  if (rc == CH_ERR_NOT_CONVERGED)
+    return ch_fail(rc, "potential solve: ||r|| = %.3e > rtol ||b|| = %.3e after %d iterations", st.rnorm,
+                   c->p.ksp_rtol * st.bnorm, st.iterations);
+  if (rc) return rc;
+  if (!isfinite(st.rnorm)) return ch_fail(CH_ERR_NAN, "non-finite potential residual");
+  return CH_OK;
+}
+
+extern "C" ch_status ch_compute_potential(ch_ctx* c, double* phi_out, ch_solve_info* info) {
+  if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
+  ch_status rc = potential(c, info);
+  if (rc) return rc;
+  if (phi_out) {
+    CH_CUDA_OK(cudaMemcpyAsync(phi_out, c->phi, sizeof(double) * c->g.N, cudaMemcpyDeviceToHost, c->stream));
+    CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  }
+  return CH_OK;
+}
+
+extern "C" ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_step_info* info) {
+  if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
+  if (c->np == 0) return ch_fail(CH_ERR_STATE, "no ions");
+  if (!c->solved_once) return ch_fail(CH_ERR_STATE, "initial potential not computed");
+  if (nsteps < 0) return ch_fail(CH_ERR_ARG, "nsteps < 0");
+  ch_step_info local;
+  for (int32_t s = 0; s < nsteps; ++s) {
+    memset(&local, 0, sizeof(local));
+    ch_status rc = run_pass(c, PH_PUSH | PH_MOVE | PH_DEPOSIT, first_step + s, &local);
+    if (rc) return rc;
+    rc = finalize_moments(c, &local);
+    if (rc) return rc;
+    rc = potential(c, &local.solve);
+    if (rc) return rc;
+    if (c->p.sort_period > 0 && c->since_sort >= c->p.sort_period) do_sort(c);
+  }
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  if (info) *info = local;
+  return CH_OK;
+}
+
+extern "C" ch_status ch_set_moments(ch_ctx* c, const ch_grid_node* in) {
+  if (!c || !in) return ch_fail(CH_ERR_ARG, "null argument");
+  const int64_t N = c->g.N;
+  for (int q = 0; q < 4; ++q)
+    CH_CUDA_OK(cudaMemcpy2DAsync(c->mom + q * N, sizeof(double), (const char*)in + q * sizeof(double),
+                                 sizeof(ch_grid_node), sizeof(double), N, cudaMemcpyHostToDevice, c->stream));
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  c->moments_valid = true;
+  return CH_OK;
+}
+
+extern "C" ch_status ch_get_phi(ch_ctx* c, double* out) {
+  if (!c || !out) return ch_fail(CH_ERR_ARG, "null argument");
+  CH_CUDA_OK(cudaMemcpyAsync(out, c->phi, sizeof(double) * c->g.N, cudaMemcpyDeviceToHost, c->stream));
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  return CH_OK;
+}
+
+extern "C" ch_status ch_set_phi(ch_ctx* c, const double* in) {
+  if (!c || !in) return ch_fail(CH_ERR_ARG, "null argument");
+  CH_CUDA_OK(cudaMemcpyAsync(c->phi, in, sizeof(double) * c->g.N, cudaMemcpyHostToDevice, c->stream));
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  c->solved_once = true;
+  return CH_OK;
+}
+
+extern "C" ch_status ch_get_rhs(ch_ctx* c, double* out) {
+  if (!c || !out) return ch_fail(CH_ERR_ARG, "null argument");
+  if (!c->moments_valid) return ch_fail(CH_ERR_STATE, "no moments");
+  c->solver.build_rhs(c->mom, c->rhs, c->stream);
+  CH_CUDA_OK(cudaMemcpyAsync(out, c->rhs, sizeof(double) * c->g.N, cudaMemcpyDeviceToHost, c->stream));
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  return CH_OK;
+}
+
+extern "C" ch_status ch_apply_operator(ch_ctx* c, const double* x, double* y) {
+  if (!c || !x || !y) return ch_fail(CH_ERR_ARG, "null argument");
+  if (!c->moments_valid) return ch_fail(CH_ERR_STATE, "no moments");
+  const int64_t N = c->g.N;
+  double* dx = c->rhs;  // scratch: the next RHS build overwrites it
+  double* dy = c->nfz;
+  if (c->p.faithful & CH_FAITHFUL_D7) return ch_fail(CH_ERR_UNSUPPORTED, "apply with a frozen operator");
+  CH_CUDA_OK(cudaMemcpyAsync(dx, x, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+  c->solver.apply64(c->mom, dx, dy, c->stream);
+  CH_CUDA_OK(cudaMemcpyAsync(y, dy, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  return CH_OK;
+}
+
+extern "C" ch_status ch_host_register(void* ptr, uint64_t bytes) {
+  if (!ptr || !bytes) return ch_fail(CH_ERR_ARG, "null argument");
+  CH_CUDA_OK(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+  return CH_OK;
+}
+
+extern "C" ch_status ch_host_unregister(void* ptr) {
+  if (!ptr) return ch_fail(CH_ERR_ARG, "null argument");
+  CH_CUDA_OK(cudaHostUnregister(ptr));
+  return CH_OK;
+}

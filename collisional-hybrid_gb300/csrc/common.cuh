@@ -1,0 +1,104 @@
+// common.cuh -- shared device definitions of the hybrid-PIC hot path.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/chybrid.h"
+
+#define CH_PI 3.14159265358979323846
+
+// Philox counter word 2 = purpose << 24 | block (same layout as the CPU oracle).
+#define CH_PURPOSE_COLLIDE 1u
+#define CH_PURPOSE_LOAD 2u
+#define CH_STEP_LOADER 0xFFFFFFFFu
+
+// Fixed-point scales of the order-independent (deterministic) reductions.
+#define CH_SBAR_SCALE 16777216.0          // 2^24, sum of mean relative speeds
+#define CH_EXPECT_SCALE 4294967296.0      // 2^32, sum of collision probabilities
+
+// Packed cell of the mixed form: i | j << 11 | k << 22.
+#define CH_PACK_BX 11
+#define CH_PACK_BY 11
+#define CH_MAX_NX 2048
+#define CH_MAX_NY 2048
+#define CH_MAX_NZ 1024
+
+struct GridDesc {
+  int Nx, Ny, Nz;
+  int64_t N;
+  double x0, y0, z0;
+  double Lx, Ly, Lz;
+  double dx, dy, dz;
+};
+
+__host__ __device__ inline int ch_wrap(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+__host__ __device__ inline int64_t ch_nid(const GridDesc& g, int i, int j, int k) {
+  return ((int64_t)ch_wrap(k, g.Nz) * g.Ny + ch_wrap(j, g.Ny)) * g.Nx + ch_wrap(i, g.Nx);
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), written from the paper.
+struct U4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ U4 ch_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                        uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+    uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+    uint32_t n0 = hi1 ^ c1 ^ k0;
+    uint32_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  return U4{c0, c1, c2, c3};
+}
+
+// (r + 1/2) 2^-32: in (0, 1), exact in FP64.
+__device__ __forceinline__ double ch_unit(uint32_t r) { return ((double)r + 0.5) * 2.3283064365386962890625e-10; }
+// 24-bit FP32 variant: ((r >> 8) + 1/2) 2^-24, in (0, 1).
+__device__ __forceinline__ float ch_unitf(uint32_t r) { return ((float)(r >> 8) + 0.5f) * 5.9604644775390625e-8f; }
+
+// Run-wide constants of one particle pass.
+struct StepConsts {
+  GridDesc g;
+  double tscale;        // (q/m) dt/2
+  double t[3], s[3];    // Boris rotation vectors
+  double E0[3];
+  int push_E0;
+  uint32_t faithful;
+  double dt;
+  // collisions
+  int collide;
+  double pscale;        // Nc / S
+  double vnT, vn0[3], mi, mn, viTr, m1;
+  int nn_profile;
+  double nn_center, nn_sigma, nn_floor;
+  uint32_t seed_lo, seed_hi, run, step;
+  // deposit
+  double dep_scale;     // fixed-point scale 2^s
+};
+
+// Device-side counters; every sum is integer so the result does not depend
+// on the order in which blocks finish.
+struct DevCounters {
+  unsigned long long collisions;
+  unsigned long long refused;
+  long long sbar_fx;
+  long long expected_fx;
+  int range_error;
+  int pad;
+};
+
+#define CH_CUDA_OK(expr)                         \
+  do {                                           \
+    cudaError_t e_ = (expr);                     \
+    if (e_ != cudaSuccess) return ch_cuda_fail(e_, #expr, __FILE__, __LINE__); \
+  } while (0)
+
+ch_status ch_cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+ch_status ch_fail(ch_status code, const char* fmt, ...);

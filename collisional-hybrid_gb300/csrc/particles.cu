@@ -1,0 +1,802 @@
+// particles.cu -- ion kernels of the hybrid-PIC hot path on sm_103a.
+//
+// Two state forms:
+//   FP64 plain form: SoA x, y, z, vx, vy, vz (FP64, absolute positions, the
+//     reference's RealVector semantics) + uint32 ion id.
+//   mixed form: float4 pos = (ox, oy, oz, packed cell i | j<<11 | k<<22) with
+//     within-cell offsets in [0, 1), float4 vel = (vx, vy, vz, id bits).
+//     Absolute positions are rebuilt in FP64 as x0 + (i + ox) dx.
+//
+// One templated pass kernel per form implements UpdateVelocities
+// (src/particles.c:628-643), UpdatePositions (:647-718) and
+// CollectVlasovQuantities (:136-255); the phases are compile-time flags so
+// that the separate entry points and the fused step share one code path.
+// The CIC deposit accumulates 64-bit fixed-point integers (scale 2^s): the
+// sums do not depend on the order of the additions, so the moments are
+// identical run to run whatever the thread schedule or particle order.
+#include "particles.cuh"
+#include "physics.cuh"
+
+namespace ch {
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ void red_add(unsigned long long* a, long long v) {
+  atomicAdd(a, (unsigned long long)v);
+}
+
+template <typename R>
+__device__ __forceinline__ long long to_fx(R v, R scale) {
+  return __double2ll_rn((double)(v * scale));
+}
+template <>
+__device__ __forceinline__ long long to_fx<float>(float v, float scale) {
+  return __float2ll_rn(v * scale);
+}
+
+// Deposit one ion's CIC weights: nodes (i..i+1, j..j+1, k..k+1), weights in
+// the order of src/particles.c:204-211.
+template <typename R>
+__device__ __forceinline__ void deposit_cic(const GridDesc& g, unsigned long long* __restrict__ acc, int i, int j,
+                                            int k, R wxh, R wyh, R wzh, R vx, R vy, R vz, R scale) {
+  const R wxl = R(1) - wxh, wyl = R(1) - wyh, wzl = R(1) - wzh;
+  const int i1 = (i + 1 == g.Nx) ? 0 : i + 1;
+  const int j1 = (j + 1 == g.Ny) ? 0 : j + 1;
+  const int k1 = (k + 1 == g.Nz) ? 0 : k + 1;
+  const int64_t N = g.N;
+  const int64_t rz0 = (int64_t)k * g.Ny, rz1 = (int64_t)k1 * g.Ny;
+  const int64_t c[8] = {(rz1 + j1) * g.Nx + i1, (rz0 + j1) * g.Nx + i1, (rz1 + j) * g.Nx + i1,
+                        (rz0 + j) * g.Nx + i1,  (rz1 + j1) * g.Nx + i,  (rz0 + j1) * g.Nx + i,
+                        (rz1 + j) * g.Nx + i,   (rz0 + j) * g.Nx + i};
+  const R w[8] = {wzh * wyh * wxh, wzl * wyh * wxh, wzh * wyl * wxh, wzl * wyl * wxh,
+                  wzh * wyh * wxl, wzl * wyh * wxl, wzh * wyl * wxl, wzl * wyl * wxl};
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    red_add(acc + c[q], to_fx<R>(w[q], scale));
+    red_add(acc + N + c[q], to_fx<R>(vx * w[q], scale));
+    red_add(acc + 2 * N + c[q], to_fx<R>(vy * w[q], scale));
+    red_add(acc + 3 * N + c[q], to_fx<R>(vz * w[q], scale));
+  }
+}
+
+// Block-wide sum of K doubles into part[blockIdx.x * K + q], fixed order.
+template <int K>
+__device__ __forceinline__ void block_partials(double (&v)[K], double* __restrict__ part) {
+  __shared__ double sm[K][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    double x = v[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sm[q][wid] = x;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      double x = lane < nw ? sm[q][lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0) part[(size_t)blockIdx.x * K + q] = x;
+    }
+  }
+}
+
+__device__ __forceinline__ void count_add(DevCounters* cnt, unsigned ncol, unsigned nref) {
+  unsigned long long a = ncol, b = nref;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (a) atomicAdd(&cnt->collisions, a);
+    if (b) atomicAdd(&cnt->refused, b);
+  }
+}
+
+// ------------------------------------------------------------------ loader
+// Inverse CDF of n(x) = 1 + sum_m a_m sin(2 pi m x/L + ph_m); same iteration
+// as the oracle (safeguarded Newton, 40 iterations at most).
+__device__ double inv_cdf_x(const ch_loader& L, double Lx, double u) {
+  double target = u * Lx, lo = 0.0, hi = Lx, x = target;
+  for (int it = 0; it < 40; ++it) {
+    double F = x, dF = 1.0;
+    for (int m = 1; m <= 3; ++m) {
+      const double a = L.amp[m - 1];
+      if (a == 0.0) continue;
+      const double w = 2.0 * CH_PI * m / Lx;
+      F += a * (cos(L.phase[m - 1]) - cos(w * x + L.phase[m - 1])) / w;
+      dF += a * sin(w * x + L.phase[m - 1]);
+    }
+    const double r = F - target;
+    if (r > 0.0) hi = x; else lo = x;
+    double xn = x - r / dF;
+    if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
+    if (fabs(xn - x) <= 1e-15 * Lx) { x = xn; break; }
+    x = xn;
+  }
+  if (x < 0.0) x = 0.0;
+  if (x >= Lx) x = Lx * (1.0 - 1e-16);
+  return x;
+}
+
+__device__ __forceinline__ void load_one(const GridDesc& g, const ch_loader& L, uint32_t seed_lo, uint32_t seed_hi,
+                                         uint32_t run, uint32_t id, double out[6]) {
+  const U4 a = ch_philox(id, CH_STEP_LOADER, (CH_PURPOSE_LOAD << 24) | 0u, run, seed_lo, seed_hi);
+  const U4 b = ch_philox(id, CH_STEP_LOADER, (CH_PURPOSE_LOAD << 24) | 1u, run, seed_lo, seed_hi);
+  out[0] = g.x0 + inv_cdf_x(L, g.Lx, ch_unit(a.x));
+  out[1] = g.y0 + ch_unit(a.y) * g.Ly;
+  out[2] = g.z0 + ch_unit(a.z) * g.Lz;
+  const double r1 = sqrt(-2.0 * log(ch_unit(b.x))), t1 = 2.0 * CH_PI * ch_unit(b.y);
+  const double r2 = sqrt(-2.0 * log(ch_unit(b.z))), t2 = 2.0 * CH_PI * ch_unit(b.w);
+  out[3] = L.v0[0] + L.vT[0] * (r1 * cos(t1));
+  out[4] = L.v0[1] + L.vT[1] * (r1 * sin(t1));
+  out[5] = L.v0[2] + L.vT[2] * (r2 * cos(t2));
+}
+
+// FP64 absolute position -> (cell index, offset in [0, 1)), periodic.
+__device__ __forceinline__ void locate(double x, double x0, double d, int n, int* i, double* f) {
+  const double X = (x - x0) / d;
+  const double fl = floor(X);
+  int ii = (int)fl;
+  *f = X - fl;
+  ii %= n;
+  if (ii < 0) ii += n;
+  *i = ii;
+}
+
+__device__ __forceinline__ float4 pack_mixed(const GridDesc& g, const double* s) {
+  int i, j, k;
+  double fx, fy, fz;
+  locate(s[0], g.x0, g.dx, g.Nx, &i, &fx);
+  locate(s[1], g.y0, g.dy, g.Ny, &j, &fy);
+  locate(s[2], g.z0, g.dz, g.Nz, &k, &fz);
+  float ox = (float)fx, oy = (float)fy, oz = (float)fz;
+  // rounding to FP32 may reach 1.0f: carry into the next cell
+  if (ox >= 1.0f) { ox = 0.0f; i = (i + 1 == g.Nx) ? 0 : i + 1; }
+  if (oy >= 1.0f) { oy = 0.0f; j = (j + 1 == g.Ny) ? 0 : j + 1; }
+  if (oz >= 1.0f) { oz = 0.0f; k = (k + 1 == g.Nz) ? 0 : k + 1; }
+  const uint32_t cell = (uint32_t)i | ((uint32_t)j << CH_PACK_BX) | ((uint32_t)k << (CH_PACK_BX + CH_PACK_BY));
+  return make_float4(ox, oy, oz, __uint_as_float(cell));
+}
+
+__global__ void k_load_f64(GridDesc g, ch_loader L, uint32_t slo, uint32_t shi, uint32_t run, F64Particles P) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.np; i += (int64_t)gridDim.x * blockDim.x) {
+    double s[6];
+    load_one(g, L, slo, shi, run, (uint32_t)i, s);
+    P.x[i] = s[0]; P.y[i] = s[1]; P.z[i] = s[2];
+    P.vx[i] = s[3]; P.vy[i] = s[4]; P.vz[i] = s[5];
+    P.id[i] = (uint32_t)i;
+  }
+}
+
+__global__ void k_load_mixed(GridDesc g, ch_loader L, uint32_t slo, uint32_t shi, uint32_t run, MixParticles P) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.np; i += (int64_t)gridDim.x * blockDim.x) {
+    double s[6];
+    load_one(g, L, slo, shi, run, (uint32_t)i, s);
+    P.pos[i] = pack_mixed(g, s);
+    P.vel[i] = make_float4((float)s[3], (float)s[4], (float)s[5], __uint_as_float((uint32_t)i));
+  }
+}
+
+// AoS RealVector (x, y, z, r) staging -> state, id = index.
+__global__ void k_aos_to_f64(const double4_32a* __restrict__ pos, const double4_32a* __restrict__ vel, F64Particles P) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.np; i += (int64_t)gridDim.x * blockDim.x) {
+    const double4_32a p = pos[i], v = vel[i];
+    P.x[i] = p.x; P.y[i] = p.y; P.z[i] = p.z;
+    P.vx[i] = v.x; P.vy[i] = v.y; P.vz[i] = v.z;
+    P.id[i] = (uint32_t)i;
+  }
+}
+
+__global__ void k_aos_to_mixed(GridDesc g, const double4_32a* __restrict__ pos, const double4_32a* __restrict__ vel,
+                               MixParticles P) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.np; i += (int64_t)gridDim.x * blockDim.x) {
+    const double4_32a p = pos[i], v = vel[i];
+    const double s[3] = {p.x, p.y, p.z};
+    P.pos[i] = pack_mixed(g, s);
+    P.vel[i] = make_float4((float)v.x, (float)v.y, (float)v.z, __uint_as_float((uint32_t)i));
+  }
+}
+
+// state -> AoS staging in id order (undoes the cell sort).
+__global__ void k_f64_to_aos(F64Particles P, double4_32a* __restrict__ pos, double4_32a* __restrict__ vel) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.np; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t id = P.id[i];
+    pos[id] = make_double4_32a(P.x[i], P.y[i], P.z[i], 0.0);
+    vel[id] = make_double4_32a(P.vx[i], P.vy[i], P.vz[i], 0.0);
+  }
+}
+
+__global__ void k_mixed_to_aos(GridDesc g, MixParticles P, double4_32a* __restrict__ pos, double4_32a* __restrict__ vel) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.np; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 p = P.pos[i], v = P.vel[i];
+    const uint32_t cell = __float_as_uint(p.w);
+    const int ci = cell & (CH_MAX_NX - 1), cj = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
+              ck = cell >> (CH_PACK_BX + CH_PACK_BY);
+    const uint32_t id = __float_as_uint(v.w);
+    pos[id] = make_double4_32a(g.x0 + ((double)ci + (double)p.x) * g.dx, g.y0 + ((double)cj + (double)p.y) * g.dy,
+                           g.z0 + ((double)ck + (double)p.z) * g.dz, 0.0);
+    vel[id] = make_double4_32a((double)v.x, (double)v.y, (double)v.z, 0.0);
+  }
+}
+
+// ------------------------------------------------------------------ node field
+// E = -grad phi by periodic central differences (the Escale of
+// src/particles.c:391-393 applied at the nodes).
+__global__ void k_node_efield_f64(GridDesc g, const double* __restrict__ phi, double* __restrict__ E) {
+  const int64_t N = g.N;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c % g.Nx), j = (int)((c / g.Nx) % g.Ny), k = (int)(c / ((int64_t)g.Nx * g.Ny));
+    const int ip = i + 1 == g.Nx ? 0 : i + 1, im = i == 0 ? g.Nx - 1 : i - 1;
+    const int jp = j + 1 == g.Ny ? 0 : j + 1, jm = j == 0 ? g.Ny - 1 : j - 1;
+    const int kp = k + 1 == g.Nz ? 0 : k + 1, km = k == 0 ? g.Nz - 1 : k - 1;
+    const int64_t row = ((int64_t)k * g.Ny + j) * g.Nx;
+    E[c] = -(phi[row + ip] - phi[row + im]) / (2.0 * g.dx);
+    E[N + c] = -(phi[((int64_t)k * g.Ny + jp) * g.Nx + i] - phi[((int64_t)k * g.Ny + jm) * g.Nx + i]) / (2.0 * g.dy);
+    E[2 * N + c] =
+        -(phi[((int64_t)kp * g.Ny + j) * g.Nx + i] - phi[((int64_t)km * g.Ny + j) * g.Nx + i]) / (2.0 * g.dz);
+  }
+}
+
+__global__ void k_node_efield_mixed(GridDesc g, float tscale, const double* __restrict__ phi, float4* __restrict__ E) {
+  const int64_t N = g.N;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c % g.Nx), j = (int)((c / g.Nx) % g.Ny), k = (int)(c / ((int64_t)g.Nx * g.Ny));
+    const int ip = i + 1 == g.Nx ? 0 : i + 1, im = i == 0 ? g.Nx - 1 : i - 1;
+    const int jp = j + 1 == g.Ny ? 0 : j + 1, jm = j == 0 ? g.Ny - 1 : j - 1;
+    const int kp = k + 1 == g.Nz ? 0 : k + 1, km = k == 0 ? g.Nz - 1 : k - 1;
+    const int64_t row = ((int64_t)k * g.Ny + j) * g.Nx;
+    const double ex = -(phi[row + ip] - phi[row + im]) / (2.0 * g.dx);
+    const double ey =
+        -(phi[((int64_t)k * g.Ny + jp) * g.Nx + i] - phi[((int64_t)k * g.Ny + jm) * g.Nx + i]) / (2.0 * g.dy);
+    const double ez =
+        -(phi[((int64_t)kp * g.Ny + j) * g.Nx + i] - phi[((int64_t)km * g.Ny + j) * g.Nx + i]) / (2.0 * g.dz);
+    // stored premultiplied by the push scale (q/m) dt/2
+    E[c] = make_float4((float)(ex * tscale), (float)(ey * tscale), (float)(ez * tscale), 0.0f);
+  }
+}
+
+// DifferenceVector as written (src/vectors.c:12-138): CH_FAITHFUL_D3 / D4.
+__device__ void diffvec_faithful(const GridDesc& g, const double* __restrict__ phi, double X, double Y, double Z,
+                                 uint32_t faithful, double f[3]) {
+  const int ixl = (int)floor(X), iyl = (int)floor(Y), izl = (int)floor(Z);
+  const double wxh = X - ixl, wyh = Y - iyl, wzh = Z - izl;
+  const int ixh = ixl + 1, iyh = iyl + 1, izh = izl + 1;
+  const bool onesided = (faithful & CH_FAITHFUL_D4) != 0;
+  auto F = [&](int k, int j, int i) { return phi[ch_nid(g, i, j, k)]; };
+  for (int d = 0; d < 3; ++d) {
+    auto diff = [&](int k, int j, int i) -> double {
+      if (d == 0) {
+        if (onesided && i == g.Nx) return 3.0 * F(k, j, i) - 4.0 * F(k, j, i - 1) + F(k, j, i - 2);
+        return F(k, j, i + 1) - F(k, j, i - 1);
+      } else if (d == 1) {
+        if (onesided && j == g.Ny) return 3.0 * F(k, j, i) - 4.0 * F(k, j - 1, i) + F(k, j - 2, i);
+        return F(k, j + 1, i) - F(k, j - 1, i);
+      }
+      if (onesided && k == g.Nz) return 3.0 * F(k, j, i) - 4.0 * F(k - 1, j, i) + F(k - 2, j, i);
+      return F(k + 1, j, i) - F(k - 1, j, i);
+    };
+    const double hhh = diff(izh, iyh, ixh), lhh = diff(izl, iyh, ixh), hlh = diff(izh, iyl, ixh),
+                 llh = diff(izl, iyl, ixh), hhl = diff(izh, iyh, ixl), lhl = diff(izl, iyh, ixl),
+                 hll = diff(izh, iyl, ixl), lll = diff(izl, iyl, ixl);
+    const double whh = hlh + wyh * (hhh - hlh), whl = hll + wyh * (hhl - hll);
+    const double wlh = llh + wyh * (lhh - llh), wll = lll + wyh * (lhl - lll);
+    if (faithful & CH_FAITHFUL_D3) {
+      const double Ewh = wlh + wxh * (whh - wlh), Ewl = wll + wxh * (whl - wll);
+      f[d] = Ewl + wzh * (Ewh - Ewh);
+    } else {
+      const double Ezl = wll + wxh * (wlh - wll), Ezh = whl + wxh * (whh - whl);
+      f[d] = Ezl + wzh * (Ezh - Ezl);
+    }
+  }
+}
+
+__device__ __forceinline__ double wrap_pos(double x, double x0, double L) {
+  double u = x - x0;
+  if (u < 0.0 || u >= L) u -= L * floor(u / L);
+  if (u >= L) u -= L;
+  if (u < 0.0) u = 0.0;
+  return x0 + u;
+}
+
+// ------------------------------------------------------------------ FP64 pass
+// Block partials: 0 expected, 1 S(next).
+template <int PH>
+__global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, const double* __restrict__ E,
+                                                  const double* __restrict__ phi, unsigned long long* __restrict__ acc,
+                                                  double Nc, double sbar, DevCounters* cnt, double* part) {
+  const GridDesc& g = c.g;
+  const int64_t N = g.N;
+  double vsum[2] = {0.0, 0.0};
+  unsigned ncol = 0, nref = 0;
+  const bool gather_faithful = (c.faithful & (CH_FAITHFUL_D3 | CH_FAITHFUL_D4)) != 0;
+  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
+    double x = P.x[ip], y = P.y[ip], z = P.z[ip];
+    double v[3] = {P.vx[ip], P.vy[ip], P.vz[ip]};
+    if (PH & PH_PUSH) {
+      const double X = (x - g.x0) / g.dx, Y = (y - g.y0) / g.dy, Z = (z - g.z0) / g.dz;
+      double Ef[3];
+      if (gather_faithful) {
+        double f[3];
+        diffvec_faithful(g, phi, X, Y, Z, c.faithful, f);
+        Ef[0] = -f[0] / (2.0 * g.dx); Ef[1] = -f[1] / (2.0 * g.dy); Ef[2] = -f[2] / (2.0 * g.dz);
+      } else {
+        const double fi = floor(X), fj = floor(Y), fk = floor(Z);
+        const double wx = X - fi, wy = Y - fj, wz = Z - fk;
+        const int i = ch_wrap((int)fi, g.Nx), j = ch_wrap((int)fj, g.Ny), k = ch_wrap((int)fk, g.Nz);
+        const int i1 = i + 1 == g.Nx ? 0 : i + 1, j1 = j + 1 == g.Ny ? 0 : j + 1, k1 = k + 1 == g.Nz ? 0 : k + 1;
+        const int64_t c000 = ((int64_t)k * g.Ny + j) * g.Nx + i, c100 = ((int64_t)k * g.Ny + j) * g.Nx + i1,
+                      c010 = ((int64_t)k * g.Ny + j1) * g.Nx + i, c110 = ((int64_t)k * g.Ny + j1) * g.Nx + i1,
+                      c001 = ((int64_t)k1 * g.Ny + j) * g.Nx + i, c101 = ((int64_t)k1 * g.Ny + j) * g.Nx + i1,
+                      c011 = ((int64_t)k1 * g.Ny + j1) * g.Nx + i, c111 = ((int64_t)k1 * g.Ny + j1) * g.Nx + i1;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const double* e = E + d * N;
+          const double wll = e[c000] + wy * (e[c010] - e[c000]);
+          const double wlh = e[c100] + wy * (e[c110] - e[c100]);
+          const double whl = e[c001] + wy * (e[c011] - e[c001]);
+          const double whh = e[c101] + wy * (e[c111] - e[c101]);
+          const double ezl = wll + wx * (wlh - wll);
+          const double ezh = whl + wx * (whh - whl);
+          Ef[d] = ezl + wz * (ezh - ezl);
+        }
+      }
+      if (c.push_E0) { Ef[0] += c.E0[0]; Ef[1] += c.E0[1]; Ef[2] += c.E0[2]; }
+      ch_boris<double>(c, Ef, v);
+      if (c.collide) {
+        const double wx = v[0] - c.vn0[0], wy = v[1] - c.vn0[1], wz = v[2] - c.vn0[2];
+        const double gi = ch_gmean<double>(sqrt(wx * wx + wy * wy + wz * wz), c.vnT);
+        double pc = sbar > 0.0 ? (Nc * gi * ch_neutral_density<double>(c, x)) / sbar : 0.0;
+        if (pc > 1.0) pc = 1.0;
+        vsum[0] += pc;
+        const int rc = ch_collide<double>(c, P.id[ip], pc, v);
+        if (rc > 0) ++ncol; else if (rc < 0) ++nref;
+        const double qx = v[0] - c.vn0[0], qy = v[1] - c.vn0[1], qz = v[2] - c.vn0[2];
+        vsum[1] += ch_gmean<double>(sqrt(qx * qx + qy * qy + qz * qz), c.vnT);
+      }
+      P.vx[ip] = v[0]; P.vy[ip] = v[1]; P.vz[ip] = v[2];
+    }
+    if ((PH & PH_MOVE) && !(c.faithful & CH_FAITHFUL_D5)) {
+      x = wrap_pos(x + v[0] * c.dt, g.x0, g.Lx);
+      y = wrap_pos(y + v[1] * c.dt, g.y0, g.Ly);
+      z = wrap_pos(z + v[2] * c.dt, g.z0, g.Lz);
+      P.x[ip] = x; P.y[ip] = y; P.z[ip] = z;
+    }
+    if (PH & PH_DEPOSIT) {
+      const double X = (x - g.x0) / g.dx, Y = (y - g.y0) / g.dy, Z = (z - g.z0) / g.dz;
+      const double fi = floor(X), fj = floor(Y), fk = floor(Z);
+      deposit_cic<double>(g, acc, ch_wrap((int)fi, g.Nx), ch_wrap((int)fj, g.Ny), ch_wrap((int)fk, g.Nz), X - fi,
+                          Y - fj, Z - fk, v[0], v[1], v[2], c.dep_scale);
+    }
+  }
+  if (PH & PH_PUSH) {
+    count_add(cnt, ncol, nref);
+    block_partials<2>(vsum, part);
+  }
+}
+
+// ------------------------------------------------------------------ mixed pass
+template <int PH>
+__global__ void __launch_bounds__(256) k_pass_mixed(StepConsts c, MixParticles P, const float4* __restrict__ E,
+                                                    unsigned long long* __restrict__ acc, float pscale,
+                                                    DevCounters* cnt, double* part) {
+  const GridDesc& g = c.g;
+  double vsum[2] = {0.0, 0.0};
+  unsigned ncol = 0, nref = 0;
+  const float dtx = (float)(c.dt / g.dx), dty = (float)(c.dt / g.dy), dtz = (float)(c.dt / g.dz);
+  const float vnTf = (float)c.vnT, vn0x = (float)c.vn0[0], vn0y = (float)c.vn0[1], vn0z = (float)c.vn0[2];
+  const float scale = (float)c.dep_scale;
+  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
+    float4 p = P.pos[ip];
+    float4 vv = P.vel[ip];
+    uint32_t cell = __float_as_uint(p.w);
+    int i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1), k = cell >> (CH_PACK_BX + CH_PACK_BY);
+    float v[3] = {vv.x, vv.y, vv.z};
+    if (PH & PH_PUSH) {
+      const int i1 = i + 1 == g.Nx ? 0 : i + 1, j1 = j + 1 == g.Ny ? 0 : j + 1, k1 = k + 1 == g.Nz ? 0 : k + 1;
+      const int64_t r00 = ((int64_t)k * g.Ny + j) * g.Nx, r10 = ((int64_t)k * g.Ny + j1) * g.Nx,
+                    r01 = ((int64_t)k1 * g.Ny + j) * g.Nx, r11 = ((int64_t)k1 * g.Ny + j1) * g.Nx;
+      const float4 e000 = __ldg(E + r00 + i), e100 = __ldg(E + r00 + i1), e010 = __ldg(E + r10 + i),
+                   e110 = __ldg(E + r10 + i1), e001 = __ldg(E + r01 + i), e101 = __ldg(E + r01 + i1),
+                   e011 = __ldg(E + r11 + i), e111 = __ldg(E + r11 + i1);
+      const float wx = p.x, wy = p.y, wz = p.z;
+      float Ef[3];
+#define LERP3(f)                                                                   \
+  {                                                                                \
+    const float wll = e000.f + wy * (e010.f - e000.f);                             \
+    const float wlh = e100.f + wy * (e110.f - e100.f);                             \
+    const float whl = e001.f + wy * (e011.f - e001.f);                             \
+    const float whh = e101.f + wy * (e111.f - e101.f);                             \
+    const float ezl = wll + wx * (wlh - wll), ezh = whl + wx * (whh - whl);        \
+    Ef_##f = ezl + wz * (ezh - ezl);                                               \
+  }
+      float Ef_x, Ef_y, Ef_z;
+      LERP3(x) LERP3(y) LERP3(z)
+#undef LERP3
+      // E is stored premultiplied by (q/m) dt/2; the Boris helper multiplies
+      // by tscale, so divide it back out through a unit scale.
+      Ef[0] = Ef_x; Ef[1] = Ef_y; Ef[2] = Ef_z;
+      if (c.push_E0) {
+        Ef[0] += (float)(c.E0[0] * c.tscale); Ef[1] += (float)(c.E0[1] * c.tscale); Ef[2] += (float)(c.E0[2] * c.tscale);
+      }
+      {
+        // Boris with pre-scaled E (ts = 1)
+        float vm0 = v[0] + Ef[0], vm1 = v[1] + Ef[1], vm2 = v[2] + Ef[2];
+        float vp0 = vm0, vp1 = vm1, vp2 = vm2;
+        if (!(c.faithful & CH_FAITHFUL_D2)) {
+          const float t0 = (float)c.t[0], t1 = (float)c.t[1], t2 = (float)c.t[2];
+          const float s0 = (float)c.s[0], s1 = (float)c.s[1], s2 = (float)c.s[2];
+          const float q0 = vm0 + (vm1 * t2 - vm2 * t1);
+          const float q1 = vm1 + (vm2 * t0 - vm0 * t2);
+          const float q2 = vm2 + (vm0 * t1 - vm1 * t0);
+          vp0 = vm0 + (q1 * s2 - q2 * s1);
+          vp1 = vm1 + (q2 * s0 - q0 * s2);
+          vp2 = vm2 + (q0 * s1 - q1 * s0);
+        }
+        v[0] = vp0 + Ef[0]; v[1] = vp1 + Ef[1]; v[2] = vp2 + Ef[2];
+      }
+      if (c.collide) {
+        const float wx2 = v[0] - vn0x, wy2 = v[1] - vn0y, wz2 = v[2] - vn0z;
+        const float gi = ch_gmean<float>(sqrtf(wx2 * wx2 + wy2 * wy2 + wz2 * wz2), vnTf);
+        float nd = 1.0f;
+        if (c.nn_profile == CH_NN_GAUSSIAN_X)
+          nd = ch_neutral_density<float>(c, (float)(g.x0 + ((double)i + (double)p.x) * g.dx));
+        float pc = pscale * gi * nd;
+        if (pc > 1.0f) pc = 1.0f;
+        vsum[0] += (double)pc;
+        const int rc = ch_collide<float>(c, __float_as_uint(vv.w), pc, v);
+        if (rc > 0) ++ncol; else if (rc < 0) ++nref;
+        const float qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
+        vsum[1] += (double)ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), vnTf);
+      }
+      vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
+      P.vel[ip] = vv;
+    }
+    if ((PH & PH_MOVE) && !(c.faithful & CH_FAITHFUL_D5)) {
+      // offsets move in cell units; integer cell wrap is exact
+      float ox = p.x + v[0] * dtx, oy = p.y + v[1] * dty, oz = p.z + v[2] * dtz;
+      const float fx = floorf(ox), fy = floorf(oy), fz = floorf(oz);
+      ox -= fx; oy -= fy; oz -= fz;
+      if (ox >= 1.0f) { ox = 0.0f; } // x - floor(x) can round up to 1
+      if (oy >= 1.0f) { oy = 0.0f; }
+      if (oz >= 1.0f) { oz = 0.0f; }
+      i = ch_wrap(i + (int)fx, g.Nx); j = ch_wrap(j + (int)fy, g.Ny); k = ch_wrap(k + (int)fz, g.Nz);
+      cell = (uint32_t)i | ((uint32_t)j << CH_PACK_BX) | ((uint32_t)k << (CH_PACK_BX + CH_PACK_BY));
+      p = make_float4(ox, oy, oz, __uint_as_float(cell));
+      P.pos[ip] = p;
+    }
+    if (PH & PH_DEPOSIT) {
+      deposit_cic<float>(g, acc, i, j, k, p.x, p.y, p.z, v[0], v[1], v[2], scale);
+    }
+  }
+  if (PH & PH_PUSH) {
+    count_add(cnt, ncol, nref);
+    block_partials<2>(vsum, part);
+  }
+}
+
+// ------------------------------------------------------------------ S at upload
+__global__ void k_sbar_f64(F64Particles P, double vnT, double vn0x, double vn0y, double vn0z, double* part) {
+  double s[1] = {0.0};
+  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
+    const double wx = P.vx[ip] - vn0x, wy = P.vy[ip] - vn0y, wz = P.vz[ip] - vn0z;
+    s[0] += ch_gmean<double>(sqrt(wx * wx + wy * wy + wz * wz), vnT);
+  }
+  block_partials<1>(s, part);
+}
+
+__global__ void k_sbar_mixed(MixParticles P, float vnT, float vn0x, float vn0y, float vn0z, double* part) {
+  double s[1] = {0.0};
+  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
+    const float4 v = P.vel[ip];
+    const float wx = v.x - vn0x, wy = v.y - vn0y, wz = v.z - vn0z;
+    s[0] += (double)ch_gmean<float>(sqrtf(wx * wx + wy * wy + wz * wz), vnT);
+  }
+  block_partials<1>(s, part);
+}
+
+// Fixed-order sum of per-block partials: out[q] = sum_b part[b*K + q].
+__global__ void k_reduce_partials(const double* __restrict__ part, int nblocks, int K, double* out) {
+  __shared__ double sm[32];
+  for (int q = 0; q < K; ++q) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += part[(size_t)b * K + q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double t = threadIdx.x < (blockDim.x >> 5) ? sm[threadIdx.x] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      if (threadIdx.x == 0) out[q] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ moments
+// Fixed-point accumulators -> FP64 moments (SoA n, Gx, Gy, Gz), optional
+// reset, block partials of the four global sums, and the range check: the
+// density contributions are non-negative, so a wrapped sum shows up as a
+// negative or near-limit value.
+__global__ void k_finalize_moments(int64_t N, unsigned long long* __restrict__ acc, double inv_scale, int reset,
+                                   double* __restrict__ mom, double* part, DevCounters* cnt) {
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  int bad = 0;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const long long a = (long long)acc[q * N + c];
+      if (q == 0 && (a < 0 || a > (1LL << 61))) bad = 1;
+      const double v = (double)a * inv_scale;
+      mom[q * N + c] = v;
+      s[q] += v;
+      if (reset) acc[q * N + c] = 0ull;
+    }
+  }
+  if (bad) atomicOr(&cnt->range_error, 1);
+  block_partials<4>(s, part);
+}
+
+// ------------------------------------------------------------------ counting sort
+// key = natural cell index (k*Ny + j)*Nx + i of the ion's current cell.
+__device__ __forceinline__ uint32_t key_f64(const GridDesc& g, double x, double y, double z) {
+  int i, j, k;
+  double f;
+  locate(x, g.x0, g.dx, g.Nx, &i, &f);
+  locate(y, g.y0, g.dy, g.Ny, &j, &f);
+  locate(z, g.z0, g.dz, g.Nz, &k, &f);
+  return (uint32_t)(((int64_t)k * g.Ny + j) * g.Nx + i);
+}
+__device__ __forceinline__ uint32_t key_mixed(const GridDesc& g, float w) {
+  const uint32_t cell = __float_as_uint(w);
+  const uint32_t i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
+                 k = cell >> (CH_PACK_BX + CH_PACK_BY);
+  return (k * (uint32_t)g.Ny + j) * (uint32_t)g.Nx + i;
+}
+
+// Warp-aggregated increment of counts[key]; returns this lane's rank among
+// the lanes that share its key, and the group's base from the atomic.
+__device__ __forceinline__ uint32_t agg_inc(uint32_t* counts, uint32_t key, bool active) {
+  const unsigned mask = __activemask();
+  const unsigned grp = __match_any_sync(mask, active ? key : 0xFFFFFFFFu);
+  const int leader = __ffs(grp) - 1;
+  const int lane = threadIdx.x & 31;
+  const uint32_t rank = __popc(grp & ((1u << lane) - 1u));
+  uint32_t base = 0;
+  if (active && lane == leader) base = atomicAdd(counts + key, (uint32_t)__popc(grp));
+  base = __shfl_sync(mask, base, leader);
+  return base + rank;
+}
+
+__global__ void k_hist_f64(GridDesc g, F64Particles P, uint32_t* counts, uint32_t* keys) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t n_pad = (P.np + 31) / 32 * 32;
+  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < n_pad; ip += stride) {
+    const bool act = ip < P.np;
+    uint32_t key = 0;
+    if (act) key = key_f64(g, P.x[ip], P.y[ip], P.z[ip]);
+    agg_inc(counts, key, act);
+    if (act) keys[ip] = key;
+  }
+}
+
+__global__ void k_hist_mixed(GridDesc g, MixParticles P, uint32_t* counts, uint32_t* keys) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t n_pad = (P.np + 31) / 32 * 32;
+  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < n_pad; ip += stride) {
+    const bool act = ip < P.np;
+    uint32_t key = 0;
+    if (act) key = key_mixed(g, P.pos[ip].w);
+    agg_inc(counts, key, act);
+    if (act) keys[ip] = key;
+  }
+}
+
+__global__ void k_scatter_f64(F64Particles P, F64Particles Q, const uint32_t* __restrict__ keys, uint32_t* cursor) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t n_pad = (P.np + 31) / 32 * 32;
+  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < n_pad; ip += stride) {
+    const bool act = ip < P.np;
+    const uint32_t key = act ? keys[ip] : 0u;
+    const uint32_t dst = agg_inc(cursor, key, act);
+    if (act) {
+      Q.x[dst] = P.x[ip]; Q.y[dst] = P.y[ip]; Q.z[dst] = P.z[ip];
+      Q.vx[dst] = P.vx[ip]; Q.vy[dst] = P.vy[ip]; Q.vz[dst] = P.vz[ip];
+      Q.id[dst] = P.id[ip];
+    }
+  }
+}
+
+__global__ void k_scatter_mixed(MixParticles P, MixParticles Q, const uint32_t* __restrict__ keys, uint32_t* cursor) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t n_pad = (P.np + 31) / 32 * 32;
+  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < n_pad; ip += stride) {
+    const bool act = ip < P.np;
+    const uint32_t key = act ? keys[ip] : 0u;
+    const uint32_t dst = agg_inc(cursor, key, act);
+    if (act) {
+      Q.pos[dst] = P.pos[ip];
+      Q.vel[dst] = P.vel[ip];
+    }
+  }
+}
+
+// Exclusive scan of counts[0..n) into starts[0..n] (three phases).
+__global__ void k_scan_blocks(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint32_t* block_sums,
+                              int64_t n) {
+  __shared__ uint32_t sm[1024];
+  const int64_t base = (int64_t)blockIdx.x * 1024;
+  const int t = threadIdx.x;  // 512 threads, 2 items each
+  uint32_t a = base + 2 * t < n ? in[base + 2 * t] : 0u;
+  uint32_t b = base + 2 * t + 1 < n ? in[base + 2 * t + 1] : 0u;
+  sm[2 * t] = a;
+  sm[2 * t + 1] = b;
+  // Blelloch up-sweep / down-sweep
+  int off = 1;
+  for (int d = 512; d > 0; d >>= 1) {
+    __syncthreads();
+    if (t < d) {
+      const int ai = off * (2 * t + 1) - 1, bi = off * (2 * t + 2) - 1;
+      sm[bi] += sm[ai];
+    }
+    off <<= 1;
+  }
+  if (t == 0) {
+    block_sums[blockIdx.x] = sm[1023];
+    sm[1023] = 0;
+  }
+  for (int d = 1; d < 1024; d <<= 1) {
+    off >>= 1;
+    __syncthreads();
+    if (t < d) {
+      const int ai = off * (2 * t + 1) - 1, bi = off * (2 * t + 2) - 1;
+      const uint32_t tmp = sm[ai];
+      sm[ai] = sm[bi];
+      sm[bi] += tmp;
+    }
+  }
+  __syncthreads();
+  if (base + 2 * t < n) out[base + 2 * t] = sm[2 * t];
+  if (base + 2 * t + 1 < n) out[base + 2 * t + 1] = sm[2 * t + 1];
+}
+
+__global__ void k_scan_sums(uint32_t* block_sums, int nb, uint32_t* total) {
+  // single block, serial over chunks of 1024 with a running offset
+  __shared__ uint32_t sm[1024];
+  uint32_t run = 0;
+  for (int base = 0; base < nb; base += 1024) {
+    const int t = threadIdx.x;
+    const int idx = base + t;
+    const uint32_t v = idx < nb ? block_sums[idx] : 0u;
+    sm[t] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+      const uint32_t add = t >= off ? sm[t - off] : 0u;
+      __syncthreads();
+      sm[t] += add;
+      __syncthreads();
+    }
+    if (idx < nb) block_sums[idx] = run + sm[t] - v;  // exclusive
+    const uint32_t chunk = sm[1023];
+    __syncthreads();
+    run += chunk;
+  }
+  if (threadIdx.x == 0) *total = run;
+}
+
+__global__ void k_scan_add(uint32_t* out, const uint32_t* block_sums, int64_t n, uint32_t* cursor) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) {
+    const uint32_t v = out[i] + block_sums[i / 1024];
+    out[i] = v;
+    cursor[i] = v;
+  }
+}
+
+// ------------------------------------------------------------------ launchers
+int grid_for(int64_t n, int threads, int sms, int per_sm) {
+  int64_t need = (n + threads - 1) / threads;
+  int64_t cap = (int64_t)sms * per_sm;
+  if (need < 1) need = 1;
+  return (int)(need < cap ? need : cap);
+}
+
+void launch_load(bool mixed, const GridDesc& g, const ch_loader& L, uint64_t seed, uint32_t run, F64Particles P,
+                 MixParticles M, int sms, cudaStream_t s) {
+  const uint32_t lo = (uint32_t)seed, hi = (uint32_t)(seed >> 32);
+  if (mixed) k_load_mixed<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, L, lo, hi, run, M);
+  else k_load_f64<<<grid_for(P.np, 256, sms, 8), 256, 0, s>>>(g, L, lo, hi, run, P);
+}
+
+void launch_aos_in(bool mixed, const GridDesc& g, const double4_32a* pos, const double4_32a* vel, F64Particles P,
+                   MixParticles M, int sms, cudaStream_t s) {
+  if (mixed) k_aos_to_mixed<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, pos, vel, M);
+  else k_aos_to_f64<<<grid_for(P.np, 256, sms, 8), 256, 0, s>>>(pos, vel, P);
+}
+
+void launch_aos_out(bool mixed, const GridDesc& g, F64Particles P, MixParticles M, double4_32a* pos, double4_32a* vel,
+                    int sms, cudaStream_t s) {
+  if (mixed) k_mixed_to_aos<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, M, pos, vel);
+  else k_f64_to_aos<<<grid_for(P.np, 256, sms, 8), 256, 0, s>>>(P, pos, vel);
+}
+
+void launch_node_efield(bool mixed, const GridDesc& g, double tscale, const double* phi, double* E64, float4* E32,
+                        int sms, cudaStream_t s) {
+  if (mixed) k_node_efield_mixed<<<grid_for(g.N, 256, sms, 8), 256, 0, s>>>(g, (float)tscale, phi, E32);
+  else k_node_efield_f64<<<grid_for(g.N, 256, sms, 8), 256, 0, s>>>(g, phi, E64);
+}
+
+template <int PH>
+static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticles M, const double* E64,
+                    const float4* E32, const double* phi, unsigned long long* acc, double Nc, double sbar,
+                    DevCounters* cnt, double* part, int sms, cudaStream_t s) {
+  const int64_t np = mixed ? M.np : P.np;
+  const int nb = grid_for(np, 256, sms, 8);
+  if (mixed) {
+    const float pscale = sbar > 0.0 ? (float)(Nc / sbar) : 0.0f;
+    k_pass_mixed<PH><<<nb, 256, 0, s>>>(c, M, E32, acc, pscale, cnt, part);
+  } else {
+    k_pass_f64<PH><<<nb, 256, 0, s>>>(c, P, E64, phi, acc, Nc, sbar, cnt, part);
+  }
+  return nb;
+}
+
+int launch_pass(bool mixed, int phases, const StepConsts& c, F64Particles P, MixParticles M, const double* E64,
+                const float4* E32, const double* phi, unsigned long long* acc, double Nc, double sbar,
+                DevCounters* cnt, double* part, int sms, cudaStream_t s) {
+  switch (phases) {
+    case PH_PUSH: return pass_one<PH_PUSH>(mixed, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, sms, s);
+    case PH_MOVE: return pass_one<PH_MOVE>(mixed, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, sms, s);
+    case PH_DEPOSIT: return pass_one<PH_DEPOSIT>(mixed, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, sms, s);
+    case PH_MOVE | PH_DEPOSIT:
+      return pass_one<PH_MOVE | PH_DEPOSIT>(mixed, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, sms, s);
+    default:
+      return pass_one<PH_PUSH | PH_MOVE | PH_DEPOSIT>(mixed, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, sms,
+                                                      s);
+  }
+}
+
+int launch_sbar(bool mixed, const StepConsts& c, F64Particles P, MixParticles M, double* part, int sms,
+                cudaStream_t s) {
+  const int64_t np = mixed ? M.np : P.np;
+  const int nb = grid_for(np, 256, sms, 8);
+  if (mixed)
+    k_sbar_mixed<<<nb, 256, 0, s>>>(M, (float)c.vnT, (float)c.vn0[0], (float)c.vn0[1], (float)c.vn0[2], part);
+  else
+    k_sbar_f64<<<nb, 256, 0, s>>>(P, c.vnT, c.vn0[0], c.vn0[1], c.vn0[2], part);
+  return nb;
+}
+
+void launch_reduce_partials(const double* part, int nblocks, int K, double* out, cudaStream_t s) {
+  k_reduce_partials<<<1, 256, 0, s>>>(part, nblocks, K, out);
+}
+
+int launch_finalize(int64_t N, unsigned long long* acc, double inv_scale, int reset, double* mom, double* part,
+                    DevCounters* cnt, int sms, cudaStream_t s) {
+  const int nb = grid_for(N, 256, sms, 4);
+  k_finalize_moments<<<nb, 256, 0, s>>>(N, acc, inv_scale, reset, mom, part, cnt);
+  return nb;
+}
+
+void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, MixParticles M, MixParticles MQ,
+                 uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* keys, uint32_t* block_sums, int sms,
+                 cudaStream_t s) {
+  const int64_t np = mixed ? M.np : P.np;
+  const int64_t N = g.N;
+  cudaMemsetAsync(counts, 0, sizeof(uint32_t) * N, s);
+  const int nb = grid_for(np, 256, sms, 8);
+  if (mixed) k_hist_mixed<<<nb, 256, 0, s>>>(g, M, counts, keys);
+  else k_hist_f64<<<nb, 256, 0, s>>>(g, P, counts, keys);
+  const int nsb = (int)((N + 1023) / 1024);
+  k_scan_blocks<<<nsb, 512, 0, s>>>(counts, starts, block_sums, N);
+  k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nsb, starts + N);
+  k_scan_add<<<(int)((N + 255) / 256), 256, 0, s>>>(starts, block_sums, N, cursor);
+  if (mixed) k_scatter_mixed<<<nb, 256, 0, s>>>(M, MQ, keys, cursor);
+  else k_scatter_f64<<<nb, 256, 0, s>>>(P, Q, keys, cursor);
+}
+
+}  // namespace ch

@@ -1,0 +1,142 @@
+// physics.cuh -- per-ion device physics shared by the FP64 and mixed forms:
+// Boris rotation, mean relative speed, Philox ion-neutral collision.
+#pragma once
+
+#include "common.cuh"
+
+template <typename R> __device__ __forceinline__ R unitR(uint32_t r);
+template <> __device__ __forceinline__ double unitR<double>(uint32_t r) { return ch_unit(r); }
+template <> __device__ __forceinline__ float unitR<float>(uint32_t r) { return ch_unitf(r); }
+
+__device__ __forceinline__ double ch_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float ch_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double ch_log(double x) { return log(x); }
+__device__ __forceinline__ float ch_log(float x) { return logf(x); }
+__device__ __forceinline__ double ch_exp(double x) { return exp(x); }
+__device__ __forceinline__ float ch_exp(float x) { return expf(x); }
+__device__ __forceinline__ double ch_erf(double x) { return erf(x); }
+__device__ __forceinline__ float ch_erf(float x) { return erff(x); }
+__device__ __forceinline__ void ch_sincos2pi(double u, double* s, double* c) { sincos(2.0 * CH_PI * u, s, c); }
+__device__ __forceinline__ void ch_sincos2pi(float u, float* s, float* c) { sincospif(2.0f * u, s, c); }
+
+// E|w - V| for |w - vn0| = w and V Maxwellian with per-component std sigma:
+// sigma sqrt(2/pi) exp(-a^2) + (w + sigma^2/w) erf(a), a = w/(sigma sqrt 2);
+// series 2 sigma sqrt(2/pi)(1 + a^2/3) for small a.
+template <typename R>
+__device__ __forceinline__ R ch_gmean(R w, R sigma) {
+  if (!(sigma > R(0))) return w;
+  const R a = w / (sigma * R(1.4142135623730951));
+  const R c = sigma * R(0.7978845608028654);
+  if (a < R(1e-4)) return R(2) * c * (R(1) + a * a / R(3));
+  return c * ch_exp(-a * a) + (w + sigma * sigma / w) * ch_erf(a);
+}
+
+template <typename R>
+__device__ __forceinline__ R ch_neutral_density(const StepConsts& c, R x_abs) {
+  if (c.nn_profile != CH_NN_GAUSSIAN_X) return R(1);
+  const R u = (x_abs - R(c.nn_center)) / R(c.nn_sigma);
+  const R v = ch_exp(R(-0.5) * u * u);
+  return v > R(c.nn_floor) ? v : R(c.nn_floor);
+}
+
+// Boris push (src/particles.c:374-447), E already includes the push scale.
+template <typename R>
+__device__ __forceinline__ void ch_boris(const StepConsts& c, const R E[3], R v[3]) {
+  const R ts = R(c.tscale);
+  R vm0 = v[0] + ts * E[0], vm1 = v[1] + ts * E[1], vm2 = v[2] + ts * E[2];
+  R vp0, vp1, vp2;
+  if (c.faithful & CH_FAITHFUL_D2) {
+    vp0 = vm0; vp1 = vm1; vp2 = vm2;
+  } else {
+    const R t0 = R(c.t[0]), t1 = R(c.t[1]), t2 = R(c.t[2]);
+    const R s0 = R(c.s[0]), s1 = R(c.s[1]), s2 = R(c.s[2]);
+    const R q0 = vm0 + (vm1 * t2 - vm2 * t1);
+    const R q1 = vm1 + (vm2 * t0 - vm0 * t2);
+    const R q2 = vm2 + (vm0 * t1 - vm1 * t0);
+    vp0 = vm0 + (q1 * s2 - q2 * s1);
+    vp1 = vm1 + (q2 * s0 - q0 * s2);
+    vp2 = vm2 + (q0 * s1 - q1 * s0);
+  }
+  v[0] = vp0 + ts * E[0];
+  v[1] = vp1 + ts * E[1];
+  v[2] = vp2 + ts * E[2];
+}
+
+// Ion-neutral collision of one ion with probability pcol.
+// Returns 1 collided, 0 no collision, -1 refused (|v_f| > 10 vT or the
+// neutral sampler ran out of its 64 proposals).
+template <typename R>
+__device__ __noinline__ int ch_collide(const StepConsts& c, uint32_t id, R pcol, R v[3]) {
+  const U4 r0 = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | 0u, c.run, c.seed_lo, c.seed_hi);
+  if (!(unitR<R>(r0.x) < pcol)) return 0;
+  const R sig = R(c.vnT);
+  const R vn0x = R(c.vn0[0]), vn0y = R(c.vn0[1]), vn0z = R(c.vn0[2]);
+  const R vix = v[0], viy = v[1], viz = v[2];
+  const R wx = vix - vn0x, wy = viy - vn0y, wz = viz - vn0z;
+  const R w = ch_sqrt(wx * wx + wy * wy + wz * wz);
+  const R m1 = R(c.m1);
+  R Vx = 0, Vy = 0, Vz = 0, uz = 0, uphi = 0;
+  bool ok = false;
+  for (int it = 0; it < 64 && !ok; ++it) {
+    const U4 a = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (uint32_t)(1 + 2 * it), c.run, c.seed_lo,
+                           c.seed_hi);
+    const U4 b = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (uint32_t)(2 + 2 * it), c.run, c.seed_lo,
+                           c.seed_hi);
+    R nx, ny, nz;
+    if (unitR<R>(a.x) * (w + m1) < w) {
+      // plain Maxwellian proposal, Box-Muller
+      R s1, c1, s2, c2;
+      const R r1 = ch_sqrt(R(-2) * ch_log(unitR<R>(a.y)));
+      ch_sincos2pi(unitR<R>(a.z), &s1, &c1);
+      const R r2 = ch_sqrt(R(-2) * ch_log(unitR<R>(a.w)));
+      ch_sincos2pi(unitR<R>(b.x), &s2, &c2);
+      nx = sig * (r1 * c1); ny = sig * (r1 * s1); nz = sig * (r2 * c2);
+    } else {
+      // speed-biased proposal: |V - vn0|^2 / (2 sigma^2) ~ Gamma(2, 1)
+      const R s = sig * ch_sqrt(R(-2) * ch_log(unitR<R>(a.y) * unitR<R>(a.z)));
+      const R ct = R(2) * unitR<R>(a.w) - R(1);
+      R st = R(1) - ct * ct;
+      st = ch_sqrt(st > R(0) ? st : R(0));
+      R sp, cp;
+      ch_sincos2pi(unitR<R>(b.x), &sp, &cp);
+      nx = s * st * cp; ny = s * st * sp; nz = s * ct;
+    }
+    Vx = vn0x + nx; Vy = vn0y + ny; Vz = vn0z + nz;
+    const R dV = ch_sqrt(nx * nx + ny * ny + nz * nz);
+    const R rx = vix - Vx, ry = viy - Vy, rz = viz - Vz;
+    const R D = ch_sqrt(rx * rx + ry * ry + rz * rz);
+    if (unitR<R>(b.y) * (w + dV) < D) {
+      ok = true;
+      uz = R(2) * unitR<R>(b.z) - R(1);
+      uphi = unitR<R>(b.w);
+    }
+  }
+  if (!ok) return -1;
+  // centre-of-mass scatter (src/particles.c:552-591)
+  const R mi = R(c.mi), mn = R(c.mn), M = mn + mi;
+  const R vrx = vix - Vx, vry = viy - Vy, vrz = viz - Vz;
+  const R vrr = ch_sqrt(vrx * vrx + vry * vry + vrz * vrz);
+  const R vcx = (vix * mi + Vx * mn) / M, vcy = (viy * mi + Vy * mn) / M, vcz = (viz * mi + Vz * mn) / M;
+  const R ax = vix - vcx, ay = viy - vcy, az = viz - vcz;
+  const R vcr = ch_sqrt(ax * ax + ay * ay + az * az);
+  R up = R(1) - uz * uz;
+  const R uperp = ch_sqrt(up > R(0) ? up : R(0));
+  R sph, cph;
+  ch_sincos2pi(uphi, &sph, &cph);
+  const R ux = uperp * cph, uy = uperp * sph;
+  const R costht = vrr > R(0) ? vrz / vrr : R(1);
+  R st2 = R(1) - costht * costht;
+  const R sintht = ch_sqrt(st2 > R(0) ? st2 : R(0));
+  R cosphi = R(1), sinphi = R(0);
+  if (vrr * sintht > R(0)) {
+    cosphi = vrx / (vrr * sintht);
+    sinphi = vry / (vrr * sintht);
+  }
+  const R ux1 = uz * sintht + ux * costht, uy1 = uy, uz1 = uz * costht - ux * sintht;
+  const R ux2 = ux1 * cosphi - uy1 * sinphi, uy2 = ux1 * sinphi + uy1 * cosphi, uz2 = uz1;
+  const R vfx = vcx + vcr * ux2, vfy = vcy + vcr * uy2, vfz = vcz + vcr * uz2;
+  const R vfr = ch_sqrt(vfx * vfx + vfy * vfy + vfz * vfz);
+  if (vfr / R(c.viTr) > R(10)) return -1;
+  v[0] = vfx; v[1] = vfy; v[2] = vfz;
+  return 1;
+}

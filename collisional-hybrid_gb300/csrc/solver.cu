@@ -1,0 +1,691 @@
+// solver.cu -- matrix-free 19-point potential solve on sm_103a.
+//
+// The operator is ComputeFullLHS (src/lhs.c:350-543) applied without ever
+// assembling it: each row's 19 values are rebuilt on the fly from the
+// density at the node and its six face neighbours, so one application reads
+// x and n once and writes y once.  ComputeLaplacianLHS (:168-347) and
+// ComputeIdentityLHS (:144) are selectable.  The RHS is ComputeFullRHS
+// (src/rhs.c:133-303) with its null-space removal.  Krylov drivers: CG for
+// the symmetric (kappa_e = 0) operator, BiCGStab otherwise, Jacobi
+// preconditioned, constant null space projected out of b and phi; the
+// mixed form runs the Krylov iterations in FP32 inside an FP64 iterative
+// refinement of phi.  Reductions use fixed block partials summed in fixed
+// order, so every solve is deterministic.
+#include <math.h>
+#include <string.h>
+
+#include "solver.cuh"
+
+namespace ch {
+
+OpCoefs op_coefs(const ch_params& p, const GridDesc& g) {
+  OpCoefs c;
+  memset(&c, 0, sizeof(c));
+  c.type = p.lhs_type;
+  if (p.lhs_type == CH_LHS_LAPLACIAN) {
+    // src/lhs.c:204-218 (finite-volume scaled)
+    c.sxx = g.dy * g.dz / g.dx;
+    c.syy = g.dx * g.dz / g.dy;
+    c.szz = g.dx * g.dy / g.dz;
+    return c;
+  }
+  const double Kx = p.kappa_e[0], Ky = p.kappa_e[1], Kz = p.kappa_e[2];
+  const double det = 1 + Kx * Kx + Ky * Ky + Kz * Kz;
+  const double rxx = 1 + Kx * Kx, rxy = Ky * Kx - Kz, rxz = Kz * Kx + Ky;
+  const double ryx = Kx * Ky + Kz, ryy = 1 + Ky * Ky, ryz = Kz * Ky - Kx;
+  const double rzx = Kx * Kz - Ky, rzy = Ky * Kz + Kx, rzz = 1 + Kz * Kz;
+  const double hxx = 1.0 / (2.0 * g.dx * g.dx), hyy = 1.0 / (2.0 * g.dy * g.dy), hzz = 1.0 / (2.0 * g.dz * g.dz);
+  const double hxy = 1.0 / (8.0 * g.dy * g.dx), hxz = 1.0 / (8.0 * g.dz * g.dx), hyz = 1.0 / (8.0 * g.dy * g.dz);
+  const double scale = 1.0 / det;
+  c.sxx = scale * rxx * hxx; c.syy = scale * ryy * hyy; c.szz = scale * rzz * hzz;
+  c.sxy = scale * rxy * hxy; c.sxz = scale * rxz * hxz; c.syz = scale * ryz * hyz;
+  c.syx = scale * ryx * hxy; c.szx = scale * rzx * hxz; c.szy = scale * rzy * hyz;
+  return c;
+}
+
+// ------------------------------------------------------------------ device helpers
+struct Nb {
+  int64_t c, e, w, n, s, u, d;       // centre and faces (x+, x-, y+, y-, z+, z-)
+  int64_t en, es, wn, ws, eu, ed, wu, wd, nu, nd, su, sd;  // 12 edges
+};
+
+__device__ __forceinline__ Nb neighbours(const GridDesc& g, int64_t c) {
+  const int i = (int)(c % g.Nx);
+  const int j = (int)((c / g.Nx) % g.Ny);
+  const int k = (int)(c / ((int64_t)g.Nx * g.Ny));
+  const int ip = i + 1 == g.Nx ? 0 : i + 1, im = i == 0 ? g.Nx - 1 : i - 1;
+  const int jp = j + 1 == g.Ny ? 0 : j + 1, jm = j == 0 ? g.Ny - 1 : j - 1;
+  const int kp = k + 1 == g.Nz ? 0 : k + 1, km = k == 0 ? g.Nz - 1 : k - 1;
+  const int64_t X = g.Nx, XY = (int64_t)g.Nx * g.Ny;
+  const int64_t r0 = k * XY, rp = kp * XY, rm = km * XY;
+  const int64_t y0 = j * X, yp = jp * X, ym = jm * X;
+  Nb b;
+  b.c = r0 + y0 + i;
+  b.e = r0 + y0 + ip; b.w = r0 + y0 + im;
+  b.n = r0 + yp + i;  b.s = r0 + ym + i;
+  b.u = rp + y0 + i;  b.d = rm + y0 + i;
+  b.en = r0 + yp + ip; b.es = r0 + ym + ip; b.wn = r0 + yp + im; b.ws = r0 + ym + im;
+  b.eu = rp + y0 + ip; b.ed = rm + y0 + ip; b.wu = rp + y0 + im; b.wd = rm + y0 + im;
+  b.nu = rp + yp + i;  b.nd = rm + yp + i;  b.su = rp + ym + i;  b.sd = rm + ym + i;
+  return b;
+}
+
+template <typename T>
+struct DevCoefs {
+  T sxx, syy, szz, sxy, sxz, syz, syx, szx, szy;
+  int type;
+  int cross;
+};
+
+template <typename T>
+DevCoefs<T> dev_coefs(const OpCoefs& c) {
+  DevCoefs<T> d;
+  d.sxx = (T)c.sxx; d.syy = (T)c.syy; d.szz = (T)c.szz;
+  d.sxy = (T)c.sxy; d.sxz = (T)c.sxz; d.syz = (T)c.syz;
+  d.syx = (T)c.syx; d.szx = (T)c.szx; d.szy = (T)c.szy;
+  d.type = c.type;
+  d.cross = (c.sxy != 0 || c.sxz != 0 || c.syz != 0 || c.syx != 0 || c.szx != 0 || c.szy != 0);
+  return d;
+}
+
+// One row of A(n) x.  Values follow src/lhs.c:488-511 (f[...] assignments)
+// and src/lhs.c:7-106 (stencil order).
+template <typename T>
+__device__ __forceinline__ T apply_row(const DevCoefs<T>& C, const T* __restrict__ n, const T* __restrict__ x,
+                                       const Nb& b) {
+  if (C.type == CH_LHS_IDENTITY) return x[b.c];
+  const T xc = x[b.c];
+  if (C.type == CH_LHS_LAPLACIAN)
+    return C.sxx * (x[b.e] + x[b.w]) + C.syy * (x[b.n] + x[b.s]) + C.szz * (x[b.u] + x[b.d]) -
+           T(2) * (C.sxx + C.syy + C.szz) * xc;
+  const T nijk = n[b.c], npjk = n[b.e], nmjk = n[b.w], nipk = n[b.n], nimk = n[b.s], nijp = n[b.u], nijm = n[b.d];
+  // star terms: sum of f_face (x_face - x_c) over the six faces reproduces
+  // the diagonal value -(sum of the star values) exactly in exact arithmetic
+  T acc = C.sxx * ((npjk + nijk) * (x[b.e] - xc) + (nijk + nmjk) * (x[b.w] - xc)) +
+          C.syy * ((nipk + nijk) * (x[b.n] - xc) + (nijk + nimk) * (x[b.s] - xc)) +
+          C.szz * ((nijp + nijk) * (x[b.u] - xc) + (nijk + nijm) * (x[b.d] - xc));
+  if (C.cross) {
+    const T sxy = C.sxy, sxz = C.sxz, syz = C.syz, syx = C.syx, szx = C.szx, szy = C.szy;
+    // cross parts of the six star values
+    acc += (syx * (nipk - nimk) + szx * (nijp - nijm)) * (x[b.e] - x[b.w]);
+    acc += (sxy * (npjk - nmjk) + szy * (nijp - nijm)) * (x[b.n] - x[b.s]);
+    acc += (sxz * (npjk - nmjk) + syz * (nipk - nimk)) * (x[b.u] - x[b.d]);
+    // x-y corners
+    acc += (sxy * (npjk + nijk) + syx * (nipk + nijk)) * x[b.en];
+    acc += (-sxy * (npjk + nijk) - syx * (nijk + nimk)) * x[b.es];
+    acc += (-sxy * (nijk + nmjk) - syx * (nipk + nijk)) * x[b.wn];
+    acc += (sxy * (nijk + nmjk) + syx * (nijk + nimk)) * x[b.ws];
+    // x-z corners
+    acc += (sxz * (npjk + nijk) + szx * (nijp + nijk)) * x[b.eu];
+    acc += (-sxz * (npjk + nijk) - szx * (nijk + nijm)) * x[b.ed];
+    acc += (-sxz * (nijk + nmjk) - szx * (nijp + nijk)) * x[b.wu];
+    acc += (sxz * (nijk + nmjk) + szx * (nijk + nijm)) * x[b.wd];
+    // y-z corners
+    acc += (syz * (nipk + nijk) + szy * (nijp + nijk)) * x[b.nu];
+    acc += (-syz * (nipk + nijk) - szy * (nijk + nijm)) * x[b.nd];
+    acc += (-syz * (nijk + nimk) - szy * (nijp + nijk)) * x[b.su];
+    acc += (syz * (nijk + nimk) + szy * (nijk + nijm)) * x[b.sd];
+  }
+  return acc;
+}
+
+template <typename T>
+__device__ __forceinline__ T diag_row(const DevCoefs<T>& C, const T* __restrict__ n, const Nb& b) {
+  if (C.type == CH_LHS_IDENTITY) return T(1);
+  if (C.type == CH_LHS_LAPLACIAN) return -T(2) * (C.sxx + C.syy + C.szz);
+  const T nijk = n[b.c];
+  return -(C.sxx * (n[b.e] + T(2) * nijk + n[b.w]) + C.syy * (n[b.n] + T(2) * nijk + n[b.s]) +
+           C.szz * (n[b.u] + T(2) * nijk + n[b.d]));
+}
+
+// Block partial sums of K doubles (fixed order).
+template <int K>
+__device__ __forceinline__ void partials(double (&v)[K], double* __restrict__ part) {
+  __shared__ double sm[K][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    double x = v[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sm[q][wid] = x;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      double x = lane < nw ? sm[q][lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0) part[(size_t)blockIdx.x * K + q] = x;
+    }
+  }
+}
+
+#define GRID_LOOP(c, N) for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < (N); c += (int64_t)gridDim.x * blockDim.x)
+
+// ------------------------------------------------------------------ kernels
+// y = A x; partial w.y (w may be null).
+template <typename T>
+__global__ void __launch_bounds__(256) k_apply(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
+                                               const T* __restrict__ x, T* __restrict__ y, const T* __restrict__ w,
+                                               double* part) {
+  double d[1] = {0.0};
+  GRID_LOOP(c, g.N) {
+    const Nb b = neighbours(g, c);
+    const T v = apply_row<T>(C, n, x, b);
+    y[c] = v;
+    if (w) d[0] += (double)w[c] * (double)v;
+  }
+  if (part) partials<1>(d, part);
+}
+
+// t = A x; partials (t.s, t.t).
+template <typename T>
+__global__ void __launch_bounds__(256) k_apply_dot2(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
+                                                    const T* __restrict__ x, T* __restrict__ t,
+                                                    const T* __restrict__ s, double* part) {
+  double d[2] = {0.0, 0.0};
+  GRID_LOOP(c, g.N) {
+    const Nb b = neighbours(g, c);
+    const T v = apply_row<T>(C, n, x, b);
+    t[c] = v;
+    d[0] += (double)v * (double)s[c];
+    d[1] += (double)v * (double)v;
+  }
+  partials<2>(d, part);
+}
+
+// r = b - A x; partial r.r
+template <typename T>
+__global__ void __launch_bounds__(256) k_residual(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
+                                                  const T* __restrict__ b, const T* __restrict__ x,
+                                                  T* __restrict__ r, double* part) {
+  double d[1] = {0.0};
+  GRID_LOOP(c, g.N) {
+    const Nb nb = neighbours(g, c);
+    const T v = b[c] - apply_row<T>(C, n, x, nb);
+    r[c] = v;
+    d[0] += (double)v * (double)v;
+  }
+  partials<1>(d, part);
+}
+
+template <typename T>
+__global__ void k_jacobi(GridDesc g, DevCoefs<T> C, const T* __restrict__ n, T* __restrict__ dinv, int jacobi) {
+  GRID_LOOP(c, g.N) {
+    const T d = jacobi ? diag_row<T>(C, n, neighbours(g, c)) : T(1);
+    dinv[c] = d != T(0) ? T(1) / d : T(1);
+  }
+}
+
+// z = dinv r; partials (r.z, r.r)
+template <typename T>
+__global__ void k_prec_dot(int64_t N, const T* __restrict__ dinv, const T* __restrict__ r, T* __restrict__ z,
+                           double* part) {
+  double d[2] = {0.0, 0.0};
+  GRID_LOOP(c, N) {
+    const T rv = r[c];
+    const T zv = dinv[c] * rv;
+    z[c] = zv;
+    d[0] += (double)rv * (double)zv;
+    d[1] += (double)rv * (double)rv;
+  }
+  partials<2>(d, part);
+}
+
+// scalar slots
+enum {
+  S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_RHO, S_OMEGA, S_TS, S_TT, S_RV, S_SS, S_RR0, S_MEAN, S_TMP, S_NSLOT
+};
+enum { OP_SET_RZ_RR = 0, OP_CG_ALPHA, OP_CG_BETA, OP_RR, OP_BI_ALPHA, OP_BI_OMEGA, OP_BI_BETA, OP_SS, OP_MEAN, OP_TMP };
+
+// Fixed-order reduction of K partials and the scalar update of one step.
+__global__ void k_scalar(const double* __restrict__ part, int nb, int K, int op, double* scal, double invN) {
+  __shared__ double sm[3][32];
+  __shared__ double red[3];
+  for (int q = 0; q < K; ++q) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += part[(size_t)b * K + q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sm[q][threadIdx.x >> 5] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    for (int q = 0; q < K; ++q) {
+      double t = threadIdx.x < (blockDim.x >> 5) ? sm[q][threadIdx.x] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      if (threadIdx.x == 0) red[q] = t;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  switch (op) {
+    case OP_SET_RZ_RR: scal[S_RZ] = red[0]; scal[S_RR] = red[1]; break;
+    case OP_CG_ALPHA: scal[S_PQ] = red[0]; scal[S_ALPHA] = red[0] != 0.0 ? scal[S_RZ] / red[0] : 0.0; break;
+    case OP_CG_BETA:
+      scal[S_BETA] = scal[S_RZ] != 0.0 ? red[0] / scal[S_RZ] : 0.0;
+      scal[S_RZ] = red[0];
+      scal[S_RR] = red[1];
+      break;
+    case OP_RR: scal[S_RR] = red[0]; break;
+    case OP_BI_ALPHA: scal[S_RV] = red[0]; scal[S_ALPHA] = red[0] != 0.0 ? scal[S_RHO] / red[0] : 0.0; break;
+    case OP_SS: scal[S_SS] = red[0]; break;
+    case OP_BI_OMEGA:
+      scal[S_TS] = red[0]; scal[S_TT] = red[1];
+      scal[S_OMEGA] = red[1] != 0.0 ? red[0] / red[1] : 0.0;
+      break;
+    case OP_BI_BETA: {
+      // red[0] = r.r, red[1] = rh.r (rho new)
+      scal[S_RR] = red[0];
+      const double rho1 = red[1];
+      scal[S_BETA] = (scal[S_RHO] != 0.0 && scal[S_OMEGA] != 0.0)
+                         ? (rho1 / scal[S_RHO]) * (scal[S_ALPHA] / scal[S_OMEGA]) : 0.0;
+      scal[S_RHO] = rho1;
+      break;
+    }
+    case OP_MEAN: scal[S_MEAN] = red[0] * invN; break;
+    case OP_TMP: scal[S_TMP] = red[0]; break;
+  }
+}
+
+// CG: x += a p; r -= a q; z = dinv r; partials (r.z, r.r)
+template <typename T>
+__global__ void k_cg_xr(int64_t N, const double* __restrict__ scal, T* __restrict__ x, T* __restrict__ r,
+                        const T* __restrict__ p, const T* __restrict__ q, const T* __restrict__ dinv,
+                        T* __restrict__ z, double* part) {
+  const T a = (T)scal[S_ALPHA];
+  double d[2] = {0.0, 0.0};
+  GRID_LOOP(c, N) {
+    x[c] += a * p[c];
+    const T rv = r[c] - a * q[c];
+    r[c] = rv;
+    const T zv = dinv[c] * rv;
+    z[c] = zv;
+    d[0] += (double)rv * (double)zv;
+    d[1] += (double)rv * (double)rv;
+  }
+  partials<2>(d, part);
+}
+
+template <typename T>
+__global__ void k_cg_p(int64_t N, const double* __restrict__ scal, const T* __restrict__ z, T* __restrict__ p,
+                       int first) {
+  const T b = first ? T(0) : (T)scal[S_BETA];
+  GRID_LOOP(c, N) p[c] = z[c] + b * p[c];
+}
+
+// BiCGStab: p = r + beta (p - omega v); y = dinv p
+template <typename T>
+__global__ void k_bi_p(int64_t N, const double* __restrict__ scal, const T* __restrict__ r, T* __restrict__ p,
+                       const T* __restrict__ v, const T* __restrict__ dinv, T* __restrict__ y, int first) {
+  const T b = first ? T(0) : (T)scal[S_BETA], w = first ? T(0) : (T)scal[S_OMEGA];
+  GRID_LOOP(c, N) {
+    const T pv = r[c] + b * (p[c] - w * v[c]);
+    p[c] = pv;
+    y[c] = dinv[c] * pv;
+  }
+}
+
+// s = r - alpha v; sh = dinv s; partial s.s
+template <typename T>
+__global__ void k_bi_s(int64_t N, const double* __restrict__ scal, const T* __restrict__ r, const T* __restrict__ v,
+                       const T* __restrict__ dinv, T* __restrict__ s, T* __restrict__ sh, double* part) {
+  const T a = (T)scal[S_ALPHA];
+  double d[1] = {0.0};
+  GRID_LOOP(c, N) {
+    const T sv = r[c] - a * v[c];
+    s[c] = sv;
+    sh[c] = dinv[c] * sv;
+    d[0] += (double)sv * (double)sv;
+  }
+  partials<1>(d, part);
+}
+
+// x += alpha y + omega sh; r = s - omega t; partials (r.r, rh.r)
+template <typename T>
+__global__ void k_bi_xr(int64_t N, const double* __restrict__ scal, T* __restrict__ x, const T* __restrict__ y,
+                        const T* __restrict__ sh, T* __restrict__ r, const T* __restrict__ s, const T* __restrict__ t,
+                        const T* __restrict__ rh, double* part) {
+  const T a = (T)scal[S_ALPHA], w = (T)scal[S_OMEGA];
+  double d[2] = {0.0, 0.0};
+  GRID_LOOP(c, N) {
+    x[c] += a * y[c] + w * sh[c];
+    const T rv = s[c] - w * t[c];
+    r[c] = rv;
+    d[0] += (double)rv * (double)rv;
+    d[1] += (double)rh[c] * (double)rv;
+  }
+  partials<2>(d, part);
+}
+
+// x += alpha y (early exit of BiCGStab when |s| is small); r = s
+template <typename T>
+__global__ void k_bi_half(int64_t N, const double* __restrict__ scal, T* __restrict__ x, const T* __restrict__ y,
+                          T* __restrict__ r, const T* __restrict__ s) {
+  const T a = (T)scal[S_ALPHA];
+  GRID_LOOP(c, N) {
+    x[c] += a * y[c];
+    r[c] = s[c];
+  }
+}
+
+template <typename T>
+__global__ void k_copy(int64_t N, const T* __restrict__ a, T* __restrict__ b) { GRID_LOOP(c, N) b[c] = a[c]; }
+template <typename T>
+__global__ void k_zero(int64_t N, T* __restrict__ a) { GRID_LOOP(c, N) a[c] = T(0); }
+
+template <typename T>
+__global__ void k_sum(int64_t N, const T* __restrict__ a, double* part) {
+  double d[1] = {0.0};
+  GRID_LOOP(c, N) d[0] += (double)a[c];
+  partials<1>(d, part);
+}
+__global__ void k_sub_mean(int64_t N, double* __restrict__ a, const double* __restrict__ scal) {
+  const double m = scal[S_MEAN];
+  GRID_LOOP(c, N) a[c] -= m;
+}
+template <typename T>
+__global__ void k_dot(int64_t N, const T* __restrict__ a, const T* __restrict__ b, double* part) {
+  double d[1] = {0.0};
+  GRID_LOOP(c, N) d[0] += (double)a[c] * (double)b[c];
+  partials<1>(d, part);
+}
+__global__ void k_dot64(int64_t N, const double* __restrict__ a, const double* __restrict__ b, double* part) {
+  double d[1] = {0.0};
+  GRID_LOOP(c, N) d[0] += a[c] * b[c];
+  partials<1>(d, part);
+}
+// r32 = (float)(r64 * s)
+__global__ void k_down(int64_t N, const double* __restrict__ a, double s, float* __restrict__ b) {
+  GRID_LOOP(c, N) b[c] = (float)(a[c] * s);
+}
+// x64 += (double)x32 * s
+__global__ void k_up_add(int64_t N, const float* __restrict__ a, double s, double* __restrict__ x) {
+  GRID_LOOP(c, N) x[c] += (double)a[c] * s;
+}
+
+// ComputeFullRHS (src/rhs.c:244-283) with the FD helpers of src/calculus.c;
+// ComputeConstantRHS / ComputeSinusoidalRHS for the other --rhs-type values.
+__global__ void k_rhs(GridDesc g, int rhs_type, double R00, double R01, double R02, double R10, double R11,
+                      double R12, double R20, double R21, double R22, double det, double E0x, double E0y, double E0z,
+                      double cth, double cG, int d8, const double* __restrict__ mom, const double* __restrict__ scal,
+                      double* __restrict__ b) {
+  const int64_t N = g.N;
+  const double* n = mom;
+  const double* Gx = mom + N;
+  const double* Gy = mom + 2 * N;
+  const double* Gz = mom + 3 * N;
+  GRID_LOOP(c, N) {
+    if (rhs_type == CH_RHS_CONSTANT) {
+      b[c] = scal[S_MEAN] * (2.0 * g.dx * g.dy * g.dz / det);
+      continue;
+    }
+    const int i = (int)(c % g.Nx), j = (int)((c / g.Nx) % g.Ny), k = (int)(c / ((int64_t)g.Nx * g.Ny));
+    if (rhs_type == CH_RHS_SINUSOIDAL) {
+      const double x = ((double)i + 0.5) * g.dx, y = ((double)j + 0.5) * g.dy, z = ((double)k + 0.5) * g.dz;
+      const double val = cos(2 * CH_PI * x) * cos(2 * CH_PI * y) * cos(2 * CH_PI * z);
+      b[c] = scal[S_MEAN] * val * (2.0 * g.dx * g.dy * g.dz / det);
+      continue;
+    }
+    const Nb q = neighbours(g, c);
+    const double dx = g.dx, dy = g.dy, dz = g.dz;
+    const double dndx = (n[q.e] - n[q.w]) / (2.0 * dx);
+    const double dndy = (n[q.n] - n[q.s]) / (2.0 * dy);
+    const double dndz = (n[q.u] - n[q.d]) / (2.0 * dz);
+    const double dGxdx = (Gx[q.e] - Gx[q.w]) / (2.0 * dx);
+    const double dGydy = (Gy[q.n] - Gy[q.s]) / (2.0 * dy);
+    const double dGzdz = (Gz[q.u] - Gz[q.d]) / (2.0 * dz);
+    const double d2ndxx = (n[q.e] - 2.0 * n[q.c] + n[q.w]) / (dx * dx);
+    const double d2ndyy = (n[q.n] - 2.0 * n[q.c] + n[q.s]) / (dy * dy);
+    const double d2ndzz = (n[q.u] - 2.0 * n[q.c] + n[q.d]) / (dz * dz);
+    const double d2ndxy = (n[q.en] - n[q.wn] - n[q.es] + n[q.ws]) / (4.0 * dx * dy);
+    const double d2ndxz = (n[q.eu] - n[q.wu] - n[q.ed] + n[q.wd]) / (4.0 * dx * dz);
+    const double vyz = d8 ? (n[q.eu] - n[q.wu] - n[q.ed] + n[q.wd]) : (n[q.nu] - n[q.su] - n[q.nd] + n[q.sd]);
+    const double d2ndyz = vyz / (4.0 * dy * dz);
+    const double Eterm = (R00 * E0x + R01 * E0y + R02 * E0z) * dndx + (R10 * E0x + R11 * E0y + R12 * E0z) * dndy +
+                         (R20 * E0x + R21 * E0y + R22 * E0z) * dndz;
+    const double Pterm = cth * (R00 * d2ndxx + R01 * d2ndxy + R02 * d2ndxz + R10 * d2ndxy + R11 * d2ndyy +
+                                R12 * d2ndyz + R20 * d2ndxz + R21 * d2ndyz + R22 * d2ndzz);
+    const double Gterm = det * cG * (dGxdx + dGydy + dGzdz);
+    b[c] = (1.0 / det) * (Eterm + Pterm + Gterm);
+  }
+}
+
+// ------------------------------------------------------------------ host side
+static int grid_n(int64_t n, int sms) {
+  int64_t need = (n + 255) / 256;
+  int64_t cap = (int64_t)sms * 4;
+  return (int)(need < cap ? (need < 1 ? 1 : need) : cap);
+}
+
+ch_status PotentialSolver::init(const ch_params& p, const GridDesc& g, int sms) {
+  p_ = p;
+  g_ = g;
+  c_ = op_coefs(p, g);
+  sms_ = sms;
+  N_ = g.N;
+  nb_ = grid_n(N_, sms);
+  const size_t b64 = sizeof(double) * N_;
+  double** v64[] = {&r_, &z_, &pd_, &q_, &rh_, &s_, &t_, &sh_, &dinv_};
+  for (double** v : v64) CH_CUDA_OK(cudaMalloc(v, b64));
+  if (p.precision == CH_MIXED) {
+    const size_t b32 = sizeof(float) * N_;
+    float** v32[] = {&n32_, &b32_, &x32_, &r32_, &z32_, &p32_, &q32_, &rh32_, &s32_, &t32_, &sh32_, &dinv32_};
+    for (float** v : v32) CH_CUDA_OK(cudaMalloc(v, b32));
+  }
+  CH_CUDA_OK(cudaMalloc(&part_, sizeof(double) * 4 * nb_));
+  CH_CUDA_OK(cudaMalloc(&scal_, sizeof(double) * S_NSLOT));
+  CH_CUDA_OK(cudaMemset(scal_, 0, sizeof(double) * S_NSLOT));
+  CH_CUDA_OK(cudaMallocHost(&hscal_, sizeof(double) * S_NSLOT));
+  return CH_OK;
+}
+
+void PotentialSolver::release() {
+  void* all[] = {r_, z_, pd_, q_, rh_, s_, t_, sh_, dinv_, n32_, b32_, x32_, r32_, z32_, p32_, q32_, rh32_,
+                 s32_, t32_, sh32_, dinv32_, part_, scal_};
+  for (void* v : all)
+    if (v) cudaFree(v);
+  if (hscal_) cudaFreeHost(hscal_);
+  r_ = z_ = pd_ = q_ = rh_ = s_ = t_ = sh_ = dinv_ = nullptr;
+  n32_ = b32_ = x32_ = r32_ = z32_ = p32_ = q32_ = rh32_ = s32_ = t32_ = sh32_ = dinv32_ = nullptr;
+  part_ = scal_ = hscal_ = nullptr;
+}
+
+double PotentialSolver::dot64(const double* a, const double* b, cudaStream_t s) {
+  k_dot64<<<nb_, 256, 0, s>>>(N_, a, b, part_);
+  k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_RR, scal_, 0.0);
+  cudaMemcpyAsync(hscal_, scal_, sizeof(double) * S_NSLOT, cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  return hscal_[S_RR];
+}
+
+void PotentialSolver::remove_mean64(double* v, cudaStream_t s) {
+  k_sum<double><<<nb_, 256, 0, s>>>(N_, v, part_);
+  k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_MEAN, scal_, 1.0 / (double)N_);
+  k_sub_mean<<<nb_, 256, 0, s>>>(N_, v, scal_);
+}
+
+void PotentialSolver::build_rhs(const double* mom, double* b, cudaStream_t s) {
+  const double Kx = p_.kappa_e[0], Ky = p_.kappa_e[1], Kz = p_.kappa_e[2];
+  const double det = 1 + Kx * Kx + Ky * Ky + Kz * Kz;
+  const double R00 = 1 + Kx * Kx, R01 = Ky * Kx - Kz, R02 = Kz * Kx + Ky;
+  const double R10 = Kx * Ky + Kz, R11 = 1 + Ky * Ky, R12 = Kz * Ky - Kx;
+  const double R20 = Kx * Kz - Ky, R21 = Ky * Kz + Kx, R22 = 1 + Kz * Kz;
+  if (p_.rhs_type != CH_RHS_FULL) {
+    // mean density (VecMean, src/rhs.c:34,93)
+    k_sum<double><<<nb_, 256, 0, s>>>(N_, mom, part_);
+    k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_MEAN, scal_, 1.0 / (double)N_);
+  }
+  k_rhs<<<nb_, 256, 0, s>>>(g_, p_.rhs_type, R00, R01, R02, R10, R11, R12, R20, R21, R22, det, p_.E0[0], p_.E0[1],
+                            p_.E0[2], p_.cth, p_.cG, (p_.faithful & CH_FAITHFUL_D8) != 0, mom, scal_, b);
+  if (p_.rhs_type != CH_RHS_CONSTANT) remove_mean64(b, s);  // MatNullSpaceRemove (src/rhs.c:294-296)
+}
+
+void PotentialSolver::apply64(const double* n, const double* x, double* y, cudaStream_t s) {
+  k_apply<double><<<nb_, 256, 0, s>>>(g_, dev_coefs<double>(c_), n, x, y, nullptr, nullptr);
+}
+
+// Preconditioned Krylov solve of A x = b in precision T (x holds the start).
+// Converged when ||r||_2 <= rtol ||b||_2 (recurrence residual).
+template <typename T>
+ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* x, double rtol, int maxit,
+                                  bool zero_guess, int* its, double* rnorm_out, cudaStream_t s) {
+  const DevCoefs<T> C = dev_coefs<T>(c_);
+  const int64_t N = g.N;
+  const bool f64 = sizeof(T) == 8;
+  T* r = f64 ? (T*)r_ : (T*)r32_;
+  T* z = f64 ? (T*)z_ : (T*)z32_;
+  T* pp = f64 ? (T*)pd_ : (T*)p32_;
+  T* q = f64 ? (T*)q_ : (T*)q32_;
+  T* rh = f64 ? (T*)rh_ : (T*)rh32_;
+  T* sv = f64 ? (T*)s_ : (T*)s32_;
+  T* tv = f64 ? (T*)t_ : (T*)t32_;
+  T* sh = f64 ? (T*)sh_ : (T*)sh32_;
+  T* dinv = f64 ? (T*)dinv_ : (T*)dinv32_;
+  const int nb = nb_;
+  k_jacobi<T><<<nb, 256, 0, s>>>(g, C, n, dinv, p_.pc_type == CH_PC_JACOBI);
+  // ||b||
+  if (zero_guess) {
+    k_zero<T><<<nb, 256, 0, s>>>(N, x);
+    k_copy<T><<<nb, 256, 0, s>>>(N, b, r);
+    k_prec_dot<T><<<nb, 256, 0, s>>>(N, dinv, r, z, part_);
+  } else {
+    k_residual<T><<<nb, 256, 0, s>>>(g, C, n, b, x, r, part_);
+    k_prec_dot<T><<<nb, 256, 0, s>>>(N, dinv, r, z, part_);
+  }
+  k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_SET_RZ_RR, scal_, 0.0);
+  k_dot<T><<<nb, 256, 0, s>>>(N, b, b, part_);
+  k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_TMP, scal_, 0.0);
+  CH_CUDA_OK(cudaMemcpyAsync(hscal_, scal_, sizeof(double) * S_NSLOT, cudaMemcpyDeviceToHost, s));
+  CH_CUDA_OK(cudaStreamSynchronize(s));
+  const double bnorm = sqrt(hscal_[S_TMP]);
+  double rr = hscal_[S_RR];
+  const double tol = rtol * bnorm;
+  int it = 0;
+  if (sqrt(rr) <= tol || bnorm == 0.0) {
+    *its = 0;
+    *rnorm_out = sqrt(rr);
+    return CH_OK;
+  }
+  if (p_.ksp_type == CH_KSP_CG) {
+    k_cg_p<T><<<nb, 256, 0, s>>>(N, scal_, z, pp, 1);
+    while (it < maxit) {
+      k_apply<T><<<nb, 256, 0, s>>>(g, C, n, pp, q, pp, part_);
+      k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_CG_ALPHA, scal_, 0.0);
+      k_cg_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, r, pp, q, dinv, z, part_);
+      k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_CG_BETA, scal_, 0.0);
+      ++it;
+      CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_RR, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s));
+      CH_CUDA_OK(cudaStreamSynchronize(s));
+      rr = hscal_[S_RR];
+      if (!(sqrt(rr) > tol)) break;
+      k_cg_p<T><<<nb, 256, 0, s>>>(N, scal_, z, pp, 0);
+    }
+  } else {
+    // BiCGStab, right preconditioned (van der Vorst 1992)
+    k_copy<T><<<nb, 256, 0, s>>>(N, r, rh);
+    k_zero<T><<<nb, 256, 0, s>>>(N, pp);
+    k_zero<T><<<nb, 256, 0, s>>>(N, q);  // v
+    // rho = rh.r = r.r
+    CH_CUDA_OK(cudaMemcpyAsync(scal_ + S_RHO, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    bool first = true;
+    while (it < maxit) {
+      k_bi_p<T><<<nb, 256, 0, s>>>(N, scal_, r, pp, q, dinv, z, first ? 1 : 0);  // z = y
+      first = false;
+      k_apply<T><<<nb, 256, 0, s>>>(g, C, n, z, q, rh, part_);                  // v = A y; rh.v
+      k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_BI_ALPHA, scal_, 0.0);
+      k_bi_s<T><<<nb, 256, 0, s>>>(N, scal_, r, q, dinv, sv, sh, part_);
+      k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_SS, scal_, 0.0);
+      ++it;
+      CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_SS, scal_ + S_SS, sizeof(double), cudaMemcpyDeviceToHost, s));
+      CH_CUDA_OK(cudaStreamSynchronize(s));
+      if (!(sqrt(hscal_[S_SS]) > tol)) {
+        k_bi_half<T><<<nb, 256, 0, s>>>(N, scal_, x, z, r, sv);
+        rr = hscal_[S_SS];
+        break;
+      }
+      k_apply_dot2<T><<<nb, 256, 0, s>>>(g, C, n, sh, tv, sv, part_);
+      k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_OMEGA, scal_, 0.0);
+      k_bi_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, z, sh, r, sv, tv, rh, part_);
+      k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_BETA, scal_, 0.0);
+      CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_RR, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s));
+      CH_CUDA_OK(cudaStreamSynchronize(s));
+      rr = hscal_[S_RR];
+      if (!(sqrt(rr) > tol)) break;
+    }
+  }
+  *its = it;
+  *rnorm_out = sqrt(rr);
+  return CH_OK;
+}
+
+ch_status PotentialSolver::solve(const double* n, const double* b, double* phi, SolveStats* st, cudaStream_t s) {
+  st->iterations = 0;
+  st->refinements = 0;
+  ch_status rc = (p_.precision == CH_MIXED && p_.lhs_type != CH_LHS_IDENTITY) ? solve_mixed(n, b, phi, st, s)
+                                                                             : solve_fp64(n, b, phi, st, s);
+  return rc;
+}
+
+ch_status PotentialSolver::solve_fp64(const double* n, const double* b, double* phi, SolveStats* st,
+                                      cudaStream_t s) {
+  const bool singular = p_.lhs_type != CH_LHS_IDENTITY;
+  if (singular) remove_mean64(phi, s);
+  int its = 0;
+  double rn = 0.0;
+  ch_status rc = krylov<double>(g_, n, b, phi, p_.ksp_rtol, p_.ksp_max_it, false, &its, &rn, s);
+  if (rc) return rc;
+  if (singular) remove_mean64(phi, s);
+  // true residual
+  k_residual<double><<<nb_, 256, 0, s>>>(g_, dev_coefs<double>(c_), n, b, phi, r_, part_);
+  k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_RR, scal_, 0.0);
+  CH_CUDA_OK(cudaMemcpyAsync(hscal_, scal_, sizeof(double) * S_NSLOT, cudaMemcpyDeviceToHost, s));
+  CH_CUDA_OK(cudaStreamSynchronize(s));
+  st->iterations = its;
+  st->rnorm = sqrt(hscal_[S_RR]);
+  st->bnorm = sqrt(dot64(b, b, s));
+  const double tol = fmax(p_.ksp_rtol * st->bnorm, p_.ksp_atol);
+  if (st->rnorm > tol * 1.01 && st->rnorm > 0.0) return CH_ERR_NOT_CONVERGED;
+  return CH_OK;
+}
+
+// FP64 iterative refinement around FP32 Krylov solves of the correction.
+ch_status PotentialSolver::solve_mixed(const double* n, const double* b, double* phi, SolveStats* st,
+                                       cudaStream_t s) {
+  const DevCoefs<double> C64 = dev_coefs<double>(c_);
+  k_down<<<nb_, 256, 0, s>>>(N_, n, 1.0, n32_);
+  remove_mean64(phi, s);
+  const double bnorm = sqrt(dot64(b, b, s));
+  st->bnorm = bnorm;
+  const double tol = fmax(p_.ksp_rtol * bnorm, p_.ksp_atol);
+  const double inner_rtol = 1e-4;
+  int total = 0, ref = 0;
+  double rn = 0.0;
+  for (; ref < 50; ++ref) {
+    k_residual<double><<<nb_, 256, 0, s>>>(g_, C64, n, b, phi, r_, part_);
+    k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_RR, scal_, 0.0);
+    CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_RR, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CH_CUDA_OK(cudaStreamSynchronize(s));
+    rn = sqrt(hscal_[S_RR]);
+    if (rn <= tol || rn == 0.0) break;
+    const double sc = 1.0 / rn;
+    k_down<<<nb_, 256, 0, s>>>(N_, r_, sc, b32_);
+    int its = 0;
+    double rin = 0.0;
+    ch_status rc = krylov<float>(g_, n32_, b32_, x32_, inner_rtol, p_.ksp_max_it, true, &its, &rin, s);
+    if (rc) return rc;
+    total += its;
+    k_up_add<<<nb_, 256, 0, s>>>(N_, x32_, rn, phi);
+    remove_mean64(phi, s);
+  }
+  st->iterations = total;
+  st->refinements = ref;
+  st->rnorm = rn;
+  if (rn > tol * 1.01 && rn > 0.0) return CH_ERR_NOT_CONVERGED;
+  return CH_OK;
+}
+
+}  // namespace ch

@@ -1,0 +1,69 @@
+// solver.cuh -- potential solve of the hybrid-PIC hot path (src/potential.c,
+// src/lhs.c, src/rhs.c) as matrix-free sm_103a kernels.
+#pragma once
+
+#include "common.cuh"
+
+namespace ch {
+
+// Stencil scale factors of ComputeFullLHS (src/lhs.c:404-447) or of the
+// Laplacian/identity operators, by --lhs-type.
+struct OpCoefs {
+  int type;                 // CH_LHS_*
+  double sxx, syy, szz, sxy, sxz, syz, syx, szx, szy;
+};
+OpCoefs op_coefs(const ch_params& p, const GridDesc& g);
+
+// One level of the operator: grid, coefficients, density.
+template <typename T>
+struct Level {
+  GridDesc g;
+  OpCoefs c;
+  const T* n;               // density the operator is built from
+};
+
+struct SolveStats {
+  int iterations;
+  int refinements;
+  double rnorm, bnorm;
+};
+
+// Workspace and driver for the Krylov solves of one run.
+class PotentialSolver {
+ public:
+  ch_status init(const ch_params& p, const GridDesc& g, int sms);
+  void release();
+  // RHS from the moments (SoA n, Gx, Gy, Gz; FP64), mean removed.
+  void build_rhs(const double* mom, double* b, cudaStream_t s);
+  // Solve A(n) phi = b; phi holds the warm start.  n is FP64.
+  ch_status solve(const double* n, const double* b, double* phi, SolveStats* st, cudaStream_t s);
+  // y = A(n) x in FP64.
+  void apply64(const double* n, const double* x, double* y, cudaStream_t s);
+
+ private:
+  ch_status solve_fp64(const double* n, const double* b, double* phi, SolveStats* st, cudaStream_t s);
+  ch_status solve_mixed(const double* n, const double* b, double* phi, SolveStats* st, cudaStream_t s);
+  template <typename T>
+  ch_status krylov(const GridDesc& g, const T* n, const T* b, T* x, double rtol, int maxit, bool zero_guess,
+                   int* its, double* rnorm_out, cudaStream_t s);
+  double dot64(const double* a, const double* b, cudaStream_t s);
+  void remove_mean64(double* v, cudaStream_t s);
+
+  ch_params p_{};
+  GridDesc g_{};
+  OpCoefs c_{};
+  int sms_ = 0;
+  int64_t N_ = 0;
+  int nb_ = 0;              // blocks of the vector kernels
+  // FP64 workspace
+  double *r_ = nullptr, *z_ = nullptr, *pd_ = nullptr, *q_ = nullptr, *rh_ = nullptr, *s_ = nullptr, *t_ = nullptr,
+         *sh_ = nullptr, *dinv_ = nullptr;
+  // FP32 workspace (mixed form)
+  float *n32_ = nullptr, *b32_ = nullptr, *x32_ = nullptr, *r32_ = nullptr, *z32_ = nullptr, *p32_ = nullptr,
+        *q32_ = nullptr, *rh32_ = nullptr, *s32_ = nullptr, *t32_ = nullptr, *sh32_ = nullptr, *dinv32_ = nullptr;
+  double* part_ = nullptr;  // block partials
+  double* scal_ = nullptr;  // device scalars
+  double* hscal_ = nullptr; // pinned host mirror
+};
+
+}  // namespace ch

@@ -192,6 +192,12 @@ ch_status ch_get_rhs(ch_ctx* c, double* out);   /* ctx->rhs after the last RHS b
 /* y = A(n) x with the current operator (matrix-free ComputeFullLHS). */
 ch_status ch_apply_operator(ch_ctx* c, const double* x, double* y);
 
+/* Page-locks caller memory so that the copies of upload/download run at
+ * full link speed (no counterpart in the reference: its arrays never leave
+ * the host). */
+ch_status ch_host_register(void* ptr, uint64_t bytes);
+ch_status ch_host_unregister(void* ptr);
+
 #ifdef __cplusplus
 }
 #endif

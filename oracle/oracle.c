@@ -786,3 +786,6 @@ int orc_step(orc_state* s, int64_t step, orc_counters* cnt, int* its, double* rn
   orc_collect(&s->p, &s->P, s->nodes, (s->p.faithful & CH_FAITHFUL_D6) != 0);
   return potential(s, its, rnorm, bnorm);
 }
+
+/* sizeof(ch_params) as the C compiler lays it out, for the binding checks. */
+int64_t orc_sizeof_params(void) { return (int64_t)sizeof(ch_params); }

@@ -104,6 +104,8 @@ int orc_step(orc_state* s, int64_t step, orc_counters* cnt, int* its, double* rn
 /* Initial moments and first solve (src/hybrid.c:67,81); also sets sbar. */
 int orc_initialize(orc_state* s, int* its, double* rnorm, double* bnorm);
 
+int64_t orc_sizeof_params(void);
+
 /* Threads used by the loops (1 = serial, as the reference's per-rank loops). */
 void orc_set_threads(int n);
 int orc_get_threads(void);

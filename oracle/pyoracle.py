@@ -61,9 +61,9 @@ class State(C.Structure):
 
 
 def build(ref: bool = False) -> None:
-    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True, stdout=subprocess.DEVNULL)
     if ref and os.path.isdir("/root/reference/src"):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True, stdout=subprocess.DEVNULL)
 
 
 _lib = None
@@ -99,6 +99,7 @@ def lib():
         L.orc_initialize.argtypes = [C.POINTER(State), C.POINTER(C.c_int), _dp, _dp]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_get_threads.restype = C.c_int
+        L.orc_sizeof_params.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -332,3 +333,15 @@ class Run:
     @property
     def sbar(self):
         return self.s.sbar
+
+
+def params_from(src) -> Params:
+    """Copies a product ch_params mirror (same field names) into the oracle's."""
+    p = Params()
+    for name, _ in Params._fields_:
+        v = getattr(src, name)
+        if hasattr(v, "__len__"):
+            getattr(p, name)[:] = list(v)
+        else:
+            setattr(p, name, v)
+    return p

@@ -1,0 +1,388 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle and with
+the reference's own outputs.  Tolerances are stated per check:
+
+* FP64 plain form, collisionless: 1e-12 relative (norm-wise, max over
+  entries / max magnitude) for positions, velocities, moments, RHS, A x.
+* potential: zero-mean phi within 1e-11 relative after both solve to rtol
+  1e-14 (the difference is bounded by cond(A) x rtol).
+* collisions: identical Philox streams, so per-ion results agree to 1e-12
+  except for ions whose draw lies within rounding of the threshold; counts
+  and velocity moments against the reference within 4 standard errors.
+* mixed form: errors against the FP64 oracle stated per output below.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def make(chy, po, N=(8, 8, 8), L=None, precision="fp64", **kw):
+    p = chy.params_for(N, L, precision=chy.PRECISION[precision], **kw)
+    return p, po.params_from(p)
+
+
+def ions_from(po, golden, tag):
+    pos = golden[f"{tag}_pos"]
+    vel = golden[f"{tag}_vel"]
+    s = po.Ions(pos.shape[0])
+    s.a[0:3] = pos.T
+    s.a[3:6] = vel.T
+    return s
+
+
+def golden_case(chy, po, golden, tag, **kw):
+    m = golden[f"{tag}_meta"]
+    N = tuple(int(v) for v in m[0:3])
+    L = tuple(float(v) for v in m[3:6])
+    p, q = make(chy, po, N, L, **kw)
+    return p, q, ions_from(po, golden, tag)
+
+
+def upload(h, ions):
+    pos, vel = ions.aos()
+    h.upload(pos, vel)
+
+
+# ------------------------------------------------------------------ loader
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_loader_matches_oracle(chy, po, precision):
+    p, q = make(chy, po, (16, 12, 10), (16.0, 12.0, 10.0), precision=precision)
+    L = chy.loader(amp=(0.05, 0.02, 0.01), phase=tuple(chy.mode_phases(3)), vT=(1.0, 0.9, 1.1), v0=(0, 0.3, 0))
+    n = 20000
+    with chy.Hybrid(p) as h:
+        h.load(n, L)
+        pos, vel = h.download()
+    ref = po.load(q, po.make_loader(amp=(0.05, 0.02, 0.01), phase=tuple(po.mode_phases(3)), vT=(1.0, 0.9, 1.1),
+                                    v0=(0, 0.3, 0)), n)
+    rp, rv = ref.aos()
+    if precision == "fp64":
+        assert rel(pos[:, :3], rp[:, :3]) < 1e-13
+        assert rel(vel[:, :3], rv[:, :3]) < 1e-13
+    else:
+        # FP32 offsets in unit cells: |dx| <= 2^-24 cell; FP32 velocities
+        assert np.abs(pos[:, :3] - rp[:, :3]).max() < 2e-7
+        assert rel(vel[:, :3], rv[:, :3]) < 2e-7
+
+
+# ------------------------------------------------------------------ deposit
+@pytest.mark.parametrize("tag", ["g8", "g15x10x8"])
+def test_deposit_matches_reference(chy, po, golden, tag):
+    p, q, ions = golden_case(chy, po, golden, tag)
+    with chy.Hybrid(p) as h:
+        upload(h, ions)
+        nodes = h.CollectVlasovQuantities()
+    ref = golden[f"{tag}_collect1"].reshape(-1, 4)
+    assert rel(nodes, ref) < 1e-12
+    assert rel(nodes, po.collect(q, ions).reshape(-1, 4)) < 1e-12
+
+
+def test_deposit_accumulates_as_written(chy, po, golden):
+    p, q, ions = golden_case(chy, po, golden, "g8", faithful=chy.FAITHFUL[6])
+    with chy.Hybrid(p) as h:
+        upload(h, ions)
+        h.CollectVlasovQuantities()
+        nodes = h.CollectVlasovQuantities()
+    assert rel(nodes, golden["g8_collect2"].reshape(-1, 4)) < 1e-12
+
+
+def test_deposit_mixed_error(chy, po, golden):
+    p, q, ions = golden_case(chy, po, golden, "g8", precision="mixed")
+    with chy.Hybrid(p) as h:
+        upload(h, ions)
+        nodes = h.CollectVlasovQuantities()
+    # FP32 offsets and velocities: moments within 1e-6 of the FP64 reference
+    assert rel(nodes, golden["g8_collect1"].reshape(-1, 4)) < 1e-6
+
+
+# ------------------------------------------------------------------ RHS and operator
+@pytest.mark.parametrize("tag", ["g8", "g15x10x8"])
+@pytest.mark.parametrize("ki,kappa", [(0, (0.0, 0.0, 0.0)), (1, (0.3, -0.2, 1.0))])
+@pytest.mark.parametrize("rt", [0, 1, 2])
+def test_rhs_matches_reference(chy, po, golden, tag, ki, kappa, rt):
+    p, q, _ = golden_case(chy, po, golden, tag, kappa_e=kappa, rhs_type=rt, E0=(0.5, 0.1, -0.2), cth=1.0, cG=0.1,
+                          faithful=chy.FAITHFUL[8])
+    nodes = golden[f"{tag}_collect1"]
+    with chy.Hybrid(p) as h:
+        h.set_moments(nodes)
+        b = h.rhs()
+    ref = golden[f"{tag}_rhs{rt}_k{ki}"]
+    assert np.abs(b - ref).max() <= 1e-12 * max(np.abs(ref).max(), 1e-300) + 1e-14
+
+
+@pytest.mark.parametrize("tag", ["g8", "g15x10x8"])
+@pytest.mark.parametrize("ki,kappa", [(0, (0.0, 0.0, 0.0)), (1, (0.3, -0.2, 1.0))])
+@pytest.mark.parametrize("lt", [0, 1, 2])
+def test_operator_matches_reference(chy, po, golden, tag, ki, kappa, lt):
+    p, q, _ = golden_case(chy, po, golden, tag, kappa_e=kappa, lhs_type=lt)
+    nodes = golden[f"{tag}_collect1"]
+    n = nodes[0::4]
+    cols = golden[f"{tag}_lhs{lt}_k{ki}_cols"]
+    vals = golden[f"{tag}_lhs{lt}_k{ki}_vals"]
+    A = np.zeros((n.size, n.size))
+    for r in range(n.size):
+        for c, v in zip(cols[r], vals[r]):
+            A[r, c] += v
+    x = np.random.default_rng(11).standard_normal(n.size)
+    with chy.Hybrid(p) as h:
+        h.set_moments(nodes)
+        y = h.apply_operator(x)
+    assert np.abs(y - A @ x).max() <= 1e-12 * np.abs(A).max() * np.abs(x).max() * 19
+
+
+# ------------------------------------------------------------------ solve
+@pytest.mark.parametrize("ksp,kappa", [("cg", (0.0, 0.0, 0.0)), ("bcgs", (0.0, 0.0, 1.0))])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solve_matches_oracle(chy, po, golden, ksp, kappa, precision):
+    p, q, _ = golden_case(chy, po, golden, "g8", kappa_e=kappa, ksp_type=chy.KSP[ksp], ksp_rtol=1e-12,
+                          precision=precision)
+    nodes = golden["g8_collect1"]
+    with chy.Hybrid(p) as h:
+        h.set_moments(nodes)
+        phi = h.ComputePotential()
+        info = h.last_solve
+    assert info["rnorm"] <= 1e-12 * info["bnorm"] * 1.01
+    b = po.rhs(q, nodes)
+    ref, rinfo = po.solve(q, nodes[0::4], b, rtol=1e-14, maxit=20000)
+    assert rinfo["rc"] == 0
+    assert abs(phi.mean()) < 1e-12 * np.abs(phi).max()
+    assert rel(phi, ref) < 1e-9
+
+
+# ------------------------------------------------------------------ push and move
+def random_phi(N, seed=5):
+    rng = np.random.default_rng(seed)
+    x = np.arange(N[0])[None, None, :]
+    y = np.arange(N[1])[None, :, None]
+    z = np.arange(N[2])[:, None, None]
+    phi = 0.3 * np.sin(2 * np.pi * x / N[0] + 0.4) * np.cos(2 * np.pi * y / N[1]) + 0.1 * np.sin(
+        4 * np.pi * z / N[2] + 1.0) + 0.01 * rng.standard_normal((N[2], N[1], N[0]))
+    return phi.ravel()
+
+
+@pytest.mark.parametrize("faithful", [0, 2, 3, 4, 34])
+def test_push_collisionless_matches_oracle(chy, po, golden, faithful):
+    fl = {0: 0, 2: chy.FAITHFUL[2], 3: chy.FAITHFUL[3], 4: chy.FAITHFUL[4],
+          34: chy.FAITHFUL[3] | chy.FAITHFUL[4]}[faithful]
+    p, q, ions = golden_case(chy, po, golden, "g15x10x8", mn=0.0, faithful=fl, B0=(0.3, -0.2, 1.0), dt=0.2)
+    N = (p.Nx, p.Ny, p.Nz)
+    phi = random_phi(N)
+    with chy.Hybrid(p) as h:
+        upload(h, ions)
+        h.set_phi(phi)
+        h.UpdateVelocities(3)
+        pos, vel = h.download()
+    ref = ions.copy()
+    po.update_velocities(q, phi, ref, 3, 0.0)
+    rp, rv = ref.aos()
+    assert rel(vel[:, :3], rv[:, :3]) < 1e-12
+    assert np.array_equal(pos[:, :3], ions.aos()[0][:, :3])
+
+
+def test_move_matches_oracle(chy, po, golden):
+    p, q, ions = golden_case(chy, po, golden, "g8", dt=0.7)
+    with chy.Hybrid(p) as h:
+        upload(h, ions)
+        h.UpdatePositions()
+        pos, _ = h.download()
+    ref = ions.copy()
+    po.update_positions(q, ref)
+    assert rel(pos[:, :3], ref.aos()[0][:, :3]) < 1e-12
+    assert (pos[:, 0] >= 0).all() and (pos[:, 0] < p.x1).all()
+
+
+def test_move_as_written_is_noop(chy, po, golden):
+    p, q, ions = golden_case(chy, po, golden, "g8", faithful=chy.FAITHFUL[5])
+    with chy.Hybrid(p) as h:
+        upload(h, ions)
+        h.UpdatePositions()
+        pos, _ = h.download()
+    assert np.array_equal(pos[:, :3], golden["g8_moved"])
+
+
+def test_download_returns_upload_order(chy, po, golden):
+    p, q, ions = golden_case(chy, po, golden, "g15x10x8")
+    pos0, vel0 = ions.aos()
+    with chy.Hybrid(p) as h:
+        h.upload(pos0, vel0)  # the upload sorts by cell on the device
+        pos, vel = h.download()
+    assert np.array_equal(pos[:, :3], pos0[:, :3]) and np.array_equal(vel[:, :3], vel0[:, :3])
+
+
+# ------------------------------------------------------------------ whole steps
+def run_pair(chy, po, p, q, ions, nsteps, fused=True):
+    N = p.Nx * p.Ny * p.Nz
+    out = []
+    ref = po.Run(q, ions.copy())
+    rc, _ = ref.initialize()
+    assert rc == 0
+    with chy.Hybrid(p) as h:
+        upload(h, ions)
+        h.CollectVlasovQuantities()
+        h.ComputePotential()
+        for s in range(nsteps):
+            if fused:
+                info = h.step(s, 1)
+            else:
+                info = h.UpdateVelocities(s)
+                h.UpdatePositions()
+                h.CollectVlasovQuantities()
+                h.ComputePotential()
+            rc, rinfo = ref.step(s)
+            assert rc == 0
+            pos, vel = h.download()
+            out.append(dict(phi=h.phi(), pos=pos, vel=vel, info=info, rinfo=rinfo, rphi=ref.phi.copy(),
+                            rnodes=ref.nodes.copy(), rions=ref.ions.aos()))
+    return out, N
+
+
+def test_steps_collisionless_fp64(chy, po, golden):
+    p, q, ions = golden_case(chy, po, golden, "g8", mn=0.0, ksp_rtol=1e-13)
+    out, N = run_pair(chy, po, p, q, ions, 4)
+    for s, o in enumerate(out):
+        rp, rv = o["rions"]
+        assert rel(o["pos"][:, :3], rp[:, :3]) < 1e-12, s
+        assert rel(o["vel"][:, :3], rv[:, :3]) < 1e-12, s
+        assert rel(o["phi"], o["rphi"]) < 1e-8, s
+
+
+def test_fused_step_equals_separate_calls(chy, po, golden):
+    p, q, ions = golden_case(chy, po, golden, "g8", ksp_rtol=1e-10)
+    a, _ = run_pair(chy, po, p, q, ions, 3, fused=True)
+    b, _ = run_pair(chy, po, p, q, ions, 3, fused=False)
+    for x, y in zip(a, b):
+        assert np.array_equal(x["vel"], y["vel"]) and np.array_equal(x["pos"], y["pos"])
+        assert np.array_equal(x["phi"], y["phi"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_deterministic_run_to_run(chy, po, golden, precision):
+    p, q, ions = golden_case(chy, po, golden, "g8", precision=precision, sort_period=1)
+    res = []
+    for _ in range(2):
+        with chy.Hybrid(p) as h:
+            upload(h, ions)
+            h.CollectVlasovQuantities()
+            h.ComputePotential()
+            h.step(0, 4)
+            res.append((h.phi(), *h.download(), h.CollectVlasovQuantities()))
+    for x, y in zip(res[0], res[1]):
+        assert np.array_equal(x, y)
+
+
+def test_collisions_match_oracle_per_ion(chy, po, golden):
+    p, q, ions = golden_case(chy, po, golden, "g8", nui=2.0, ksp_rtol=1e-12)
+    out, N = run_pair(chy, po, p, q, ions, 3)
+    for s, o in enumerate(out):
+        rp, rv = o["rions"]
+        dv = np.abs(o["vel"][:, :3] - rv[:, :3]).max(axis=1)
+        bad = (dv > 1e-10 * np.abs(rv).max()).sum()
+        # identical Philox streams: only ions whose uniform draw sits within
+        # rounding of the acceptance threshold may differ
+        assert bad <= max(1, ions.np // 10000), (s, bad)
+        assert abs(o["info"]["collisions"] - o["rinfo"]["collisions"]) <= bad
+        assert o["info"]["Nc"] == o["rinfo"]["Nc"]
+        assert abs(o["info"]["expected"] - o["rinfo"]["expected"]) < 1e-9 * o["rinfo"]["expected"]
+
+
+@pytest.mark.parametrize("case", [0, 1])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_collision_statistics_vs_reference(chy, po, golden, case, precision):
+    """One ComputeCollisions of the reference (golden) against one collision
+    pass here on the same Maxwellian population."""
+    prm = golden[f"coll{case}_params"]
+    st = golden[f"coll{case}_stats"]
+    col = golden[f"coll{case}_collided"]
+    n = int(prm[0])
+    viT, vi0 = tuple(prm[1:4]), tuple(prm[4:7])
+    nu, dt, vnT, vn0 = prm[7], prm[8], prm[9], tuple(prm[10:13])
+    p, q = make(chy, po, (8, 8, 8), precision=precision, viT=viT, vi0=vi0, nui=nu, dt=dt, vnT=vnT, vn0=vn0,
+                B0=(0, 0, 0), seed=1)
+    ions = po.load(po.default_params((8, 8, 8)), po.make_loader(v0=vi0, vT=viT), n)
+    before = ions.aos()[1][:, :3].copy()
+    with chy.Hybrid(p) as h:
+        upload(h, ions)  # phi = 0 and B = 0: the push leaves v unchanged
+        info = h.UpdateVelocities(0)
+        _, vel = h.download()
+    after = vel[:, :3]
+    Nc = int(st[0])
+    assert info["Nc"] == Nc
+    # expected count equals the reference's Nc; the realised count is within
+    # 4 sigma of it (Poisson-binomial, sigma <= sqrt(Nc))
+    assert abs(info["expected"] - Nc) < 1e-6 * Nc + 1.0
+    assert abs(info["collisions"] - Nc) < 4 * np.sqrt(Nc)
+    changed = np.any(after != before, axis=1)
+    assert changed.sum() == info["collisions"]
+    # the reference's distinct collided ions are Nc minus repeats
+    assert abs(changed.sum() - st[1]) < 4 * np.sqrt(Nc) + (Nc - st[1])
+    # moments of the whole population within 4 standard errors
+    m, var = after.mean(axis=0), after.var(axis=0)
+    se_m = np.sqrt(var / n)
+    assert np.all(np.abs(m - st[2:5]) < 4 * np.sqrt(2) * se_m)
+    assert np.all(np.abs(var - st[5:8]) < 4 * np.sqrt(2) * var * np.sqrt(2.0 / n))
+    # moments of the collided ions (the scattered distribution)
+    a = after[changed]
+    k = a.shape[0]
+    se = np.sqrt(a.var(axis=0) / k)
+    assert np.all(np.abs(a.mean(axis=0) - col[0:3]) < 4 * np.sqrt(2) * se)
+    assert np.all(np.abs(a.var(axis=0) - col[3:6]) < 4 * np.sqrt(2) * a.var(axis=0) * np.sqrt(2.5 / k))
+
+
+@pytest.mark.parametrize("rtol", [1e-10])
+def test_mixed_form_error_vs_fp64_oracle(chy, po, golden, rtol):
+    """Mixed form (FP32 ions and inner solves, FP64 refinement and sums)
+    against the FP64 oracle, 4 collisionless steps: stated errors."""
+    p, q, ions = golden_case(chy, po, golden, "g8", precision="mixed", mn=0.0, ksp_rtol=rtol)
+    out, N = run_pair(chy, po, p, q, ions, 4)
+    for s, o in enumerate(out):
+        rp, rv = o["rions"]
+        assert np.abs(o["pos"][:, :3] - rp[:, :3]).max() < 1e-5 * (s + 1)
+        assert rel(o["vel"][:, :3], rv[:, :3]) < 1e-5 * (s + 1)
+        assert rel(o["phi"], o["rphi"]) < 1e-4
+        assert o["info"]["rnorm"] <= rtol * o["info"]["bnorm"] * 1.01
+
+
+# ------------------------------------------------------------------ failure reporting
+def test_not_converged_is_reported(chy, po, golden):
+    p, q, _ = golden_case(chy, po, golden, "g8", ksp_max_it=1, ksp_rtol=1e-12)
+    with chy.Hybrid(p) as h:
+        h.set_moments(golden["g8_collect1"])
+        with pytest.raises(chy.HybridError) as e:
+            h.ComputePotential()
+    assert e.value.status == -4
+
+
+def test_nan_in_ions_is_reported(chy, po, golden):
+    p, q, ions = golden_case(chy, po, golden, "g8")
+    pos, vel = ions.aos()
+    vel[17, 1] = np.nan
+    with chy.Hybrid(p) as h:
+        h.upload(pos, vel)
+        with pytest.raises(chy.HybridError) as e:
+            h.CollectVlasovQuantities()
+    assert e.value.status in (-6, -7)
+
+
+def test_collision_refusal_limit_is_reported(chy, po, golden):
+    # hot neutrals: scattered ions exceed 10 vT and are refused
+    # (src/particles.c:597-606 aborts after 10 refusals)
+    p, q, ions = golden_case(chy, po, golden, "g8", vnT=40.0, nui=50.0, dt=0.5, B0=(0, 0, 0))
+    with chy.Hybrid(p) as h:
+        upload(h, ions)
+        with pytest.raises(chy.HybridError) as e:
+            h.UpdateVelocities(0)
+    assert e.value.status == -5
+
+
+def test_bad_arguments_are_rejected(chy):
+    with pytest.raises(chy.HybridError) as e:
+        chy.Hybrid(chy.params_for((2, 8, 8)))
+    assert e.value.status == -1
+    with pytest.raises(chy.HybridError) as e:
+        chy.Hybrid(chy.params_for((8, 8, 8), precision=1, faithful=chy.FAITHFUL[3]))
+    assert e.value.status == -10
