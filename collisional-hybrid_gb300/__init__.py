@@ -90,6 +90,15 @@ class StepInfo(C.Structure):
                     refinements=self.solve.refinements, rnorm=self.solve.rnorm, bnorm=self.solve.bnorm)
 
 
+class Profile(C.Structure):
+    _fields_ = [("pass_ms", C.c_double), ("pass_calls", C.c_int64), ("solve_ms", C.c_double),
+                ("solve_calls", C.c_int64), ("sort_ms", C.c_double), ("sort_calls", C.c_int64),
+                ("moments_ms", C.c_double), ("moments_calls", C.c_int64), ("launches", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -120,6 +129,10 @@ def lib():
             "ch_set_phi": [vp, vp],
             "ch_get_rhs": [vp, vp],
             "ch_apply_operator": [vp, vp, vp],
+            "ch_set_profiling": [vp, C.c_int32],
+            "ch_get_profile": [vp, C.POINTER(Profile)],
+            "ch_reset_profile": [vp],
+            "ch_get_stream": [vp, C.POINTER(vp)],
             "ch_host_register": [vp, C.c_uint64],
             "ch_host_unregister": [vp],
         }
@@ -243,20 +256,24 @@ class Hybrid:
     def UpdatePositions(self):
         _check(lib().ch_update_positions(self._h))
 
-    def CollectVlasovQuantities(self, out: np.ndarray | None = None):
-        """Returns the dof-4 GridNode array (N x 4: n, Gx, Gy, Gz)."""
-        out = np.empty((self.N, 4)) if out is None else out
+    def CollectVlasovQuantities(self, out: np.ndarray | None = None, copy: bool = True):
+        """Returns the dof-4 GridNode array (N x 4: n, Gx, Gy, Gz); with
+        copy=False the moments stay on the device and None is returned."""
+        if copy:
+            out = np.empty((self.N, 4)) if out is None else out
         info = StepInfo()
-        _check(lib().ch_collect_moments(self._h, out.ctypes.data, C.byref(info)))
-        return out
+        _check(lib().ch_collect_moments(self._h, out.ctypes.data if copy else None, C.byref(info)))
+        self.last_moments = info.as_dict()
+        return out if copy else None
 
-    def ComputePotential(self, out: np.ndarray | None = None):
-        out = np.empty(self.N) if out is None else out
+    def ComputePotential(self, out: np.ndarray | None = None, copy: bool = True):
+        if copy:
+            out = np.empty(self.N) if out is None else out
         info = SolveInfo()
-        _check(lib().ch_compute_potential(self._h, out.ctypes.data, C.byref(info)))
+        _check(lib().ch_compute_potential(self._h, out.ctypes.data if copy else None, C.byref(info)))
         self.last_solve = dict(iterations=info.iterations, refinements=info.refinements, rnorm=info.rnorm,
                                bnorm=info.bnorm)
-        return out
+        return out if copy else None
 
     def step(self, first_step: int, nsteps: int = 1) -> dict:
         info = StepInfo()
@@ -287,3 +304,29 @@ class Hybrid:
         y = np.empty_like(x)
         _check(lib().ch_apply_operator(self._h, x.ctypes.data, y.ctypes.data))
         return y
+
+    # ---------------------------------------------------------------- profiling
+    def set_profiling(self, on: bool = True):
+        _check(lib().ch_set_profiling(self._h, int(on)))
+
+    def reset_profile(self):
+        _check(lib().ch_reset_profile(self._h))
+
+    def profile(self) -> dict:
+        pr = Profile()
+        _check(lib().ch_get_profile(self._h, C.byref(pr)))
+        return pr.as_dict()
+
+    def stream_handle(self) -> int:
+        s = C.c_void_p()
+        _check(lib().ch_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+
+def host_register(a: np.ndarray):
+    """Page-locks a numpy array for full-speed upload/download."""
+    _check(lib().ch_host_register(a.ctypes.data, a.nbytes))
+
+
+def host_unregister(a: np.ndarray):
+    _check(lib().ch_host_unregister(a.ctypes.data))

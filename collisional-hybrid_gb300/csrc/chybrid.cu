@@ -8,6 +8,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <new>
 
 #include "particles.cuh"
@@ -29,6 +30,9 @@ ch_status ch_cuda_fail(cudaError_t e, const char* what, const char* file, int li
   return ch_fail(e == cudaErrorMemoryAllocation ? CH_ERR_NOMEM : CH_ERR_CUDA, "%s failed: %s (%s:%d)", what,
                  cudaGetErrorString(e), file, line);
 }
+
+static std::atomic<unsigned long long> g_launches{0};
+void ch::note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 struct ch_ctx {
   ch_params p;
@@ -63,7 +67,25 @@ struct ch_ctx {
   bool moments_valid = false;
   int64_t since_sort = 0;
   PotentialSolver solver;
+  // profiling
+  bool prof = false;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  ch_profile pr{};
 };
+
+// Times [begin, end) of one phase on the context stream when profiling.
+static void prof_begin(ch_ctx* c) {
+  if (c->prof) cudaEventRecord(c->ev[0], c->stream);
+}
+static void prof_end(ch_ctx* c, double* ms, int64_t* calls) {
+  if (!c->prof) return;
+  cudaEventRecord(c->ev[1], c->stream);
+  cudaEventSynchronize(c->ev[1]);
+  float t = 0.0f;
+  cudaEventElapsedTime(&t, c->ev[0], c->ev[1]);
+  *ms += t;
+  *calls += 1;
+}
 
 extern "C" const char* ch_last_error(void) { return g_err; }
 extern "C" int32_t ch_abi_version(void) { return CH_ABI_VERSION; }
@@ -159,6 +181,8 @@ extern "C" ch_status ch_destroy(ch_ctx* c) {
   if (c->hcnt) cudaFreeHost(c->hcnt);
   if (c->hred) cudaFreeHost(c->hred);
   c->solver.release();
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return CH_OK;
@@ -304,8 +328,10 @@ static ch_status ensure_staging(ch_ctx* c) {
 }
 
 static void do_sort(ch_ctx* c) {
+  prof_begin(c);
   launch_sort(c->mixed, c->g, c->P, c->Q, c->M, c->MQ, c->counts, c->starts, c->cursor, c->keys, c->block_sums,
               c->sms, c->stream);
+  prof_end(c, &c->pr.sort_ms, &c->pr.sort_calls);
   std::swap(c->P, c->Q);
   std::swap(c->M, c->MQ);
   c->since_sort = 0;
@@ -370,8 +396,11 @@ static ch_status run_pass(ch_ctx* c, int phases, int64_t step, ch_step_info* inf
     CH_CUDA_OK(cudaMemsetAsync(c->cnt, 0, sizeof(DevCounters), c->stream));
     if (k.collide) Nc = collision_count(c->p, c->np);
   }
+  if (phases & PH_DEPOSIT) CH_CUDA_OK(cudaMemsetAsync(&c->cnt->range_error, 0, sizeof(int), c->stream));
+  prof_begin(c);
   const int nb = launch_pass(c->mixed, phases, k, c->P, c->M, c->E64, c->E32, c->phi, c->acc, (double)Nc, c->sbar,
                              c->cnt, c->part, c->sms, c->stream);
+  prof_end(c, &c->pr.pass_ms, &c->pr.pass_calls);
   if (push) {
     launch_reduce_partials(c->part, nb, 2, c->red, c->stream);
     CH_CUDA_OK(cudaMemcpyAsync(c->hred, c->red, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
@@ -393,10 +422,11 @@ static ch_status run_pass(ch_ctx* c, int phases, int64_t step, ch_step_info* inf
 }
 
 static ch_status finalize_moments(ch_ctx* c, ch_step_info* info) {
-  CH_CUDA_OK(cudaMemsetAsync(&c->cnt->range_error, 0, sizeof(int), c->stream));
   const int reset = (c->p.faithful & CH_FAITHFUL_D6) ? 0 : 1;
+  prof_begin(c);
   const int nb = launch_finalize(c->g.N, c->acc, 1.0 / c->dep_scale, reset, c->mom, c->part, c->cnt, c->sms,
                                  c->stream);
+  prof_end(c, &c->pr.moments_ms, &c->pr.moments_calls);
   launch_reduce_partials(c->part, nb, 4, c->red + 4, c->stream);
   CH_CUDA_OK(cudaMemcpyAsync(c->hred + 4, c->red + 4, sizeof(double) * 4, cudaMemcpyDeviceToHost, c->stream));
   CH_CUDA_OK(cudaMemcpyAsync(&c->hcnt->range_error, &c->cnt->range_error, sizeof(int), cudaMemcpyDeviceToHost,
@@ -405,6 +435,7 @@ static ch_status finalize_moments(ch_ctx* c, ch_step_info* info) {
   c->moments_valid = true;
   if (info)
     for (int q = 0; q < 4; ++q) info->moment_sum[q] = c->hred[4 + q];
+  if (c->hcnt->range_error & 2) return ch_fail(CH_ERR_NAN, "non-finite ion position or velocity");
   if (c->hcnt->range_error)
     return ch_fail(CH_ERR_RANGE, "deposit exceeded the fixed-point range 2^%d; lower deposit_scale_log2",
                    63 - (int)log2(c->dep_scale));
@@ -454,6 +485,7 @@ extern "C" ch_status ch_collect_moments(ch_ctx* c, ch_grid_node* host_out, ch_st
 static ch_status potential(ch_ctx* c, ch_solve_info* info) {
   if (!c->moments_valid) return ch_fail(CH_ERR_STATE, "no moments: call ch_collect_moments first");
   const int64_t N = c->g.N;
+  prof_begin(c);
   c->solver.build_rhs(c->mom, c->rhs, c->stream);
   const double* n = c->mom;
   if (c->p.faithful & CH_FAITHFUL_D7) {
@@ -464,6 +496,7 @@ static ch_status potential(ch_ctx* c, ch_solve_info* info) {
   if (!c->solved_once) CH_CUDA_OK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));  // ComputeInitialPhi
   SolveStats st{};
   ch_status rc = c->solver.solve(n, c->rhs, c->phi, &st, c->stream);
+  prof_end(c, &c->pr.solve_ms, &c->pr.solve_calls);
   c->solved_once = true;
   if (info) {
     info->iterations = st.iterations;
@@ -569,5 +602,34 @@ extern "C" ch_status ch_host_register(void* ptr, uint64_t bytes) {
 extern "C" ch_status ch_host_unregister(void* ptr) {
   if (!ptr) return ch_fail(CH_ERR_ARG, "null argument");
   CH_CUDA_OK(cudaHostUnregister(ptr));
+  return CH_OK;
+}
+
+extern "C" ch_status ch_set_profiling(ch_ctx* c, int32_t enable) {
+  if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
+  if (enable && !c->ev[0]) {
+    CH_CUDA_OK(cudaEventCreate(&c->ev[0]));
+    CH_CUDA_OK(cudaEventCreate(&c->ev[1]));
+  }
+  c->prof = enable != 0;
+  return CH_OK;
+}
+
+extern "C" ch_status ch_get_profile(ch_ctx* c, ch_profile* out) {
+  if (!c || !out) return ch_fail(CH_ERR_ARG, "null argument");
+  *out = c->pr;
+  out->launches = (int64_t)g_launches.load();
+  return CH_OK;
+}
+
+extern "C" ch_status ch_reset_profile(ch_ctx* c) {
+  if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
+  c->pr = ch_profile{};
+  return CH_OK;
+}
+
+extern "C" ch_status ch_get_stream(ch_ctx* c, void** stream) {
+  if (!c || !stream) return ch_fail(CH_ERR_ARG, "null argument");
+  *stream = (void*)c->stream;
   return CH_OK;
 }

@@ -101,4 +101,9 @@ struct DevCounters {
   } while (0)
 
 ch_status ch_cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+namespace ch {
+// Counts kernel launches made by this library (reported by ch_get_profile).
+void note_launch();
+}
 ch_status ch_fail(ch_status code, const char* fmt, ...);

@@ -311,6 +311,7 @@ __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, 
   const int64_t N = g.N;
   double vsum[2] = {0.0, 0.0};
   unsigned ncol = 0, nref = 0;
+  int bad = 0;
   const bool gather_faithful = (c.faithful & (CH_FAITHFUL_D3 | CH_FAITHFUL_D4)) != 0;
   for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
     double x = P.x[ip], y = P.y[ip], z = P.z[ip];
@@ -348,11 +349,12 @@ __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, 
       if (c.collide) {
         const double wx = v[0] - c.vn0[0], wy = v[1] - c.vn0[1], wz = v[2] - c.vn0[2];
         const double gi = ch_gmean<double>(sqrt(wx * wx + wy * wy + wz * wz), c.vnT);
-        double pc = sbar > 0.0 ? (Nc * gi * ch_neutral_density<double>(c, x)) / sbar : 0.0;
-        if (pc > 1.0) pc = 1.0;
-        vsum[0] += pc;
-        const int rc = ch_collide<double>(c, P.id[ip], pc, v);
-        if (rc > 0) ++ncol; else if (rc < 0) ++nref;
+        const double lscale = sbar > 0.0 ? (Nc * ch_neutral_density<double>(c, x)) / sbar : 0.0;
+        const double lam = lscale * gi;
+        vsum[0] += lam;
+        // first waiting time inline; the event loop runs only for colliding ions
+        const U4 r0 = ch_philox(P.id[ip], c.step, CH_PURPOSE_COLLIDE << 24, c.run, c.seed_lo, c.seed_hi);
+        if (lam > 0.0 && -log(ch_unit(r0.x)) / lam < 1.0) ncol += ch_collide<double>(c, P.id[ip], lscale, v, &nref);
         const double qx = v[0] - c.vn0[0], qy = v[1] - c.vn0[1], qz = v[2] - c.vn0[2];
         vsum[1] += ch_gmean<double>(sqrt(qx * qx + qy * qy + qz * qz), c.vnT);
       }
@@ -365,12 +367,17 @@ __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, 
       P.x[ip] = x; P.y[ip] = y; P.z[ip] = z;
     }
     if (PH & PH_DEPOSIT) {
+      if (!(isfinite(x) && isfinite(y) && isfinite(z) && isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) {
+        bad = 1;  // a non-finite ion is reported, never deposited
+        continue;
+      }
       const double X = (x - g.x0) / g.dx, Y = (y - g.y0) / g.dy, Z = (z - g.z0) / g.dz;
       const double fi = floor(X), fj = floor(Y), fk = floor(Z);
       deposit_cic<double>(g, acc, ch_wrap((int)fi, g.Nx), ch_wrap((int)fj, g.Ny), ch_wrap((int)fk, g.Nz), X - fi,
                           Y - fj, Z - fk, v[0], v[1], v[2], c.dep_scale);
     }
   }
+  if (bad) atomicOr(&cnt->range_error, 2);
   if (PH & PH_PUSH) {
     count_add(cnt, ncol, nref);
     block_partials<2>(vsum, part);
@@ -385,6 +392,7 @@ __global__ void __launch_bounds__(256) k_pass_mixed(StepConsts c, MixParticles P
   const GridDesc& g = c.g;
   double vsum[2] = {0.0, 0.0};
   unsigned ncol = 0, nref = 0;
+  int bad = 0;
   const float dtx = (float)(c.dt / g.dx), dty = (float)(c.dt / g.dy), dtz = (float)(c.dt / g.dz);
   const float vnTf = (float)c.vnT, vn0x = (float)c.vn0[0], vn0y = (float)c.vn0[1], vn0z = (float)c.vn0[2];
   const float scale = (float)c.dep_scale;
@@ -443,11 +451,12 @@ __global__ void __launch_bounds__(256) k_pass_mixed(StepConsts c, MixParticles P
         float nd = 1.0f;
         if (c.nn_profile == CH_NN_GAUSSIAN_X)
           nd = ch_neutral_density<float>(c, (float)(g.x0 + ((double)i + (double)p.x) * g.dx));
-        float pc = pscale * gi * nd;
-        if (pc > 1.0f) pc = 1.0f;
-        vsum[0] += (double)pc;
-        const int rc = ch_collide<float>(c, __float_as_uint(vv.w), pc, v);
-        if (rc > 0) ++ncol; else if (rc < 0) ++nref;
+        const float lscale = pscale * nd;
+        const float lam = lscale * gi;
+        vsum[0] += (double)lam;
+        const uint32_t id = __float_as_uint(vv.w);
+        const U4 r0 = ch_philox(id, c.step, CH_PURPOSE_COLLIDE << 24, c.run, c.seed_lo, c.seed_hi);
+        if (lam > 0.0f && -logf(ch_unitf(r0.x)) / lam < 1.0f) ncol += ch_collide<float>(c, id, lscale, v, &nref);
         const float qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
         vsum[1] += (double)ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), vnTf);
       }
@@ -468,9 +477,14 @@ __global__ void __launch_bounds__(256) k_pass_mixed(StepConsts c, MixParticles P
       P.pos[ip] = p;
     }
     if (PH & PH_DEPOSIT) {
+      if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) {
+        bad = 1;
+        continue;
+      }
       deposit_cic<float>(g, acc, i, j, k, p.x, p.y, p.z, v[0], v[1], v[2], scale);
     }
   }
+  if (bad) atomicOr(&cnt->range_error, 2);
   if (PH & PH_PUSH) {
     count_add(cnt, ncol, nref);
     block_partials<2>(vsum, part);
@@ -708,26 +722,26 @@ int grid_for(int64_t n, int threads, int sms, int per_sm) {
 void launch_load(bool mixed, const GridDesc& g, const ch_loader& L, uint64_t seed, uint32_t run, F64Particles P,
                  MixParticles M, int sms, cudaStream_t s) {
   const uint32_t lo = (uint32_t)seed, hi = (uint32_t)(seed >> 32);
-  if (mixed) k_load_mixed<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, L, lo, hi, run, M);
-  else k_load_f64<<<grid_for(P.np, 256, sms, 8), 256, 0, s>>>(g, L, lo, hi, run, P);
+  if (mixed) k_load_mixed<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, L, lo, hi, run, M), ::ch::note_launch();
+  else k_load_f64<<<grid_for(P.np, 256, sms, 8), 256, 0, s>>>(g, L, lo, hi, run, P), ::ch::note_launch();
 }
 
 void launch_aos_in(bool mixed, const GridDesc& g, const double4_32a* pos, const double4_32a* vel, F64Particles P,
                    MixParticles M, int sms, cudaStream_t s) {
-  if (mixed) k_aos_to_mixed<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, pos, vel, M);
-  else k_aos_to_f64<<<grid_for(P.np, 256, sms, 8), 256, 0, s>>>(pos, vel, P);
+  if (mixed) k_aos_to_mixed<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, pos, vel, M), ::ch::note_launch();
+  else k_aos_to_f64<<<grid_for(P.np, 256, sms, 8), 256, 0, s>>>(pos, vel, P), ::ch::note_launch();
 }
 
 void launch_aos_out(bool mixed, const GridDesc& g, F64Particles P, MixParticles M, double4_32a* pos, double4_32a* vel,
                     int sms, cudaStream_t s) {
-  if (mixed) k_mixed_to_aos<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, M, pos, vel);
-  else k_f64_to_aos<<<grid_for(P.np, 256, sms, 8), 256, 0, s>>>(P, pos, vel);
+  if (mixed) k_mixed_to_aos<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, M, pos, vel), ::ch::note_launch();
+  else k_f64_to_aos<<<grid_for(P.np, 256, sms, 8), 256, 0, s>>>(P, pos, vel), ::ch::note_launch();
 }
 
 void launch_node_efield(bool mixed, const GridDesc& g, double tscale, const double* phi, double* E64, float4* E32,
                         int sms, cudaStream_t s) {
-  if (mixed) k_node_efield_mixed<<<grid_for(g.N, 256, sms, 8), 256, 0, s>>>(g, (float)tscale, phi, E32);
-  else k_node_efield_f64<<<grid_for(g.N, 256, sms, 8), 256, 0, s>>>(g, phi, E64);
+  if (mixed) k_node_efield_mixed<<<grid_for(g.N, 256, sms, 8), 256, 0, s>>>(g, (float)tscale, phi, E32), ::ch::note_launch();
+  else k_node_efield_f64<<<grid_for(g.N, 256, sms, 8), 256, 0, s>>>(g, phi, E64), ::ch::note_launch();
 }
 
 template <int PH>
@@ -738,9 +752,9 @@ static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticle
   const int nb = grid_for(np, 256, sms, 8);
   if (mixed) {
     const float pscale = sbar > 0.0 ? (float)(Nc / sbar) : 0.0f;
-    k_pass_mixed<PH><<<nb, 256, 0, s>>>(c, M, E32, acc, pscale, cnt, part);
+    k_pass_mixed<PH><<<nb, 256, 0, s>>>(c, M, E32, acc, pscale, cnt, part), ::ch::note_launch();
   } else {
-    k_pass_f64<PH><<<nb, 256, 0, s>>>(c, P, E64, phi, acc, Nc, sbar, cnt, part);
+    k_pass_f64<PH><<<nb, 256, 0, s>>>(c, P, E64, phi, acc, Nc, sbar, cnt, part), ::ch::note_launch();
   }
   return nb;
 }
@@ -765,20 +779,20 @@ int launch_sbar(bool mixed, const StepConsts& c, F64Particles P, MixParticles M,
   const int64_t np = mixed ? M.np : P.np;
   const int nb = grid_for(np, 256, sms, 8);
   if (mixed)
-    k_sbar_mixed<<<nb, 256, 0, s>>>(M, (float)c.vnT, (float)c.vn0[0], (float)c.vn0[1], (float)c.vn0[2], part);
+    k_sbar_mixed<<<nb, 256, 0, s>>>(M, (float)c.vnT, (float)c.vn0[0], (float)c.vn0[1], (float)c.vn0[2], part), ::ch::note_launch();
   else
-    k_sbar_f64<<<nb, 256, 0, s>>>(P, c.vnT, c.vn0[0], c.vn0[1], c.vn0[2], part);
+    k_sbar_f64<<<nb, 256, 0, s>>>(P, c.vnT, c.vn0[0], c.vn0[1], c.vn0[2], part), ::ch::note_launch();
   return nb;
 }
 
 void launch_reduce_partials(const double* part, int nblocks, int K, double* out, cudaStream_t s) {
-  k_reduce_partials<<<1, 256, 0, s>>>(part, nblocks, K, out);
+  k_reduce_partials<<<1, 256, 0, s>>>(part, nblocks, K, out), ::ch::note_launch();
 }
 
 int launch_finalize(int64_t N, unsigned long long* acc, double inv_scale, int reset, double* mom, double* part,
                     DevCounters* cnt, int sms, cudaStream_t s) {
   const int nb = grid_for(N, 256, sms, 4);
-  k_finalize_moments<<<nb, 256, 0, s>>>(N, acc, inv_scale, reset, mom, part, cnt);
+  k_finalize_moments<<<nb, 256, 0, s>>>(N, acc, inv_scale, reset, mom, part, cnt), ::ch::note_launch();
   return nb;
 }
 
@@ -789,14 +803,14 @@ void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, 
   const int64_t N = g.N;
   cudaMemsetAsync(counts, 0, sizeof(uint32_t) * N, s);
   const int nb = grid_for(np, 256, sms, 8);
-  if (mixed) k_hist_mixed<<<nb, 256, 0, s>>>(g, M, counts, keys);
-  else k_hist_f64<<<nb, 256, 0, s>>>(g, P, counts, keys);
+  if (mixed) k_hist_mixed<<<nb, 256, 0, s>>>(g, M, counts, keys), ::ch::note_launch();
+  else k_hist_f64<<<nb, 256, 0, s>>>(g, P, counts, keys), ::ch::note_launch();
   const int nsb = (int)((N + 1023) / 1024);
-  k_scan_blocks<<<nsb, 512, 0, s>>>(counts, starts, block_sums, N);
-  k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nsb, starts + N);
-  k_scan_add<<<(int)((N + 255) / 256), 256, 0, s>>>(starts, block_sums, N, cursor);
-  if (mixed) k_scatter_mixed<<<nb, 256, 0, s>>>(M, MQ, keys, cursor);
-  else k_scatter_f64<<<nb, 256, 0, s>>>(P, Q, keys, cursor);
+  k_scan_blocks<<<nsb, 512, 0, s>>>(counts, starts, block_sums, N), ::ch::note_launch();
+  k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nsb, starts + N), ::ch::note_launch();
+  k_scan_add<<<(int)((N + 255) / 256), 256, 0, s>>>(starts, block_sums, N, cursor), ::ch::note_launch();
+  if (mixed) k_scatter_mixed<<<nb, 256, 0, s>>>(M, MQ, keys, cursor), ::ch::note_launch();
+  else k_scatter_f64<<<nb, 256, 0, s>>>(P, Q, keys, cursor), ::ch::note_launch();
 }
 
 }  // namespace ch

@@ -62,81 +62,94 @@ __device__ __forceinline__ void ch_boris(const StepConsts& c, const R E[3], R v[
   v[2] = vp2 + ts * E[2];
 }
 
-// Ion-neutral collision of one ion with probability pcol.
-// Returns 1 collided, 0 no collision, -1 refused (|v_f| > 10 vT or the
-// neutral sampler ran out of its 64 proposals).
+// Collisions of one ion over one step (src/particles.c:471-624 in its
+// many-ion limit): the ion's events form a Poisson process in the step's unit
+// time with rate lambda(v) = lscale g(|v - vn0|), lscale = Nc rho_n(x) / S.
+// Event e draws its exponential waiting time from Philox block e << 8 and
+// its neutral V ~ |v - V| N(V) from blocks (e << 8) | (1 + 2 it), (2 + 2 it);
+// the centre-of-mass scatter and the 10 vT refusal follow the reference.
+// Returns the accepted collisions; *refused counts refused events.
+#define CH_MAX_EVENTS 32
 template <typename R>
-__device__ __noinline__ int ch_collide(const StepConsts& c, uint32_t id, R pcol, R v[3]) {
-  const U4 r0 = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | 0u, c.run, c.seed_lo, c.seed_hi);
-  if (!(unitR<R>(r0.x) < pcol)) return 0;
+__device__ __noinline__ int ch_collide(const StepConsts& c, uint32_t id, R lscale, R v[3], unsigned* refused) {
   const R sig = R(c.vnT);
   const R vn0x = R(c.vn0[0]), vn0y = R(c.vn0[1]), vn0z = R(c.vn0[2]);
-  const R vix = v[0], viy = v[1], viz = v[2];
-  const R wx = vix - vn0x, wy = viy - vn0y, wz = viz - vn0z;
-  const R w = ch_sqrt(wx * wx + wy * wy + wz * wz);
   const R m1 = R(c.m1);
-  R Vx = 0, Vy = 0, Vz = 0, uz = 0, uphi = 0;
-  bool ok = false;
-  for (int it = 0; it < 64 && !ok; ++it) {
-    const U4 a = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (uint32_t)(1 + 2 * it), c.run, c.seed_lo,
-                           c.seed_hi);
-    const U4 b = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (uint32_t)(2 + 2 * it), c.run, c.seed_lo,
-                           c.seed_hi);
-    R nx, ny, nz;
-    if (unitR<R>(a.x) * (w + m1) < w) {
-      // plain Maxwellian proposal, Box-Muller
-      R s1, c1, s2, c2;
-      const R r1 = ch_sqrt(R(-2) * ch_log(unitR<R>(a.y)));
-      ch_sincos2pi(unitR<R>(a.z), &s1, &c1);
-      const R r2 = ch_sqrt(R(-2) * ch_log(unitR<R>(a.w)));
-      ch_sincos2pi(unitR<R>(b.x), &s2, &c2);
-      nx = sig * (r1 * c1); ny = sig * (r1 * s1); nz = sig * (r2 * c2);
-    } else {
-      // speed-biased proposal: |V - vn0|^2 / (2 sigma^2) ~ Gamma(2, 1)
-      const R s = sig * ch_sqrt(R(-2) * ch_log(unitR<R>(a.y) * unitR<R>(a.z)));
-      const R ct = R(2) * unitR<R>(a.w) - R(1);
-      R st = R(1) - ct * ct;
-      st = ch_sqrt(st > R(0) ? st : R(0));
-      R sp, cp;
-      ch_sincos2pi(unitR<R>(b.x), &sp, &cp);
-      nx = s * st * cp; ny = s * st * sp; nz = s * ct;
-    }
-    Vx = vn0x + nx; Vy = vn0y + ny; Vz = vn0z + nz;
-    const R dV = ch_sqrt(nx * nx + ny * ny + nz * nz);
-    const R rx = vix - Vx, ry = viy - Vy, rz = viz - Vz;
-    const R D = ch_sqrt(rx * rx + ry * ry + rz * rz);
-    if (unitR<R>(b.y) * (w + dV) < D) {
-      ok = true;
-      uz = R(2) * unitR<R>(b.z) - R(1);
-      uphi = unitR<R>(b.w);
-    }
-  }
-  if (!ok) return -1;
-  // centre-of-mass scatter (src/particles.c:552-591)
   const R mi = R(c.mi), mn = R(c.mn), M = mn + mi;
-  const R vrx = vix - Vx, vry = viy - Vy, vrz = viz - Vz;
-  const R vrr = ch_sqrt(vrx * vrx + vry * vry + vrz * vrz);
-  const R vcx = (vix * mi + Vx * mn) / M, vcy = (viy * mi + Vy * mn) / M, vcz = (viz * mi + Vz * mn) / M;
-  const R ax = vix - vcx, ay = viy - vcy, az = viz - vcz;
-  const R vcr = ch_sqrt(ax * ax + ay * ay + az * az);
-  R up = R(1) - uz * uz;
-  const R uperp = ch_sqrt(up > R(0) ? up : R(0));
-  R sph, cph;
-  ch_sincos2pi(uphi, &sph, &cph);
-  const R ux = uperp * cph, uy = uperp * sph;
-  const R costht = vrr > R(0) ? vrz / vrr : R(1);
-  R st2 = R(1) - costht * costht;
-  const R sintht = ch_sqrt(st2 > R(0) ? st2 : R(0));
-  R cosphi = R(1), sinphi = R(0);
-  if (vrr * sintht > R(0)) {
-    cosphi = vrx / (vrr * sintht);
-    sinphi = vry / (vrr * sintht);
+  R t = R(0);
+  int ncol = 0;
+  for (uint32_t e = 0; e < CH_MAX_EVENTS; ++e) {
+    const R vix = v[0], viy = v[1], viz = v[2];
+    const R wx = vix - vn0x, wy = viy - vn0y, wz = viz - vn0z;
+    const R w = ch_sqrt(wx * wx + wy * wy + wz * wz);
+    const R lam = lscale * ch_gmean<R>(w, sig);
+    if (!(lam > R(0))) break;
+    const U4 r0 = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (e << 8), c.run, c.seed_lo, c.seed_hi);
+    t += -ch_log(unitR<R>(r0.x)) / lam;
+    if (!(t < R(1))) break;
+    R Vx = 0, Vy = 0, Vz = 0, uz = 0, uphi = 0;
+    bool ok = false;
+    for (uint32_t it = 0; it < 64 && !ok; ++it) {
+      const U4 a = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (e << 8) | (1 + 2 * it), c.run, c.seed_lo,
+                             c.seed_hi);
+      const U4 b = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (e << 8) | (2 + 2 * it), c.run, c.seed_lo,
+                             c.seed_hi);
+      R nx, ny, nz;
+      if (unitR<R>(a.x) * (w + m1) < w) {
+        // plain Maxwellian proposal, Box-Muller
+        R s1, c1, s2, c2;
+        const R r1 = ch_sqrt(R(-2) * ch_log(unitR<R>(a.y)));
+        ch_sincos2pi(unitR<R>(a.z), &s1, &c1);
+        const R r2 = ch_sqrt(R(-2) * ch_log(unitR<R>(a.w)));
+        ch_sincos2pi(unitR<R>(b.x), &s2, &c2);
+        nx = sig * (r1 * c1); ny = sig * (r1 * s1); nz = sig * (r2 * c2);
+      } else {
+        // speed-weighted proposal: |V - vn0|^2 / (2 sigma^2) ~ Gamma(2, 1)
+        const R sp = sig * ch_sqrt(R(-2) * ch_log(unitR<R>(a.y) * unitR<R>(a.z)));
+        const R ct = R(2) * unitR<R>(a.w) - R(1);
+        R st = R(1) - ct * ct;
+        st = ch_sqrt(st > R(0) ? st : R(0));
+        R sph, cph;
+        ch_sincos2pi(unitR<R>(b.x), &sph, &cph);
+        nx = sp * st * cph; ny = sp * st * sph; nz = sp * ct;
+      }
+      Vx = vn0x + nx; Vy = vn0y + ny; Vz = vn0z + nz;
+      const R dV = ch_sqrt(nx * nx + ny * ny + nz * nz);
+      const R rx = vix - Vx, ry = viy - Vy, rz = viz - Vz;
+      const R D = ch_sqrt(rx * rx + ry * ry + rz * rz);
+      if (unitR<R>(b.y) * (w + dV) < D) {
+        ok = true;
+        uz = R(2) * unitR<R>(b.z) - R(1);
+        uphi = unitR<R>(b.w);
+      }
+    }
+    if (!ok) { ++*refused; continue; }
+    // centre-of-mass scatter (src/particles.c:552-591)
+    const R vrx = vix - Vx, vry = viy - Vy, vrz = viz - Vz;
+    const R vrr = ch_sqrt(vrx * vrx + vry * vry + vrz * vrz);
+    const R vcx = (vix * mi + Vx * mn) / M, vcy = (viy * mi + Vy * mn) / M, vcz = (viz * mi + Vz * mn) / M;
+    const R ax = vix - vcx, ay = viy - vcy, az = viz - vcz;
+    const R vcr = ch_sqrt(ax * ax + ay * ay + az * az);
+    R up = R(1) - uz * uz;
+    const R uperp = ch_sqrt(up > R(0) ? up : R(0));
+    R sph, cph;
+    ch_sincos2pi(uphi, &sph, &cph);
+    const R ux = uperp * cph, uy = uperp * sph;
+    const R costht = vrr > R(0) ? vrz / vrr : R(1);
+    R st2 = R(1) - costht * costht;
+    const R sintht = ch_sqrt(st2 > R(0) ? st2 : R(0));
+    R cosphi = R(1), sinphi = R(0);
+    if (vrr * sintht > R(0)) {
+      cosphi = vrx / (vrr * sintht);
+      sinphi = vry / (vrr * sintht);
+    }
+    const R ux1 = uz * sintht + ux * costht, uy1 = uy, uz1 = uz * costht - ux * sintht;
+    const R ux2 = ux1 * cosphi - uy1 * sinphi, uy2 = ux1 * sinphi + uy1 * cosphi, uz2 = uz1;
+    const R vfx = vcx + vcr * ux2, vfy = vcy + vcr * uy2, vfz = vcz + vcr * uz2;
+    const R vfr = ch_sqrt(vfx * vfx + vfy * vfy + vfz * vfz);
+    if (vfr / R(c.viTr) > R(10)) { ++*refused; continue; }
+    v[0] = vfx; v[1] = vfy; v[2] = vfz;
+    ++ncol;
   }
-  const R ux1 = uz * sintht + ux * costht, uy1 = uy, uz1 = uz * costht - ux * sintht;
-  const R ux2 = ux1 * cosphi - uy1 * sinphi, uy2 = ux1 * sinphi + uy1 * cosphi, uz2 = uz1;
-  const R vfx = vcx + vcr * ux2, vfy = vcy + vcr * uy2, vfz = vcz + vcr * uz2;
-  const R vfr = ch_sqrt(vfx * vfx + vfy * vfy + vfz * vfz);
-  if (vfr / R(c.viTr) > R(10)) return -1;
-  v[0] = vfx; v[1] = vfy; v[2] = vfz;
-  return 1;
+  return ncol;
 }

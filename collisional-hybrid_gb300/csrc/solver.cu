@@ -495,17 +495,17 @@ void PotentialSolver::release() {
 }
 
 double PotentialSolver::dot64(const double* a, const double* b, cudaStream_t s) {
-  k_dot64<<<nb_, 256, 0, s>>>(N_, a, b, part_);
-  k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_RR, scal_, 0.0);
+  k_dot64<<<nb_, 256, 0, s>>>(N_, a, b, part_), ::ch::note_launch();
+  k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_RR, scal_, 0.0), ::ch::note_launch();
   cudaMemcpyAsync(hscal_, scal_, sizeof(double) * S_NSLOT, cudaMemcpyDeviceToHost, s);
   cudaStreamSynchronize(s);
   return hscal_[S_RR];
 }
 
 void PotentialSolver::remove_mean64(double* v, cudaStream_t s) {
-  k_sum<double><<<nb_, 256, 0, s>>>(N_, v, part_);
-  k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_MEAN, scal_, 1.0 / (double)N_);
-  k_sub_mean<<<nb_, 256, 0, s>>>(N_, v, scal_);
+  k_sum<double><<<nb_, 256, 0, s>>>(N_, v, part_), ::ch::note_launch();
+  k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_MEAN, scal_, 1.0 / (double)N_), ::ch::note_launch();
+  k_sub_mean<<<nb_, 256, 0, s>>>(N_, v, scal_), ::ch::note_launch();
 }
 
 void PotentialSolver::build_rhs(const double* mom, double* b, cudaStream_t s) {
@@ -516,16 +516,16 @@ void PotentialSolver::build_rhs(const double* mom, double* b, cudaStream_t s) {
   const double R20 = Kx * Kz - Ky, R21 = Ky * Kz + Kx, R22 = 1 + Kz * Kz;
   if (p_.rhs_type != CH_RHS_FULL) {
     // mean density (VecMean, src/rhs.c:34,93)
-    k_sum<double><<<nb_, 256, 0, s>>>(N_, mom, part_);
-    k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_MEAN, scal_, 1.0 / (double)N_);
+    k_sum<double><<<nb_, 256, 0, s>>>(N_, mom, part_), ::ch::note_launch();
+    k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_MEAN, scal_, 1.0 / (double)N_), ::ch::note_launch();
   }
   k_rhs<<<nb_, 256, 0, s>>>(g_, p_.rhs_type, R00, R01, R02, R10, R11, R12, R20, R21, R22, det, p_.E0[0], p_.E0[1],
-                            p_.E0[2], p_.cth, p_.cG, (p_.faithful & CH_FAITHFUL_D8) != 0, mom, scal_, b);
+                            p_.E0[2], p_.cth, p_.cG, (p_.faithful & CH_FAITHFUL_D8) != 0, mom, scal_, b), ::ch::note_launch();
   if (p_.rhs_type != CH_RHS_CONSTANT) remove_mean64(b, s);  // MatNullSpaceRemove (src/rhs.c:294-296)
 }
 
 void PotentialSolver::apply64(const double* n, const double* x, double* y, cudaStream_t s) {
-  k_apply<double><<<nb_, 256, 0, s>>>(g_, dev_coefs<double>(c_), n, x, y, nullptr, nullptr);
+  k_apply<double><<<nb_, 256, 0, s>>>(g_, dev_coefs<double>(c_), n, x, y, nullptr, nullptr), ::ch::note_launch();
 }
 
 // Preconditioned Krylov solve of A x = b in precision T (x holds the start).
@@ -546,19 +546,19 @@ ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* 
   T* sh = f64 ? (T*)sh_ : (T*)sh32_;
   T* dinv = f64 ? (T*)dinv_ : (T*)dinv32_;
   const int nb = nb_;
-  k_jacobi<T><<<nb, 256, 0, s>>>(g, C, n, dinv, p_.pc_type == CH_PC_JACOBI);
+  k_jacobi<T><<<nb, 256, 0, s>>>(g, C, n, dinv, p_.pc_type == CH_PC_JACOBI), ::ch::note_launch();
   // ||b||
   if (zero_guess) {
-    k_zero<T><<<nb, 256, 0, s>>>(N, x);
-    k_copy<T><<<nb, 256, 0, s>>>(N, b, r);
-    k_prec_dot<T><<<nb, 256, 0, s>>>(N, dinv, r, z, part_);
+    k_zero<T><<<nb, 256, 0, s>>>(N, x), ::ch::note_launch();
+    k_copy<T><<<nb, 256, 0, s>>>(N, b, r), ::ch::note_launch();
+    k_prec_dot<T><<<nb, 256, 0, s>>>(N, dinv, r, z, part_), ::ch::note_launch();
   } else {
-    k_residual<T><<<nb, 256, 0, s>>>(g, C, n, b, x, r, part_);
-    k_prec_dot<T><<<nb, 256, 0, s>>>(N, dinv, r, z, part_);
+    k_residual<T><<<nb, 256, 0, s>>>(g, C, n, b, x, r, part_), ::ch::note_launch();
+    k_prec_dot<T><<<nb, 256, 0, s>>>(N, dinv, r, z, part_), ::ch::note_launch();
   }
-  k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_SET_RZ_RR, scal_, 0.0);
-  k_dot<T><<<nb, 256, 0, s>>>(N, b, b, part_);
-  k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_TMP, scal_, 0.0);
+  k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_SET_RZ_RR, scal_, 0.0), ::ch::note_launch();
+  k_dot<T><<<nb, 256, 0, s>>>(N, b, b, part_), ::ch::note_launch();
+  k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_TMP, scal_, 0.0), ::ch::note_launch();
   CH_CUDA_OK(cudaMemcpyAsync(hscal_, scal_, sizeof(double) * S_NSLOT, cudaMemcpyDeviceToHost, s));
   CH_CUDA_OK(cudaStreamSynchronize(s));
   const double bnorm = sqrt(hscal_[S_TMP]);
@@ -571,46 +571,46 @@ ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* 
     return CH_OK;
   }
   if (p_.ksp_type == CH_KSP_CG) {
-    k_cg_p<T><<<nb, 256, 0, s>>>(N, scal_, z, pp, 1);
+    k_cg_p<T><<<nb, 256, 0, s>>>(N, scal_, z, pp, 1), ::ch::note_launch();
     while (it < maxit) {
-      k_apply<T><<<nb, 256, 0, s>>>(g, C, n, pp, q, pp, part_);
-      k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_CG_ALPHA, scal_, 0.0);
-      k_cg_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, r, pp, q, dinv, z, part_);
-      k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_CG_BETA, scal_, 0.0);
+      k_apply<T><<<nb, 256, 0, s>>>(g, C, n, pp, q, pp, part_), ::ch::note_launch();
+      k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_CG_ALPHA, scal_, 0.0), ::ch::note_launch();
+      k_cg_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, r, pp, q, dinv, z, part_), ::ch::note_launch();
+      k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_CG_BETA, scal_, 0.0), ::ch::note_launch();
       ++it;
       CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_RR, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s));
       CH_CUDA_OK(cudaStreamSynchronize(s));
       rr = hscal_[S_RR];
       if (!(sqrt(rr) > tol)) break;
-      k_cg_p<T><<<nb, 256, 0, s>>>(N, scal_, z, pp, 0);
+      k_cg_p<T><<<nb, 256, 0, s>>>(N, scal_, z, pp, 0), ::ch::note_launch();
     }
   } else {
     // BiCGStab, right preconditioned (van der Vorst 1992)
-    k_copy<T><<<nb, 256, 0, s>>>(N, r, rh);
-    k_zero<T><<<nb, 256, 0, s>>>(N, pp);
-    k_zero<T><<<nb, 256, 0, s>>>(N, q);  // v
+    k_copy<T><<<nb, 256, 0, s>>>(N, r, rh), ::ch::note_launch();
+    k_zero<T><<<nb, 256, 0, s>>>(N, pp), ::ch::note_launch();
+    k_zero<T><<<nb, 256, 0, s>>>(N, q), ::ch::note_launch();  // v
     // rho = rh.r = r.r
     CH_CUDA_OK(cudaMemcpyAsync(scal_ + S_RHO, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToDevice, s));
     bool first = true;
     while (it < maxit) {
-      k_bi_p<T><<<nb, 256, 0, s>>>(N, scal_, r, pp, q, dinv, z, first ? 1 : 0);  // z = y
+      k_bi_p<T><<<nb, 256, 0, s>>>(N, scal_, r, pp, q, dinv, z, first ? 1 : 0), ::ch::note_launch();  // z = y
       first = false;
-      k_apply<T><<<nb, 256, 0, s>>>(g, C, n, z, q, rh, part_);                  // v = A y; rh.v
-      k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_BI_ALPHA, scal_, 0.0);
-      k_bi_s<T><<<nb, 256, 0, s>>>(N, scal_, r, q, dinv, sv, sh, part_);
-      k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_SS, scal_, 0.0);
+      k_apply<T><<<nb, 256, 0, s>>>(g, C, n, z, q, rh, part_), ::ch::note_launch();                  // v = A y; rh.v
+      k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_BI_ALPHA, scal_, 0.0), ::ch::note_launch();
+      k_bi_s<T><<<nb, 256, 0, s>>>(N, scal_, r, q, dinv, sv, sh, part_), ::ch::note_launch();
+      k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_SS, scal_, 0.0), ::ch::note_launch();
       ++it;
       CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_SS, scal_ + S_SS, sizeof(double), cudaMemcpyDeviceToHost, s));
       CH_CUDA_OK(cudaStreamSynchronize(s));
       if (!(sqrt(hscal_[S_SS]) > tol)) {
-        k_bi_half<T><<<nb, 256, 0, s>>>(N, scal_, x, z, r, sv);
+        k_bi_half<T><<<nb, 256, 0, s>>>(N, scal_, x, z, r, sv), ::ch::note_launch();
         rr = hscal_[S_SS];
         break;
       }
-      k_apply_dot2<T><<<nb, 256, 0, s>>>(g, C, n, sh, tv, sv, part_);
-      k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_OMEGA, scal_, 0.0);
-      k_bi_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, z, sh, r, sv, tv, rh, part_);
-      k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_BETA, scal_, 0.0);
+      k_apply_dot2<T><<<nb, 256, 0, s>>>(g, C, n, sh, tv, sv, part_), ::ch::note_launch();
+      k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_OMEGA, scal_, 0.0), ::ch::note_launch();
+      k_bi_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, z, sh, r, sv, tv, rh, part_), ::ch::note_launch();
+      k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_BETA, scal_, 0.0), ::ch::note_launch();
       CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_RR, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s));
       CH_CUDA_OK(cudaStreamSynchronize(s));
       rr = hscal_[S_RR];
@@ -640,8 +640,8 @@ ch_status PotentialSolver::solve_fp64(const double* n, const double* b, double* 
   if (rc) return rc;
   if (singular) remove_mean64(phi, s);
   // true residual
-  k_residual<double><<<nb_, 256, 0, s>>>(g_, dev_coefs<double>(c_), n, b, phi, r_, part_);
-  k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_RR, scal_, 0.0);
+  k_residual<double><<<nb_, 256, 0, s>>>(g_, dev_coefs<double>(c_), n, b, phi, r_, part_), ::ch::note_launch();
+  k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_RR, scal_, 0.0), ::ch::note_launch();
   CH_CUDA_OK(cudaMemcpyAsync(hscal_, scal_, sizeof(double) * S_NSLOT, cudaMemcpyDeviceToHost, s));
   CH_CUDA_OK(cudaStreamSynchronize(s));
   st->iterations = its;
@@ -656,7 +656,7 @@ ch_status PotentialSolver::solve_fp64(const double* n, const double* b, double* 
 ch_status PotentialSolver::solve_mixed(const double* n, const double* b, double* phi, SolveStats* st,
                                        cudaStream_t s) {
   const DevCoefs<double> C64 = dev_coefs<double>(c_);
-  k_down<<<nb_, 256, 0, s>>>(N_, n, 1.0, n32_);
+  k_down<<<nb_, 256, 0, s>>>(N_, n, 1.0, n32_), ::ch::note_launch();
   remove_mean64(phi, s);
   const double bnorm = sqrt(dot64(b, b, s));
   st->bnorm = bnorm;
@@ -665,20 +665,20 @@ ch_status PotentialSolver::solve_mixed(const double* n, const double* b, double*
   int total = 0, ref = 0;
   double rn = 0.0;
   for (; ref < 50; ++ref) {
-    k_residual<double><<<nb_, 256, 0, s>>>(g_, C64, n, b, phi, r_, part_);
-    k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_RR, scal_, 0.0);
+    k_residual<double><<<nb_, 256, 0, s>>>(g_, C64, n, b, phi, r_, part_), ::ch::note_launch();
+    k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_RR, scal_, 0.0), ::ch::note_launch();
     CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_RR, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s));
     CH_CUDA_OK(cudaStreamSynchronize(s));
     rn = sqrt(hscal_[S_RR]);
     if (rn <= tol || rn == 0.0) break;
     const double sc = 1.0 / rn;
-    k_down<<<nb_, 256, 0, s>>>(N_, r_, sc, b32_);
+    k_down<<<nb_, 256, 0, s>>>(N_, r_, sc, b32_), ::ch::note_launch();
     int its = 0;
     double rin = 0.0;
     ch_status rc = krylov<float>(g_, n32_, b32_, x32_, inner_rtol, p_.ksp_max_it, true, &its, &rin, s);
     if (rc) return rc;
     total += its;
-    k_up_add<<<nb_, 256, 0, s>>>(N_, x32_, rn, phi);
+    k_up_add<<<nb_, 256, 0, s>>>(N_, x32_, rn, phi), ::ch::note_launch();
     remove_mean64(phi, s);
   }
   st->iterations = total;

@@ -192,6 +192,26 @@ ch_status ch_get_rhs(ch_ctx* c, double* out);   /* ctx->rhs after the last RHS b
 /* y = A(n) x with the current operator (matrix-free ComputeFullLHS). */
 ch_status ch_apply_operator(ch_ctx* c, const double* x, double* y);
 
+/* Per-phase device timing (CUDA events on the context's stream) and the
+ * number of kernels this library launched, for profiling hosts.  No
+ * counterpart in the reference (its only timing is src/hybrid.c:133-137). */
+typedef struct ch_profile {
+  double pass_ms;      /* ion passes (push / move / deposit, fused or not) */
+  int64_t pass_calls;
+  double solve_ms;     /* RHS + Krylov solve */
+  int64_t solve_calls;
+  double sort_ms;      /* counting sort by cell */
+  int64_t sort_calls;
+  double moments_ms;   /* fixed-point -> FP64 moment conversion */
+  int64_t moments_calls;
+  int64_t launches;    /* kernels launched by this library, all contexts */
+} ch_profile;
+ch_status ch_set_profiling(ch_ctx* c, int32_t enable);
+ch_status ch_get_profile(ch_ctx* c, ch_profile* out);
+ch_status ch_reset_profile(ch_ctx* c);
+/* The cudaStream_t every call of this context is ordered on. */
+ch_status ch_get_stream(ch_ctx* c, void** stream);
+
 /* Page-locks caller memory so that the copies of upload/download run at
  * full link speed (no counterpart in the reference: its arrays never leave
  * the host). */

@@ -108,6 +108,7 @@ static double inv_cdf_x(const ch_loader* L, double Lx, double u) {
 
 int orc_load(const ch_params* p, const ch_loader* L, orc_particles* P) {
   grid g = mkgrid(p);
+#pragma omp parallel for num_threads(g_threads) schedule(static)
   for (int64_t i = 0; i < P->np; ++i) {
     uint32_t a[4], b[4];
     draw(p, (uint32_t)i, STEP_LOADER, PURPOSE_LOAD, 0, a);
@@ -198,19 +199,18 @@ void orc_node_efield(const ch_params* p, const double* phi, double* Ex, double* 
 }
 
 /* ------------------------------------------------------------------ */
-/* Collisions.
+/* Collisions (src/particles.c:471-624).
  *
- * The reference (src/particles.c:471-624) draws Nc accepted events: ion i
- * uniformly, a Maxwellian neutral V, acceptance with probability
- * min(1, |v_i - V|/vrm).  Each accepted event therefore lands on ion i with
- * probability g_i / sum_j g_j, g = E_V|v - V|, and carries the neutral V
- * drawn from the density proportional to |v_i - V| N(V).  The per-ion form
- * used here collides ion i with probability
- *     p_i = min(1, Nc g_i rho_n(x_i) / S),  S = sum_j g_j,
- * keyed by Philox(id, step), then samples V from that same conditional
- * density by rejection, and scatters with the reference's centre-of-mass
- * rule and 10 vT refusal (src/particles.c:552-611).  S uses the velocities
- * the ions carry into the step. */
+ * The reference draws Nc accepted events: ion i uniformly, a Maxwellian
+ * neutral V, acceptance with probability min(1, |v_i - V|/vrm); it repeats
+ * until Nc events are accepted, so one ion may collide more than once.
+ * Each accepted event lands on ion i with probability g_i / sum_j g_j,
+ * g = E_V|v - V|, and carries a neutral drawn from the density proportional
+ * to |v_i - V| N(V).  The per-ion form used here (collide_ion) runs each
+ * ion's events as a Poisson process of rate Nc g(v) rho_n(x) / S over the
+ * step, S = sum_j g_j over the velocities the ions carry into the step,
+ * keyed by Philox(id, step), with the same neutral law and the reference's
+ * centre-of-mass scatter and 10 vT refusal. */
 double orc_gmean(double w, double sigma) {
   if (sigma <= 0.0) return w;
   double a = w / (sigma * sqrt(2.0));
@@ -249,66 +249,85 @@ static double neutral_density(const ch_params* p, double x) {
   return v > p->nn_floor ? v : p->nn_floor;
 }
 
-/* Returns 1 = collided, 0 = no collision, -1 = refused. */
-static int collide_one(const ch_params* p, uint32_t id, uint32_t step, double pcol, double* vx,
-                       double* vy, double* vz) {
-  uint32_t r[4];
-  draw(p, id, step, PURPOSE_COLLIDE, 0, r);
-  if (!(unit(r[0]) < pcol)) return 0;
+/* Collisions of one ion over one step.  The ion's events form a Poisson
+ * process in the step's unit time with the state-dependent rate
+ *     lambda(v) = lscale * g(|v - vn0|),  lscale = Nc rho_n(x) / S,
+ * which is the many-ion limit of the reference's sequential sampler (each
+ * of its Nc accepted events picks ion i with probability g_i / sum_j g_j
+ * at the current velocities, with replacement).  Exponential waiting times
+ * come from Philox block (e << 8); the neutral of event e is drawn from the
+ * density proportional to |v - V| N(V) by the speed-weighted proposal with
+ * blocks (e << 8) | (1 + 2 it), (e << 8) | (2 + 2 it).  Refused events
+ * (|v_f| > 10 vT, src/particles.c:597-606) leave v unchanged.
+ * Returns the number of accepted collisions; *refused counts refusals. */
+#define MAX_EVENTS 32
+static int collide_ion(const ch_params* p, uint32_t id, uint32_t step, double lscale, double* vx, double* vy,
+                       double* vz, int* refused) {
   const double sig = p->vnT;
-  const double vix = *vx, viy = *vy, viz = *vz;
-  double wx = vix - p->vn0[0], wy = viy - p->vn0[1], wz = viz - p->vn0[2];
-  double w = sqrt(wx * wx + wy * wy + wz * wz);
-  double m1 = 2.0 * sig * sqrt(2.0 / PI);
-  double Vx = 0, Vy = 0, Vz = 0, uz = 0, uphi = 0;
-  int ok = 0;
-  for (int it = 0; it < 64 && !ok; ++it) {
-    uint32_t a[4], c[4];
-    draw(p, id, step, PURPOSE_COLLIDE, 1 + 2 * it, a);
-    draw(p, id, step, PURPOSE_COLLIDE, 2 + 2 * it, c);
-    double nx, ny, nz;
-    if (unit(a[0]) * (w + m1) < w) {
-      double r1 = sqrt(-2.0 * log(unit(a[1]))), t1 = 2.0 * PI * unit(a[2]);
-      double r2 = sqrt(-2.0 * log(unit(a[3]))), t2 = 2.0 * PI * unit(c[0]);
-      nx = sig * (r1 * cos(t1)); ny = sig * (r1 * sin(t1)); nz = sig * (r2 * cos(t2));
-    } else {
-      double s = sig * sqrt(-2.0 * log(unit(a[1]) * unit(a[2])));
-      double ct = 2.0 * unit(a[3]) - 1.0, st = sqrt(fmax(0.0, 1.0 - ct * ct));
-      double ph = 2.0 * PI * unit(c[0]);
-      nx = s * st * cos(ph); ny = s * st * sin(ph); nz = s * ct;
-    }
-    Vx = p->vn0[0] + nx; Vy = p->vn0[1] + ny; Vz = p->vn0[2] + nz;
-    double dV = sqrt(nx * nx + ny * ny + nz * nz);
-    double rx = vix - Vx, ry = viy - Vy, rz = viz - Vz;
-    double D = sqrt(rx * rx + ry * ry + rz * rz);
-    if (unit(c[1]) * (w + dV) < D) {
-      ok = 1;
-      uz = 2.0 * unit(c[2]) - 1.0;
-      uphi = 2.0 * PI * unit(c[3]);
-    }
-  }
-  if (!ok) return -1;
-  /* centre-of-mass scatter (src/particles.c:552-591) */
+  const double m1 = 2.0 * sig * sqrt(2.0 / PI);
+  const double viTr = sqrt(p->viT[0] * p->viT[0] + p->viT[1] * p->viT[1] + p->viT[2] * p->viT[2]);
   const double mi = p->mi, mn = p->mn, M = mn + mi;
-  double vrx = vix - Vx, vry = viy - Vy, vrz = viz - Vz;
-  double vrr = sqrt(vrx * vrx + vry * vry + vrz * vrz);
-  double vcx = (vix * mi + Vx * mn) / M, vcy = (viy * mi + Vy * mn) / M, vcz = (viz * mi + Vz * mn) / M;
-  double ax = vix - vcx, ay = viy - vcy, az = viz - vcz;
-  double vcr = sqrt(ax * ax + ay * ay + az * az);
-  double uperp = sqrt(fmax(0.0, 1.0 - uz * uz));
-  double ux = uperp * cos(uphi), uy = uperp * sin(uphi);
-  double costht = vrr > 0.0 ? vrz / vrr : 1.0;
-  double sintht = sqrt(fmax(0.0, 1.0 - costht * costht));
-  double cosphi = 1.0, sinphi = 0.0;
-  if (vrr * sintht > 0.0) { cosphi = vrx / (vrr * sintht); sinphi = vry / (vrr * sintht); }
-  double ux1 = uz * sintht + ux * costht, uy1 = uy, uz1 = uz * costht - ux * sintht;
-  double ux2 = ux1 * cosphi - uy1 * sinphi, uy2 = ux1 * sinphi + uy1 * cosphi, uz2 = uz1;
-  double vfx = vcx + vcr * ux2, vfy = vcy + vcr * uy2, vfz = vcz + vcr * uz2;
-  double viTr = sqrt(p->viT[0] * p->viT[0] + p->viT[1] * p->viT[1] + p->viT[2] * p->viT[2]);
-  double vfr = sqrt(vfx * vfx + vfy * vfy + vfz * vfz);
-  if (vfr / viTr > 10.0) return -1;
-  *vx = vfx; *vy = vfy; *vz = vfz;
-  return 1;
+  double t = 0.0;
+  int ncol = 0;
+  for (uint32_t e = 0; e < MAX_EVENTS; ++e) {
+    const double vix = *vx, viy = *vy, viz = *vz;
+    const double wx = vix - p->vn0[0], wy = viy - p->vn0[1], wz = viz - p->vn0[2];
+    const double w = sqrt(wx * wx + wy * wy + wz * wz);
+    const double lam = lscale * orc_gmean(w, sig);
+    if (!(lam > 0.0)) break;
+    uint32_t r[4];
+    draw(p, id, step, PURPOSE_COLLIDE, e << 8, r);
+    t += -log(unit(r[0])) / lam;
+    if (!(t < 1.0)) break;
+    double Vx = 0, Vy = 0, Vz = 0, uz = 0, uphi = 0;
+    int ok = 0;
+    for (uint32_t it = 0; it < 64 && !ok; ++it) {
+      uint32_t a[4], c[4];
+      draw(p, id, step, PURPOSE_COLLIDE, (e << 8) | (1 + 2 * it), a);
+      draw(p, id, step, PURPOSE_COLLIDE, (e << 8) | (2 + 2 * it), c);
+      double nx, ny, nz;
+      if (unit(a[0]) * (w + m1) < w) {
+        double r1 = sqrt(-2.0 * log(unit(a[1]))), t1 = 2.0 * PI * unit(a[2]);
+        double r2 = sqrt(-2.0 * log(unit(a[3]))), t2 = 2.0 * PI * unit(c[0]);
+        nx = sig * (r1 * cos(t1)); ny = sig * (r1 * sin(t1)); nz = sig * (r2 * cos(t2));
+      } else {
+        double sp = sig * sqrt(-2.0 * log(unit(a[1]) * unit(a[2])));
+        double ct = 2.0 * unit(a[3]) - 1.0, st = sqrt(fmax(0.0, 1.0 - ct * ct));
+        double ph = 2.0 * PI * unit(c[0]);
+        nx = sp * st * cos(ph); ny = sp * st * sin(ph); nz = sp * ct;
+      }
+      Vx = p->vn0[0] + nx; Vy = p->vn0[1] + ny; Vz = p->vn0[2] + nz;
+      double dV = sqrt(nx * nx + ny * ny + nz * nz);
+      double rx = vix - Vx, ry = viy - Vy, rz = viz - Vz;
+      double D = sqrt(rx * rx + ry * ry + rz * rz);
+      if (unit(c[1]) * (w + dV) < D) {
+        ok = 1;
+        uz = 2.0 * unit(c[2]) - 1.0;
+        uphi = 2.0 * PI * unit(c[3]);
+      }
+    }
+    if (!ok) { (*refused)++; continue; }
+    /* centre-of-mass scatter (src/particles.c:552-591) */
+    double vrx = vix - Vx, vry = viy - Vy, vrz = viz - Vz;
+    double vrr = sqrt(vrx * vrx + vry * vry + vrz * vrz);
+    double vcx = (vix * mi + Vx * mn) / M, vcy = (viy * mi + Vy * mn) / M, vcz = (viz * mi + Vz * mn) / M;
+    double ax = vix - vcx, ay = viy - vcy, az = viz - vcz;
+    double vcr = sqrt(ax * ax + ay * ay + az * az);
+    double uperp = sqrt(fmax(0.0, 1.0 - uz * uz));
+    double ux = uperp * cos(uphi), uy = uperp * sin(uphi);
+    double costht = vrr > 0.0 ? vrz / vrr : 1.0;
+    double sintht = sqrt(fmax(0.0, 1.0 - costht * costht));
+    double cosphi = 1.0, sinphi = 0.0;
+    if (vrr * sintht > 0.0) { cosphi = vrx / (vrr * sintht); sinphi = vry / (vrr * sintht); }
+    double ux1 = uz * sintht + ux * costht, uy1 = uy, uz1 = uz * costht - ux * sintht;
+    double ux2 = ux1 * cosphi - uy1 * sinphi, uy2 = ux1 * sinphi + uy1 * cosphi, uz2 = uz1;
+    double vfx = vcx + vcr * ux2, vfy = vcy + vcr * uy2, vfz = vcz + vcr * uz2;
+    double vfr = sqrt(vfx * vfx + vfy * vfy + vfz * vfz);
+    if (vfr / viTr > 10.0) { (*refused)++; continue; }
+    *vx = vfx; *vy = vfy; *vz = vfz;
+    ncol++;
+  }
+  return ncol;
 }
 
 /* ------------------------------------------------------------------ */
@@ -373,12 +392,11 @@ int orc_update_velocities(const ch_params* p, const double* phi, orc_particles* 
     if (collide) {
       double wx = vx - p->vn0[0], wy = vy - p->vn0[1], wz = vz - p->vn0[2];
       double gi = orc_gmean(sqrt(wx * wx + wy * wy + wz * wz), p->vnT);
-      double pc = sbar > 0.0 ? ((double)Nc * gi * neutral_density(p, P->x[ip])) / sbar : 0.0;
-      if (pc > 1.0) pc = 1.0;
-      expct += pc;
-      int rc = collide_one(p, (uint32_t)ip, (uint32_t)step, pc, &vx, &vy, &vz);
-      if (rc > 0) ncol++;
-      else if (rc < 0) nref++;
+      double lscale = sbar > 0.0 ? ((double)Nc * neutral_density(p, P->x[ip])) / sbar : 0.0;
+      expct += lscale * gi;
+      int nr = 0;
+      ncol += collide_ion(p, (uint32_t)ip, (uint32_t)step, lscale, &vx, &vy, &vz, &nr);
+      nref += nr;
       double qx = vx - p->vn0[0], qy = vy - p->vn0[1], qz = vz - p->vn0[2];
       snext += orc_gmean(sqrt(qx * qx + qy * qy + qz * qz), p->vnT);
     }
@@ -475,8 +493,10 @@ static void kappa_tensor(const ch_params* p, double R[3][3], double* det) {
 
 static void remove_mean(double* b, int64_t N) {
   double s = 0.0;
+#pragma omp parallel for num_threads(g_threads) reduction(+ : s) schedule(static)
   for (int64_t i = 0; i < N; ++i) s += b[i];
   s /= (double)N;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
   for (int64_t i = 0; i < N; ++i) b[i] -= s;
 }
 
@@ -626,16 +646,29 @@ void orc_lhs_row(const ch_params* p, const double* n, int i, int j, int k, doubl
 void orc_apply(const ch_params* p, const double* n, const double* x, double* y) {
   grid g = mkgrid(p);
   coefs C = full_coefs(p, &g);
+  const int64_t X = g.Nx, XY = (int64_t)g.Nx * g.Ny;
 #pragma omp parallel for num_threads(g_threads) collapse(2) schedule(static)
   for (int k = 0; k < g.Nz; ++k)
-    for (int j = 0; j < g.Ny; ++j)
+    for (int j = 0; j < g.Ny; ++j) {
+      const int kp = k + 1 == g.Nz ? 0 : k + 1, km = k == 0 ? g.Nz - 1 : k - 1;
+      const int jp = j + 1 == g.Ny ? 0 : j + 1, jm = j == 0 ? g.Ny - 1 : j - 1;
       for (int i = 0; i < g.Nx; ++i) {
+        const int ip = i + 1 == g.Nx ? 0 : i + 1, im = i == 0 ? g.Nx - 1 : i - 1;
+        /* natural indices of the 19 stencil points in ComputeInteriorStencil order */
+        const int64_t c[19] = {k * XY + j * X + ip,   k * XY + j * X + im,   k * XY + jp * X + i,
+                               k * XY + jm * X + i,   kp * XY + j * X + i,   km * XY + j * X + i,
+                               k * XY + jp * X + ip,  k * XY + jm * X + ip,  k * XY + jp * X + im,
+                               k * XY + jm * X + im,  kp * XY + j * X + ip,  km * XY + j * X + ip,
+                               kp * XY + j * X + im,  km * XY + j * X + im,  kp * XY + jp * X + i,
+                               km * XY + jp * X + i,  kp * XY + jm * X + i,  km * XY + jm * X + i,
+                               k * XY + j * X + i};
         double v[19];
         row_values(p, &g, &C, n, i, j, k, v);
         double acc = 0.0;
-        for (int s = 0; s < 19; ++s) acc += v[s] * x[nid(&g, i + OFF[s][0], j + OFF[s][1], k + OFF[s][2])];
-        y[nid(&g, i, j, k)] = acc;
+        for (int s2 = 0; s2 < 19; ++s2) acc += v[s2] * x[c[s2]];
+        y[c[18]] = acc;
       }
+    }
 }
 
 static double dot(const double* a, const double* b, int64_t N) {
@@ -673,23 +706,27 @@ int orc_solve(const ch_params* p, const double* n, const double* b, double* phi,
   double tol = fmax(rtol * bn, p->ksp_atol);
   if (singular) remove_mean(phi, N);
   orc_apply(p, n, phi, q);
+  #pragma omp parallel for num_threads(g_threads) schedule(static)
   for (int64_t i = 0; i < N; ++i) r[i] = b[i] - q[i];
   double rn = sqrt(dot(r, r, N));
   int it = 0, rc = 0;
 #define PREC(dst, src)                                            \
   do {                                                            \
+    _Pragma("omp parallel for num_threads(g_threads) schedule(static)") \
     for (int64_t i_ = 0; i_ < N; ++i_) (dst)[i_] = jac ? (src)[i_] * dinv[i_] : (src)[i_]; \
     if (singular) remove_mean((dst), N);                          \
   } while (0)
   if (rn > tol) {
     if (p->ksp_type == CH_KSP_CG) {
       PREC(z, r);
+      #pragma omp parallel for num_threads(g_threads) schedule(static)
       for (int64_t i = 0; i < N; ++i) pp[i] = z[i];
       double rz = dot(r, z, N);
       while (it < maxit) {
         orc_apply(p, n, pp, q);
         double pq = dot(pp, q, N);
         double alpha = rz / pq;
+        #pragma omp parallel for num_threads(g_threads) schedule(static)
         for (int64_t i = 0; i < N; ++i) { phi[i] += alpha * pp[i]; r[i] -= alpha * q[i]; }
         ++it;
         rn = sqrt(dot(r, r, N));
@@ -698,10 +735,12 @@ int orc_solve(const ch_params* p, const double* n, const double* b, double* phi,
         double rz2 = dot(r, z, N);
         double beta = rz2 / rz;
         rz = rz2;
+        #pragma omp parallel for num_threads(g_threads) schedule(static)
         for (int64_t i = 0; i < N; ++i) pp[i] = z[i] + beta * pp[i];
       }
     } else {
       /* BiCGStab (van der Vorst 1992), right preconditioned */
+      #pragma omp parallel for num_threads(g_threads) schedule(static)
       for (int64_t i = 0; i < N; ++i) { rh[i] = r[i]; pp[i] = 0.0; sv[i] = 0.0; }
       double rho = 1.0, alpha = 1.0, omega = 1.0;
       double* vv = sv; /* v vector */
@@ -716,15 +755,19 @@ int orc_solve(const ch_params* p, const double* n, const double* b, double* phi,
         if (rho1 == 0.0) break;
         double beta = (rho1 / rho) * (alpha / omega);
         rho = rho1;
+        #pragma omp parallel for num_threads(g_threads) schedule(static)
         for (int64_t i = 0; i < N; ++i) pp[i] = r[i] + beta * (pp[i] - omega * vvec[i]);
         PREC(y, pp);
         orc_apply(p, n, y, vvec);
         alpha = rho / dot(rh, vvec, N);
+        #pragma omp parallel for num_threads(g_threads) schedule(static)
         for (int64_t i = 0; i < N; ++i) s[i] = r[i] - alpha * vvec[i];
         ++it;
         double sn = sqrt(dot(s, s, N));
         if (sn <= tol) {
+          #pragma omp parallel for num_threads(g_threads) schedule(static)
           for (int64_t i = 0; i < N; ++i) phi[i] += alpha * y[i];
+          #pragma omp parallel for num_threads(g_threads) schedule(static)
           for (int64_t i = 0; i < N; ++i) r[i] = s[i];
           rn = sn;
           break;
@@ -732,6 +775,7 @@ int orc_solve(const ch_params* p, const double* n, const double* b, double* phi,
         PREC(sh, s);
         orc_apply(p, n, sh, ts);
         omega = dot(ts, s, N) / dot(ts, ts, N);
+        #pragma omp parallel for num_threads(g_threads) schedule(static)
         for (int64_t i = 0; i < N; ++i) {
           phi[i] += alpha * y[i] + omega * sh[i];
           r[i] = s[i] - omega * ts[i];
@@ -746,6 +790,7 @@ int orc_solve(const ch_params* p, const double* n, const double* b, double* phi,
   if (singular) remove_mean(phi, N);
   /* true residual */
   orc_apply(p, n, phi, q);
+  #pragma omp parallel for num_threads(g_threads) schedule(static)
   for (int64_t i = 0; i < N; ++i) r[i] = b[i] - q[i];
   rn = sqrt(dot(r, r, N));
   if (rn > tol * 1.0000001 && rn > 0.0) rc = CH_ERR_NOT_CONVERGED;
