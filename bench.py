@@ -1,0 +1,407 @@
+#!/usr/bin/env python3
+"""Throughput of the hybrid-PIC step (ion push + collisions + move + CIC
+deposit + 19-point potential solve) on one GB300, as particle-steps/s.
+
+Default workload: 128^3 periodic grid, unit spacing, 64 ions/cell
+(134,217,728 ions), Maxwellian ions (vT = 1 per component), B = z (Omega_i
+= 1), E_x = 1.0, nu = 0.5, equal-mass neutrals at Ti, density
+1 + 0.02 sum_m sin(2 pi m x/Lx + phi_m) (3 seeded random-phase modes),
+dt = 0.05, mixed precision (FP32 ions and inner solves, FP64 refinement
+to rtol 1e-10).  Seeded synthetic plasma generated on the device.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the FP64 CPU restatement of the same step (the
+reference's PETSc code does not build here) on the host cores.  Under
+torchrun each rank runs an independent replica (the step does not shard:
+replicas only) and rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "particle-steps/s incl. potential solve"
+UNIT = "particle-steps/s"
+
+WORKLOADS = {
+    "128cubed-64ppc-mixed": dict(N=(128, 128, 128), ppc=64, E0=(1.0, 0.0, 0.0), nu=0.5, amp=0.02, modes=3,
+                                 rtol=1e-10, precision="mixed", drift=(0.0, 0.0, 0.0), nn=False),
+    "128cubed-64ppc-fp64": dict(N=(128, 128, 128), ppc=64, E0=(1.0, 0.0, 0.0), nu=0.5, amp=0.02, modes=3,
+                                rtol=1e-10, precision="fp64", drift=(0.0, 0.0, 0.0), nn=False),
+    "64cubed-32ppc-mixed": dict(N=(64, 64, 64), ppc=32, E0=(0.5, 0.1, 0.0), nu=0.3, amp=0.02, modes=3,
+                                rtol=1e-10, precision="mixed", drift=(0.0, 0.0, 0.0), nn=False),
+    "32cubed-16ppc-fp64": dict(N=(32, 32, 32), ppc=16, E0=(0.5, 0.0, 0.0), nu=0.1, amp=0.01, modes=1,
+                               rtol=1e-8, precision="fp64", drift=(0.0, 0.0, 0.0), nn=False),
+    "256x256x64-32ppc-mixed": dict(N=(256, 256, 64), ppc=32, E0=(0.8, 0.0, 0.0), nu=1.0, amp=0.0, modes=0,
+                                   rtol=1e-10, precision="mixed", drift=(0.0, 0.3, 0.0), nn=True),
+}
+DEFAULT = "128cubed-64ppc-mixed"
+
+
+def chy():
+    return importlib.import_module("collisional-hybrid_gb300")
+
+
+def make_params(w, seed=1, run=0):
+    m = chy()
+    N = w["N"]
+    kw = dict(precision=m.PRECISION[w["precision"]], E0=w["E0"], nui=w["nu"], ksp_rtol=w["rtol"], seed=seed,
+              run=run, vi0=w["drift"], pc_type=m.PC["jacobi"])
+    if w["nn"]:
+        kw.update(nn_profile=1, nn_center=N[0] / 2.0, nn_sigma=N[0] / 6.0, nn_floor=0.1)
+    return m.params_for(N, **kw)
+
+
+def make_loader(w, seed=1, run=0):
+    m = chy()
+    amp = [0.0, 0.0, 0.0]
+    ph = [0.0, 0.0, 0.0]
+    if w["modes"] == 1:
+        amp[0] = w["amp"]
+    elif w["modes"] == 3:
+        amp = [w["amp"]] * 3
+        ph = m.mode_phases(seed, run)
+    return m.loader(amp=tuple(amp), phase=tuple(ph), v0=w["drift"], vT=(1.0, 1.0, 1.0))
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read only)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ GPU arm
+def measured_peak():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic(kernel: str):
+    """dram bytes per launch from the committed ncu summary, if present."""
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+class DeviceTimer:
+    """CUDA events on the library's stream."""
+
+    def __init__(self, h):
+        import torch
+
+        self.torch = torch
+        self.stream = torch.cuda.ExternalStream(h.stream_handle())
+
+    def event(self):
+        e = self.torch.cuda.Event(enable_timing=True)
+        e.record(self.stream)
+        return e
+
+
+def ions_for(w):
+    return w["N"][0] * w["N"][1] * w["N"][2] * w["ppc"]
+
+
+def run_gpu(args, w, rank, world, dist):
+    m = chy()
+    import torch
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    np_ = ions_for(w)
+    p = make_params(w, seed=1 + rank, run=rank)
+    h = m.Hybrid(p, device=dev)
+    h.load(np_, make_loader(w, seed=1 + rank, run=rank))
+    h.CollectVlasovQuantities(copy=False)
+    h.ComputePotential(copy=False)
+    step = 0
+    for _ in range(args.warmup):
+        h.step(step, 1)
+        step += 1
+    timer = DeviceTimer(h)
+    h.set_profiling(True)
+    h.reset_profile()
+    launches0 = h.profile()["launches"]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    infos = []
+    with ClockSampler(dev) as clk:
+        e0 = timer.event()
+        for _ in range(args.steps):
+            infos.append(h.step(step, 1))
+            step += 1
+        e1 = timer.event()
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    prof = h.profile()
+    h.set_profiling(False)
+    launches = prof["launches"] - launches0
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    res = dict(ms=ms, prof=prof, launches=launches, infos=infos, clocks=clk.summary(), np=np_, step=step)
+    # end to end through the C ABI with host buffers (rank-local)
+    if not args.no_e2e:
+        res["e2e"] = e2e(args, h, w, step)
+    h.close()
+    return res
+
+
+def e2e(args, h, w, step):
+    """Per step: host->device copy of the ions (DMSwarm RealVector arrays,
+    pinned), the step, device->host copy of the ions and phi."""
+    m = chy()
+    import torch
+
+    pos, vel = h.download()
+    phi = np.empty(h.N)
+    for a in (pos, vel, phi):
+        m.host_register(a)
+    K = max(1, min(args.steps, args.e2e_steps))
+    try:
+        h.upload(pos, vel)
+        h.step(step, 1)
+        h.download(pos, vel)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s in range(K):
+            h.upload(pos, vel)
+            h.step(step + 1 + s, 1)
+            h.download(pos, vel)
+            phi[:] = h.phi()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    finally:
+        for a in (pos, vel, phi):
+            m.host_unregister(a)
+    Bi = pos.nbytes + vel.nbytes
+    Bo = pos.nbytes + vel.nbytes + phi.nbytes
+    return {"value": h.np * K / dt, "unit": UNIT, "h2d_bytes_per_step": int(Bi), "d2h_bytes_per_step": int(Bo),
+            "steps": K, "ms_per_step": 1e3 * dt / K}
+
+
+# ------------------------------------------------------------------ CPU arm
+def cpu_sample(w, threads, np_sample, steps, warmup):
+    """FP64 CPU restatement of the step on the host cores: particle phases
+    timed on np_sample ions, the potential solve on the full grid;
+    particle-steps/s of the full workload = Np / (t_ion * Np / np_sample +
+    t_solve)."""
+    from oracle import pyoracle as po
+
+    po.build()
+    po.lib().orc_set_threads(threads)
+    p = make_params(w)
+    q = po.params_from(p)
+    q.precision = 0
+    L = make_loader(w)
+    ions = po.load(q, po.make_loader(amp=tuple(L.amp), phase=tuple(L.phase), v0=tuple(L.v0), vT=tuple(L.vT)),
+                   np_sample)
+    run = po.Run(q, ions)
+    rc, _ = run.initialize()
+    N = q.Nx * q.Ny * q.Nz
+    t_ion, t_solve = [], []
+    for s in range(warmup + steps):
+        t0 = time.perf_counter()
+        rc, snext, _ = po.update_velocities(q, run.phi, ions, s, run.s.sbar)
+        run.s.sbar = snext
+        po.update_positions(q, ions)
+        po.collect(q, ions, nodes=run.nodes)
+        t1 = time.perf_counter()
+        b = po.rhs(q, run.nodes)
+        phi, info = po.solve(q, run.nodes[0::4].copy(), b, phi0=run.phi)
+        run.phi[:] = phi
+        t2 = time.perf_counter()
+        if s >= warmup:
+            t_ion.append(t1 - t0)
+            t_solve.append(t2 - t1)
+    Np = ions_for(w)
+    per_ion = statistics.mean(t_ion) / np_sample
+    ts = statistics.mean(t_solve)
+    value = Np / (per_ion * Np + ts)
+    return dict(value=value, per_ion_s=per_ion, solve_s=ts, threads=threads, np_sample=np_sample, N=N)
+
+
+def cpu_desc(c, w):
+    return (f"FP64 CPU restatement (OpenMP, {c['threads']} threads): ion phases timed on {c['np_sample']:,} ions "
+            f"of the {w['N'][0]}x{w['N'][1]}x{w['N'][2]} grid, full-grid potential solve; scaled to "
+            f"{ions_for(w):,} ions as Np/(t_ion*Np + t_solve)")
+
+
+# ------------------------------------------------------------------ main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-ions", type=int, default=1 << 22)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form comparison line")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        dist.init_process_group("gloo")
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank == 0:
+            c = cpu_sample(w, threads, args.cpu_ions, max(1, args.steps), max(0, min(args.warmup, 1)))
+            line = {"metric": METRIC, "value": c["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                    "warmup": args.warmup, "ms_per_step": 1e3 * ions_for(w) / c["value"],
+                    "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                    "data": "synthetic", "impl": "reference",
+                    "config": {"workload": args.workload, "grid": list(w["N"]), "ions": ions_for(w),
+                               "precision": "fp64"},
+                    "cpu_baseline": {"value": c["value"], "unit": UNIT, "cores": threads, "kind": "port",
+                                     "sample": cpu_desc(c, w)},
+                    "e2e": {"value": c["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            print(json.dumps(line), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    r = run_gpu(args, w, rank, world, dist)
+    fp64 = None
+    if not args.no_fp64 and w["precision"] == "mixed" and rank == 0:
+        w64 = dict(w, precision="fp64")
+        a64 = argparse.Namespace(**vars(args))
+        a64.steps, a64.warmup, a64.no_e2e = max(2, min(args.steps, 5)), 1, True
+        r64 = run_gpu(a64, w64, 0, 1, None)
+        fp64 = {"value": r64["np"] * a64.steps / (r64["ms"] / 1e3), "unit": UNIT,
+                "ms_per_step": r64["ms"] / a64.steps, "steps": a64.steps}
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    K = args.steps
+    ms_step = r["ms"] / K
+    value = r["np"] * world * K / (r["ms"] / 1e3)
+    prof = r["prof"]
+    peak, peak_kind = measured_peak()
+    pass_ms = prof["pass_ms"] / max(1, prof["pass_calls"])
+    N = w["N"][0] * w["N"][1] * w["N"][2]
+    bytes_ion = 64 if w["precision"] == "mixed" else 104
+    grid_bytes = N * (16 + 32) if w["precision"] == "mixed" else N * (24 + 32)
+    alg = r["np"] * bytes_ion + grid_bytes
+    achieved = alg / (pass_ms / 1e3) / 1e9
+    kname = "k_pass_mixed" if w["precision"] == "mixed" else "k_pass_f64"
+    tr = committed_traffic(kname)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if w["precision"] == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "grid": list(w["N"]), "ions": r["np"], "ions_per_cell": w["ppc"],
+                   "precision": w["precision"], "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "l2": "inputs larger than L2 (ion state 4.3 GB)", "ksp_rtol": w["rtol"]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "kernel": kname, "algorithmic_bytes_per_launch": alg,
+                     "avg_launch_ms": pass_ms,
+                     "traffic": (tr * (r["np"] / tr.get("ions", r["np"])) if isinstance(tr, (int, float)) else
+                                 (tr.get("bytes_per_launch") if isinstance(tr, dict) else None))},
+        "phase_ms_per_step": {k.replace("_ms", ""): prof[k] / K for k in ("pass_ms", "solve_ms", "sort_ms",
+                                                                          "moments_ms")},
+        "solve": {"iterations_last": r["infos"][-1]["iterations"], "refinements_last": r["infos"][-1]["refinements"],
+                  "rel_residual_last": r["infos"][-1]["rnorm"] / max(r["infos"][-1]["bnorm"], 1e-300)},
+        "collisions_last": {"Nc": r["infos"][-1]["Nc"], "events": r["infos"][-1]["collisions"]},
+        "gpu_launches": int(r["launches"]),
+        "clocks": r["clocks"],
+    }
+    if fp64:
+        line["fp64_form"] = fp64
+        line["mixed_over_fp64"] = value / world / fp64["value"]
+    if "e2e" in r:
+        e = r["e2e"]
+        line["e2e"] = {k: e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")}
+        line["e2e"]["value"] *= world
+        line["e2e"]["ms_per_step"] = e["ms_per_step"]
+    if not args.no_cpu:
+        c = cpu_sample(w, os.cpu_count() or 1, args.cpu_ions, 1, 0)
+        line["cpu_baseline"] = {"value": c["value"], "unit": UNIT, "cores": c["threads"], "kind": "port",
+                                "sample": cpu_desc(c, w)}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -65,7 +65,27 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if r.returncode:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
+    build_host()
     return OUT
+
+
+HOST = os.path.join(HERE, "host")
+DRIVER = os.path.join(HERE, "hybrid_gpu")
+
+
+def build_host() -> str:
+    """The C driver mirroring src/hybrid.c over the C ABI (plain C, gcc)."""
+    srcs = [os.path.join(HOST, "hybrid_gpu.c"), os.path.join(HOST, "ch_options.c")]
+    if not _stale(DRIVER, srcs + [os.path.join(HOST, "ch_options.h"), OUT]):
+        return DRIVER
+    cc = shutil.which("gcc") or shutil.which("cc")
+    cmd = [cc, "-O2", "-std=c11", "-Wall", "-I", os.path.join(REPO, "include"), "-I", HOST, *srcs, "-o", DRIVER,
+           "-L", HERE, "-lchybrid", f"-Wl,-rpath,{HERE}", "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        sys.stderr.write(r.stdout + r.stderr)
+        raise RuntimeError("host driver build failed")
+    return DRIVER
 
 
 if __name__ == "__main__":

@@ -42,6 +42,8 @@ typedef int MPI_Comm;
 #define PETSC_ERR_ARG_UNKNOWN_TYPE 86
 #define PETSC_ERR_ARG_INCOMP 75
 #define PETSC_ERR_SIG 59
+#define PETSC_ERR_SUP 56
+#define PETSC_ERR_LIB 76
 
 typedef enum { INSERT_VALUES = 1, ADD_VALUES = 2 } InsertMode;
 typedef enum { MAT_FLUSH_ASSEMBLY = 1, MAT_FINAL_ASSEMBLY = 0 } MatAssemblyType;
@@ -83,6 +85,7 @@ int ch_standin_error(int code, const char* func, const char* fmt, ...);
 #define PetscRealPart(x) (x)
 #define PetscImaginaryPart(x) (0.0)
 
+int MPI_Comm_size(MPI_Comm comm, PetscMPIInt* size);
 PetscErrorCode PetscPrintf(MPI_Comm comm, const char* fmt, ...);
 PetscErrorCode PetscSynchronizedPrintf(MPI_Comm comm, const char* fmt, ...);
 PetscErrorCode PetscSynchronizedFlush(MPI_Comm comm, FILE* f);

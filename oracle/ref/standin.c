@@ -33,6 +33,7 @@ PetscErrorCode PetscPrintf(MPI_Comm c, const char* fmt, ...) {
   }
   return 0;
 }
+int MPI_Comm_size(MPI_Comm comm, PetscMPIInt* size) { (void)comm; *size = 1; return 0; }
 PetscErrorCode PetscSynchronizedPrintf(MPI_Comm c, const char* fmt, ...) { (void)c; (void)fmt; return 0; }
 PetscErrorCode PetscSynchronizedFlush(MPI_Comm c, FILE* f) { (void)c; (void)f; return 0; }
 PetscErrorCode PetscStrcmp(const char* a, const char* b, PetscBool* flg) {

@@ -114,8 +114,9 @@ def test_rhs_matches_reference(chy, po, golden, tag, ki, kappa, rt):
     ref = golden[f"{tag}_rhs{rt}_k{ki}"]
     # scale of the terms before the mean is removed: the sinusoidal RHS of a
     # unit-spacing grid is a constant whose remainder is pure rounding
-    scale = max(np.abs(ref).max(), 1e-12 * np.abs(nodes[0::4]).mean() * 2 * np.prod(np.array(
-        [p.x1 / p.Nx, p.y1 / p.Ny, p.z1 / p.Nz])))
+    det = 1.0 + float(np.sum(np.square(kappa)))
+    scale = max(np.abs(ref).max(), np.abs(nodes[0::4]).mean() * 2 * np.prod(np.array(
+        [p.x1 / p.Nx, p.y1 / p.Ny, p.z1 / p.Nz])) / det)
     assert np.abs(b - ref).max() <= 1e-12 * scale + 1e-14, (np.abs(b - ref).max(), scale)
 
 

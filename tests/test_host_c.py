@@ -1,0 +1,104 @@
+"""The C host side: option parsing (ProcessOptions names and derivations),
+the PETSc drop-in's compilation against the reference's own headers, and
+the C driver mirroring src/hybrid.c (GPU)."""
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import pytest
+
+from conftest import REPO
+
+HOST = os.path.join(REPO, "collisional-hybrid_gb300", "host")
+PKG = os.path.join(REPO, "collisional-hybrid_gb300")
+
+
+@pytest.fixture(scope="module")
+def optlib(chy):
+    chy.lib()
+    d = tempfile.mkdtemp()
+    so = os.path.join(d, "libchopts.so")
+    subprocess.run(["gcc", "-O1", "-shared", "-fPIC", "-std=c11", "-I", os.path.join(REPO, "include"), "-I", HOST,
+                    os.path.join(HOST, "ch_options.c"), "-o", so, "-L", PKG, "-lchybrid", f"-Wl,-rpath,{PKG}",
+                    "-lm"], check=True)
+    L = C.CDLL(so)
+    L.ch_parse_options.restype = C.c_int32
+    return L
+
+
+class RunOpts(C.Structure):
+    _fields_ = [("Nt", C.c_int32), ("Np", C.c_int64), ("density_type", C.c_int32), ("amp", C.c_double * 3),
+                ("phase", C.c_double * 3), ("random_phases", C.c_int32), ("verbose", C.c_int32)]
+
+
+def parse(optlib, chy, args):
+    argv = ["hybrid"] + args
+    arr = (C.c_char_p * len(argv))(*[a.encode() for a in argv])
+    p = chy.Params()
+    r = RunOpts()
+    err = C.create_string_buffer(256)
+    rc = optlib.ch_parse_options(len(argv), arr, C.byref(p), C.byref(r), err, 256)
+    return rc, p, r, err.value.decode()
+
+
+def test_reference_option_names_and_derivations(optlib, chy):
+    # the 32^3 case in the reference's option names (run-case style)
+    rc, p, r, err = parse(optlib, chy, ["-Nx", "32", "-Ny", "32", "-Nz", "32", "-x1", "32", "-y1", "32", "-z1",
+                                        "32", "-Np", "524288", "-viT", "1", "-B0z", "1", "-E0x", "0.5", "-nui",
+                                        "0.1", "-dt", "0.05", "-Nt", "100", "-ksp_rtol", "1e-8",
+                                        "--lhs-type", "full", "--rhs-type", "full", "-ksp_type", "bcgs"])
+    assert rc == 0, err
+    assert (p.Nx, p.Ny, p.Nz) == (32, 32, 32) and p.x1 == 32.0
+    assert r.Np == 524288 and r.Nt == 100
+    assert p.nui == 0.1 and p.dt == 0.05 and p.E0[0] == 0.5 and p.B0[2] == 1.0
+    assert tuple(p.viT) == (1.0, 1.0, 1.0)
+    # Ti = m vT.r^2 / 2 (src/parameters.c:537), Tn = Ti, vnT = sqrt(2 Tn / mn) (:556)
+    assert abs(p.vnT - (2 * 1.5) ** 0.5) < 1e-15
+    # electron magnetisation |q B / m| / nu (src/parameters.c:519-528)
+    assert abs(p.kappa_e[2] - 1836.15267343) < 1e-6
+    assert p.ksp_rtol == 1e-8 and p.ksp_type == 1
+    assert p.lhs_type == 2 and p.rhs_type == 2
+
+
+def test_defaults_and_extensions(optlib, chy):
+    rc, p, r, err = parse(optlib, chy, ["-nui", "4", "-ch_vnT", "1", "-ch_precision", "mixed", "-ch_pc", "mg",
+                                        "-ch_seed", "7", "-ch_faithful", "256", "-ch_amp1", "0.02"])
+    assert rc == 0, err
+    assert p.dt == 0.25  # dt = 1/nu (src/parameters.c:417)
+    assert (p.Nx, p.Ny, p.Nz) == (7, 7, 7) and r.Np == 343  # src/setup.c:10-12, 44-46
+    assert p.vnT == 1.0 and p.precision == 1 and p.pc_type == 2 and p.seed == 7 and p.faithful == 256
+    assert r.amp[0] == 0.02
+
+
+def test_rejects_unsupported_options(optlib, chy):
+    rc, p, r, err = parse(optlib, chy, ["--x0-bc", "neumann"])
+    assert rc == -1 and "periodic" in err
+    rc, p, r, err = parse(optlib, chy, ["--lhs-type", "bogus"])
+    assert rc == -1
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/src"), reason="reference headers not present")
+def test_petsc_dropin_compiles_against_reference_headers():
+    with tempfile.TemporaryDirectory() as d:
+        r = subprocess.run(["gcc", "-std=gnu11", "-Wall", "-Werror", "-Wno-unused-function", "-DCH_WITH_PETSC",
+                            "-I", os.path.join(REPO, "oracle", "ref", "shim"), "-I", "/root/reference/src",
+                            "-I", os.path.join(REPO, "include"), "-c", os.path.join(HOST, "petsc_dropin.c"),
+                            "-o", os.path.join(d, "dropin.o")], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        syms = subprocess.run(["nm", os.path.join(d, "dropin.o")], capture_output=True, text=True).stdout
+        for f in ("UpdateVelocities", "UpdatePositions", "CollectVlasovQuantities", "ComputePotential"):
+            assert f" T {f}" in syms
+
+
+@pytest.mark.gpu
+def test_c_driver_runs_reference_loop(chy):
+    exe = os.path.join(PKG, "hybrid_gpu")
+    r = subprocess.run([exe, "-Nx", "16", "-Ny", "16", "-Nz", "16", "-x1", "16", "-y1", "16", "-z1", "16",
+                        "-Np", "65536", "-viT", "1", "-B0z", "1", "-E0x", "0.5", "-nui", "0.1", "-dt", "0.05",
+                        "-Nt", "5", "-ch_vnT", "1", "-ch_cth", "1", "-ch_cG", "0.1", "-ch_kappa_ez", "0",
+                        "-ch_amp1", "0.01", "-ksp_rtol", "1e-8"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("Time step")]
+    assert len(lines) == 5
+    assert "Elapsed time" in r.stdout
