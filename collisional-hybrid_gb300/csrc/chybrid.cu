@@ -327,10 +327,10 @@ static ch_status ensure_staging(ch_ctx* c) {
   return CH_OK;
 }
 
-static void do_sort(ch_ctx* c) {
+static void do_sort(ch_ctx* c, bool have_hist = false) {
   prof_begin(c);
   launch_sort(c->mixed, c->g, c->P, c->Q, c->M, c->MQ, c->counts, c->starts, c->cursor, c->keys, c->block_sums,
-              c->sms, c->stream);
+              have_hist, c->sms, c->stream);
   prof_end(c, &c->pr.sort_ms, &c->pr.sort_calls);
   std::swap(c->P, c->Q);
   std::swap(c->M, c->MQ);
@@ -387,7 +387,7 @@ extern "C" ch_status ch_particles_download(ch_ctx* c, ch_real_vector* pos, ch_re
 }
 
 // ------------------------------------------------------------------ phases
-static ch_status run_pass(ch_ctx* c, int phases, int64_t step, ch_step_info* info) {
+static ch_status run_pass(ch_ctx* c, int phases, int64_t step, ch_step_info* info, bool count_cells = false) {
   StepConsts k = consts(c, step);
   const bool push = (phases & PH_PUSH) != 0;
   int64_t Nc = 0;
@@ -398,8 +398,13 @@ static ch_status run_pass(ch_ctx* c, int phases, int64_t step, ch_step_info* inf
   }
   if (phases & PH_DEPOSIT) CH_CUDA_OK(cudaMemsetAsync(&c->cnt->range_error, 0, sizeof(int), c->stream));
   prof_begin(c);
+  uint32_t* hist = nullptr;
+  if (count_cells && c->mixed) {
+    CH_CUDA_OK(cudaMemsetAsync(c->counts, 0, sizeof(uint32_t) * c->g.N, c->stream));
+    hist = c->counts;
+  }
   const int nb = launch_pass(c->mixed, phases, k, c->P, c->M, c->E64, c->E32, c->phi, c->acc, (double)Nc, c->sbar,
-                             c->cnt, c->part, c->sms, c->stream);
+                             c->cnt, c->part, c->starts, hist, c->sms, c->stream);
   prof_end(c, &c->pr.pass_ms, &c->pr.pass_calls);
   if (push) {
     launch_reduce_partials(c->part, nb, 2, c->red, c->stream);
@@ -531,13 +536,14 @@ extern "C" ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_s
   ch_step_info local;
   for (int32_t s = 0; s < nsteps; ++s) {
     memset(&local, 0, sizeof(local));
-    ch_status rc = run_pass(c, PH_PUSH | PH_MOVE | PH_DEPOSIT, first_step + s, &local);
+    const bool sort_due = c->p.sort_period > 0 && c->since_sort + 1 >= c->p.sort_period;
+    ch_status rc = run_pass(c, PH_PUSH | PH_MOVE | PH_DEPOSIT, first_step + s, &local, sort_due);
     if (rc) return rc;
     rc = finalize_moments(c, &local);
     if (rc) return rc;
     rc = potential(c, &local.solve);
     if (rc) return rc;
-    if (c->p.sort_period > 0 && c->since_sort >= c->p.sort_period) do_sort(c);
+    if (sort_due) do_sort(c, c->mixed);
   }
   CH_CUDA_OK(cudaStreamSynchronize(c->stream));
   if (info) *info = local;

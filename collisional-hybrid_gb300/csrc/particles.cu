@@ -58,6 +58,20 @@ __device__ __forceinline__ void deposit_cic(const GridDesc& g, unsigned long lon
   }
 }
 
+// Warp-aggregated increment of counts[key]; returns this lane's rank among
+// the lanes that share its key, and the group's base from the atomic.
+__device__ __forceinline__ uint32_t agg_inc(uint32_t* counts, uint32_t key, bool active) {
+  const unsigned mask = __activemask();
+  const unsigned grp = __match_any_sync(mask, active ? key : 0xFFFFFFFFu);
+  const int leader = __ffs(grp) - 1;
+  const int lane = threadIdx.x & 31;
+  const uint32_t rank = __popc(grp & ((1u << lane) - 1u));
+  uint32_t base = 0;
+  if (active && lane == leader) base = atomicAdd(counts + key, (uint32_t)__popc(grp));
+  base = __shfl_sync(mask, base, leader);
+  return base + rank;
+}
+
 // Block-wide sum of K doubles into part[blockIdx.x * K + q], fixed order.
 template <int K>
 __device__ __forceinline__ void block_partials(double (&v)[K], double* __restrict__ part) {
@@ -384,58 +398,151 @@ __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, 
   }
 }
 
-// ------------------------------------------------------------------ mixed pass
+// ------------------------------------------------------------------ mixed pass, tiled
+// The ions are sorted by cell; starts[c] is the first slot of cell c at the
+// last sort.  One CTA owns a brick of TX x TY x TZ cells (persistent loop
+// over bricks): it stages the node field of the brick plus a one-cell halo
+// in shared memory, pushes the brick's ions (any ion still within one cell
+// of its brick gathers from shared memory), and deposits into a shared
+// fixed-point tile that is flushed to the global accumulators once per
+// brick.  Within a warp, lanes whose ions share a cell are summed with
+// integer warp reductions before one lane updates the shared tile.  Ions
+// that left the halo, or move faster than CH_TILE_VMAX cells/dt units, take
+// the direct global path.  Every sum is an integer sum, so the moments do
+// not depend on the order of the ions or of the threads.
+#define TX 16
+#define TY 4
+#define TZ 4
+#define BX (TX + 3)
+#define BY (TY + 3)
+#define BZ (TZ + 3)
+#define BNODES (BX * BY * BZ)
+#define CH_TILE_DSCALE 16777216.0f   // 2^24: density contributions (w <= 1)
+#define CH_TILE_FSCALE 1048576.0f    // 2^20: flux contributions (|v| < CH_TILE_VMAX)
+#define CH_TILE_VMAX 32.0f
+
+struct TileShared {
+  float4 E[BNODES];
+  long long acc[4][BNODES];
+  uint32_t rowbeg[TY * TZ];
+  uint32_t pre[TY * TZ + 1];
+};
+
 template <int PH>
-__global__ void __launch_bounds__(256) k_pass_mixed(StepConsts c, MixParticles P, const float4* __restrict__ E,
-                                                    unsigned long long* __restrict__ acc, float pscale,
-                                                    DevCounters* cnt, double* part) {
+__global__ void __launch_bounds__(256, 2)
+    k_pass_tiled(StepConsts c, MixParticles P, const float4* __restrict__ E, const uint32_t* __restrict__ starts,
+                 unsigned long long* __restrict__ acc, float pscale, int shift_d, int shift_f, DevCounters* cnt,
+                 double* part, uint32_t* hist) {
+  extern __shared__ __align__(16) unsigned char smem_tiled[];
+  TileShared& sh = *reinterpret_cast<TileShared*>(smem_tiled);
   const GridDesc& g = c.g;
+  const int lane = threadIdx.x & 31;
   double vsum[2] = {0.0, 0.0};
   unsigned ncol = 0, nref = 0;
   int bad = 0;
   const float dtx = (float)(c.dt / g.dx), dty = (float)(c.dt / g.dy), dtz = (float)(c.dt / g.dz);
   const float vnTf = (float)c.vnT, vn0x = (float)c.vn0[0], vn0y = (float)c.vn0[1], vn0z = (float)c.vn0[2];
-  const float scale = (float)c.dep_scale;
-  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
-    float4 p = P.pos[ip];
-    float4 vv = P.vel[ip];
-    uint32_t cell = __float_as_uint(p.w);
-    int i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1), k = cell >> (CH_PACK_BX + CH_PACK_BY);
-    float v[3] = {vv.x, vv.y, vv.z};
-    if (PH & PH_PUSH) {
-      const int i1 = i + 1 == g.Nx ? 0 : i + 1, j1 = j + 1 == g.Ny ? 0 : j + 1, k1 = k + 1 == g.Nz ? 0 : k + 1;
-      const int64_t r00 = ((int64_t)k * g.Ny + j) * g.Nx, r10 = ((int64_t)k * g.Ny + j1) * g.Nx,
-                    r01 = ((int64_t)k1 * g.Ny + j) * g.Nx, r11 = ((int64_t)k1 * g.Ny + j1) * g.Nx;
-      const float4 e000 = __ldg(E + r00 + i), e100 = __ldg(E + r00 + i1), e010 = __ldg(E + r10 + i),
-                   e110 = __ldg(E + r10 + i1), e001 = __ldg(E + r01 + i), e101 = __ldg(E + r01 + i1),
-                   e011 = __ldg(E + r11 + i), e111 = __ldg(E + r11 + i1);
-      const float wx = p.x, wy = p.y, wz = p.z;
-      float Ef[3];
-#define LERP3(f)                                                                   \
+  const float t0 = (float)c.t[0], t1 = (float)c.t[1], t2 = (float)c.t[2];
+  const float s0 = (float)c.s[0], s1 = (float)c.s[1], s2 = (float)c.s[2];
+  const float pE0x = (float)(c.E0[0] * c.tscale), pE0y = (float)(c.E0[1] * c.tscale),
+              pE0z = (float)(c.E0[2] * c.tscale);
+  const bool cross = !(c.faithful & CH_FAITHFUL_D2);
+  const bool move = (PH & PH_MOVE) && !(c.faithful & CH_FAITHFUL_D5);
+  const int ntx = (g.Nx + TX - 1) / TX, nty = (g.Ny + TY - 1) / TY, ntz = (g.Nz + TZ - 1) / TZ;
+  const int ntiles = ntx * nty * ntz;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int i0 = (tile % ntx) * TX, j0 = ((tile / ntx) % nty) * TY, k0 = (tile / (ntx * nty)) * TZ;
+    const int i1 = min(i0 + TX, g.Nx), j1 = min(j0 + TY, g.Ny), k1 = min(k0 + TZ, g.Nz);
+    const int bi0 = i0 - 1, bj0 = j0 - 1, bk0 = k0 - 1;  // box origin (node)
+    __syncthreads();  // previous brick's flush is done
+    // stage the node field, clear the deposit tile, row ranges
+    for (int q = threadIdx.x; q < BNODES; q += blockDim.x) {
+      const int bi = q % BX, bj = (q / BX) % BY, bk = q / (BX * BY);
+      if (PH & PH_PUSH) {
+        const int gi = ch_wrap(bi0 + bi, g.Nx), gj = ch_wrap(bj0 + bj, g.Ny), gk = ch_wrap(bk0 + bk, g.Nz);
+        sh.E[q] = __ldg(E + ((int64_t)gk * g.Ny + gj) * g.Nx + gi);
+      }
+      if (PH & PH_DEPOSIT) {
+        sh.acc[0][q] = 0; sh.acc[1][q] = 0; sh.acc[2][q] = 0; sh.acc[3][q] = 0;
+      }
+    }
+    if (threadIdx.x == 0) {
+      uint32_t tot = 0;
+      int r = 0;
+      for (int tk = k0; tk < k0 + TZ; ++tk)
+        for (int tj = j0; tj < j0 + TY; ++tj, ++r) {
+          sh.pre[r] = tot;
+          if (tk < k1 && tj < j1) {
+            const int64_t cf = ((int64_t)tk * g.Ny + tj) * g.Nx + i0;
+            const uint32_t b = starts[cf], e = starts[cf + (i1 - i0)];
+            sh.rowbeg[r] = b;
+            tot += e - b;
+          } else {
+            sh.rowbeg[r] = 0;
+          }
+        }
+      sh.pre[TY * TZ] = tot;
+    }
+    __syncthreads();
+    const uint32_t total = sh.pre[TY * TZ];
+    for (uint32_t base = 0; base < total; base += blockDim.x) {
+      const uint32_t idx = base + threadIdx.x;
+      const bool active = idx < total;
+      int64_t ip = 0;
+      if (active) {
+        int r = 0;
+#pragma unroll
+        for (int st = 8; st > 0; st >>= 1)
+          if (r + st < TY * TZ && sh.pre[r + st] <= idx) r += st;
+        ip = (int64_t)sh.rowbeg[r] + (idx - sh.pre[r]);
+      }
+      float4 p = make_float4(0.f, 0.f, 0.f, 0.f), vv = make_float4(0.f, 0.f, 0.f, 0.f);
+      int i = 0, j = 0, k = 0;
+      float v[3] = {0.f, 0.f, 0.f};
+      if (active) {
+        p = P.pos[ip];
+        vv = P.vel[ip];
+        const uint32_t cell = __float_as_uint(p.w);
+        i = cell & (CH_MAX_NX - 1); j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1); k = cell >> (CH_PACK_BX + CH_PACK_BY);
+        v[0] = vv.x; v[1] = vv.y; v[2] = vv.z;
+      }
+      if ((PH & PH_PUSH) && active) {
+        int di = i - bi0, dj = j - bj0, dk = k - bk0;
+        di += di < 0 ? g.Nx : 0; di -= di >= g.Nx ? g.Nx : 0;
+        dj += dj < 0 ? g.Ny : 0; dj -= dj >= g.Ny ? g.Ny : 0;
+        dk += dk < 0 ? g.Nz : 0; dk -= dk >= g.Nz ? g.Nz : 0;
+        float4 e000, e100, e010, e110, e001, e101, e011, e111;
+        if (di <= BX - 2 && dj <= BY - 2 && dk <= BZ - 2) {
+          const int q = (dk * BY + dj) * BX + di;
+          e000 = sh.E[q]; e100 = sh.E[q + 1]; e010 = sh.E[q + BX]; e110 = sh.E[q + BX + 1];
+          e001 = sh.E[q + BX * BY]; e101 = sh.E[q + BX * BY + 1]; e011 = sh.E[q + BX * BY + BX];
+          e111 = sh.E[q + BX * BY + BX + 1];
+        } else {
+          const int ii1 = i + 1 == g.Nx ? 0 : i + 1, jj1 = j + 1 == g.Ny ? 0 : j + 1, kk1 = k + 1 == g.Nz ? 0 : k + 1;
+          const int64_t r00 = ((int64_t)k * g.Ny + j) * g.Nx, r10 = ((int64_t)k * g.Ny + jj1) * g.Nx,
+                        r01 = ((int64_t)kk1 * g.Ny + j) * g.Nx, r11 = ((int64_t)kk1 * g.Ny + jj1) * g.Nx;
+          e000 = __ldg(E + r00 + i); e100 = __ldg(E + r00 + ii1); e010 = __ldg(E + r10 + i);
+          e110 = __ldg(E + r10 + ii1); e001 = __ldg(E + r01 + i); e101 = __ldg(E + r01 + ii1);
+          e011 = __ldg(E + r11 + i); e111 = __ldg(E + r11 + ii1);
+        }
+        const float wx = p.x, wy = p.y, wz = p.z;
+        float Ef[3];
+#define LERP3(f, d)                                                                \
   {                                                                                \
     const float wll = e000.f + wy * (e010.f - e000.f);                             \
     const float wlh = e100.f + wy * (e110.f - e100.f);                             \
     const float whl = e001.f + wy * (e011.f - e001.f);                             \
     const float whh = e101.f + wy * (e111.f - e101.f);                             \
     const float ezl = wll + wx * (wlh - wll), ezh = whl + wx * (whh - whl);        \
-    Ef_##f = ezl + wz * (ezh - ezl);                                               \
+    Ef[d] = ezl + wz * (ezh - ezl);                                                \
   }
-      float Ef_x, Ef_y, Ef_z;
-      LERP3(x) LERP3(y) LERP3(z)
+        LERP3(x, 0) LERP3(y, 1) LERP3(z, 2)
 #undef LERP3
-      // E is stored premultiplied by (q/m) dt/2; the Boris helper multiplies
-      // by tscale, so divide it back out through a unit scale.
-      Ef[0] = Ef_x; Ef[1] = Ef_y; Ef[2] = Ef_z;
-      if (c.push_E0) {
-        Ef[0] += (float)(c.E0[0] * c.tscale); Ef[1] += (float)(c.E0[1] * c.tscale); Ef[2] += (float)(c.E0[2] * c.tscale);
-      }
-      {
-        // Boris with pre-scaled E (ts = 1)
-        float vm0 = v[0] + Ef[0], vm1 = v[1] + Ef[1], vm2 = v[2] + Ef[2];
+        if (c.push_E0) { Ef[0] += pE0x; Ef[1] += pE0y; Ef[2] += pE0z; }
+        // Boris (src/particles.c:374-447) with E premultiplied by (q/m) dt/2
+        const float vm0 = v[0] + Ef[0], vm1 = v[1] + Ef[1], vm2 = v[2] + Ef[2];
         float vp0 = vm0, vp1 = vm1, vp2 = vm2;
-        if (!(c.faithful & CH_FAITHFUL_D2)) {
-          const float t0 = (float)c.t[0], t1 = (float)c.t[1], t2 = (float)c.t[2];
-          const float s0 = (float)c.s[0], s1 = (float)c.s[1], s2 = (float)c.s[2];
+        if (cross) {
           const float q0 = vm0 + (vm1 * t2 - vm2 * t1);
           const float q1 = vm1 + (vm2 * t0 - vm0 * t2);
           const float q2 = vm2 + (vm0 * t1 - vm1 * t0);
@@ -444,44 +551,96 @@ __global__ void __launch_bounds__(256) k_pass_mixed(StepConsts c, MixParticles P
           vp2 = vm2 + (q0 * s1 - q1 * s0);
         }
         v[0] = vp0 + Ef[0]; v[1] = vp1 + Ef[1]; v[2] = vp2 + Ef[2];
+        if (c.collide) {
+          const float wx2 = v[0] - vn0x, wy2 = v[1] - vn0y, wz2 = v[2] - vn0z;
+          const float gi = ch_gmean<float>(sqrtf(wx2 * wx2 + wy2 * wy2 + wz2 * wz2), vnTf);
+          float nd = 1.0f;
+          if (c.nn_profile == CH_NN_GAUSSIAN_X)
+            nd = ch_neutral_density<float>(c, (float)(g.x0 + ((double)i + (double)p.x) * g.dx));
+          const float lscale = pscale * nd;
+          const float lam = lscale * gi;
+          vsum[0] += (double)lam;
+          const uint32_t id = __float_as_uint(vv.w);
+          const U4 r0 = ch_philox(id, c.step, CH_PURPOSE_COLLIDE << 24, c.run, c.seed_lo, c.seed_hi);
+          if (lam > 0.0f && -logf(ch_unitf(r0.x)) / lam < 1.0f) ncol += ch_collide<float>(c, id, lscale, v, &nref);
+          const float qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
+          vsum[1] += (double)ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), vnTf);
+        }
+        vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
+        P.vel[ip] = vv;
       }
-      if (c.collide) {
-        const float wx2 = v[0] - vn0x, wy2 = v[1] - vn0y, wz2 = v[2] - vn0z;
-        const float gi = ch_gmean<float>(sqrtf(wx2 * wx2 + wy2 * wy2 + wz2 * wz2), vnTf);
-        float nd = 1.0f;
-        if (c.nn_profile == CH_NN_GAUSSIAN_X)
-          nd = ch_neutral_density<float>(c, (float)(g.x0 + ((double)i + (double)p.x) * g.dx));
-        const float lscale = pscale * nd;
-        const float lam = lscale * gi;
-        vsum[0] += (double)lam;
-        const uint32_t id = __float_as_uint(vv.w);
-        const U4 r0 = ch_philox(id, c.step, CH_PURPOSE_COLLIDE << 24, c.run, c.seed_lo, c.seed_hi);
-        if (lam > 0.0f && -logf(ch_unitf(r0.x)) / lam < 1.0f) ncol += ch_collide<float>(c, id, lscale, v, &nref);
-        const float qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
-        vsum[1] += (double)ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), vnTf);
+      if (move && active) {
+        float ox = p.x + v[0] * dtx, oy = p.y + v[1] * dty, oz = p.z + v[2] * dtz;
+        const float fx = floorf(ox), fy = floorf(oy), fz = floorf(oz);
+        ox -= fx; oy -= fy; oz -= fz;
+        if (ox >= 1.0f) ox = 0.0f;
+        if (oy >= 1.0f) oy = 0.0f;
+        if (oz >= 1.0f) oz = 0.0f;
+        if (isfinite(fx) && isfinite(fy) && isfinite(fz)) {
+          i = ch_wrap(i + (int)fx, g.Nx); j = ch_wrap(j + (int)fy, g.Ny); k = ch_wrap(k + (int)fz, g.Nz);
+        }
+        const uint32_t cell = (uint32_t)i | ((uint32_t)j << CH_PACK_BX) | ((uint32_t)k << (CH_PACK_BX + CH_PACK_BY));
+        p = make_float4(ox, oy, oz, __uint_as_float(cell));
+        P.pos[ip] = p;
       }
-      vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
-      P.vel[ip] = vv;
-    }
-    if ((PH & PH_MOVE) && !(c.faithful & CH_FAITHFUL_D5)) {
-      // offsets move in cell units; integer cell wrap is exact
-      float ox = p.x + v[0] * dtx, oy = p.y + v[1] * dty, oz = p.z + v[2] * dtz;
-      const float fx = floorf(ox), fy = floorf(oy), fz = floorf(oz);
-      ox -= fx; oy -= fy; oz -= fz;
-      if (ox >= 1.0f) { ox = 0.0f; } // x - floor(x) can round up to 1
-      if (oy >= 1.0f) { oy = 0.0f; }
-      if (oz >= 1.0f) { oz = 0.0f; }
-      i = ch_wrap(i + (int)fx, g.Nx); j = ch_wrap(j + (int)fy, g.Ny); k = ch_wrap(k + (int)fz, g.Nz);
-      cell = (uint32_t)i | ((uint32_t)j << CH_PACK_BX) | ((uint32_t)k << (CH_PACK_BX + CH_PACK_BY));
-      p = make_float4(ox, oy, oz, __uint_as_float(cell));
-      P.pos[ip] = p;
+      if (hist) agg_inc(hist, (uint32_t)(((int64_t)k * g.Ny + j) * g.Nx + i), active);
+      if (PH & PH_DEPOSIT) {
+        const bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v[0]) && isfinite(v[1]) &&
+                            isfinite(v[2]);
+        if (active && !finite) bad = 1;
+        int di = i - bi0, dj = j - bj0, dk = k - bk0;
+        di += di < 0 ? g.Nx : 0; di -= di >= g.Nx ? g.Nx : 0;
+        dj += dj < 0 ? g.Ny : 0; dj -= dj >= g.Ny ? g.Ny : 0;
+        dk += dk < 0 ? g.Nz : 0; dk -= dk >= g.Nz ? g.Nz : 0;
+        const bool inbox = di <= BX - 2 && dj <= BY - 2 && dk <= BZ - 2;
+        const bool slow = fabsf(v[0]) >= CH_TILE_VMAX || fabsf(v[1]) >= CH_TILE_VMAX || fabsf(v[2]) >= CH_TILE_VMAX;
+        const bool valid = active && finite && inbox && !slow;
+        if (active && finite && !valid)
+          deposit_cic<float>(g, acc, i, j, k, p.x, p.y, p.z, v[0], v[1], v[2], (float)c.dep_scale);
+        // fixed-point contributions: 8 corners x {n, Gx, Gy, Gz}
+        const float wxh = p.x, wyh = p.y, wzh = p.z;
+        const float wxl = 1.0f - wxh, wyl = 1.0f - wyh, wzl = 1.0f - wzh;
+        const float w[8] = {wzl * wyl * wxl, wzl * wyl * wxh, wzl * wyh * wxl, wzl * wyh * wxh,
+                            wzh * wyl * wxl, wzh * wyl * wxh, wzh * wyh * wxl, wzh * wyh * wxh};
+        const int key = valid ? (dk * BY + dj) * BX + di : -1;
+        unsigned todo = __ballot_sync(0xffffffffu, valid);
+        while (todo) {
+          const int leader = __ffs(todo) - 1;
+          const int lkey = __shfl_sync(0xffffffffu, key, leader);
+          const bool mine = valid && key == lkey;
+          todo &= ~__ballot_sync(0xffffffffu, mine);
+#pragma unroll
+          for (int cn = 0; cn < 8; ++cn) {
+            const int node = lkey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
+            const int cd = mine ? __float2int_rn(w[cn] * CH_TILE_DSCALE) : 0;
+            const int cx = mine ? __float2int_rn(v[0] * w[cn] * CH_TILE_FSCALE) : 0;
+            const int cy = mine ? __float2int_rn(v[1] * w[cn] * CH_TILE_FSCALE) : 0;
+            const int cz = mine ? __float2int_rn(v[2] * w[cn] * CH_TILE_FSCALE) : 0;
+            const int sd = (int)__reduce_add_sync(0xffffffffu, (unsigned)cd);
+            const int sx = (int)__reduce_add_sync(0xffffffffu, (unsigned)cx);
+            const int sy = (int)__reduce_add_sync(0xffffffffu, (unsigned)cy);
+            const int sz = (int)__reduce_add_sync(0xffffffffu, (unsigned)cz);
+            if (lane == leader) {
+              atomicAdd((unsigned long long*)&sh.acc[0][node], (unsigned long long)((long long)sd << shift_d));
+              atomicAdd((unsigned long long*)&sh.acc[1][node], (unsigned long long)((long long)sx << shift_f));
+              atomicAdd((unsigned long long*)&sh.acc[2][node], (unsigned long long)((long long)sy << shift_f));
+              atomicAdd((unsigned long long*)&sh.acc[3][node], (unsigned long long)((long long)sz << shift_f));
+            }
+          }
+        }
+      }
     }
     if (PH & PH_DEPOSIT) {
-      if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) {
-        bad = 1;
-        continue;
+      __syncthreads();
+      for (int q = threadIdx.x; q < 4 * BNODES; q += blockDim.x) {
+        const int m = q / BNODES, nd = q % BNODES;
+        const long long a = sh.acc[m][nd];
+        if (a != 0) {
+          const int bi = nd % BX, bj = (nd / BX) % BY, bk = nd / (BX * BY);
+          const int gi = ch_wrap(bi0 + bi, g.Nx), gj = ch_wrap(bj0 + bj, g.Ny), gk = ch_wrap(bk0 + bk, g.Nz);
+          atomicAdd(acc + (int64_t)m * g.N + ((int64_t)gk * g.Ny + gj) * g.Nx + gi, (unsigned long long)a);
+        }
       }
-      deposit_cic<float>(g, acc, i, j, k, p.x, p.y, p.z, v[0], v[1], v[2], scale);
     }
   }
   if (bad) atomicOr(&cnt->range_error, 2);
@@ -490,6 +649,13 @@ __global__ void __launch_bounds__(256) k_pass_mixed(StepConsts c, MixParticles P
     block_partials<2>(vsum, part);
   }
 }
+#undef TX
+#undef TY
+#undef TZ
+#undef BX
+#undef BY
+#undef BZ
+#undef BNODES
 
 // ------------------------------------------------------------------ S at upload
 __global__ void k_sbar_f64(F64Particles P, double vnT, double vn0x, double vn0y, double vn0z, double* part) {
@@ -572,20 +738,6 @@ __device__ __forceinline__ uint32_t key_mixed(const GridDesc& g, float w) {
   return (k * (uint32_t)g.Ny + j) * (uint32_t)g.Nx + i;
 }
 
-// Warp-aggregated increment of counts[key]; returns this lane's rank among
-// the lanes that share its key, and the group's base from the atomic.
-__device__ __forceinline__ uint32_t agg_inc(uint32_t* counts, uint32_t key, bool active) {
-  const unsigned mask = __activemask();
-  const unsigned grp = __match_any_sync(mask, active ? key : 0xFFFFFFFFu);
-  const int leader = __ffs(grp) - 1;
-  const int lane = threadIdx.x & 31;
-  const uint32_t rank = __popc(grp & ((1u << lane) - 1u));
-  uint32_t base = 0;
-  if (active && lane == leader) base = atomicAdd(counts + key, (uint32_t)__popc(grp));
-  base = __shfl_sync(mask, base, leader);
-  return base + rank;
-}
-
 __global__ void k_hist_f64(GridDesc g, F64Particles P, uint32_t* counts, uint32_t* keys) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t n_pad = (P.np + 31) / 32 * 32;
@@ -625,15 +777,17 @@ __global__ void k_scatter_f64(F64Particles P, F64Particles Q, const uint32_t* __
   }
 }
 
-__global__ void k_scatter_mixed(MixParticles P, MixParticles Q, const uint32_t* __restrict__ keys, uint32_t* cursor) {
+__global__ void k_scatter_mixed(GridDesc g, MixParticles P, MixParticles Q, uint32_t* cursor) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t n_pad = (P.np + 31) / 32 * 32;
   for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < n_pad; ip += stride) {
     const bool act = ip < P.np;
-    const uint32_t key = act ? keys[ip] : 0u;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (act) p = P.pos[ip];
+    const uint32_t key = act ? key_mixed(g, p.w) : 0u;
     const uint32_t dst = agg_inc(cursor, key, act);
     if (act) {
-      Q.pos[dst] = P.pos[ip];
+      Q.pos[dst] = p;
       Q.vel[dst] = P.vel[ip];
     }
   }
@@ -747,12 +901,17 @@ void launch_node_efield(bool mixed, const GridDesc& g, double tscale, const doub
 template <int PH>
 static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticles M, const double* E64,
                     const float4* E32, const double* phi, unsigned long long* acc, double Nc, double sbar,
-                    DevCounters* cnt, double* part, int sms, cudaStream_t s) {
+                    DevCounters* cnt, double* part, const uint32_t* starts, uint32_t* hist, int sms,
+                    cudaStream_t s) {
   const int64_t np = mixed ? M.np : P.np;
-  const int nb = grid_for(np, 256, sms, 8);
+  int nb = grid_for(np, 256, sms, 8);
   if (mixed) {
     const float pscale = sbar > 0.0 ? (float)(Nc / sbar) : 0.0f;
-    k_pass_mixed<PH><<<nb, 256, 0, s>>>(c, M, E32, acc, pscale, cnt, part), ::ch::note_launch();
+    const int ntiles = ((c.g.Nx + 15) / 16) * ((c.g.Ny + 3) / 4) * ((c.g.Nz + 3) / 4);
+    nb = ntiles < 2 * sms ? ntiles : 2 * sms;
+    const int s2 = (int)lround(log2(c.dep_scale));
+    k_pass_tiled<PH><<<nb, 256, sizeof(TileShared), s>>>(c, M, E32, starts, acc, pscale, s2 - 24, s2 - 20, cnt, part,
+                                                         hist), ::ch::note_launch();
   } else {
     k_pass_f64<PH><<<nb, 256, 0, s>>>(c, P, E64, phi, acc, Nc, sbar, cnt, part), ::ch::note_launch();
   }
@@ -761,17 +920,16 @@ static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticle
 
 int launch_pass(bool mixed, int phases, const StepConsts& c, F64Particles P, MixParticles M, const double* E64,
                 const float4* E32, const double* phi, unsigned long long* acc, double Nc, double sbar,
-                DevCounters* cnt, double* part, int sms, cudaStream_t s) {
+                DevCounters* cnt, double* part, const uint32_t* starts, uint32_t* hist, int sms, cudaStream_t s) {
+#define CH_PASS(PHV) pass_one<PHV>(mixed, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, starts, hist, sms, s)
   switch (phases) {
-    case PH_PUSH: return pass_one<PH_PUSH>(mixed, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, sms, s);
-    case PH_MOVE: return pass_one<PH_MOVE>(mixed, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, sms, s);
-    case PH_DEPOSIT: return pass_one<PH_DEPOSIT>(mixed, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, sms, s);
-    case PH_MOVE | PH_DEPOSIT:
-      return pass_one<PH_MOVE | PH_DEPOSIT>(mixed, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, sms, s);
-    default:
-      return pass_one<PH_PUSH | PH_MOVE | PH_DEPOSIT>(mixed, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, sms,
-                                                      s);
+    case PH_PUSH: return CH_PASS(PH_PUSH);
+    case PH_MOVE: return CH_PASS(PH_MOVE);
+    case PH_DEPOSIT: return CH_PASS(PH_DEPOSIT);
+    case PH_MOVE | PH_DEPOSIT: return CH_PASS(PH_MOVE | PH_DEPOSIT);
+    default: return CH_PASS(PH_PUSH | PH_MOVE | PH_DEPOSIT);
   }
+#undef CH_PASS
 }
 
 int launch_sbar(bool mixed, const StepConsts& c, F64Particles P, MixParticles M, double* part, int sms,
@@ -797,19 +955,21 @@ int launch_finalize(int64_t N, unsigned long long* acc, double inv_scale, int re
 }
 
 void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, MixParticles M, MixParticles MQ,
-                 uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* keys, uint32_t* block_sums, int sms,
-                 cudaStream_t s) {
+                 uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* keys, uint32_t* block_sums,
+                 bool have_hist, int sms, cudaStream_t s) {
   const int64_t np = mixed ? M.np : P.np;
   const int64_t N = g.N;
-  cudaMemsetAsync(counts, 0, sizeof(uint32_t) * N, s);
   const int nb = grid_for(np, 256, sms, 8);
-  if (mixed) k_hist_mixed<<<nb, 256, 0, s>>>(g, M, counts, keys), ::ch::note_launch();
-  else k_hist_f64<<<nb, 256, 0, s>>>(g, P, counts, keys), ::ch::note_launch();
+  if (!(mixed && have_hist)) {
+    cudaMemsetAsync(counts, 0, sizeof(uint32_t) * N, s);
+    if (mixed) k_hist_mixed<<<nb, 256, 0, s>>>(g, M, counts, keys), ::ch::note_launch();
+    else k_hist_f64<<<nb, 256, 0, s>>>(g, P, counts, keys), ::ch::note_launch();
+  }
   const int nsb = (int)((N + 1023) / 1024);
   k_scan_blocks<<<nsb, 512, 0, s>>>(counts, starts, block_sums, N), ::ch::note_launch();
   k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nsb, starts + N), ::ch::note_launch();
   k_scan_add<<<(int)((N + 255) / 256), 256, 0, s>>>(starts, block_sums, N, cursor), ::ch::note_launch();
-  if (mixed) k_scatter_mixed<<<nb, 256, 0, s>>>(M, MQ, keys, cursor), ::ch::note_launch();
+  if (mixed) k_scatter_mixed<<<nb, 256, 0, s>>>(g, M, MQ, cursor), ::ch::note_launch();
   else k_scatter_f64<<<nb, 256, 0, s>>>(P, Q, keys, cursor), ::ch::note_launch();
 }
 

@@ -31,9 +31,12 @@ void launch_aos_out(bool mixed, const GridDesc& g, F64Particles P, MixParticles 
 void launch_node_efield(bool mixed, const GridDesc& g, double tscale, const double* phi, double* E64, float4* E32,
                         int sms, cudaStream_t s);
 // PUSH/MOVE/DEPOSIT mask; part receives nblocks x 2 partials (expected, S next).
+// Mixed form: a brick-tiled kernel over the cell-sorted ions (starts = first
+// slot of each cell at the last sort); hist (nullable) counts the ions' new
+// cells for the next sort.
 int launch_pass(bool mixed, int phases, const StepConsts& c, F64Particles P, MixParticles M, const double* E64,
                 const float4* E32, const double* phi, unsigned long long* acc, double Nc, double sbar,
-                DevCounters* cnt, double* part, int sms, cudaStream_t s);
+                DevCounters* cnt, double* part, const uint32_t* starts, uint32_t* hist, int sms, cudaStream_t s);
 int launch_sbar(bool mixed, const StepConsts& c, F64Particles P, MixParticles M, double* part, int sms,
                 cudaStream_t s);
 void launch_reduce_partials(const double* part, int nblocks, int K, double* out, cudaStream_t s);
@@ -41,8 +44,10 @@ int launch_finalize(int64_t N, unsigned long long* acc, double inv_scale, int re
                     DevCounters* cnt, int sms, cudaStream_t s);
 // Counting sort by cell: counts (N), starts (N+1), cursor (N), keys (np),
 // block_sums (ceil(N/1024)+1).  Results land in the Q buffers.
+// have_hist: counts already hold the per-cell ion counts (mixed form, counted
+// by the preceding pass).
 void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, MixParticles M, MixParticles MQ,
-                 uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* keys, uint32_t* block_sums, int sms,
-                 cudaStream_t s);
+                 uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* keys, uint32_t* block_sums,
+                 bool have_hist, int sms, cudaStream_t s);
 
 }  // namespace ch

@@ -71,13 +71,6 @@ __device__ __forceinline__ Nb neighbours(const GridDesc& g, int64_t c) {
 }
 
 template <typename T>
-struct DevCoefs {
-  T sxx, syy, szz, sxy, sxz, syz, syx, szx, szy;
-  int type;
-  int cross;
-};
-
-template <typename T>
 DevCoefs<T> dev_coefs(const OpCoefs& c) {
   DevCoefs<T> d;
   d.sxx = (T)c.sxx; d.syy = (T)c.syy; d.szz = (T)c.szz;
@@ -310,6 +303,17 @@ __global__ void k_cg_xr(int64_t N, const double* __restrict__ scal, T* __restric
   partials<2>(d, part);
 }
 
+// CG: x += a p; r -= a q (the preconditioner runs after)
+template <typename T>
+__global__ void k_cg_xr_plain(int64_t N, const double* __restrict__ scal, T* __restrict__ x, T* __restrict__ r,
+                              const T* __restrict__ p, const T* __restrict__ q) {
+  const T a = (T)scal[S_ALPHA];
+  GRID_LOOP(c, N) {
+    x[c] += a * p[c];
+    r[c] -= a * q[c];
+  }
+}
+
 template <typename T>
 __global__ void k_cg_p(int64_t N, const double* __restrict__ scal, const T* __restrict__ z, T* __restrict__ p,
                        int first) {
@@ -325,7 +329,7 @@ __global__ void k_bi_p(int64_t N, const double* __restrict__ scal, const T* __re
   GRID_LOOP(c, N) {
     const T pv = r[c] + b * (p[c] - w * v[c]);
     p[c] = pv;
-    y[c] = dinv[c] * pv;
+    if (dinv) y[c] = dinv[c] * pv;
   }
 }
 
@@ -338,7 +342,7 @@ __global__ void k_bi_s(int64_t N, const double* __restrict__ scal, const T* __re
   GRID_LOOP(c, N) {
     const T sv = r[c] - a * v[c];
     s[c] = sv;
-    sh[c] = dinv[c] * sv;
+    if (dinv) sh[c] = dinv[c] * sv;
     d[0] += (double)sv * (double)sv;
   }
   partials<1>(d, part);
@@ -454,6 +458,114 @@ __global__ void k_rhs(GridDesc g, int rhs_type, double R00, double R01, double R
   }
 }
 
+
+// ------------------------------------------------------------------ multigrid
+// Damped-Jacobi smoothing: y = x + w dinv (b - A x); x == nullptr means x = 0.
+template <typename T>
+__global__ void __launch_bounds__(256) k_smooth(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
+                                                const T* __restrict__ dinv, const T* __restrict__ b,
+                                                const T* __restrict__ x, T* __restrict__ y, T w) {
+  GRID_LOOP(c, g.N) {
+    if (!x) {
+      y[c] = w * dinv[c] * b[c];
+    } else {
+      const Nb nb = neighbours(g, c);
+      y[c] = x[c] + w * dinv[c] * (b[c] - apply_row<T>(C, n, x, nb));
+    }
+  }
+}
+
+// r = b - A x without a norm (MG levels).
+template <typename T>
+__global__ void __launch_bounds__(256) k_resid(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
+                                               const T* __restrict__ b, const T* __restrict__ x,
+                                               T* __restrict__ r) {
+  GRID_LOOP(c, g.N) r[c] = b[c] - apply_row<T>(C, n, x, neighbours(g, c));
+}
+
+// Full weighting onto the coarse vertex grid (coarse node I = fine node 2I
+// along each halved axis): 1D weights 1/4, 1/2, 1/4; axes that are not
+// halved take the fine value.  out = scale * R in.
+template <typename T>
+__global__ void k_restrict(GridDesc gf, GridDesc gc, int hx, int hy, int hz, const T* __restrict__ in,
+                           T* __restrict__ out, T scale) {
+  GRID_LOOP(c, gc.N) {
+    const int I = (int)(c % gc.Nx), J = (int)((c / gc.Nx) % gc.Ny), K = (int)(c / ((int64_t)gc.Nx * gc.Ny));
+    const int i0 = hx ? 2 * I : I, j0 = hy ? 2 * J : J, k0 = hz ? 2 * K : K;
+    T acc = T(0);
+    for (int dk = -hz; dk <= hz; ++dk) {
+      const T wk = hz ? (dk == 0 ? T(0.5) : T(0.25)) : T(1);
+      const int k = ch_wrap(k0 + dk, gf.Nz);
+      for (int dj = -hy; dj <= hy; ++dj) {
+        const T wj = hy ? (dj == 0 ? T(0.5) : T(0.25)) : T(1);
+        const int j = ch_wrap(j0 + dj, gf.Ny);
+        const int64_t row = ((int64_t)k * gf.Ny + j) * gf.Nx;
+        for (int di = -hx; di <= hx; ++di) {
+          const T wi = hx ? (di == 0 ? T(0.5) : T(0.25)) : T(1);
+          acc += wk * wj * wi * in[row + ch_wrap(i0 + di, gf.Nx)];
+        }
+      }
+    }
+    out[c] = scale * acc;
+  }
+}
+
+// Trilinear prolongation, added: xf += P ec.
+template <typename T>
+__global__ void k_prolong_add(GridDesc gf, GridDesc gc, int hx, int hy, int hz, const T* __restrict__ ec,
+                              T* __restrict__ xf) {
+  GRID_LOOP(c, gf.N) {
+    const int i = (int)(c % gf.Nx), j = (int)((c / gf.Nx) % gf.Ny), k = (int)(c / ((int64_t)gf.Nx * gf.Ny));
+    int I0, I1, J0, J1, K0, K1;
+    T wi1, wj1, wk1;
+    if (hx) { I0 = i >> 1; I1 = (i & 1) ? ch_wrap(I0 + 1, gc.Nx) : I0; wi1 = (i & 1) ? T(0.5) : T(0); }
+    else { I0 = I1 = i; wi1 = T(0); }
+    if (hy) { J0 = j >> 1; J1 = (j & 1) ? ch_wrap(J0 + 1, gc.Ny) : J0; wj1 = (j & 1) ? T(0.5) : T(0); }
+    else { J0 = J1 = j; wj1 = T(0); }
+    if (hz) { K0 = k >> 1; K1 = (k & 1) ? ch_wrap(K0 + 1, gc.Nz) : K0; wk1 = (k & 1) ? T(0.5) : T(0); }
+    else { K0 = K1 = k; wk1 = T(0); }
+    const T wi0 = T(1) - wi1, wj0 = T(1) - wj1, wk0 = T(1) - wk1;
+    auto at = [&](int I, int J, int K) { return ec[((int64_t)K * gc.Ny + J) * gc.Nx + I]; };
+    const T v = wk0 * (wj0 * (wi0 * at(I0, J0, K0) + wi1 * at(I1, J0, K0)) +
+                       wj1 * (wi0 * at(I0, J1, K0) + wi1 * at(I1, J1, K0))) +
+                wk1 * (wj0 * (wi0 * at(I0, J0, K1) + wi1 * at(I1, J0, K1)) +
+                       wj1 * (wi0 * at(I0, J1, K1) + wi1 * at(I1, J1, K1)));
+    xf[c] += v;
+  }
+}
+
+// Coarsest level: `sweeps` damped-Jacobi sweeps from zero in one block,
+// iterates in shared memory (N <= 4096 nodes).
+template <typename T>
+__global__ void __launch_bounds__(1024) k_coarse(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
+                                                 const T* __restrict__ dinv, const T* __restrict__ b,
+                                                 T* __restrict__ x, int sweeps, T w) {
+  extern __shared__ unsigned char smem_raw[];
+  T* xa = reinterpret_cast<T*>(smem_raw);
+  T* xb = xa + g.N;
+  for (int64_t c = threadIdx.x; c < g.N; c += blockDim.x) xa[c] = w * dinv[c] * b[c];
+  __syncthreads();
+  for (int s = 1; s < sweeps; ++s) {
+    for (int64_t c = threadIdx.x; c < g.N; c += blockDim.x)
+      xb[c] = xa[c] + w * dinv[c] * (b[c] - apply_row<T>(C, n, xa, neighbours(g, c)));
+    __syncthreads();
+    T* t = xa; xa = xb; xb = t;
+  }
+  for (int64_t c = threadIdx.x; c < g.N; c += blockDim.x) x[c] = xa[c];
+}
+
+// partials (r.z, r.r) after a multigrid preconditioner application
+template <typename T>
+__global__ void k_dot_rz_rr(int64_t N, const T* __restrict__ r, const T* __restrict__ z, double* part) {
+  double d[2] = {0.0, 0.0};
+  GRID_LOOP(c, N) {
+    const double rv = (double)r[c];
+    d[0] += rv * (double)z[c];
+    d[1] += rv * rv;
+  }
+  partials<2>(d, part);
+}
+
 // ------------------------------------------------------------------ host side
 static int grid_n(int64_t n, int sms) {
   int64_t need = (n + 255) / 256;
@@ -484,6 +596,8 @@ ch_status PotentialSolver::init(const ch_params& p, const GridDesc& g, int sms) 
 }
 
 void PotentialSolver::release() {
+  mg_release<float>(mg32_);
+  mg_release<double>(mg64_);
   void* all[] = {r_, z_, pd_, q_, rh_, s_, t_, sh_, dinv_, n32_, b32_, x32_, r32_, z32_, p32_, q32_, rh32_,
                  s32_, t32_, sh32_, dinv32_, part_, scal_};
   for (void* v : all)
@@ -492,6 +606,112 @@ void PotentialSolver::release() {
   r_ = z_ = pd_ = q_ = rh_ = s_ = t_ = sh_ = dinv_ = nullptr;
   n32_ = b32_ = x32_ = r32_ = z32_ = p32_ = q32_ = rh32_ = s32_ = t32_ = sh32_ = dinv32_ = nullptr;
   part_ = scal_ = hscal_ = nullptr;
+}
+
+
+// ------------------------------------------------------------------ multigrid (host)
+static constexpr int MG_NU = 2;            // pre- and post-smoothing sweeps (even)
+static constexpr double MG_OMEGA = 0.8;    // Jacobi damping
+static constexpr int MG_COARSE_SWEEPS = 64;
+static constexpr int64_t MG_COARSE_MAX = 4096;
+
+template <typename T>
+ch_status PotentialSolver::mg_build(MGHier<T>& h) {
+  if (h.built) return CH_OK;
+  h.g[0] = g_;
+  int L = 1;
+  while (L < CH_MG_MAX_LEVELS) {
+    const GridDesc& f = h.g[L - 1];
+    const int hx = (f.Nx % 2 == 0 && f.Nx / 2 >= 4), hy = (f.Ny % 2 == 0 && f.Ny / 2 >= 4),
+              hz = (f.Nz % 2 == 0 && f.Nz / 2 >= 4);
+    if (!(hx || hy || hz) || f.N <= 64) break;
+    GridDesc c = f;
+    c.Nx = hx ? f.Nx / 2 : f.Nx; c.Ny = hy ? f.Ny / 2 : f.Ny; c.Nz = hz ? f.Nz / 2 : f.Nz;
+    c.dx = hx ? 2 * f.dx : f.dx; c.dy = hy ? 2 * f.dy : f.dy; c.dz = hz ? 2 * f.dz : f.dz;
+    c.N = (int64_t)c.Nx * c.Ny * c.Nz;
+    h.hx[L - 1] = hx; h.hy[L - 1] = hy; h.hz[L - 1] = hz;
+    // the full operator is finite-difference scaled (averaged residuals);
+    // the Laplacian of src/lhs.c:205-207 is finite-volume scaled
+    h.sR[L - 1] = p_.lhs_type == CH_LHS_LAPLACIAN ? (c.dx * c.dy * c.dz) / (f.dx * f.dy * f.dz) : 1.0;
+    h.g[L] = c;
+    ++L;
+  }
+  if (h.g[L - 1].N > MG_COARSE_MAX)
+    return ch_fail(CH_ERR_UNSUPPORTED, "multigrid: coarsest grid %dx%dx%d exceeds %lld nodes; use -ch_pc jacobi",
+                   h.g[L - 1].Nx, h.g[L - 1].Ny, h.g[L - 1].Nz, (long long)MG_COARSE_MAX);
+  h.L = L;
+  for (int l = 0; l < L; ++l) {
+    const size_t b = sizeof(T) * h.g[l].N;
+    h.C[l] = dev_coefs<T>(op_coefs(p_, h.g[l]));
+    h.n[l] = nullptr;
+    if (l > 0) CH_CUDA_OK(cudaMalloc(&h.n[l], b));
+    CH_CUDA_OK(cudaMalloc(&h.dinv[l], b));
+    CH_CUDA_OK(cudaMalloc(&h.r[l], b));
+    CH_CUDA_OK(cudaMalloc(&h.t[l], b));
+    h.x[l] = h.b[l] = nullptr;
+    if (l > 0) {
+      CH_CUDA_OK(cudaMalloc(&h.x[l], b));
+      CH_CUDA_OK(cudaMalloc(&h.b[l], b));
+    }
+  }
+  const size_t sh = 2 * sizeof(T) * h.g[L - 1].N;
+  if (sh > 48 * 1024) CH_CUDA_OK(cudaFuncSetAttribute(k_coarse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      (int)sh));
+  h.built = true;
+  return CH_OK;
+}
+
+template <typename T>
+void PotentialSolver::mg_release(MGHier<T>& h) {
+  for (int l = 0; l < h.L; ++l) {
+    T* v[] = {l > 0 ? h.n[l] : nullptr, h.dinv[l], h.r[l], h.t[l], l > 0 ? h.x[l] : nullptr,
+              l > 0 ? h.b[l] : nullptr};
+    for (T* q : v)
+      if (q) cudaFree(q);
+  }
+  h.L = 0;
+  h.built = false;
+}
+
+// New density: restrict it down the hierarchy and rebuild the diagonals.
+template <typename T>
+void PotentialSolver::mg_update(MGHier<T>& h, const T* n_fine, cudaStream_t s) {
+  h.n[0] = const_cast<T*>(n_fine);
+  for (int l = 0; l < h.L; ++l) {
+    if (l > 0)
+      k_restrict<T><<<grid_n(h.g[l].N, sms_), 256, 0, s>>>(h.g[l - 1], h.g[l], h.hx[l - 1], h.hy[l - 1], h.hz[l - 1],
+                                                          h.n[l - 1], h.n[l], T(1)), ::ch::note_launch();
+    k_jacobi<T><<<grid_n(h.g[l].N, sms_), 256, 0, s>>>(h.g[l], h.C[l], h.n[l], h.dinv[l], 1), ::ch::note_launch();
+  }
+}
+
+// One V(2,2) cycle from a zero guess: x ~= A_l^{-1} b.
+template <typename T>
+void PotentialSolver::mg_vcycle(MGHier<T>& h, int l, const T* b, T* x, cudaStream_t s) {
+  const GridDesc& g = h.g[l];
+  const int nb = grid_n(g.N, sms_);
+  const T w = (T)MG_OMEGA;
+  if (l == h.L - 1) {
+    const size_t sh = 2 * sizeof(T) * g.N;
+    k_coarse<T><<<1, 1024, sh, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, x, MG_COARSE_SWEEPS, w), ::ch::note_launch();
+    return;
+  }
+  T* t = h.t[l];
+  // pre-smoothing (MG_NU = 2 sweeps): zero -> t -> x
+  k_smooth<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, (const T*)nullptr, t, w), ::ch::note_launch();
+  k_smooth<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, t, x, w), ::ch::note_launch();
+  // residual, restriction, coarse correction, prolongation
+  k_resid<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], b, x, h.r[l]), ::ch::note_launch();
+  k_restrict<T><<<grid_n(h.g[l + 1].N, sms_), 256, 0, s>>>(g, h.g[l + 1], h.hx[l], h.hy[l], h.hz[l], h.r[l],
+                                                          h.b[l + 1], (T)h.sR[l]), ::ch::note_launch();
+  mg_vcycle<T>(h, l + 1, h.b[l + 1], h.x[l + 1], s);
+  k_prolong_add<T><<<nb, 256, 0, s>>>(g, h.g[l + 1], h.hx[l], h.hy[l], h.hz[l], h.x[l + 1], x), ::ch::note_launch();
+  // post-smoothing: x -> t -> x
+  for (int k = 0; k < MG_NU; ++k) {
+    T* src = (k % 2 == 0) ? x : h.t[l];
+    T* dst = (k % 2 == 0) ? h.t[l] : x;
+    k_smooth<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, src, dst, w), ::ch::note_launch();
+  }
 }
 
 double PotentialSolver::dot64(const double* a, const double* b, cudaStream_t s) {
@@ -532,7 +752,7 @@ void PotentialSolver::apply64(const double* n, const double* x, double* y, cudaS
 // Converged when ||r||_2 <= rtol ||b||_2 (recurrence residual).
 template <typename T>
 ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* x, double rtol, int maxit,
-                                  bool zero_guess, int* its, double* rnorm_out, cudaStream_t s) {
+                                  bool zero_guess, int* its, double* rnorm_out, MGHier<T>* mg, cudaStream_t s) {
   const DevCoefs<T> C = dev_coefs<T>(c_);
   const int64_t N = g.N;
   const bool f64 = sizeof(T) == 8;
@@ -546,16 +766,23 @@ ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* 
   T* sh = f64 ? (T*)sh_ : (T*)sh32_;
   T* dinv = f64 ? (T*)dinv_ : (T*)dinv32_;
   const int nb = nb_;
-  k_jacobi<T><<<nb, 256, 0, s>>>(g, C, n, dinv, p_.pc_type == CH_PC_JACOBI), ::ch::note_launch();
-  // ||b||
+  if (!mg) k_jacobi<T><<<nb, 256, 0, s>>>(g, C, n, dinv, p_.pc_type == CH_PC_JACOBI), ::ch::note_launch();
+  // z = M r with M = Jacobi (fused) or one multigrid V-cycle
+  auto precond = [&](const T* rr_, T* zz_) {
+    if (mg) {
+      mg_vcycle<T>(*mg, 0, rr_, zz_, s);
+      k_dot_rz_rr<T><<<nb, 256, 0, s>>>(N, rr_, zz_, part_), ::ch::note_launch();
+    } else {
+      k_prec_dot<T><<<nb, 256, 0, s>>>(N, dinv, rr_, zz_, part_), ::ch::note_launch();
+    }
+  };
   if (zero_guess) {
     k_zero<T><<<nb, 256, 0, s>>>(N, x), ::ch::note_launch();
     k_copy<T><<<nb, 256, 0, s>>>(N, b, r), ::ch::note_launch();
-    k_prec_dot<T><<<nb, 256, 0, s>>>(N, dinv, r, z, part_), ::ch::note_launch();
   } else {
     k_residual<T><<<nb, 256, 0, s>>>(g, C, n, b, x, r, part_), ::ch::note_launch();
-    k_prec_dot<T><<<nb, 256, 0, s>>>(N, dinv, r, z, part_), ::ch::note_launch();
   }
+  precond(r, z);
   k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_SET_RZ_RR, scal_, 0.0), ::ch::note_launch();
   k_dot<T><<<nb, 256, 0, s>>>(N, b, b, part_), ::ch::note_launch();
   k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_TMP, scal_, 0.0), ::ch::note_launch();
@@ -575,7 +802,12 @@ ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* 
     while (it < maxit) {
       k_apply<T><<<nb, 256, 0, s>>>(g, C, n, pp, q, pp, part_), ::ch::note_launch();
       k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_CG_ALPHA, scal_, 0.0), ::ch::note_launch();
-      k_cg_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, r, pp, q, dinv, z, part_), ::ch::note_launch();
+      if (mg) {
+        k_cg_xr_plain<T><<<nb, 256, 0, s>>>(N, scal_, x, r, pp, q), ::ch::note_launch();
+        precond(r, z);
+      } else {
+        k_cg_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, r, pp, q, dinv, z, part_), ::ch::note_launch();
+      }
       k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_CG_BETA, scal_, 0.0), ::ch::note_launch();
       ++it;
       CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_RR, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -593,11 +825,14 @@ ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* 
     CH_CUDA_OK(cudaMemcpyAsync(scal_ + S_RHO, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToDevice, s));
     bool first = true;
     while (it < maxit) {
-      k_bi_p<T><<<nb, 256, 0, s>>>(N, scal_, r, pp, q, dinv, z, first ? 1 : 0), ::ch::note_launch();  // z = y
+      k_bi_p<T><<<nb, 256, 0, s>>>(N, scal_, r, pp, q, mg ? (const T*)nullptr : dinv, z, first ? 1 : 0),
+          ::ch::note_launch();  // z = y = M p
+      if (mg) mg_vcycle<T>(*mg, 0, pp, z, s);
       first = false;
       k_apply<T><<<nb, 256, 0, s>>>(g, C, n, z, q, rh, part_), ::ch::note_launch();                  // v = A y; rh.v
       k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_BI_ALPHA, scal_, 0.0), ::ch::note_launch();
-      k_bi_s<T><<<nb, 256, 0, s>>>(N, scal_, r, q, dinv, sv, sh, part_), ::ch::note_launch();
+      k_bi_s<T><<<nb, 256, 0, s>>>(N, scal_, r, q, mg ? (const T*)nullptr : dinv, sv, sh, part_),
+          ::ch::note_launch();
       k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_SS, scal_, 0.0), ::ch::note_launch();
       ++it;
       CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_SS, scal_ + S_SS, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -607,6 +842,7 @@ ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* 
         rr = hscal_[S_SS];
         break;
       }
+      if (mg) mg_vcycle<T>(*mg, 0, sv, sh, s);
       k_apply_dot2<T><<<nb, 256, 0, s>>>(g, C, n, sh, tv, sv, part_), ::ch::note_launch();
       k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_OMEGA, scal_, 0.0), ::ch::note_launch();
       k_bi_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, z, sh, r, sv, tv, rh, part_), ::ch::note_launch();
@@ -636,7 +872,14 @@ ch_status PotentialSolver::solve_fp64(const double* n, const double* b, double* 
   if (singular) remove_mean64(phi, s);
   int its = 0;
   double rn = 0.0;
-  ch_status rc = krylov<double>(g_, n, b, phi, p_.ksp_rtol, p_.ksp_max_it, false, &its, &rn, s);
+  MGHier<double>* mg = nullptr;
+  if (p_.pc_type == CH_PC_MG) {
+    ch_status rm = mg_build<double>(mg64_);
+    if (rm) return rm;
+    mg_update<double>(mg64_, n, s);
+    mg = &mg64_;
+  }
+  ch_status rc = krylov<double>(g_, n, b, phi, p_.ksp_rtol, p_.ksp_max_it, false, &its, &rn, mg, s);
   if (rc) return rc;
   if (singular) remove_mean64(phi, s);
   // true residual
@@ -657,6 +900,13 @@ ch_status PotentialSolver::solve_mixed(const double* n, const double* b, double*
                                        cudaStream_t s) {
   const DevCoefs<double> C64 = dev_coefs<double>(c_);
   k_down<<<nb_, 256, 0, s>>>(N_, n, 1.0, n32_), ::ch::note_launch();
+  MGHier<float>* mg = nullptr;
+  if (p_.pc_type == CH_PC_MG) {
+    ch_status rm = mg_build<float>(mg32_);
+    if (rm) return rm;
+    mg_update<float>(mg32_, n32_, s);
+    mg = &mg32_;
+  }
   remove_mean64(phi, s);
   const double bnorm = sqrt(dot64(b, b, s));
   st->bnorm = bnorm;
@@ -675,7 +925,7 @@ ch_status PotentialSolver::solve_mixed(const double* n, const double* b, double*
     k_down<<<nb_, 256, 0, s>>>(N_, r_, sc, b32_), ::ch::note_launch();
     int its = 0;
     double rin = 0.0;
-    ch_status rc = krylov<float>(g_, n32_, b32_, x32_, inner_rtol, p_.ksp_max_it, true, &its, &rin, s);
+    ch_status rc = krylov<float>(g_, n32_, b32_, x32_, inner_rtol, p_.ksp_max_it, true, &its, &rin, mg, s);
     if (rc) return rc;
     total += its;
     k_up_add<<<nb_, 256, 0, s>>>(N_, x32_, rn, phi), ::ch::note_launch();

@@ -28,6 +28,29 @@ struct SolveStats {
   double rnorm, bnorm;
 };
 
+// Device coefficients of one operator level (defined in solver.cu).
+template <typename T>
+struct DevCoefs {
+  T sxx, syy, szz, sxy, sxz, syz, syx, szx, szy;
+  int type;
+  int cross;
+};
+
+// Geometric multigrid hierarchy in precision T.  Level 0 is the fine grid;
+// level l+1 halves every axis of level l that stays >= 4 nodes when halved.
+constexpr int CH_MG_MAX_LEVELS = 16;
+template <typename T>
+struct MGHier {
+  int L = 0;
+  GridDesc g[CH_MG_MAX_LEVELS];
+  DevCoefs<T> C[CH_MG_MAX_LEVELS];
+  int hx[CH_MG_MAX_LEVELS], hy[CH_MG_MAX_LEVELS], hz[CH_MG_MAX_LEVELS];  // halving to level l+1
+  double sR[CH_MG_MAX_LEVELS];                                           // residual scale into l+1
+  T *n[CH_MG_MAX_LEVELS], *dinv[CH_MG_MAX_LEVELS], *x[CH_MG_MAX_LEVELS], *b[CH_MG_MAX_LEVELS],
+      *r[CH_MG_MAX_LEVELS], *t[CH_MG_MAX_LEVELS];
+  bool built = false;
+};
+
 // Workspace and driver for the Krylov solves of one run.
 class PotentialSolver {
  public:
@@ -45,8 +68,16 @@ class PotentialSolver {
   ch_status solve_mixed(const double* n, const double* b, double* phi, SolveStats* st, cudaStream_t s);
   template <typename T>
   ch_status krylov(const GridDesc& g, const T* n, const T* b, T* x, double rtol, int maxit, bool zero_guess,
-                   int* its, double* rnorm_out, cudaStream_t s);
+                   int* its, double* rnorm_out, MGHier<T>* mg, cudaStream_t s);
   double dot64(const double* a, const double* b, cudaStream_t s);
+  template <typename T>
+  ch_status mg_build(MGHier<T>& h);
+  template <typename T>
+  void mg_update(MGHier<T>& h, const T* n_fine, cudaStream_t s);
+  template <typename T>
+  void mg_vcycle(MGHier<T>& h, int l, const T* b, T* x, cudaStream_t s);
+  template <typename T>
+  void mg_release(MGHier<T>& h);
   void remove_mean64(double* v, cudaStream_t s);
 
   ch_params p_{};
@@ -61,6 +92,8 @@ class PotentialSolver {
   // FP32 workspace (mixed form)
   float *n32_ = nullptr, *b32_ = nullptr, *x32_ = nullptr, *r32_ = nullptr, *z32_ = nullptr, *p32_ = nullptr,
         *q32_ = nullptr, *rh32_ = nullptr, *s32_ = nullptr, *t32_ = nullptr, *sh32_ = nullptr, *dinv32_ = nullptr;
+  MGHier<float> mg32_;
+  MGHier<double> mg64_;
   double* part_ = nullptr;  // block partials
   double* scal_ = nullptr;  // device scalars
   double* hscal_ = nullptr; // pinned host mirror

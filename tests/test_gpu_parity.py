@@ -143,9 +143,10 @@ def test_operator_matches_reference(chy, po, golden, tag, ki, kappa, lt):
 # ------------------------------------------------------------------ solve
 @pytest.mark.parametrize("ksp,kappa", [("cg", (0.0, 0.0, 0.0)), ("bcgs", (0.0, 0.0, 1.0))])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_solve_matches_oracle(chy, po, golden, ksp, kappa, precision):
+@pytest.mark.parametrize("pc", ["jacobi", "mg"])
+def test_solve_matches_oracle(chy, po, golden, ksp, kappa, precision, pc):
     p, q, _ = golden_case(chy, po, golden, "g8", kappa_e=kappa, ksp_type=chy.KSP[ksp], ksp_rtol=1e-12,
-                          precision=precision)
+                          precision=precision, pc_type=chy.PC[pc])
     nodes = golden["g8_collect1"]
     with chy.Hybrid(p) as h:
         h.set_moments(nodes)
@@ -157,6 +158,29 @@ def test_solve_matches_oracle(chy, po, golden, ksp, kappa, precision):
     assert rinfo["rc"] == 0
     assert abs(phi.mean()) < 1e-12 * np.abs(phi).max()
     assert rel(phi, ref) < 1e-9
+
+
+@pytest.mark.parametrize("N", [(32, 32, 32), (48, 16, 24), (64, 64, 8)])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_multigrid_solve_on_larger_grids(chy, po, N, precision):
+    """MG-preconditioned CG against the oracle's Jacobi-CG on grids with
+    full and semi coarsening; the preconditioner must cut the iterations."""
+    p, q = make(chy, po, N, precision=precision, ksp_rtol=1e-10, pc_type=chy.PC["mg"])
+    ions = po.load(q, po.make_loader(amp=(0.05, 0.03, 0.02), phase=(0.1, 0.7, 2.0)), int(np.prod(N)) * 4)
+    nodes = po.collect(q, ions)
+    with chy.Hybrid(p) as h:
+        h.set_moments(nodes)
+        phi = h.ComputePotential()
+        mg_info = h.last_solve
+    p.pc_type = chy.PC["jacobi"]
+    with chy.Hybrid(p) as h:
+        h.set_moments(nodes)
+        h.ComputePotential()
+        jac_info = h.last_solve
+    assert mg_info["rnorm"] <= 1e-10 * mg_info["bnorm"] * 1.01
+    assert mg_info["iterations"] * 3 < jac_info["iterations"], (mg_info, jac_info)
+    ref, rinfo = po.solve(q, nodes[0::4], po.rhs(q, nodes), rtol=1e-12, maxit=50000)
+    assert rel(phi, ref) < 1e-7
 
 
 # ------------------------------------------------------------------ push and move
