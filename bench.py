@@ -59,7 +59,7 @@ def make_params(w, seed=1, run=0):
     m = chy()
     N = w["N"]
     kw = dict(precision=m.PRECISION[w["precision"]], E0=w["E0"], nui=w["nu"], ksp_rtol=w["rtol"], seed=seed,
-              run=run, vi0=w["drift"], pc_type=m.PC["jacobi"])
+              run=run, vi0=w["drift"], pc_type=m.PC["mg"], sort_period=w.get("sort_period", 4))
     if w["nn"]:
         kw.update(nn_profile=1, nn_center=N[0] / 2.0, nn_sigma=N[0] / 6.0, nn_floor=0.1)
     return m.params_for(N, **kw)
@@ -364,7 +364,7 @@ def main():
     grid_bytes = N * (16 + 32) if w["precision"] == "mixed" else N * (24 + 32)
     alg = r["np"] * bytes_ion + grid_bytes
     achieved = alg / (pass_ms / 1e3) / 1e9
-    kname = "k_pass_mixed" if w["precision"] == "mixed" else "k_pass_f64"
+    kname = "k_pass_tiled" if w["precision"] == "mixed" else "k_pass_f64"
     tr = committed_traffic(kname)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
