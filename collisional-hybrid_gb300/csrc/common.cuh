@@ -4,7 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "../../include/chybrid.h"
+#include "chybrid.h"
 
 #define CH_PI 3.14159265358979323846
 
