@@ -212,6 +212,30 @@ ch_status ch_reset_profile(ch_ctx* c);
 /* The cudaStream_t every call of this context is ordered on. */
 ch_status ch_get_stream(ch_ctx* c, void** stream);
 
+/* CollectVlasovQuantities for callers that cannot allocate device memory
+ * (no counterpart in the reference).  Hosts whose device memory belongs to
+ * their own pool allocator, code that records its launches into a CUDA graph
+ * (cudaMalloc is not allowed while a stream is being captured), and
+ * time-critical loops that cannot absorb the device-wide synchronisation of
+ * cudaMalloc/cudaFree cannot create a ch_ctx; this call needs none.  It
+ * allocates nothing: the caller passes device pointers to the ions (FP64 SoA
+ * positions and velocities, np of each) and to the output `moments`
+ * (4 * Nx*Ny*Nz doubles: n, then Gx, Gy, Gz, each in DMDA natural order),
+ * and the deposit's fixed-point scratch lives in a static device array of
+ * 4 * 2^18 * 8 bytes = 8 MiB, so grids of at most 2^18 nodes (64^3) are
+ * accepted; larger grids return CH_ERR_ARG.  Every GPU that loads the
+ * library holds that array until the process exits.  The work is queued on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream) and the call
+ * returns without waiting.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress), so make that first call before any
+ * stream capture.  All calls share the one array, and each call clears it
+ * before depositing: calls that may overlap on the GPU (different streams,
+ * or different host threads) race and must be serialised by the caller.
+ * Results equal ch_collect_moments (same fixed-point sums). */
+ch_status ch_collect_moments_noalloc(const ch_params* p, const double* x, const double* y, const double* z,
+                                     const double* vx, const double* vy, const double* vz, int64_t np,
+                                     double* moments, void* stream);
+
 /* Page-locks caller memory so that the copies of upload/download run at
  * full link speed (no counterpart in the reference: its arrays never leave
  * the host). */
