@@ -33,6 +33,8 @@ ch_status ch_cuda_fail(cudaError_t e, const char* what, const char* file, int li
 
 static std::atomic<unsigned long long> g_launches{0};
 void ch::note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void ch::note_launch_n(long long n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
+unsigned long long ch::launches_now() { return g_launches.load(); }
 
 struct ch_ctx {
   ch_params p;

@@ -103,7 +103,10 @@ struct DevCounters {
 ch_status ch_cuda_fail(cudaError_t e, const char* what, const char* file, int line);
 
 namespace ch {
-// Counts kernel launches made by this library (reported by ch_get_profile).
+// Counts kernel launches made by this library (reported by ch_get_profile);
+// a CUDA graph launch counts the kernels it holds.
 void note_launch();
+void note_launch_n(long long n);
+unsigned long long launches_now();
 }
 ch_status ch_fail(ch_status code, const char* fmt, ...);

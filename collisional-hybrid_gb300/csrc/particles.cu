@@ -408,8 +408,9 @@ __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, 
 // brick.  Within a warp, lanes whose ions share a cell are summed with
 // integer warp reductions before one lane updates the shared tile.  Ions
 // that left the halo, or move faster than CH_TILE_VMAX cells/dt units, take
-// the direct global path.  Every sum is an integer sum, so the moments do
-// not depend on the order of the ions or of the threads.
+// the direct global path.  Every sum is an integer sum (each contribution is
+// rounded to a fixed-point integer first), so the moments do not depend on
+// the order of the ions or of the threads.
 #define TX 16
 #define TY 4
 #define TZ 4
@@ -485,6 +486,7 @@ __global__ void __launch_bounds__(256, 2)
     }
     __syncthreads();
     const uint32_t total = sh.pre[TY * TZ];
+    float tsum0 = 0.0f, tsum1 = 0.0f;  // per-brick partial sums, folded into FP64 below
     for (uint32_t base = 0; base < total; base += blockDim.x) {
       const uint32_t idx = base + threadIdx.x;
       const bool active = idx < total;
@@ -559,12 +561,12 @@ __global__ void __launch_bounds__(256, 2)
             nd = ch_neutral_density<float>(c, (float)(g.x0 + ((double)i + (double)p.x) * g.dx));
           const float lscale = pscale * nd;
           const float lam = lscale * gi;
-          vsum[0] += (double)lam;
+          tsum0 += lam;
           const uint32_t id = __float_as_uint(vv.w);
           const U4 r0 = ch_philox(id, c.step, CH_PURPOSE_COLLIDE << 24, c.run, c.seed_lo, c.seed_hi);
           if (lam > 0.0f && -logf(ch_unitf(r0.x)) / lam < 1.0f) ncol += ch_collide<float>(c, id, lscale, v, &nref);
           const float qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
-          vsum[1] += (double)ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), vnTf);
+          tsum1 += ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), vnTf);
         }
         vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
         P.vel[ip] = vv;
@@ -603,15 +605,18 @@ __global__ void __launch_bounds__(256, 2)
         const float w[8] = {wzl * wyl * wxl, wzl * wyl * wxh, wzl * wyh * wxl, wzl * wyh * wxh,
                             wzh * wyl * wxl, wzh * wyl * wxh, wzh * wyh * wxl, wzh * wyh * wxh};
         const int key = valid ? (dk * BY + dj) * BX + di : -1;
-        unsigned todo = __ballot_sync(0xffffffffu, valid);
-        while (todo) {
-          const int leader = __ffs(todo) - 1;
+        // The lanes that share the first valid lane's cell (usually most of a
+        // sorted warp) are summed with integer warp reductions, and lane q
+        // then adds sum q of the 32 (corner, moment) sums; every other lane
+        // adds its own 32 contributions.  All adds land in the shared tile.
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        if (vmask) {
+          const int leader = __ffs(vmask) - 1;
           const int lkey = __shfl_sync(0xffffffffu, key, leader);
           const bool mine = valid && key == lkey;
-          todo &= ~__ballot_sync(0xffffffffu, mine);
+          long long myval = 0;
 #pragma unroll
           for (int cn = 0; cn < 8; ++cn) {
-            const int node = lkey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
             const int cd = mine ? __float2int_rn(w[cn] * CH_TILE_DSCALE) : 0;
             const int cx = mine ? __float2int_rn(v[0] * w[cn] * CH_TILE_FSCALE) : 0;
             const int cy = mine ? __float2int_rn(v[1] * w[cn] * CH_TILE_FSCALE) : 0;
@@ -620,16 +625,35 @@ __global__ void __launch_bounds__(256, 2)
             const int sx = (int)__reduce_add_sync(0xffffffffu, (unsigned)cx);
             const int sy = (int)__reduce_add_sync(0xffffffffu, (unsigned)cy);
             const int sz = (int)__reduce_add_sync(0xffffffffu, (unsigned)cz);
-            if (lane == leader) {
-              atomicAdd((unsigned long long*)&sh.acc[0][node], (unsigned long long)((long long)sd << shift_d));
-              atomicAdd((unsigned long long*)&sh.acc[1][node], (unsigned long long)((long long)sx << shift_f));
-              atomicAdd((unsigned long long*)&sh.acc[2][node], (unsigned long long)((long long)sy << shift_f));
-              atomicAdd((unsigned long long*)&sh.acc[3][node], (unsigned long long)((long long)sz << shift_f));
+            if (lane == cn) myval = (long long)sd << shift_d;
+            if (lane == 8 + cn) myval = (long long)sx << shift_f;
+            if (lane == 16 + cn) myval = (long long)sy << shift_f;
+            if (lane == 24 + cn) myval = (long long)sz << shift_f;
+          }
+          {
+            const int cn = lane & 7, m = lane >> 3;
+            const int node = lkey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
+            if (myval != 0) atomicAdd((unsigned long long*)&sh.acc[m][node], (unsigned long long)myval);
+          }
+          if (valid && !mine) {
+#pragma unroll
+            for (int cn = 0; cn < 8; ++cn) {
+              const int node = key + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
+              const long long cd = (long long)__float2int_rn(w[cn] * CH_TILE_DSCALE) << shift_d;
+              const long long cx = (long long)__float2int_rn(v[0] * w[cn] * CH_TILE_FSCALE) << shift_f;
+              const long long cy = (long long)__float2int_rn(v[1] * w[cn] * CH_TILE_FSCALE) << shift_f;
+              const long long cz = (long long)__float2int_rn(v[2] * w[cn] * CH_TILE_FSCALE) << shift_f;
+              atomicAdd((unsigned long long*)&sh.acc[0][node], (unsigned long long)cd);
+              atomicAdd((unsigned long long*)&sh.acc[1][node], (unsigned long long)cx);
+              atomicAdd((unsigned long long*)&sh.acc[2][node], (unsigned long long)cy);
+              atomicAdd((unsigned long long*)&sh.acc[3][node], (unsigned long long)cz);
             }
           }
         }
       }
     }
+    vsum[0] += (double)tsum0;
+    vsum[1] += (double)tsum1;
     if (PH & PH_DEPOSIT) {
       __syncthreads();
       for (int q = threadIdx.x; q < 4 * BNODES; q += blockDim.x) {

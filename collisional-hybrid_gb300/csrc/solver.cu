@@ -231,7 +231,8 @@ __global__ void k_prec_dot(int64_t N, const T* __restrict__ dinv, const T* __res
 enum {
   S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_RHO, S_OMEGA, S_TS, S_TT, S_RV, S_SS, S_RR0, S_MEAN, S_TMP, S_NSLOT
 };
-enum { OP_SET_RZ_RR = 0, OP_CG_ALPHA, OP_CG_BETA, OP_RR, OP_BI_ALPHA, OP_BI_OMEGA, OP_BI_BETA, OP_SS, OP_MEAN, OP_TMP };
+enum { OP_SET_RZ_RR = 0, OP_CG_ALPHA, OP_CG_BETA, OP_RR, OP_BI_ALPHA, OP_BI_OMEGA, OP_BI_BETA, OP_SS, OP_MEAN, OP_TMP,
+       OP_SET_BICG };
 
 // Fixed-order reduction of K partials and the scalar update of one step.
 __global__ void k_scalar(const double* __restrict__ part, int nb, int K, int op, double* scal, double invN) {
@@ -281,6 +282,7 @@ __global__ void k_scalar(const double* __restrict__ part, int nb, int K, int op,
     }
     case OP_MEAN: scal[S_MEAN] = red[0] * invN; break;
     case OP_TMP: scal[S_TMP] = red[0]; break;
+    case OP_SET_BICG: scal[S_RHO] = scal[S_RR]; scal[S_BETA] = 0.0; scal[S_OMEGA] = 0.0; scal[S_ALPHA] = 0.0; break;
   }
 }
 
@@ -592,10 +594,18 @@ ch_status PotentialSolver::init(const ch_params& p, const GridDesc& g, int sms) 
   CH_CUDA_OK(cudaMalloc(&scal_, sizeof(double) * S_NSLOT));
   CH_CUDA_OK(cudaMemset(scal_, 0, sizeof(double) * S_NSLOT));
   CH_CUDA_OK(cudaMallocHost(&hscal_, sizeof(double) * S_NSLOT));
+  CH_CUDA_OK(cudaMallocHost(&hring_, sizeof(double) * 4));
+  for (auto& e : evs_) CH_CUDA_OK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   return CH_OK;
 }
 
 void PotentialSolver::release() {
+  for (auto& e : graphs_) cudaGraphExecDestroy(e.exec);
+  graphs_.clear();
+  for (auto& e : evs_)
+    if (e) cudaEventDestroy(e);
+  if (hring_) cudaFreeHost(hring_);
+  hring_ = nullptr;
   mg_release<float>(mg32_);
   mg_release<double>(mg64_);
   void* all[] = {r_, z_, pd_, q_, rh_, s_, t_, sh_, dinv_, n32_, b32_, x32_, r32_, z32_, p32_, q32_, rh32_,
@@ -797,62 +807,86 @@ ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* 
     *rnorm_out = sqrt(rr);
     return CH_OK;
   }
-  if (p_.ksp_type == CH_KSP_CG) {
-    k_cg_p<T><<<nb, 256, 0, s>>>(N, scal_, z, pp, 1), ::ch::note_launch();
-    while (it < maxit) {
-      k_apply<T><<<nb, 256, 0, s>>>(g, C, n, pp, q, pp, part_), ::ch::note_launch();
-      k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_CG_ALPHA, scal_, 0.0), ::ch::note_launch();
-      if (mg) {
-        k_cg_xr_plain<T><<<nb, 256, 0, s>>>(N, scal_, x, r, pp, q), ::ch::note_launch();
-        precond(r, z);
-      } else {
-        k_cg_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, r, pp, q, dinv, z, part_), ::ch::note_launch();
-      }
-      k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_CG_BETA, scal_, 0.0), ::ch::note_launch();
-      ++it;
-      CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_RR, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s));
-      CH_CUDA_OK(cudaStreamSynchronize(s));
-      rr = hscal_[S_RR];
-      if (!(sqrt(rr) > tol)) break;
-      k_cg_p<T><<<nb, 256, 0, s>>>(N, scal_, z, pp, 0), ::ch::note_launch();
+  // One iteration, enqueued on s directly or under graph capture.  Scalars
+  // stay on the device, so an iteration has no host dependency.
+  auto cg_body = [&]() {
+    k_apply<T><<<nb, 256, 0, s>>>(g, C, n, pp, q, pp, part_), ::ch::note_launch();
+    k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_CG_ALPHA, scal_, 0.0), ::ch::note_launch();
+    if (mg) {
+      k_cg_xr_plain<T><<<nb, 256, 0, s>>>(N, scal_, x, r, pp, q), ::ch::note_launch();
+      precond(r, z);
+    } else {
+      k_cg_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, r, pp, q, dinv, z, part_), ::ch::note_launch();
     }
+    k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_CG_BETA, scal_, 0.0), ::ch::note_launch();
+    k_cg_p<T><<<nb, 256, 0, s>>>(N, scal_, z, pp, 0), ::ch::note_launch();
+  };
+  // BiCGStab, right preconditioned (van der Vorst 1992); p = v = 0 at the
+  // start makes the first p = r whatever beta and omega hold.
+  auto bi_body = [&]() {
+    k_bi_p<T><<<nb, 256, 0, s>>>(N, scal_, r, pp, q, mg ? (const T*)nullptr : dinv, z, 0),
+        ::ch::note_launch();  // z = y = M p
+    if (mg) mg_vcycle<T>(*mg, 0, pp, z, s);
+    k_apply<T><<<nb, 256, 0, s>>>(g, C, n, z, q, rh, part_), ::ch::note_launch();  // v = A y; rh.v
+    k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_BI_ALPHA, scal_, 0.0), ::ch::note_launch();
+    k_bi_s<T><<<nb, 256, 0, s>>>(N, scal_, r, q, mg ? (const T*)nullptr : dinv, sv, sh, part_),
+        ::ch::note_launch();
+    if (mg) mg_vcycle<T>(*mg, 0, sv, sh, s);
+    k_apply_dot2<T><<<nb, 256, 0, s>>>(g, C, n, sh, tv, sv, part_), ::ch::note_launch();
+    k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_OMEGA, scal_, 0.0), ::ch::note_launch();
+    k_bi_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, z, sh, r, sv, tv, rh, part_), ::ch::note_launch();
+    k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_BETA, scal_, 0.0), ::ch::note_launch();
+  };
+  const bool cg = p_.ksp_type == CH_KSP_CG;
+  if (cg) {
+    k_cg_p<T><<<nb, 256, 0, s>>>(N, scal_, z, pp, 1), ::ch::note_launch();
   } else {
-    // BiCGStab, right preconditioned (van der Vorst 1992)
     k_copy<T><<<nb, 256, 0, s>>>(N, r, rh), ::ch::note_launch();
     k_zero<T><<<nb, 256, 0, s>>>(N, pp), ::ch::note_launch();
     k_zero<T><<<nb, 256, 0, s>>>(N, q), ::ch::note_launch();  // v
-    // rho = rh.r = r.r
-    CH_CUDA_OK(cudaMemcpyAsync(scal_ + S_RHO, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToDevice, s));
-    bool first = true;
-    while (it < maxit) {
-      k_bi_p<T><<<nb, 256, 0, s>>>(N, scal_, r, pp, q, mg ? (const T*)nullptr : dinv, z, first ? 1 : 0),
-          ::ch::note_launch();  // z = y = M p
-      if (mg) mg_vcycle<T>(*mg, 0, pp, z, s);
-      first = false;
-      k_apply<T><<<nb, 256, 0, s>>>(g, C, n, z, q, rh, part_), ::ch::note_launch();                  // v = A y; rh.v
-      k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_BI_ALPHA, scal_, 0.0), ::ch::note_launch();
-      k_bi_s<T><<<nb, 256, 0, s>>>(N, scal_, r, q, mg ? (const T*)nullptr : dinv, sv, sh, part_),
-          ::ch::note_launch();
-      k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_SS, scal_, 0.0), ::ch::note_launch();
-      ++it;
-      CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_SS, scal_ + S_SS, sizeof(double), cudaMemcpyDeviceToHost, s));
-      CH_CUDA_OK(cudaStreamSynchronize(s));
-      if (!(sqrt(hscal_[S_SS]) > tol)) {
-        k_bi_half<T><<<nb, 256, 0, s>>>(N, scal_, x, z, r, sv), ::ch::note_launch();
-        rr = hscal_[S_SS];
-        break;
-      }
-      if (mg) mg_vcycle<T>(*mg, 0, sv, sh, s);
-      k_apply_dot2<T><<<nb, 256, 0, s>>>(g, C, n, sh, tv, sv, part_), ::ch::note_launch();
-      k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_OMEGA, scal_, 0.0), ::ch::note_launch();
-      k_bi_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, z, sh, r, sv, tv, rh, part_), ::ch::note_launch();
-      k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_BETA, scal_, 0.0), ::ch::note_launch();
-      CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_RR, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s));
-      CH_CUDA_OK(cudaStreamSynchronize(s));
-      rr = hscal_[S_RR];
-      if (!(sqrt(rr) > tol)) break;
+    k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_SET_BICG, scal_, 0.0), ::ch::note_launch();
+  }
+  // the iteration as one CUDA graph (captured once per buffer set)
+  GraphKey key{(int)sizeof(T), (int)p_.ksp_type, (const void*)mg, (const void*)n, (const void*)b, (const void*)x};
+  GraphEntry* ge = nullptr;
+  for (auto& e : graphs_)
+    if (e.k == key) ge = &e;
+  if (!ge) {
+    cudaGraph_t graph;
+    const unsigned long long before = ::ch::launches_now();
+    CH_CUDA_OK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    if (cg) cg_body(); else bi_body();
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (ce != cudaSuccess) return ch_cuda_fail(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
+    const long long nodes = (long long)(::ch::launches_now() - before);
+    ::ch::note_launch_n(-nodes);  // captured, not yet launched
+    GraphEntry e;
+    e.k = key;
+    e.nodes = nodes;
+    ce = cudaGraphInstantiate(&e.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return ch_cuda_fail(ce, "cudaGraphInstantiate", __FILE__, __LINE__);
+    graphs_.push_back(e);
+    ge = &graphs_.back();
+  }
+  // Launch iterations back to back; test iteration k-1's residual while
+  // iteration k runs (so a converged solve runs one extra iteration).
+  const int RING = 4;
+  bool converged = false;
+  while (it < maxit) {
+    CH_CUDA_OK(cudaGraphLaunch(ge->exec, s));
+    ::ch::note_launch_n(ge->nodes);
+    CH_CUDA_OK(cudaMemcpyAsync(hring_ + it % RING, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CH_CUDA_OK(cudaEventRecord(evs_[it % RING], s));
+    ++it;
+    if (it >= 2) {
+      CH_CUDA_OK(cudaEventSynchronize(evs_[(it - 2) % RING]));
+      if (!(sqrt(hring_[(it - 2) % RING]) > tol)) { converged = true; break; }
     }
   }
+  CH_CUDA_OK(cudaStreamSynchronize(s));
+  rr = hring_[(it - 1) % RING];
+  (void)converged;
   *its = it;
   *rnorm_out = sqrt(rr);
   return CH_OK;

@@ -2,6 +2,8 @@
 // src/lhs.c, src/rhs.c) as matrix-free sm_103a kernels.
 #pragma once
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace ch {
@@ -92,6 +94,22 @@ class PotentialSolver {
   // FP32 workspace (mixed form)
   float *n32_ = nullptr, *b32_ = nullptr, *x32_ = nullptr, *r32_ = nullptr, *z32_ = nullptr, *p32_ = nullptr,
         *q32_ = nullptr, *rh32_ = nullptr, *s32_ = nullptr, *t32_ = nullptr, *sh32_ = nullptr, *dinv32_ = nullptr;
+  // one captured Krylov iteration per (precision, method, buffers)
+  struct GraphKey {
+    int tsize, ksp;
+    const void *mg, *n, *b, *x;
+    bool operator==(const GraphKey& o) const {
+      return tsize == o.tsize && ksp == o.ksp && mg == o.mg && n == o.n && b == o.b && x == o.x;
+    }
+  };
+  struct GraphEntry {
+    GraphKey k;
+    cudaGraphExec_t exec;
+    long long nodes;
+  };
+  std::vector<GraphEntry> graphs_;
+  cudaEvent_t evs_[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* hring_ = nullptr;
   MGHier<float> mg32_;
   MGHier<double> mg64_;
   double* part_ = nullptr;  // block partials
