@@ -424,10 +424,22 @@ __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, 
 
 struct TileShared {
   float4 E[BNODES];
-  long long acc[4][BNODES];
+  unsigned acc_lo[4][BNODES];  // 64-bit fixed-point sums as lo + hi * 2^32,
+  int acc_hi[4][BNODES];       // carried exactly so the split stays order-free
   uint32_t rowbeg[TY * TZ];
   uint32_t pre[TY * TZ + 1];
 };
+
+// value += v for a 64-bit integer kept as (hi, lo) 32-bit words in shared
+// memory; the carry out of lo is detected from the returned old value, so
+// the final (hi, lo) is the exact 64-bit sum whatever the order of adds.
+__device__ __forceinline__ void shared_add64(unsigned* lo, int* hi, long long v) {
+  const unsigned vlo = (unsigned)(unsigned long long)v;
+  const int vhi = (int)(v >> 32);
+  const unsigned old = atomicAdd(lo, vlo);
+  const int carry = (old + vlo < old) ? 1 : 0;
+  if (vhi + carry != 0) atomicAdd(hi, vhi + carry);
+}
 
 template <int PH>
 __global__ void __launch_bounds__(256, 2)
@@ -464,7 +476,8 @@ __global__ void __launch_bounds__(256, 2)
         sh.E[q] = __ldg(E + ((int64_t)gk * g.Ny + gj) * g.Nx + gi);
       }
       if (PH & PH_DEPOSIT) {
-        sh.acc[0][q] = 0; sh.acc[1][q] = 0; sh.acc[2][q] = 0; sh.acc[3][q] = 0;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) { sh.acc_lo[m][q] = 0u; sh.acc_hi[m][q] = 0; }
       }
     }
     if (threadIdx.x == 0) {
@@ -564,9 +577,17 @@ __global__ void __launch_bounds__(256, 2)
           tsum0 += lam;
           const uint32_t id = __float_as_uint(vv.w);
           const U4 r0 = ch_philox(id, c.step, CH_PURPOSE_COLLIDE << 24, c.run, c.seed_lo, c.seed_hi);
-          if (lam > 0.0f && -logf(ch_unitf(r0.x)) / lam < 1.0f) ncol += ch_collide<float>(c, id, lscale, v, &nref);
-          const float qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
-          tsum1 += ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), vnTf);
+          // first event inside the step: -log(u) < lam  <=>  u > exp(-lam)
+          float gnext = gi;
+          if (lam > 0.0f && ch_unitf(r0.x) > __expf(-lam)) {
+            const float v0 = v[0], v1 = v[1], v2 = v[2];
+            ncol += ch_collide<float>(c, id, lscale, v, &nref);
+            if (v[0] != v0 || v[1] != v1 || v[2] != v2) {
+              const float qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
+              gnext = ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), vnTf);
+            }
+          }
+          tsum1 += gnext;
         }
         vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
         P.vel[ip] = vv;
@@ -633,7 +654,7 @@ __global__ void __launch_bounds__(256, 2)
           {
             const int cn = lane & 7, m = lane >> 3;
             const int node = lkey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
-            if (myval != 0) atomicAdd((unsigned long long*)&sh.acc[m][node], (unsigned long long)myval);
+            if (myval != 0) shared_add64(&sh.acc_lo[m][node], &sh.acc_hi[m][node], myval);
           }
           if (valid && !mine) {
 #pragma unroll
@@ -643,10 +664,10 @@ __global__ void __launch_bounds__(256, 2)
               const long long cx = (long long)__float2int_rn(v[0] * w[cn] * CH_TILE_FSCALE) << shift_f;
               const long long cy = (long long)__float2int_rn(v[1] * w[cn] * CH_TILE_FSCALE) << shift_f;
               const long long cz = (long long)__float2int_rn(v[2] * w[cn] * CH_TILE_FSCALE) << shift_f;
-              atomicAdd((unsigned long long*)&sh.acc[0][node], (unsigned long long)cd);
-              atomicAdd((unsigned long long*)&sh.acc[1][node], (unsigned long long)cx);
-              atomicAdd((unsigned long long*)&sh.acc[2][node], (unsigned long long)cy);
-              atomicAdd((unsigned long long*)&sh.acc[3][node], (unsigned long long)cz);
+              shared_add64(&sh.acc_lo[0][node], &sh.acc_hi[0][node], cd);
+              shared_add64(&sh.acc_lo[1][node], &sh.acc_hi[1][node], cx);
+              shared_add64(&sh.acc_lo[2][node], &sh.acc_hi[2][node], cy);
+              shared_add64(&sh.acc_lo[3][node], &sh.acc_hi[3][node], cz);
             }
           }
         }
@@ -658,7 +679,8 @@ __global__ void __launch_bounds__(256, 2)
       __syncthreads();
       for (int q = threadIdx.x; q < 4 * BNODES; q += blockDim.x) {
         const int m = q / BNODES, nd = q % BNODES;
-        const long long a = sh.acc[m][nd];
+        const long long a = (long long)(((unsigned long long)(unsigned)sh.acc_hi[m][nd] << 32) |
+                                        (unsigned long long)sh.acc_lo[m][nd]);
         if (a != 0) {
           const int bi = nd % BX, bj = (nd / BX) % BY, bk = nd / (BX * BY);
           const int gi = ch_wrap(bi0 + bi, g.Nx), gj = ch_wrap(bj0 + bj, g.Ny), gk = ch_wrap(bk0 + bk, g.Nz);
