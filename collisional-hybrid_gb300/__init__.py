@@ -90,6 +90,26 @@ class StepInfo(C.Structure):
                     refinements=self.solve.refinements, rnorm=self.solve.rnorm, bnorm=self.solve.bnorm)
 
 
+class RunInfo(C.Structure):
+    """ch_run_info: one run of a batch step."""
+
+    _fields_ = [("Nc", C.c_int64), ("collisions", C.c_int64), ("refused", C.c_int64), ("expected", C.c_double),
+                ("solve", SolveInfo), ("status", C.c_int32), ("flags", C.c_int32)]
+
+    def as_dict(self):
+        return dict(Nc=self.Nc, collisions=self.collisions, refused=self.refused, expected=self.expected,
+                    iterations=self.solve.iterations, refinements=self.solve.refinements, rnorm=self.solve.rnorm,
+                    bnorm=self.solve.bnorm, status=self.status, flags=self.flags)
+
+
+class Tuning(C.Structure):
+    _fields_ = [("cluster", C.c_int32), ("pass_ctas_per_sm", C.c_int32), ("pass_ms", C.c_double),
+                ("solve_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Profile(C.Structure):
     _fields_ = [("pass_ms", C.c_double), ("pass_calls", C.c_int64), ("solve_ms", C.c_double),
                 ("solve_calls", C.c_int64), ("sort_ms", C.c_double), ("sort_calls", C.c_int64),
@@ -135,6 +155,22 @@ def lib():
             "ch_get_stream": [vp, C.POINTER(vp)],
             "ch_host_register": [vp, C.c_uint64],
             "ch_host_unregister": [vp],
+            "ch_batch_create": [vp, vp, C.c_int32, C.c_int32, C.POINTER(vp)],
+            "ch_batch_destroy": [vp],
+            "ch_batch_load": [vp, vp],
+            "ch_batch_upload": [vp, C.c_int32, vp, vp],
+            "ch_batch_download": [vp, C.c_int32, vp, vp],
+            "ch_batch_initialize": [vp],
+            "ch_batch_step": [vp, C.c_int64, C.c_int32, vp],
+            "ch_batch_get_phi": [vp, C.c_int32, vp],
+            "ch_batch_set_phi": [vp, C.c_int32, vp],
+            "ch_batch_get_moments": [vp, C.c_int32, vp],
+            "ch_batch_autotune": [vp, C.POINTER(Tuning)],
+            "ch_batch_set_tuning": [vp, C.POINTER(Tuning)],
+            "ch_batch_get_tuning": [vp, C.POINTER(Tuning)],
+            "ch_batch_set_profiling": [vp, C.c_int32],
+            "ch_batch_get_profile": [vp, C.POINTER(Profile)],
+            "ch_batch_get_stream": [vp, C.POINTER(vp)],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -320,6 +356,112 @@ class Hybrid:
     def stream_handle(self) -> int:
         s = C.c_void_p()
         _check(lib().ch_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+
+class Batch:
+    """An ensemble of independent runs advanced together (ch_batch): every
+    phase of a step is one launch over all runs, replayed from a CUDA graph.
+    Runs may differ in grid, ion count and parameters (mixed form, full
+    operator, CG + multigrid)."""
+
+    def __init__(self, params, nions, device: int = -1):
+        self.n = len(params)
+        self.params = list(params)
+        self._p = (Params * self.n)(*self.params)
+        self.np = [int(v) for v in nions]
+        self._np = (C.c_int64 * self.n)(*self.np)
+        h = C.c_void_p()
+        _check(lib().ch_batch_create(C.cast(self._p, C.c_void_p), C.cast(self._np, C.c_void_p), self.n, device,
+                                     C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ch_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def N(self, r: int) -> int:
+        p = self.params[r]
+        return p.Nx * p.Ny * p.Nz
+
+    def load(self, loaders):
+        arr = (Loader * self.n)(*loaders)
+        _check(lib().ch_batch_load(self._h, C.cast(arr, C.c_void_p)))
+
+    def upload(self, r: int, pos: np.ndarray, vel: np.ndarray):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        assert pos.shape == vel.shape == (self.np[r], 4)
+        _check(lib().ch_batch_upload(self._h, int(r), pos.ctypes.data, vel.ctypes.data))
+
+    def download(self, r: int):
+        pos = np.empty((self.np[r], 4))
+        vel = np.empty((self.np[r], 4))
+        _check(lib().ch_batch_download(self._h, int(r), pos.ctypes.data, vel.ctypes.data))
+        return pos, vel
+
+    def initialize(self):
+        _check(lib().ch_batch_initialize(self._h))
+
+    def step(self, first_step: int, nsteps: int = 1):
+        info = (RunInfo * self.n)()
+        rc = lib().ch_batch_step(self._h, int(first_step), int(nsteps), C.cast(info, C.c_void_p))
+        self.last_info = [i.as_dict() for i in info]
+        _check(rc)
+        return self.last_info
+
+    def phi(self, r: int):
+        out = np.empty(self.N(r))
+        _check(lib().ch_batch_get_phi(self._h, int(r), out.ctypes.data))
+        return out
+
+    def set_phi(self, r: int, phi: np.ndarray):
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        _check(lib().ch_batch_set_phi(self._h, int(r), phi.ctypes.data))
+
+    def moments(self, r: int):
+        out = np.empty((self.N(r), 4))
+        _check(lib().ch_batch_get_moments(self._h, int(r), out.ctypes.data))
+        return out
+
+    def autotune(self) -> dict:
+        t = Tuning()
+        _check(lib().ch_batch_autotune(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        _check(lib().ch_batch_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, cluster: int, pass_ctas_per_sm: int = 2):
+        t = Tuning(cluster, pass_ctas_per_sm, 0.0, 0.0)
+        _check(lib().ch_batch_set_tuning(self._h, C.byref(t)))
+
+    def set_profiling(self, on: bool = True):
+        _check(lib().ch_batch_set_profiling(self._h, int(on)))
+
+    def profile(self) -> dict:
+        pr = Profile()
+        _check(lib().ch_batch_get_profile(self._h, C.byref(pr)))
+        return pr.as_dict()
+
+    def stream_handle(self) -> int:
+        s = C.c_void_p()
+        _check(lib().ch_batch_get_stream(self._h, C.byref(s)))
         return s.value or 0
 
 

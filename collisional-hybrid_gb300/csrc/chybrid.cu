@@ -142,6 +142,10 @@ static ch_status validate(const ch_params* p) {
   if (!(p->ksp_rtol > 0.0) || p->ksp_max_it < 1) return ch_fail(CH_ERR_ARG, "bad ksp tolerance / max_it");
   if (p->mn > 0.0 && !(p->viT[0] > 0.0 || p->viT[1] > 0.0 || p->viT[2] > 0.0))
     return ch_fail(CH_ERR_ARG, "collisions need a positive ion thermal speed (vrm, src/particles.c:511)");
+  if (p->deposit_scale_log2 != 0.0 &&
+      !(p->deposit_scale_log2 >= (p->precision == CH_MIXED ? 22.0 : 1.0) && p->deposit_scale_log2 <= 62.0))
+    return ch_fail(CH_ERR_ARG, "deposit_scale_log2 %g outside [%d, 62]", p->deposit_scale_log2,
+                   p->precision == CH_MIXED ? 22 : 1);
   return CH_OK;
 }
 

@@ -15,11 +15,24 @@
 // sums do not depend on the order of the additions, so the moments are
 // identical run to run whatever the thread schedule or particle order.
 #include "particles.cuh"
+
+#include <atomic>
+
 #include "physics.cuh"
 
 namespace ch {
 
 // ------------------------------------------------------------------ helpers
+// Mean relative speeds g of the mixed form are summed as integers of 2^-20:
+// the FP64 partial sums are exact while the total stays below 2^33 (2^53
+// units; 134 M ions of thermal speed 1 sum to about 2^28), so S does not
+// depend on the order of the ions.
+#define CH_G_UNIT (1.0 / 1048576.0)
+__device__ __forceinline__ unsigned long long g_fixed(float g) {
+  // g < 2^12 in any plasma the fixed-point deposit admits; 32-bit conversion
+  return (unsigned long long)__float2uint_rn(g * 1048576.0f);
+}
+
 __device__ __forceinline__ void red_add(unsigned long long* a, long long v) {
   atomicAdd(a, (unsigned long long)v);
 }
@@ -74,7 +87,7 @@ __device__ __forceinline__ uint32_t agg_inc(uint32_t* counts, uint32_t key, bool
 
 // Block-wide sum of K doubles into part[blockIdx.x * K + q], fixed order.
 template <int K>
-__device__ __forceinline__ void block_partials(double (&v)[K], double* __restrict__ part) {
+__device__ __forceinline__ void block_partials(double (&v)[K], double* __restrict__ part, int slot = -1) {
   __shared__ double sm[K][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
@@ -91,7 +104,7 @@ __device__ __forceinline__ void block_partials(double (&v)[K], double* __restric
       double x = lane < nw ? sm[q][lane] : 0.0;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-      if (lane == 0) part[(size_t)blockIdx.x * K + q] = x;
+      if (lane == 0) part[(size_t)(slot < 0 ? (int)blockIdx.x : slot) * K + q] = x;
     }
   }
 }
@@ -418,16 +431,48 @@ __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, 
 #define BY (TY + 3)
 #define BZ (TZ + 3)
 #define BNODES (BX * BY * BZ)
-#define CH_TILE_DSCALE 16777216.0f   // 2^24: density contributions (w <= 1)
-#define CH_TILE_FSCALE 1048576.0f    // 2^20: flux contributions (|v| < CH_TILE_VMAX)
-#define CH_TILE_VMAX 32.0f
+#define CH_TILE_DSCALE 4194304.0f    // 2^22: density contributions (w <= 1)
+#define CH_TILE_FSCALE 524288.0f     // 2^19: flux contributions (|v| < CH_TILE_VMAX)
+#define CH_TILE_VMAX 8.0f
+#define CH_TILE_DLOG2 22
+#define CH_TILE_FLOG2 19
+// Round-to-nearest-even of |x| <= 2^22 on the FP32 pipe: x + 1.5 * 2^23 lies
+// in [2^23, 2^24), where floats are the integers, so the bits of the sum are
+// rint(x) + CH_RNI_BIAS (the conversion unit runs at a fraction of the rate).
+#define CH_RNI_BIAS 0x4B400000
+__device__ __forceinline__ int rni_biased(float x) { return __float_as_int(__fadd_rn(x, 12582912.0f)); }
+__device__ __forceinline__ int rni(float x) { return rni_biased(x) - CH_RNI_BIAS; }
+
+#define CH_TILE_QCAP 512       // ring of deferred colliding ions (power of two, >= 2 x threads)
+#define CH_TILE_ROUNDS 3       // key groups a warp reduces before per-lane adds
+
+#define CH_TILE_K 4            // consecutive slots one thread deposits together
+#define CH_TILE_BATCH (256 * CH_TILE_K)
 
 struct TileShared {
   float4 E[BNODES];
-  unsigned acc_lo[4][BNODES];  // 64-bit fixed-point sums as lo + hi * 2^32,
-  int acc_hi[4][BNODES];       // carried exactly so the split stays order-free
+  // One batch of CH_TILE_BATCH ions staged between the push and the deposit:
+  // box key of the ion's cell (-1: nothing to deposit here), offsets and
+  // velocity.  Thread t deposits slots CH_TILE_K t .. CH_TILE_K t + K-1.
+  alignas(16) int st_key[CH_TILE_BATCH];
+  alignas(16) float st_ox[CH_TILE_BATCH];
+  alignas(16) float st_oy[CH_TILE_BATCH];
+  alignas(16) float st_oz[CH_TILE_BATCH];
+  alignas(16) float st_vx[CH_TILE_BATCH];
+  alignas(16) float st_vy[CH_TILE_BATCH];
+  alignas(16) float st_vz[CH_TILE_BATCH];
+  unsigned acc_lo[4][BNODES];  // 64-bit fixed-point sums at the tile scale as
+  int acc_hi[4][BNODES];       // lo + hi * 2^32, carried exactly (order-free)
   uint32_t rowbeg[TY * TZ];
   uint32_t pre[TY * TZ + 1];
+  // Ions whose first collision event falls inside the step are queued here
+  // after the Boris push and finished (collide, move, deposit) together, so
+  // the long collision code runs on full warps instead of one lane in 40.
+  float4 q_pos[CH_TILE_QCAP];   // offsets + packed cell, before the move
+  float4 q_vel[CH_TILE_QCAP];   // velocity after the push, rate scale in w
+  uint32_t q_ip[CH_TILE_QCAP];
+  uint32_t q_id[CH_TILE_QCAP];
+  unsigned qn;                  // enqueued in this brick (monotone; slot = qn mod CH_TILE_QCAP)
 };
 
 // value += v for a 64-bit integer kept as (hi, lo) 32-bit words in shared
@@ -441,18 +486,124 @@ __device__ __forceinline__ void shared_add64(unsigned* lo, int* hi, long long v)
   if (vhi + carry != 0) atomicAdd(hi, vhi + carry);
 }
 
+// One ion's 32 fixed-point contributions added lane by lane to the shared
+// tile (node = the ion's cell within the box).
+__device__ __forceinline__ void tile_deposit_lane(TileShared& sh, int node, float wxh, float wyh, float wzh,
+                                                  float vx, float vy, float vz) {
+  const float wxl = 1.0f - wxh, wyl = 1.0f - wyh, wzl = 1.0f - wzh;
+  const float w[8] = {wzl * wyl * wxl, wzl * wyl * wxh, wzl * wyh * wxl, wzl * wyh * wxh,
+                      wzh * wyl * wxl, wzh * wyl * wxh, wzh * wyh * wxl, wzh * wyh * wxh};
+#pragma unroll
+  for (int cn = 0; cn < 8; ++cn) {
+    const int nd = node + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
+    const float wf = w[cn] * CH_TILE_FSCALE;
+    shared_add64(&sh.acc_lo[0][nd], &sh.acc_hi[0][nd], rni(w[cn] * CH_TILE_DSCALE));
+    shared_add64(&sh.acc_lo[1][nd], &sh.acc_hi[1][nd], rni(vx * wf));
+    shared_add64(&sh.acc_lo[2][nd], &sh.acc_hi[2][nd], rni(vy * wf));
+    shared_add64(&sh.acc_lo[3][nd], &sh.acc_hi[3][nd], rni(vz * wf));
+  }
+}
+
+// Deposit of one staged batch.  Thread t sums the 32 fixed-point
+// contributions of its CH_TILE_K consecutive slots that share the cell of its
+// first valid slot (in cell-sorted ions, usually all of them) in registers;
+// a slot in another cell is added lane by lane.  The threads of a warp whose
+// first cells agree (one or two groups per sorted warp, up to
+// CH_TILE_ROUNDS) are then summed with integer warp reductions, lane q adding
+// sum q; the rest add their own sums.  Every contribution is rounded to an
+// integer before any addition, so the result does not depend on the order.
+__device__ __forceinline__ void tile_deposit_batch(TileShared& sh, int lane) {
+  const int t = threadIdx.x;
+  const int4 kq = reinterpret_cast<const int4*>(sh.st_key)[t];
+  const float4 X = reinterpret_cast<const float4*>(sh.st_ox)[t], Y = reinterpret_cast<const float4*>(sh.st_oy)[t],
+               Z = reinterpret_cast<const float4*>(sh.st_oz)[t], VX = reinterpret_cast<const float4*>(sh.st_vx)[t],
+               VY = reinterpret_cast<const float4*>(sh.st_vy)[t], VZ = reinterpret_cast<const float4*>(sh.st_vz)[t];
+  const int keys[4] = {kq.x, kq.y, kq.z, kq.w};
+  const float ox[4] = {X.x, X.y, X.z, X.w}, oy[4] = {Y.x, Y.y, Y.z, Y.w}, oz[4] = {Z.x, Z.y, Z.z, Z.w};
+  const float vx[4] = {VX.x, VX.y, VX.z, VX.w}, vy[4] = {VY.x, VY.y, VY.z, VY.w}, vz[4] = {VZ.x, VZ.y, VZ.z, VZ.w};
+  int akey = -1;
+#pragma unroll
+  for (int k = 0; k < CH_TILE_K; ++k) akey = (akey < 0) ? keys[k] : akey;
+  unsigned a[32];
+#pragma unroll
+  for (int q = 0; q < 32; ++q) a[q] = 0u;
+  unsigned cnt = 0;
+#pragma unroll
+  for (int k = 0; k < CH_TILE_K; ++k) {
+    if (keys[k] < 0) continue;
+    if (keys[k] != akey) {
+      tile_deposit_lane(sh, keys[k], ox[k], oy[k], oz[k], vx[k], vy[k], vz[k]);
+      continue;
+    }
+    ++cnt;
+    const float wxh = ox[k], wyh = oy[k], wzh = oz[k];
+    const float wxl = 1.0f - wxh, wyl = 1.0f - wyh, wzl = 1.0f - wzh;
+    const float w[8] = {wzl * wyl * wxl, wzl * wyl * wxh, wzl * wyh * wxl, wzl * wyh * wxh,
+                        wzh * wyl * wxl, wzh * wyl * wxh, wzh * wyh * wxl, wzh * wyh * wxh};
+    // (v 2^19) w equals v (w 2^19) exactly: the scale is a power of two
+    const float fx = vx[k] * CH_TILE_FSCALE, fy = vy[k] * CH_TILE_FSCALE, fz = vz[k] * CH_TILE_FSCALE;
+#pragma unroll
+    for (int cn = 0; cn < 8; ++cn) {
+      a[cn] += (unsigned)rni_biased(w[cn] * CH_TILE_DSCALE);
+      a[8 + cn] += (unsigned)rni_biased(fx * w[cn]);
+      a[16 + cn] += (unsigned)rni_biased(fy * w[cn]);
+      a[24 + cn] += (unsigned)rni_biased(fz * w[cn]);
+    }
+  }
+  const unsigned unbias = cnt * (unsigned)CH_RNI_BIAS;
+#pragma unroll
+  for (int q = 0; q < 32; ++q) a[q] -= unbias;  // exact sums, |sum| < 2^25
+  unsigned rem = __ballot_sync(0xffffffffu, akey >= 0);
+#pragma unroll 1
+  for (int round = 0; rem && round < CH_TILE_ROUNDS; ++round) {
+    const int leader = __ffs(rem) - 1;
+    const int lkey = __shfl_sync(0xffffffffu, akey, leader);
+    const bool mine = ((rem >> lane) & 1u) && akey == lkey;
+    rem &= ~__ballot_sync(0xffffffffu, mine);
+    int myval = 0;
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      const int sq = (int)__reduce_add_sync(0xffffffffu, mine ? a[q] : 0u);
+      myval = lane == q ? sq : myval;
+    }
+    const int cn = lane & 7, m = lane >> 3;
+    const int node = lkey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
+    if (myval != 0)
+      shared_add64(&sh.acc_lo[m][node], &sh.acc_hi[m][node], myval);
+  }
+  if ((rem >> lane) & 1u) {
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      const int cn = q & 7, m = q >> 3;
+      const int node = akey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
+      if (a[q] != 0u)
+        shared_add64(&sh.acc_lo[m][node], &sh.acc_hi[m][node], (long long)(int)a[q]);
+    }
+  }
+}
+
+// Box-relative cell offset of (i, j, k) from the box origin, periodic.
+__device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, int bi0, int bj0, int bk0,
+                                       bool* inbox) {
+  int di = i - bi0, dj = j - bj0, dk = k - bk0;
+  di += di < 0 ? g.Nx : 0; di -= di >= g.Nx ? g.Nx : 0;
+  dj += dj < 0 ? g.Ny : 0; dj -= dj >= g.Ny ? g.Ny : 0;
+  dk += dk < 0 ? g.Nz : 0; dk -= dk >= g.Nz ? g.Nz : 0;
+  *inbox = di <= BX - 2 && dj <= BY - 2 && dk <= BZ - 2;
+  return (dk * BY + dj) * BX + di;
+}
+
+// One brick of the tiled pass: tile index `tile` of the run described by c
+// (starts, E, acc and hist are the run's own arrays; starts holds indices
+// into P).  Per-thread sums go to vsum / ncol / nref / bad.
 template <int PH>
-__global__ void __launch_bounds__(256, 2)
-    k_pass_tiled(StepConsts c, MixParticles P, const float4* __restrict__ E, const uint32_t* __restrict__ starts,
-                 unsigned long long* __restrict__ acc, float pscale, int shift_d, int shift_f, DevCounters* cnt,
-                 double* part, uint32_t* hist) {
-  extern __shared__ __align__(16) unsigned char smem_tiled[];
-  TileShared& sh = *reinterpret_cast<TileShared*>(smem_tiled);
+__device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, MixParticles P,
+                                          const float4* __restrict__ E, const uint32_t* __restrict__ starts,
+                                          unsigned long long* __restrict__ acc, float pscale, int shift_d,
+                                          int shift_f, uint32_t* hist, int tile, double (&vsum)[2], unsigned& ncol,
+                                          unsigned& nref, int& bad) {
   const GridDesc& g = c.g;
   const int lane = threadIdx.x & 31;
-  double vsum[2] = {0.0, 0.0};
-  unsigned ncol = 0, nref = 0;
-  int bad = 0;
   const float dtx = (float)(c.dt / g.dx), dty = (float)(c.dt / g.dy), dtz = (float)(c.dt / g.dz);
   const float vnTf = (float)c.vnT, vn0x = (float)c.vn0[0], vn0y = (float)c.vn0[1], vn0z = (float)c.vn0[2];
   const float t0 = (float)c.t[0], t1 = (float)c.t[1], t2 = (float)c.t[2];
@@ -461,52 +612,79 @@ __global__ void __launch_bounds__(256, 2)
               pE0z = (float)(c.E0[2] * c.tscale);
   const bool cross = !(c.faithful & CH_FAITHFUL_D2);
   const bool move = (PH & PH_MOVE) && !(c.faithful & CH_FAITHFUL_D5);
-  const int ntx = (g.Nx + TX - 1) / TX, nty = (g.Ny + TY - 1) / TY, ntz = (g.Nz + TZ - 1) / TZ;
-  const int ntiles = ntx * nty * ntz;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int i0 = (tile % ntx) * TX, j0 = ((tile / ntx) % nty) * TY, k0 = (tile / (ntx * nty)) * TZ;
-    const int i1 = min(i0 + TX, g.Nx), j1 = min(j0 + TY, g.Ny), k1 = min(k0 + TZ, g.Nz);
-    const int bi0 = i0 - 1, bj0 = j0 - 1, bk0 = k0 - 1;  // box origin (node)
-    __syncthreads();  // previous brick's flush is done
-    // stage the node field, clear the deposit tile, row ranges
-    for (int q = threadIdx.x; q < BNODES; q += blockDim.x) {
-      const int bi = q % BX, bj = (q / BX) % BY, bk = q / (BX * BY);
-      if (PH & PH_PUSH) {
-        const int gi = ch_wrap(bi0 + bi, g.Nx), gj = ch_wrap(bj0 + bj, g.Ny), gk = ch_wrap(bk0 + bk, g.Nz);
-        sh.E[q] = __ldg(E + ((int64_t)gk * g.Ny + gj) * g.Nx + gi);
-      }
-      if (PH & PH_DEPOSIT) {
+  const bool collide = (PH & PH_PUSH) && c.collide;
+  const int ntx = (g.Nx + TX - 1) / TX, nty = (g.Ny + TY - 1) / TY;
+  // Move one ion by v dt (cell units), wrap, repack the cell.
+  auto move_ion = [&](float4& p, const float v[3], int& i, int& j, int& k) {
+    float ox = p.x + v[0] * dtx, oy = p.y + v[1] * dty, oz = p.z + v[2] * dtz;
+    const float fx = floorf(ox), fy = floorf(oy), fz = floorf(oz);
+    ox -= fx; oy -= fy; oz -= fz;
+    if (ox >= 1.0f) ox = 0.0f;
+    if (oy >= 1.0f) oy = 0.0f;
+    if (oz >= 1.0f) oz = 0.0f;
+    if (isfinite(fx) && isfinite(fy) && isfinite(fz)) {
+      i = ch_wrap(i + (int)fx, g.Nx); j = ch_wrap(j + (int)fy, g.Ny); k = ch_wrap(k + (int)fz, g.Nz);
+    }
+    const uint32_t cell = (uint32_t)i | ((uint32_t)j << CH_PACK_BX) | ((uint32_t)k << (CH_PACK_BX + CH_PACK_BY));
+    p = make_float4(ox, oy, oz, __uint_as_float(cell));
+  };
+  auto gmean_of = [&](const float v[3]) {
+    const float qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
+    return ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), vnTf);
+  };
+
+  const int i0 = (tile % ntx) * TX, j0 = ((tile / ntx) % nty) * TY, k0 = (tile / (ntx * nty)) * TZ;
+  const int i1 = min(i0 + TX, g.Nx), j1 = min(j0 + TY, g.Ny), k1 = min(k0 + TZ, g.Nz);
+  const int bi0 = i0 - 1, bj0 = j0 - 1, bk0 = k0 - 1;  // box origin (node)
+  __syncthreads();  // previous brick's flush is done
+  // stage the node field, clear the deposit tile, row ranges
+  for (int q = threadIdx.x; q < BNODES; q += blockDim.x) {
+    const int bi = q % BX, bj = (q / BX) % BY, bk = q / (BX * BY);
+    if (PH & PH_PUSH) {
+      const int gi = ch_wrap(bi0 + bi, g.Nx), gj = ch_wrap(bj0 + bj, g.Ny), gk = ch_wrap(bk0 + bk, g.Nz);
+      sh.E[q] = __ldg(E + ((int64_t)gk * g.Ny + gj) * g.Nx + gi);
+    }
+    if (PH & PH_DEPOSIT) {
 #pragma unroll
-        for (int m = 0; m < 4; ++m) { sh.acc_lo[m][q] = 0u; sh.acc_hi[m][q] = 0; }
-      }
+      for (int m = 0; m < 4; ++m) { sh.acc_lo[m][q] = 0u; sh.acc_hi[m][q] = 0; }
     }
-    if (threadIdx.x == 0) {
-      uint32_t tot = 0;
-      int r = 0;
-      for (int tk = k0; tk < k0 + TZ; ++tk)
-        for (int tj = j0; tj < j0 + TY; ++tj, ++r) {
-          sh.pre[r] = tot;
-          if (tk < k1 && tj < j1) {
-            const int64_t cf = ((int64_t)tk * g.Ny + tj) * g.Nx + i0;
-            const uint32_t b = starts[cf], e = starts[cf + (i1 - i0)];
-            sh.rowbeg[r] = b;
-            tot += e - b;
-          } else {
-            sh.rowbeg[r] = 0;
-          }
+  }
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0;
+    int r = 0;
+    for (int tk = k0; tk < k0 + TZ; ++tk)
+      for (int tj = j0; tj < j0 + TY; ++tj, ++r) {
+        sh.pre[r] = tot;
+        if (tk < k1 && tj < j1) {
+          const int64_t cf = ((int64_t)tk * g.Ny + tj) * g.Nx + i0;
+          const uint32_t b = starts[cf], e = starts[cf + (i1 - i0)];
+          sh.rowbeg[r] = b;
+          tot += e - b;
+        } else {
+          sh.rowbeg[r] = 0;
         }
-      sh.pre[TY * TZ] = tot;
-    }
-    __syncthreads();
-    const uint32_t total = sh.pre[TY * TZ];
-    float tsum0 = 0.0f, tsum1 = 0.0f;  // per-brick partial sums, folded into FP64 below
-    for (uint32_t base = 0; base < total; base += blockDim.x) {
-      const uint32_t idx = base + threadIdx.x;
+      }
+    sh.pre[TY * TZ] = tot;
+    sh.qn = 0;
+  }
+  __syncthreads();
+  const uint32_t total = sh.pre[TY * TZ];
+  unsigned qhead = 0, qtail = 0;  // block-uniform: drained / enqueued entries of this brick
+  // Per-brick sums: tsum0 (expected events, reported only) in FP32; the
+  // post-step mean relative speeds, which normalise the next step's rates,
+  // as integers of 2^-20 so that S is exact whatever the ion order.
+  float tsum0 = 0.0f;
+  unsigned long long gsum = 0ull;
+  for (uint32_t base = 0; base < total; base += CH_TILE_BATCH) {
+#pragma unroll 1
+    for (int kk = 0; kk < CH_TILE_K; ++kk) {
+      const uint32_t sidx = kk * blockDim.x + threadIdx.x;  // slot within the batch
+      const uint32_t idx = base + sidx;
       const bool active = idx < total;
       int64_t ip = 0;
       if (active) {
         int r = 0;
-#pragma unroll
+  #pragma unroll
         for (int st = 8; st > 0; st >>= 1)
           if (r + st < TY * TZ && sh.pre[r + st] <= idx) r += st;
         ip = (int64_t)sh.rowbeg[r] + (idx - sh.pre[r]);
@@ -521,14 +699,13 @@ __global__ void __launch_bounds__(256, 2)
         i = cell & (CH_MAX_NX - 1); j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1); k = cell >> (CH_PACK_BX + CH_PACK_BY);
         v[0] = vv.x; v[1] = vv.y; v[2] = vv.z;
       }
+      bool defer = false;
+      float qscale = 0.0f;  // rate scale of a deferred ion
       if ((PH & PH_PUSH) && active) {
-        int di = i - bi0, dj = j - bj0, dk = k - bk0;
-        di += di < 0 ? g.Nx : 0; di -= di >= g.Nx ? g.Nx : 0;
-        dj += dj < 0 ? g.Ny : 0; dj -= dj >= g.Ny ? g.Ny : 0;
-        dk += dk < 0 ? g.Nz : 0; dk -= dk >= g.Nz ? g.Nz : 0;
+        bool near;
+        const int q = box_key(g, i, j, k, bi0, bj0, bk0, &near);
         float4 e000, e100, e010, e110, e001, e101, e011, e111;
-        if (di <= BX - 2 && dj <= BY - 2 && dk <= BZ - 2) {
-          const int q = (dk * BY + dj) * BX + di;
+        if (near) {
           e000 = sh.E[q]; e100 = sh.E[q + 1]; e010 = sh.E[q + BX]; e110 = sh.E[q + BX + 1];
           e001 = sh.E[q + BX * BY]; e101 = sh.E[q + BX * BY + 1]; e011 = sh.E[q + BX * BY + BX];
           e111 = sh.E[q + BX * BY + BX + 1];
@@ -542,7 +719,7 @@ __global__ void __launch_bounds__(256, 2)
         }
         const float wx = p.x, wy = p.y, wz = p.z;
         float Ef[3];
-#define LERP3(f, d)                                                                \
+  #define LERP3(f, d)                                                                \
   {                                                                                \
     const float wll = e000.f + wy * (e010.f - e000.f);                             \
     const float wlh = e100.f + wy * (e110.f - e100.f);                             \
@@ -552,7 +729,7 @@ __global__ void __launch_bounds__(256, 2)
     Ef[d] = ezl + wz * (ezh - ezl);                                                \
   }
         LERP3(x, 0) LERP3(y, 1) LERP3(z, 2)
-#undef LERP3
+  #undef LERP3
         if (c.push_E0) { Ef[0] += pE0x; Ef[1] += pE0y; Ef[2] += pE0z; }
         // Boris (src/particles.c:374-447) with E premultiplied by (q/m) dt/2
         const float vm0 = v[0] + Ef[0], vm1 = v[1] + Ef[1], vm2 = v[2] + Ef[2];
@@ -566,9 +743,8 @@ __global__ void __launch_bounds__(256, 2)
           vp2 = vm2 + (q0 * s1 - q1 * s0);
         }
         v[0] = vp0 + Ef[0]; v[1] = vp1 + Ef[1]; v[2] = vp2 + Ef[2];
-        if (c.collide) {
-          const float wx2 = v[0] - vn0x, wy2 = v[1] - vn0y, wz2 = v[2] - vn0z;
-          const float gi = ch_gmean<float>(sqrtf(wx2 * wx2 + wy2 * wy2 + wz2 * wz2), vnTf);
+        if (collide) {
+          const float gi = gmean_of(v);
           float nd = 1.0f;
           if (c.nn_profile == CH_NN_GAUSSIAN_X)
             nd = ch_neutral_density<float>(c, (float)(g.x0 + ((double)i + (double)p.x) * g.dx));
@@ -578,123 +754,234 @@ __global__ void __launch_bounds__(256, 2)
           const uint32_t id = __float_as_uint(vv.w);
           const U4 r0 = ch_philox(id, c.step, CH_PURPOSE_COLLIDE << 24, c.run, c.seed_lo, c.seed_hi);
           // first event inside the step: -log(u) < lam  <=>  u > exp(-lam)
-          float gnext = gi;
           if (lam > 0.0f && ch_unitf(r0.x) > __expf(-lam)) {
-            const float v0 = v[0], v1 = v[1], v2 = v[2];
-            ncol += ch_collide<float>(c, id, lscale, v, &nref);
-            if (v[0] != v0 || v[1] != v1 || v[2] != v2) {
-              const float qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
-              gnext = ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), vnTf);
-            }
+            defer = true;
+            qscale = lscale;
+          } else {
+            gsum += g_fixed(gi);
           }
-          tsum1 += gnext;
         }
-        vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
-        P.vel[ip] = vv;
-      }
-      if (move && active) {
-        float ox = p.x + v[0] * dtx, oy = p.y + v[1] * dty, oz = p.z + v[2] * dtz;
-        const float fx = floorf(ox), fy = floorf(oy), fz = floorf(oz);
-        ox -= fx; oy -= fy; oz -= fz;
-        if (ox >= 1.0f) ox = 0.0f;
-        if (oy >= 1.0f) oy = 0.0f;
-        if (oz >= 1.0f) oz = 0.0f;
-        if (isfinite(fx) && isfinite(fy) && isfinite(fz)) {
-          i = ch_wrap(i + (int)fx, g.Nx); j = ch_wrap(j + (int)fy, g.Ny); k = ch_wrap(k + (int)fz, g.Nz);
+        if (!defer) {
+          vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
+          P.vel[ip] = vv;
         }
-        const uint32_t cell = (uint32_t)i | ((uint32_t)j << CH_PACK_BX) | ((uint32_t)k << (CH_PACK_BX + CH_PACK_BY));
-        p = make_float4(ox, oy, oz, __uint_as_float(cell));
-        P.pos[ip] = p;
       }
-      if (hist) agg_inc(hist, (uint32_t)(((int64_t)k * g.Ny + j) * g.Nx + i), active);
+      if (collide) {
+        // warp-aggregated enqueue of the deferred ions
+        const unsigned dm = __ballot_sync(0xffffffffu, defer);
+        if (dm) {
+          const int leader = __ffs(dm) - 1;
+          unsigned slot = 0;
+          if (lane == leader) slot = atomicAdd(&sh.qn, (unsigned)__popc(dm));
+          slot = (__shfl_sync(0xffffffffu, slot, leader) + __popc(dm & ((1u << lane) - 1u))) & (CH_TILE_QCAP - 1);
+          if (defer) {
+            sh.q_pos[slot] = p;
+            sh.q_vel[slot] = make_float4(v[0], v[1], v[2], qscale);
+            sh.q_ip[slot] = (uint32_t)ip;
+            sh.q_id[slot] = __float_as_uint(vv.w);
+          }
+        }
+      }
+      const bool go = active && !defer;
+      if (move && go) move_ion(p, v, i, j, k);
+      if (move && go) P.pos[ip] = p;
+      if (hist) agg_inc(hist, (uint32_t)(((int64_t)k * g.Ny + j) * g.Nx + i), go);
       if (PH & PH_DEPOSIT) {
         const bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v[0]) && isfinite(v[1]) &&
                             isfinite(v[2]);
-        if (active && !finite) bad = 1;
-        int di = i - bi0, dj = j - bj0, dk = k - bk0;
-        di += di < 0 ? g.Nx : 0; di -= di >= g.Nx ? g.Nx : 0;
-        dj += dj < 0 ? g.Ny : 0; dj -= dj >= g.Ny ? g.Ny : 0;
-        dk += dk < 0 ? g.Nz : 0; dk -= dk >= g.Nz ? g.Nz : 0;
-        const bool inbox = di <= BX - 2 && dj <= BY - 2 && dk <= BZ - 2;
+        if (go && !finite) bad = 1;
+        bool inbox;
+        const int key0 = box_key(g, i, j, k, bi0, bj0, bk0, &inbox);
         const bool slow = fabsf(v[0]) >= CH_TILE_VMAX || fabsf(v[1]) >= CH_TILE_VMAX || fabsf(v[2]) >= CH_TILE_VMAX;
-        const bool valid = active && finite && inbox && !slow;
-        if (active && finite && !valid)
+        const bool valid = go && finite && inbox && !slow;
+        if (go && finite && !valid)
           deposit_cic<float>(g, acc, i, j, k, p.x, p.y, p.z, v[0], v[1], v[2], (float)c.dep_scale);
-        // fixed-point contributions: 8 corners x {n, Gx, Gy, Gz}
-        const float wxh = p.x, wyh = p.y, wzh = p.z;
-        const float wxl = 1.0f - wxh, wyl = 1.0f - wyh, wzl = 1.0f - wzh;
-        const float w[8] = {wzl * wyl * wxl, wzl * wyl * wxh, wzl * wyh * wxl, wzl * wyh * wxh,
-                            wzh * wyl * wxl, wzh * wyl * wxh, wzh * wyh * wxl, wzh * wyh * wxh};
-        const int key = valid ? (dk * BY + dj) * BX + di : -1;
-        // The lanes that share the first valid lane's cell (usually most of a
-        // sorted warp) are summed with integer warp reductions, and lane q
-        // then adds sum q of the 32 (corner, moment) sums; every other lane
-        // adds its own 32 contributions.  All adds land in the shared tile.
-        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-        if (vmask) {
-          const int leader = __ffs(vmask) - 1;
-          const int lkey = __shfl_sync(0xffffffffu, key, leader);
-          const bool mine = valid && key == lkey;
-          long long myval = 0;
-#pragma unroll
-          for (int cn = 0; cn < 8; ++cn) {
-            const int cd = mine ? __float2int_rn(w[cn] * CH_TILE_DSCALE) : 0;
-            const int cx = mine ? __float2int_rn(v[0] * w[cn] * CH_TILE_FSCALE) : 0;
-            const int cy = mine ? __float2int_rn(v[1] * w[cn] * CH_TILE_FSCALE) : 0;
-            const int cz = mine ? __float2int_rn(v[2] * w[cn] * CH_TILE_FSCALE) : 0;
-            const int sd = (int)__reduce_add_sync(0xffffffffu, (unsigned)cd);
-            const int sx = (int)__reduce_add_sync(0xffffffffu, (unsigned)cx);
-            const int sy = (int)__reduce_add_sync(0xffffffffu, (unsigned)cy);
-            const int sz = (int)__reduce_add_sync(0xffffffffu, (unsigned)cz);
-            if (lane == cn) myval = (long long)sd << shift_d;
-            if (lane == 8 + cn) myval = (long long)sx << shift_f;
-            if (lane == 16 + cn) myval = (long long)sy << shift_f;
-            if (lane == 24 + cn) myval = (long long)sz << shift_f;
-          }
+        sh.st_key[sidx] = valid ? key0 : -1;
+        sh.st_ox[sidx] = p.x; sh.st_oy[sidx] = p.y; sh.st_oz[sidx] = p.z;
+        sh.st_vx[sidx] = v[0]; sh.st_vy[sidx] = v[1]; sh.st_vz[sidx] = v[2];
+      }
+      if (collide) {
+        // every enqueue of this iteration is visible after the barrier
+        qtail += (unsigned)__syncthreads_count(defer);
+        const bool last = base + (kk + 1) * blockDim.x >= total;
+        // drain full rounds of one queued ion per thread (the rest waits for
+        // the next iteration), and everything at the end of the brick:
+        // collide, move and deposit
+        while (qtail - qhead >= blockDim.x || (last && qtail > qhead)) {
+          const unsigned nq = min(qtail - qhead, blockDim.x);
           {
-            const int cn = lane & 7, m = lane >> 3;
-            const int node = lkey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
-            if (myval != 0) shared_add64(&sh.acc_lo[m][node], &sh.acc_hi[m][node], myval);
-          }
-          if (valid && !mine) {
-#pragma unroll
-            for (int cn = 0; cn < 8; ++cn) {
-              const int node = key + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
-              const long long cd = (long long)__float2int_rn(w[cn] * CH_TILE_DSCALE) << shift_d;
-              const long long cx = (long long)__float2int_rn(v[0] * w[cn] * CH_TILE_FSCALE) << shift_f;
-              const long long cy = (long long)__float2int_rn(v[1] * w[cn] * CH_TILE_FSCALE) << shift_f;
-              const long long cz = (long long)__float2int_rn(v[2] * w[cn] * CH_TILE_FSCALE) << shift_f;
-              shared_add64(&sh.acc_lo[0][node], &sh.acc_hi[0][node], cd);
-              shared_add64(&sh.acc_lo[1][node], &sh.acc_hi[1][node], cx);
-              shared_add64(&sh.acc_lo[2][node], &sh.acc_hi[2][node], cy);
-              shared_add64(&sh.acc_lo[3][node], &sh.acc_hi[3][node], cz);
+            const unsigned e = (qhead + threadIdx.x) & (CH_TILE_QCAP - 1);
+            const bool act = threadIdx.x < nq;
+            float4 qp = make_float4(0.f, 0.f, 0.f, 0.f);
+            float qv[3] = {0.f, 0.f, 0.f};
+            int qi = 0, qj = 0, qk = 0;
+            uint32_t qip = 0;
+            if (act) {
+              qp = sh.q_pos[e];
+              const float4 q4 = sh.q_vel[e];
+              qip = sh.q_ip[e];
+              const uint32_t qid = sh.q_id[e];
+              qv[0] = q4.x; qv[1] = q4.y; qv[2] = q4.z;
+              ncol += ch_collide<float>(c, qid, q4.w, qv, &nref);
+              gsum += g_fixed(gmean_of(qv));
+              P.vel[qip] = make_float4(qv[0], qv[1], qv[2], __uint_as_float(qid));
+              const uint32_t cell = __float_as_uint(qp.w);
+              qi = cell & (CH_MAX_NX - 1); qj = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1);
+              qk = cell >> (CH_PACK_BX + CH_PACK_BY);
+              if (move) {
+                move_ion(qp, qv, qi, qj, qk);
+                P.pos[qip] = qp;
+              }
+            }
+            if (hist) agg_inc(hist, (uint32_t)(((int64_t)qk * g.Ny + qj) * g.Nx + qi), act);
+            if ((PH & PH_DEPOSIT) && act) {
+              const bool finite = isfinite(qp.x) && isfinite(qp.y) && isfinite(qp.z) && isfinite(qv[0]) &&
+                                  isfinite(qv[1]) && isfinite(qv[2]);
+              bool inbox;
+              const int key = box_key(g, qi, qj, qk, bi0, bj0, bk0, &inbox);
+              const bool slow =
+                  fabsf(qv[0]) >= CH_TILE_VMAX || fabsf(qv[1]) >= CH_TILE_VMAX || fabsf(qv[2]) >= CH_TILE_VMAX;
+              if (!finite)
+                bad = 1;
+              else if (inbox && !slow)
+                tile_deposit_lane(sh, key, qp.x, qp.y, qp.z, qv[0], qv[1], qv[2]);
+              else
+                deposit_cic<float>(g, acc, qi, qj, qk, qp.x, qp.y, qp.z, qv[0], qv[1], qv[2], (float)c.dep_scale);
             }
           }
+          qhead += nq;
+          __syncthreads();  // the queue is read before the next enqueue reuses its slots
         }
       }
     }
-    vsum[0] += (double)tsum0;
-    vsum[1] += (double)tsum1;
     if (PH & PH_DEPOSIT) {
-      __syncthreads();
-      for (int q = threadIdx.x; q < 4 * BNODES; q += blockDim.x) {
-        const int m = q / BNODES, nd = q % BNODES;
-        const long long a = (long long)(((unsigned long long)(unsigned)sh.acc_hi[m][nd] << 32) |
-                                        (unsigned long long)sh.acc_lo[m][nd]);
-        if (a != 0) {
-          const int bi = nd % BX, bj = (nd / BX) % BY, bk = nd / (BX * BY);
-          const int gi = ch_wrap(bi0 + bi, g.Nx), gj = ch_wrap(bj0 + bj, g.Ny), gk = ch_wrap(bk0 + bk, g.Nz);
-          atomicAdd(acc + (int64_t)m * g.N + ((int64_t)gk * g.Ny + gj) * g.Nx + gi, (unsigned long long)a);
-        }
+      __syncthreads();  // the batch is staged
+      tile_deposit_batch(sh, lane);
+      __syncthreads();  // staging is read before the next batch overwrites it
+    }
+  }
+  vsum[0] += (double)tsum0;
+  vsum[1] += (double)gsum * CH_G_UNIT;
+  if (PH & PH_DEPOSIT) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < 4 * BNODES; q += blockDim.x) {
+      const int m = q / BNODES, nd = q % BNODES;
+      // tile sums are at the tile scale (2^22 density, 2^19 flux): shift
+      // them to the accumulator scale 2^s
+      const long long a = (long long)(((unsigned long long)(unsigned)sh.acc_hi[m][nd] << 32) |
+                                      (unsigned long long)sh.acc_lo[m][nd])
+                          << (m == 0 ? shift_d : shift_f);
+      if (a != 0) {
+        const int bi = nd % BX, bj = (nd / BX) % BY, bk = nd / (BX * BY);
+        const int gi = ch_wrap(bi0 + bi, g.Nx), gj = ch_wrap(bj0 + bj, g.Ny), gk = ch_wrap(bk0 + bk, g.Nz);
+        atomicAdd(acc + (int64_t)m * g.N + ((int64_t)gk * g.Ny + gj) * g.Nx + gi, (unsigned long long)a);
       }
     }
   }
+}
+
+template <int PH>
+__global__ void __launch_bounds__(256, 2)
+    k_pass_tiled(StepConsts c, MixParticles P, const float4* __restrict__ E, const uint32_t* __restrict__ starts,
+                 unsigned long long* __restrict__ acc, float pscale, int shift_d, int shift_f, DevCounters* cnt,
+                 double* part, uint32_t* hist) {
+  extern __shared__ __align__(16) unsigned char smem_tiled[];
+  TileShared& sh = *reinterpret_cast<TileShared*>(smem_tiled);
+  double vsum[2] = {0.0, 0.0};
+  unsigned ncol = 0, nref = 0;
+  int bad = 0;
+  const GridDesc& g = c.g;
+  const int ntiles = ((g.Nx + TX - 1) / TX) * ((g.Ny + TY - 1) / TY) * ((g.Nz + TZ - 1) / TZ);
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+    tile_pass<PH>(sh, c, P, E, starts, acc, pscale, shift_d, shift_f, hist, tile, vsum, ncol, nref, bad);
   if (bad) atomicOr(&cnt->range_error, 2);
   if (PH & PH_PUSH) {
     count_add(cnt, ncol, nref);
     block_partials<2>(vsum, part);
   }
 }
+// ------------------------------------------------------------------ ensembles
+// Every run's bricks in one persistent launch: brick t belongs to the run r
+// with tile_off[r] <= t < tile_off[r + 1]; the run's constants are staged in
+// shared memory and the brick is processed by the same tile_pass as a single
+// run.  Brick partials are written per brick, so the run sums are formed in
+// a fixed order afterwards.
+template <int PH>
+__global__ void __launch_bounds__(256, 2)
+    k_batch_pass(BatchDev B, const uint32_t* dstep, MixParticles P, const float4* __restrict__ E,
+                 const uint32_t* __restrict__ starts, unsigned long long* __restrict__ acc,
+                 const double* __restrict__ sbar, int shift_d, int shift_f, uint32_t* hist, double* tile_part,
+                 int* flags) {
+  extern __shared__ __align__(16) unsigned char smem_tiled[];
+  TileShared& sh = *reinterpret_cast<TileShared*>(smem_tiled);
+  __shared__ StepConsts sc;
+  __shared__ int s_run;
+  constexpr int W = (int)(sizeof(StepConsts) / sizeof(uint32_t));
+  static_assert(sizeof(StepConsts) % sizeof(uint32_t) == 0, "StepConsts is copied as words");
+  for (int t = blockIdx.x; t < B.total_tiles; t += gridDim.x) {
+    __syncthreads();  // the previous brick is done with sc
+    if (threadIdx.x == 0) {
+      int lo = 0, hi = B.nruns;  // largest r with tile_off[r] <= t
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (B.tile_off[mid] <= t) lo = mid; else hi = mid;
+      }
+      s_run = lo;
+    }
+    __syncthreads();
+    const int r = s_run;
+    const BatchRunDev& R = B.runs[r];
+    for (int w = threadIdx.x; w < W; w += blockDim.x)
+      reinterpret_cast<uint32_t*>(&sc)[w] = reinterpret_cast<const uint32_t*>(&R.c)[w];
+    __syncthreads();
+    if (threadIdx.x == 0) sc.step = *dstep;
+    const int64_t no = R.node_off;
+    const double S = sbar[r];
+    const float pscale = S > 0.0 ? (float)(R.Nc / S) : 0.0f;
+    double vsum[4] = {0.0, 0.0, 0.0, 0.0};
+    double v2[2] = {0.0, 0.0};
+    unsigned ncol = 0, nref = 0;
+    int bad = 0;
+    // tile_pass starts with a barrier, after which sc.step is visible
+    tile_pass<PH>(sh, sc, P, E + no, starts + no, acc + 4 * no, pscale, shift_d, shift_f, hist ? hist + no : nullptr,
+                  t - R.tile_off, v2, ncol, nref, bad);
+    if (bad) atomicOr(flags + r, 16);  // non-finite ion
+    vsum[0] = v2[0]; vsum[1] = v2[1]; vsum[2] = (double)ncol; vsum[3] = (double)nref;
+    block_partials<4>(vsum, tile_part, t);
+  }
+}
+
+__global__ void k_batch_runsum(BatchDev B, const double* __restrict__ tile_part, double* sums, double* sbar,
+                               int* flags, uint32_t* dstep) {
+  const int r = blockIdx.x;
+  const int t0 = B.tile_off[r], t1 = B.tile_off[r + 1];
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int t = t0 + (int)threadIdx.x; t < t1; t += blockDim.x)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] += tile_part[4 * (int64_t)t + q];
+  block_partials<4>(v, sums, r);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (B.runs[r].c.collide) sbar[r] = sums[4 * r + 1];
+    if (sums[4 * r + 3] >= 10.0) atomicOr(flags + r, 8);  // refusal limit (src/particles.c:603-605)
+    if (r == 0) ++*dstep;  // the pass of this step has read it
+  }
+}
+
+__global__ void k_batch_finalize(int64_t n4, unsigned long long* __restrict__ acc, double inv_scale,
+                                 double* __restrict__ mom, int* flag) {
+  int bad = 0;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n4; c += (int64_t)gridDim.x * blockDim.x) {
+    const long long a = (long long)acc[c];
+    if (a > (1LL << 62) || a < -(1LL << 62)) bad = 1;
+    mom[c] = (double)a * inv_scale;
+    acc[c] = 0ull;
+  }
+  if (bad) atomicOr(flag, 1);
+}
+
+int tiles_of(const GridDesc& g) { return ((g.Nx + TX - 1) / TX) * ((g.Ny + TY - 1) / TY) * ((g.Nz + TZ - 1) / TZ); }
+
 #undef TX
 #undef TY
 #undef TZ
@@ -718,7 +1005,7 @@ __global__ void k_sbar_mixed(MixParticles P, float vnT, float vn0x, float vn0y, 
   for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
     const float4 v = P.vel[ip];
     const float wx = v.x - vn0x, wy = v.y - vn0y, wz = v.z - vn0z;
-    s[0] += (double)ch_gmean<float>(sqrtf(wx * wx + wy * wy + wz * wz), vnT);
+    s[0] += (double)g_fixed(ch_gmean<float>(sqrtf(wx * wx + wy * wy + wz * wz), vnT)) * CH_G_UNIT;
   }
   block_partials<1>(s, part);
 }
@@ -911,6 +1198,50 @@ __global__ void k_scan_add(uint32_t* out, const uint32_t* block_sums, int64_t n,
   }
 }
 
+__global__ void k_batch_hist(BatchDev B, MixParticles P, uint32_t* counts) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t n_pad = (P.np + 31) / 32 * 32;
+  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < n_pad; ip += stride) {
+    const bool act = ip < P.np;
+    uint32_t key = 0u;
+    if (act) {
+      int lo = 0, hi = B.nruns;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (B.ion_off[mid] <= ip) lo = mid; else hi = mid;
+      }
+      const BatchRunDev& R = B.runs[lo];
+      key = (uint32_t)R.node_off + key_mixed(R.c.g, P.pos[ip].w);
+    }
+    agg_inc(counts, key, act);
+  }
+}
+
+__global__ void k_batch_scatter(BatchDev B, MixParticles P, MixParticles Q, uint32_t* cursor) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t n_pad = (P.np + 31) / 32 * 32;
+  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < n_pad; ip += stride) {
+    const bool act = ip < P.np;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t key = 0u;
+    if (act) {
+      p = P.pos[ip];
+      int lo = 0, hi = B.nruns;  // run of slot ip
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (B.ion_off[mid] <= ip) lo = mid; else hi = mid;
+      }
+      const BatchRunDev& R = B.runs[lo];
+      key = (uint32_t)R.node_off + key_mixed(R.c.g, p.w);
+    }
+    const uint32_t dst = agg_inc(cursor, key, act);
+    if (act) {
+      Q.pos[dst] = p;
+      Q.vel[dst] = P.vel[ip];
+    }
+  }
+}
+
 // ------------------------------------------------------------------ launchers
 int grid_for(int64_t n, int threads, int sms, int per_sm) {
   int64_t need = (n + threads - 1) / threads;
@@ -944,6 +1275,21 @@ void launch_node_efield(bool mixed, const GridDesc& g, double tscale, const doub
   else k_node_efield_f64<<<grid_for(g.N, 256, sms, 8), 256, 0, s>>>(g, phi, E64), ::ch::note_launch();
 }
 
+// The tiled pass needs more than the default 48 KB of dynamic shared memory;
+// the attribute is set once per device and instantiation.
+template <int PH>
+static void tiled_smem_attr() {
+  static std::atomic<uint32_t> done{0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint32_t bit = 1u << (dev & 31);
+  if (done.load() & bit) return;
+  // a failure here surfaces as the launch error of the pass
+  if (cudaFuncSetAttribute(k_pass_tiled<PH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileShared)) ==
+      cudaSuccess)
+    done.fetch_or(bit);
+}
+
 template <int PH>
 static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticles M, const double* E64,
                     const float4* E32, const double* phi, unsigned long long* acc, double Nc, double sbar,
@@ -956,8 +1302,10 @@ static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticle
     const int ntiles = ((c.g.Nx + 15) / 16) * ((c.g.Ny + 3) / 4) * ((c.g.Nz + 3) / 4);
     nb = ntiles < 2 * sms ? ntiles : 2 * sms;
     const int s2 = (int)lround(log2(c.dep_scale));
-    k_pass_tiled<PH><<<nb, 256, sizeof(TileShared), s>>>(c, M, E32, starts, acc, pscale, s2 - 24, s2 - 20, cnt, part,
-                                                         hist), ::ch::note_launch();
+    tiled_smem_attr<PH>();
+    k_pass_tiled<PH><<<nb, 256, sizeof(TileShared), s>>>(c, M, E32, starts, acc, pscale, s2 - CH_TILE_DLOG2,
+                                                         s2 - CH_TILE_FLOG2, cnt, part, hist),
+        ::ch::note_launch();
   } else {
     k_pass_f64<PH><<<nb, 256, 0, s>>>(c, P, E64, phi, acc, Nc, sbar, cnt, part), ::ch::note_launch();
   }
@@ -1017,6 +1365,61 @@ void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, 
   k_scan_add<<<(int)((N + 255) / 256), 256, 0, s>>>(starts, block_sums, N, cursor), ::ch::note_launch();
   if (mixed) k_scatter_mixed<<<nb, 256, 0, s>>>(g, M, MQ, cursor), ::ch::note_launch();
   else k_scatter_f64<<<nb, 256, 0, s>>>(P, Q, keys, cursor), ::ch::note_launch();
+}
+
+// ------------------------------------------------------------------ ensemble launchers
+template <int PH>
+static void batch_smem_attr() {
+  static std::atomic<uint32_t> done{0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint32_t bit = 1u << (dev & 31);
+  if (done.load() & bit) return;
+  if (cudaFuncSetAttribute(k_batch_pass<PH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileShared)) ==
+      cudaSuccess)
+    done.fetch_or(bit);
+}
+
+void batch_pass_prepare() {
+  batch_smem_attr<PH_PUSH | PH_MOVE | PH_DEPOSIT>();
+  batch_smem_attr<PH_DEPOSIT>();
+}
+
+void launch_batch_pass(bool deposit_only, const BatchDev& B, const uint32_t* dstep, MixParticles P, const float4* E,
+                       const uint32_t* starts, unsigned long long* acc, const double* sbar, int dep_log2,
+                       uint32_t* hist, double* tile_part, int* flags, int ctas_per_sm, int sms, cudaStream_t s) {
+  const int cap = (ctas_per_sm < 1 ? 1 : ctas_per_sm) * sms;
+  const int nb = B.total_tiles < cap ? B.total_tiles : cap;
+  const int sd = dep_log2 - CH_TILE_DLOG2, sf = dep_log2 - CH_TILE_FLOG2;
+  if (deposit_only)
+    k_batch_pass<PH_DEPOSIT><<<nb, 256, sizeof(TileShared), s>>>(B, dstep, P, E, starts, acc, sbar, sd, sf, hist,
+                                                                 tile_part, flags), ::ch::note_launch();
+  else
+    k_batch_pass<PH_PUSH | PH_MOVE | PH_DEPOSIT><<<nb, 256, sizeof(TileShared), s>>>(
+        B, dstep, P, E, starts, acc, sbar, sd, sf, hist, tile_part, flags), ::ch::note_launch();
+}
+
+void launch_batch_runsum(const BatchDev& B, const double* tile_part, double* sums, double* sbar, int* flags,
+                         uint32_t* dstep, cudaStream_t s) {
+  k_batch_runsum<<<B.nruns, 256, 0, s>>>(B, tile_part, sums, sbar, flags, dstep), ::ch::note_launch();
+}
+
+void launch_batch_hist(const BatchDev& B, MixParticles M, uint32_t* counts, int sms, cudaStream_t s) {
+  k_batch_hist<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(B, M, counts), ::ch::note_launch();
+}
+
+void launch_batch_finalize(int64_t n4, unsigned long long* acc, double inv_scale, double* mom, int* flag, int sms,
+                           cudaStream_t s) {
+  k_batch_finalize<<<grid_for(n4, 256, sms, 4), 256, 0, s>>>(n4, acc, inv_scale, mom, flag), ::ch::note_launch();
+}
+
+void launch_batch_sort(const BatchDev& B, int64_t Ntot, MixParticles M, MixParticles MQ, uint32_t* counts,
+                       uint32_t* starts, uint32_t* cursor, uint32_t* block_sums, int sms, cudaStream_t s) {
+  const int nsb = (int)((Ntot + 1023) / 1024);
+  k_scan_blocks<<<nsb, 512, 0, s>>>(counts, starts, block_sums, Ntot), ::ch::note_launch();
+  k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nsb, starts + Ntot), ::ch::note_launch();
+  k_scan_add<<<(int)((Ntot + 255) / 256), 256, 0, s>>>(starts, block_sums, Ntot, cursor), ::ch::note_launch();
+  k_batch_scatter<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(B, M, MQ, cursor), ::ch::note_launch();
 }
 
 }  // namespace ch

@@ -50,4 +50,50 @@ void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, 
                  uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* keys, uint32_t* block_sums,
                  bool have_hist, int sms, cudaStream_t s);
 
+// ------------------------------------------------------------------ ensembles
+// One run of a batch (independent runs of different grids and parameters
+// that share the device arrays): its constants and its slices.  Grid arrays
+// of run r start at node_off (acc and mom: 4 x N_r SoA from 4 x node_off).
+struct BatchRunDev {
+  StepConsts c;       // c.step is set by the pass
+  int64_t node_off;
+  int64_t ion_off, np;
+  int tile_off, ntiles;
+  double Nc;          // collisions per step (src/particles.c:510-519)
+};
+struct BatchDev {
+  const BatchRunDev* runs;
+  const int* tile_off;     // nruns + 1 prefix sums of bricks
+  const int64_t* ion_off;  // nruns + 1 prefix sums of ions
+  int nruns;
+  int total_tiles;
+};
+// Bricks of a run's grid in the tiled pass.
+int tiles_of(const GridDesc& g);
+// The fused pass over every run's bricks in one persistent launch.  Per
+// brick 4 partials (expected events, S next, collisions, refused) land in
+// tile_part; flags[r] |= 16 for a non-finite ion of run r.  hist (nullable)
+// counts the ions' new cells over the batch grid.
+// The step number is read from *dstep (device), so a captured step can be
+// replayed.  deposit_only: CollectVlasovQuantities alone (before the loop).
+void batch_pass_prepare();  // once, before any capture
+void launch_batch_pass(bool deposit_only, const BatchDev& B, const uint32_t* dstep, MixParticles P, const float4* E,
+                       const uint32_t* starts, unsigned long long* acc, const double* sbar, int dep_log2,
+                       uint32_t* hist, double* tile_part, int* flags, int ctas_per_sm, int sms, cudaStream_t s);
+// sums[4r + q] = the run's brick partials summed in a fixed order; sbar[r] =
+// S for the next step (runs with collisions); flags[r] |= 8 at the refusal
+// limit; *dstep advances by one.
+void launch_batch_runsum(const BatchDev& B, const double* tile_part, double* sums, double* sbar, int* flags,
+                         uint32_t* dstep, cudaStream_t s);
+// Cell counts of every run's ions over the batch grid (counts zeroed first).
+void launch_batch_hist(const BatchDev& B, MixParticles M, uint32_t* counts, int sms, cudaStream_t s);
+// acc -> mom elementwise (n4 = 4 x batch nodes), acc cleared; flag |= 1 if a
+// sum is out of the fixed-point range.
+void launch_batch_finalize(int64_t n4, unsigned long long* acc, double inv_scale, double* mom, int* flag, int sms,
+                           cudaStream_t s);
+// Counting sort over the batch grid (keys node_off[r] + cell keep the runs
+// contiguous); counts hold the cell counts from the preceding pass.
+void launch_batch_sort(const BatchDev& B, int64_t Ntot, MixParticles M, MixParticles MQ, uint32_t* counts,
+                       uint32_t* starts, uint32_t* cursor, uint32_t* block_sums, int sms, cudaStream_t s);
+
 }  // namespace ch

@@ -236,6 +236,72 @@ ch_status ch_collect_moments_noalloc(const ch_params* p, const double* x, const 
                                      const double* vx, const double* vy, const double* vz, int64_t np,
                                      double* moments, void* stream);
 
+/* ---------------------------------------------------------------------
+ * Ensembles (no counterpart in the reference, whose run-batch script starts
+ * one process per parameter set).  A ch_batch advances nruns independent
+ * runs -- each with its own grid, ion count, parameters and seed -- together:
+ * every phase of a step is one launch over all runs (one persistent pass over
+ * every run's bricks; one potential solve with a thread-block cluster per
+ * run), and a step is replayed from a captured CUDA graph.  Mixed precision,
+ * full LHS and RHS, CG with the multigrid preconditioner; the physics of
+ * each run is that of ch_step on a ch_ctx with the same parameters.
+ * --------------------------------------------------------------------- */
+typedef struct ch_batch ch_batch;
+
+/* Per-run report of the last step of a ch_batch_step call. */
+typedef struct ch_run_info {
+  int64_t Nc;                /* collisions the reference would attempt        */
+  int64_t collisions;        /* accepted ion-neutral collisions               */
+  int64_t refused;           /* refused (|v_f| > 10 vT)                       */
+  double expected;           /* sum of per-ion collision probabilities        */
+  ch_solve_info solve;       /* the run's potential solve                     */
+  int32_t status;            /* CH_OK or the run's error                      */
+  int32_t flags;             /* 1 bad density, 2 not converged, 4 non-finite residual,
+                                8 refused >= 10, 16 non-finite ion, 32 deposit range */
+} ch_run_info;
+
+/* Launch shape of the ensemble step; ch_batch_autotune picks it by timing. */
+typedef struct ch_batch_tuning {
+  int32_t cluster;           /* CTAs per run in the potential solve: 1, 2, 4, 8 */
+  int32_t pass_ctas_per_sm;  /* persistent CTAs per SM of the ion pass: 1, 2  */
+  double pass_ms;            /* measured for the chosen shape (autotune)      */
+  double solve_ms;
+} ch_batch_tuning;
+
+/* Creates the device state of nruns runs (all CH_MIXED, lhs/rhs full,
+ * ksp cg, pc mg, sort_period equal across runs).  Ion counts are fixed here:
+ * np[r] ions for run r. */
+ch_status ch_batch_create(const ch_params* runs, const int64_t* np, int32_t nruns, int32_t device,
+                          ch_batch** out);
+ch_status ch_batch_destroy(ch_batch* b);
+/* Seeded synthetic plasma of every run (loaders[r], the run's seed and run
+ * index), as ch_particles_load. */
+ch_status ch_batch_load(ch_batch* b, const ch_loader* loaders);
+/* Ions of run r from host AoS arrays (np[r] each), as ch_particles_upload. */
+ch_status ch_batch_upload(ch_batch* b, int32_t run, const ch_real_vector* pos, const ch_real_vector* vel);
+ch_status ch_batch_download(ch_batch* b, int32_t run, ch_real_vector* pos, ch_real_vector* vel);
+/* Sorts every run's ions, deposits the moments and solves the initial
+ * potential of every run (CollectVlasovQuantities + ComputePotential before
+ * the time loop, src/hybrid.c:94-99).  Call after load/upload. */
+ch_status ch_batch_initialize(ch_batch* b);
+/* nsteps steps of every run, numbered first_step, first_step + 1, ...
+ * info (nullable) receives nruns reports of the last step.  Errors of any
+ * run are reported when the call returns. */
+ch_status ch_batch_step(ch_batch* b, int64_t first_step, int32_t nsteps, ch_run_info* info);
+ch_status ch_batch_get_phi(ch_batch* b, int32_t run, double* out);
+ch_status ch_batch_get_moments(ch_batch* b, int32_t run, ch_grid_node* out);
+ch_status ch_batch_set_phi(ch_batch* b, int32_t run, const double* in);
+/* Times every launch shape on the current state (which is restored) and
+ * keeps the fastest; out (nullable) receives the choice. */
+ch_status ch_batch_autotune(ch_batch* b, ch_batch_tuning* out);
+ch_status ch_batch_set_tuning(ch_batch* b, const ch_batch_tuning* t);
+ch_status ch_batch_get_tuning(ch_batch* b, ch_batch_tuning* out);
+/* Per-phase timing of ch_batch_step (events; graphs are not used while
+ * profiling is on) and the stream of the batch. */
+ch_status ch_batch_set_profiling(ch_batch* b, int32_t enable);
+ch_status ch_batch_get_profile(ch_batch* b, ch_profile* out);
+ch_status ch_batch_get_stream(ch_batch* b, void** stream);
+
 /* Page-locks caller memory so that the copies of upload/download run at
  * full link speed (no counterpart in the reference: its arrays never leave
  * the host). */

@@ -48,3 +48,33 @@ def test_host_philox_matches_oracle(chy, po):
         key = [int(x) for x in rng.integers(0, 2**32, 2)]
         assert chy._philox4x32_10(ctr, key) == po.philox(ctr, key)
     assert chy.mode_phases(7) == po.mode_phases(7)
+
+
+def test_batch_rejects_unsupported_runs_before_touching_the_device(chy):
+    """ch_batch_create validates every run on the host first (no CUDA call)."""
+    good = chy.params_for((16, 16, 16), precision=chy.PRECISION["mixed"], pc_type=chy.PC["mg"])
+    cases = [
+        (dict(precision=chy.PRECISION["fp64"]), -10),      # mixed form only
+        (dict(pc_type=chy.PC["jacobi"]), -10),             # CG + multigrid only
+        (dict(ksp_type=chy.KSP["bcgs"]), -10),
+        (dict(kappa_e=(0.1, 0.0, 0.0)), -10),              # A non-symmetric: CG does not apply
+        (dict(sort_period=2), -1),                         # must agree across runs
+        (dict(Nx=2), -1),
+    ]
+    for kw, status in cases:
+        bad = chy.params_for((16, 16, 16), precision=chy.PRECISION["mixed"], pc_type=chy.PC["mg"])
+        for k, v in kw.items():
+            if k == "kappa_e":
+                bad.kappa_e[:] = v
+            else:
+                setattr(bad, k, v)
+        arr = (chy.Params * 2)(good, bad)
+        nions = (C.c_int64 * 2)(1000, 1000)
+        h = C.c_void_p()
+        rc = chy.lib().ch_batch_create(C.cast(arr, C.c_void_p), C.cast(nions, C.c_void_p), 2, -1, C.byref(h))
+        assert rc == status, (kw, rc, chy.lib().ch_last_error())
+        assert not h.value
+    arr = (chy.Params * 1)(good)
+    rc = chy.lib().ch_batch_create(C.cast(arr, C.c_void_p), C.cast((C.c_int64 * 1)(0), C.c_void_p), 1, -1,
+                                   C.byref(C.c_void_p()))
+    assert rc == -1 and b"no ions" in chy.lib().ch_last_error()

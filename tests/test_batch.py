@@ -1,0 +1,119 @@
+"""Ensembles (ch_batch): every run of a batch must behave as the same run on
+its own ch_ctx.
+
+Given the same phi, the ion pass of a batch is the single-run pass (same
+tile code, integer deposit, exact S sums), so ions, moments and collision
+counts agree bit for bit.  The potential solves (one thread-block cluster
+per run against the single-run graph-captured solver) agree to the solve
+tolerance: both meet rtol 1e-10, so phi agrees to about 1e-9 relative.
+Graph replay must equal eager launches, and the autotuner must leave the
+state as it found it."""
+import numpy as np
+import pytest
+
+SHAPES = [((16, 24, 32), 8, 0.3, 0.05, 11), ((32, 16, 16), 16, 1.2, 1.0, 12), ((24, 24, 24), 12, 0.7, 0.2, 13),
+          ((16, 16, 48), 10, 0.2, 0.01, 14)]
+
+
+def _runs(chy):
+    params, nions, loaders = [], [], []
+    for r, (N, ppc, Ex, nu, seed) in enumerate(SHAPES):
+        p = chy.params_for(N, precision=chy.PRECISION["mixed"], E0=(Ex, 0.0, 0.0), nui=nu, ksp_rtol=1e-10,
+                           pc_type=chy.PC["mg"], sort_period=4, seed=seed, run=r)
+        params.append(p)
+        nions.append(N[0] * N[1] * N[2] * ppc)
+        loaders.append(chy.loader(amp=(0.02, 0.02, 0.02), phase=tuple(chy.mode_phases(seed, r))))
+    return params, nions, loaders
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.mark.gpu
+def test_batch_matches_single_runs(chy):
+    params, nions, loaders = _runs(chy)
+    singles = [chy.Hybrid(p) for p in params]
+    with chy.Batch(params, nions) as b:
+        b.load(loaders)
+        b.initialize()
+        for r, h in enumerate(singles):
+            h.load(nions[r], loaders[r])
+            m1 = h.CollectVlasovQuantities()
+            phi1 = h.ComputePotential()
+            assert np.array_equal(b.moments(r), m1), r
+            assert _rel(b.phi(r), phi1) < 1e-8, (r, _rel(b.phi(r), phi1))
+            b.set_phi(r, phi1)
+        info = b.step(0, 1)
+        for r, h in enumerate(singles):
+            si = h.step(0, 1)
+            assert info[r]["status"] == 0
+            assert info[r]["collisions"] == si["collisions"] and info[r]["Nc"] == si["Nc"], (r, info[r], si)
+            pb, vb = b.download(r)
+            ps, vs = h.download()
+            assert np.array_equal(pb, ps) and np.array_equal(vb, vs), r
+            assert np.array_equal(b.moments(r), h.CollectVlasovQuantities()), r
+            # after the step both solved the same moments
+            assert _rel(b.phi(r), h.phi()) < 1e-8, r
+        # several steps, each side with its own solves (a sort at step 3)
+        info = b.step(1, 5)
+        for r, h in enumerate(singles):
+            si = h.step(1, 5)
+            assert info[r]["status"] == 0 and info[r]["rnorm"] <= 1.01e-10 * info[r]["bnorm"]
+            mb = b.moments(r)
+            ms = h.CollectVlasovQuantities()
+            assert _rel(mb, ms) < 1e-6, (r, _rel(mb, ms))
+            assert abs(info[r]["collisions"] - si["collisions"]) <= 5 + 0.01 * si["collisions"], (r, info[r], si)
+    for h in singles:
+        h.close()
+
+
+@pytest.mark.gpu
+def test_batch_graph_replay_equals_eager(chy):
+    params, nions, loaders = _runs(chy)
+    out = []
+    for eager in (False, True):
+        with chy.Batch(params, nions) as b:
+            b.load(loaders)
+            b.initialize()
+            b.set_tuning(4, 2)
+            if eager:
+                b.set_profiling(True)
+            b.step(0, 7)
+            out.append([(b.moments(r), b.phi(r), b.download(r)) for r in range(len(params))])
+    for (ma, pa, (xa, va)), (mb, pb, (xb, vb)) in zip(*out):
+        assert np.array_equal(ma, mb) and np.array_equal(pa, pb)
+        assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+
+
+@pytest.mark.gpu
+def test_batch_autotune_restores_state(chy):
+    params, nions, loaders = _runs(chy)
+    with chy.Batch(params, nions) as b:
+        b.load(loaders)
+        b.initialize()
+        b.step(0, 2)
+        before = [(b.phi(r), b.download(r)) for r in range(len(params))]
+        t = b.autotune()
+        assert t["cluster"] in (1, 2, 4, 8) and t["pass_ctas_per_sm"] in (1, 2)
+        assert t["pass_ms"] > 0 and t["solve_ms"] > 0
+        after = [(b.phi(r), b.download(r)) for r in range(len(params))]
+        for (pa, (xa, va)), (pb, (xb, vb)) in zip(before, after):
+            assert np.array_equal(pa, pb) and np.array_equal(xa, xb) and np.array_equal(va, vb)
+        info = b.step(2, 2)
+        assert all(i["status"] == 0 for i in info)
+
+
+@pytest.mark.gpu
+def test_batch_cluster_sizes_agree(chy):
+    """Every cluster size solves to the same tolerance from the same state."""
+    params, nions, loaders = _runs(chy)
+    phis = []
+    for C in (1, 2, 8):
+        with chy.Batch(params, nions) as b:
+            b.set_tuning(C, 2)
+            b.load(loaders)
+            b.initialize()
+            phis.append([b.phi(r) for r in range(len(params))])
+    for r in range(len(params)):
+        assert _rel(phis[1][r], phis[0][r]) < 1e-8 and _rel(phis[2][r], phis[0][r]) < 1e-8
