@@ -461,6 +461,8 @@ struct TileShared {
   alignas(16) float st_vx[CH_TILE_BATCH];
   alignas(16) float st_vy[CH_TILE_BATCH];
   alignas(16) float st_vz[CH_TILE_BATCH];
+  uint16_t ov_idx[CH_TILE_BATCH];  // staged slots outside their thread's cell, added one per thread
+  unsigned ov_n;
   unsigned acc_lo[4][BNODES];  // 64-bit fixed-point sums at the tile scale as
   int acc_hi[4][BNODES];       // lo + hi * 2^32, carried exactly (order-free)
   uint32_t rowbeg[TY * TZ];
@@ -521,9 +523,15 @@ __device__ __forceinline__ void tile_deposit_batch(TileShared& sh, int lane) {
   const int keys[4] = {kq.x, kq.y, kq.z, kq.w};
   const float ox[4] = {X.x, X.y, X.z, X.w}, oy[4] = {Y.x, Y.y, Y.z, Y.w}, oz[4] = {Z.x, Z.y, Z.z, Z.w};
   const float vx[4] = {VX.x, VX.y, VX.z, VX.w}, vy[4] = {VY.x, VY.y, VY.z, VY.w}, vz[4] = {VZ.x, VZ.y, VZ.z, VZ.w};
-  int akey = -1;
+  // the cell most of the thread's slots share (ties: the earliest)
+  int akey = -1, best = 0;
 #pragma unroll
-  for (int k = 0; k < CH_TILE_K; ++k) akey = (akey < 0) ? keys[k] : akey;
+  for (int k = 0; k < CH_TILE_K; ++k) {
+    int n = 0;
+#pragma unroll
+    for (int q = 0; q < CH_TILE_K; ++q) n += (keys[q] == keys[k]) ? 1 : 0;
+    if (keys[k] >= 0 && n > best) { best = n; akey = keys[k]; }
+  }
   unsigned a[32];
 #pragma unroll
   for (int q = 0; q < 32; ++q) a[q] = 0u;
@@ -532,7 +540,7 @@ __device__ __forceinline__ void tile_deposit_batch(TileShared& sh, int lane) {
   for (int k = 0; k < CH_TILE_K; ++k) {
     if (keys[k] < 0) continue;
     if (keys[k] != akey) {
-      tile_deposit_lane(sh, keys[k], ox[k], oy[k], oz[k], vx[k], vy[k], vz[k]);
+      sh.ov_idx[atomicAdd(&sh.ov_n, 1u)] = (uint16_t)(CH_TILE_K * t + k);
       continue;
     }
     ++cnt;
@@ -579,6 +587,13 @@ __device__ __forceinline__ void tile_deposit_batch(TileShared& sh, int lane) {
       if (a[q] != 0u)
         shared_add64(&sh.acc_lo[m][node], &sh.acc_hi[m][node], (long long)(int)a[q]);
     }
+  }
+  __syncthreads();  // the overflow list is complete
+  const unsigned nov = sh.ov_n;
+  for (unsigned e = t; e < nov; e += blockDim.x) {
+    const int q = sh.ov_idx[e];
+    tile_deposit_lane(sh, sh.st_key[q], sh.st_ox[q], sh.st_oy[q], sh.st_oz[q], sh.st_vx[q], sh.st_vy[q],
+                      sh.st_vz[q]);
   }
 }
 
@@ -855,6 +870,7 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
       }
     }
     if (PH & PH_DEPOSIT) {
+      if (threadIdx.x == 0) sh.ov_n = 0u;
       __syncthreads();  // the batch is staged
       tile_deposit_batch(sh, lane);
       __syncthreads();  // staging is read before the next batch overwrites it
