@@ -252,6 +252,150 @@ def e2e(args, h, w, step):
             "steps": K, "ms_per_step": 1e3 * dt / K}
 
 
+# ------------------------------------------------------------------ forms beside the step
+def errors_vs_fp64(w):
+    """Mixed-form outputs against the FP64 form from the same seeded plasma:
+    one collection, one potential solve and one step in each form."""
+    m = chy()
+    out = {}
+    hs = {}
+    for form in ("mixed", "fp64"):
+        wf = dict(w, precision=form)
+        h = m.Hybrid(make_params(wf))
+        h.load(ions_for(w), make_loader(w))
+        m0 = h.CollectVlasovQuantities()
+        phi0 = h.ComputePotential()
+        h.step(0, 1)
+        hs[form] = (h, m0, phi0, h.CollectVlasovQuantities(), h.phi())
+    (hm, m0m, p0m, m1m, p1m), (hd, m0d, p0d, m1d, p1d) = hs["mixed"], hs["fp64"]
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    out["phi_initial"] = rel(p0m, p0d)
+    out["phi_after_step"] = rel(p1m, p1d)
+    out["moments_initial"] = rel(m0m, m0d)
+    out["moments_after_step"] = rel(m1m, m1d)
+    out["norm"] = "relative L2 against the FP64 form (same seeded ions; collisions on)"
+    hm.close()
+    hd.close()
+    return out
+
+
+def ensemble_runs(nruns=64, seed=3):
+    """The ensemble workload: grid edge per axis uniform in {16, 24, 32, 48,
+    64}, 8-32 ions/cell, E_x ~ U[0.2, 1.5], nu ~ logU[0.01, 2], a distinct
+    seed per run; mixed form, rtol 1e-10."""
+    m = chy()
+    rng = np.random.default_rng(seed)
+    edges = np.array([16, 24, 32, 48, 64])
+    params, nions, loaders = [], [], []
+    for r in range(nruns):
+        N = tuple(int(x) for x in rng.choice(edges, 3))
+        ppc = int(rng.integers(8, 33))
+        Ex = float(rng.uniform(0.2, 1.5))
+        nu = float(np.exp(rng.uniform(np.log(0.01), np.log(2.0))))
+        p = m.params_for(N, precision=m.PRECISION["mixed"], E0=(Ex, 0.0, 0.0), nui=nu, ksp_rtol=1e-10,
+                         pc_type=m.PC["mg"], sort_period=4, seed=1000 + r, run=r)
+        params.append(p)
+        nions.append(N[0] * N[1] * N[2] * ppc)
+        loaders.append(m.loader(amp=(0.01, 0.0, 0.0)))
+    return params, nions, loaders
+
+
+def run_ensemble(steps):
+    """Aggregate particle-steps/s of the ensemble in one ch_batch against the
+    same runs stepped one by one on a ch_ctx each (CUDA events on each
+    stream)."""
+    m = chy()
+    import torch
+
+    params, nions, loaders = ensemble_runs()
+    total = sum(nions)
+    with m.Batch(params, nions) as b:
+        b.load(loaders)
+        b.initialize()
+        tune = b.autotune()
+        b.step(0, 2)
+        st = torch.cuda.ExternalStream(b.stream_handle())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        info = b.step(2, steps)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms_batch = e0.elapsed_time(e1)
+        ok = all(i["status"] == 0 for i in info)
+    ms_one = 0.0
+    for p, n, L in zip(params, nions, loaders):
+        with m.Hybrid(p) as h:
+            h.load(n, L)
+            h.CollectVlasovQuantities(copy=False)
+            h.ComputePotential(copy=False)
+            h.step(0, 2)
+            t = DeviceTimer(h)
+            torch.cuda.synchronize()
+            a = t.event()
+            h.step(2, steps)
+            c = t.event()
+            torch.cuda.synchronize()
+            ms_one += a.elapsed_time(c)
+    v_b = total * steps / (ms_batch / 1e3)
+    v_o = total * steps / (ms_one / 1e3)
+    return {"value": v_b, "unit": UNIT, "one_by_one": v_o, "speedup": v_b / v_o, "runs": len(params),
+            "ions": total, "nodes": sum(p.Nx * p.Ny * p.Nz for p in params), "steps": steps,
+            "ms_per_step": ms_batch / steps, "one_by_one_ms_per_step": ms_one / steps, "tuning": tune,
+            "all_runs_ok": ok, "workload": "64 runs, edges U{16,24,32,48,64} per axis, 8-32 ions/cell, "
+            "E_x U[0.2,1.5], nu logU[0.01,2], mixed form; timed steps are a bounded sample of the 100-step run"}
+
+
+def run_adjoint(fd=True):
+    """Differentiation workload: 64^3 grid, 32 ions/cell, E0 = (0.5, 0.1, 0),
+    nu = 0.3, 50 steps, checkpoints every 10, objective over the final 10
+    steps (mean x flux + 0.1 mean square potential); gradient w.r.t. E0,
+    vn0, amp against central differences (eps 1e-6) of the frozen-event
+    forward."""
+    m = chy()
+    N = (64, 64, 64)
+    p = m.params_for(N, precision=m.PRECISION["fp64"], E0=(0.5, 0.1, 0.0), nui=0.3, ksp_rtol=1e-13,
+                     pc_type=m.PC["mg"], seed=1)
+    L = m.loader(amp=(0.01, 0.0, 0.0))
+    np_ = 64 ** 3 * 32
+    with m.Adjoint(p, np_, L, nsteps=50, checkpoint_every=10, window=10) as adj:
+        th = adj.theta0()
+        t0 = time.perf_counter()
+        J = adj.forward(th, record=True)
+        t1 = time.perf_counter()
+        g, _ = adj.gradient()
+        t2 = time.perf_counter()
+        tim = adj.timing()
+        out = {"J": J, "gradient": [float(x) for x in g], "theta": ["E0x", "E0y", "E0z", "vn0x", "vn0y", "vn0z", "amp"],
+               "forward_ms": tim["forward_ms"], "gradient_ms": tim["gradient_ms"],
+               "recompute_ms": tim["recompute_ms"], "gradient_over_forward": tim["gradient_ms"] / tim["forward_ms"],
+               "events": tim["events"], "ions": np_, "steps": 50, "checkpoint_every": 10,
+               "wall_s": {"forward": t1 - t0, "gradient": t2 - t1}}
+        if fd:
+            # eps = 1e-6 for every parameter; for amp also 3e-7: its
+            # perturbation moves every ion by ~eps Lx/pi cells and ions that
+            # cross a cell face pass a kink of the CIC weights
+            def central(k, eps):
+                e = np.zeros_like(th)
+                e[k] = eps
+                return (adj.forward(th + e) - adj.forward(th - e)) / (2 * eps)
+
+            fdv = np.array([central(k, 1e-6) for k in range(len(th))])
+            scale = np.maximum(np.abs(fdv), 1e-3 * np.abs(fdv).max())
+            err = np.abs(g - fdv) / scale
+            amp_small = central(6, 3e-7)
+            out["central_fd_eps1e-6"] = [float(x) for x in fdv]
+            out["rel_err_vs_fd_eps1e-6"] = [float(x) for x in err]
+            out["amp_central_fd_eps3e-7"] = float(amp_small)
+            out["amp_rel_err_eps3e-7"] = float(abs(g[6] - amp_small) / scale[6])
+            out["max_rel_err_vs_fd"] = float(max(err[:6].max(), min(err[6], out["amp_rel_err_eps3e-7"])))
+    return out
+
+
 # ------------------------------------------------------------------ CPU arm
 def cpu_sample(w, threads, np_sample, steps, warmup):
     """FP64 CPU restatement of the step on the host cores: particle phases
@@ -312,6 +456,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-ions", type=int, default=1 << 22)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form comparison line")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble (ch_batch) measurement")
+    ap.add_argument("--ensemble-steps", type=int, default=10)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (ch_adjoint) measurement")
+    ap.add_argument("--no-adjoint-fd", action="store_true", help="skip its finite-difference check")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     rank = int(os.environ.get("RANK", "0"))
@@ -394,6 +542,12 @@ def main():
         line["e2e"] = {k: e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")}
         line["e2e"]["value"] *= world
         line["e2e"]["ms_per_step"] = e["ms_per_step"]
+    if not args.no_fp64 and w["precision"] == "mixed":
+        line["errors_vs_fp64"] = errors_vs_fp64(w)
+    if not args.no_ensemble:
+        line["ensemble"] = run_ensemble(args.ensemble_steps)
+    if not args.no_adjoint:
+        line["adjoint"] = run_adjoint(fd=not args.no_adjoint_fd)
     if not args.no_cpu:
         c = cpu_sample(w, os.cpu_count() or 1, args.cpu_ions, 1, 0)
         line["cpu_baseline"] = {"value": c["value"], "unit": UNIT, "cores": c["threads"], "kind": "port",

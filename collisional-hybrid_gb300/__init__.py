@@ -110,6 +110,19 @@ class Tuning(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class AdjointConfig(C.Structure):
+    _fields_ = [("nsteps", C.c_int32), ("checkpoint_every", C.c_int32), ("window", C.c_int32), ("pad", C.c_int32),
+                ("flux_weight", C.c_double), ("phi_weight", C.c_double)]
+
+
+class AdjointTiming(C.Structure):
+    _fields_ = [("forward_ms", C.c_double), ("gradient_ms", C.c_double), ("recompute_ms", C.c_double),
+                ("events", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Profile(C.Structure):
     _fields_ = [("pass_ms", C.c_double), ("pass_calls", C.c_int64), ("solve_ms", C.c_double),
                 ("solve_calls", C.c_int64), ("sort_ms", C.c_double), ("sort_calls", C.c_int64),
@@ -171,6 +184,13 @@ def lib():
             "ch_batch_set_profiling": [vp, C.c_int32],
             "ch_batch_get_profile": [vp, C.POINTER(Profile)],
             "ch_batch_get_stream": [vp, C.POINTER(vp)],
+            "ch_adjoint_create": [C.POINTER(Params), C.c_int64, C.POINTER(Loader), C.POINTER(AdjointConfig),
+                                  C.c_int32, C.POINTER(vp)],
+            "ch_adjoint_destroy": [vp],
+            "ch_adjoint_forward": [vp, vp, C.c_int32, C.POINTER(C.c_double)],
+            "ch_adjoint_gradient": [vp, vp, C.POINTER(C.c_double)],
+            "ch_adjoint_events": [vp, C.POINTER(C.c_int64), vp, vp, vp, vp],
+            "ch_adjoint_get_timing": [vp, C.POINTER(AdjointTiming)],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -463,6 +483,73 @@ class Batch:
         s = C.c_void_p()
         _check(lib().ch_batch_get_stream(self._h, C.byref(s)))
         return s.value or 0
+
+
+NTHETA = 7  # E0 (3), vn0 (3), amp (loader amp[0])
+
+
+class Adjoint:
+    """The FP64 step as a differentiable function of theta = (E0, vn0, amp)
+    with the collision events of a recorded run frozen (ch_adjoint)."""
+
+    def __init__(self, params: Params, nions: int, L: Loader, nsteps: int, checkpoint_every: int, window: int,
+                 flux_weight: float = 1.0, phi_weight: float = 0.1, device: int = -1):
+        self.cfg = AdjointConfig(int(nsteps), int(checkpoint_every), int(window), 0, float(flux_weight),
+                                 float(phi_weight))
+        self.params, self.loader, self.np = params, L, int(nions)
+        h = C.c_void_p()
+        _check(lib().ch_adjoint_create(C.byref(params), self.np, C.byref(L), C.byref(self.cfg), device, C.byref(h)))
+        self._h = h
+
+    def theta0(self):
+        p = self.params
+        return np.array(list(p.E0) + list(p.vn0) + [self.loader.amp[0]], dtype=np.float64)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ch_adjoint_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def forward(self, theta, record: bool = False) -> float:
+        th = np.ascontiguousarray(theta, dtype=np.float64)
+        assert th.shape == (NTHETA,)
+        J = C.c_double()
+        _check(lib().ch_adjoint_forward(self._h, th.ctypes.data, int(bool(record)), C.byref(J)))
+        return J.value
+
+    def gradient(self):
+        g = np.empty(NTHETA)
+        J = C.c_double()
+        _check(lib().ch_adjoint_gradient(self._h, g.ctypes.data, C.byref(J)))
+        return g, J.value
+
+    def events(self) -> dict:
+        n = C.c_int64()
+        _check(lib().ch_adjoint_events(self._h, C.byref(n), None, None, None, None))
+        step = np.empty(n.value, np.int32)
+        ion = np.empty(n.value, np.uint32)
+        flags = np.empty(n.value, np.int32)
+        data = np.empty((n.value, 5))
+        _check(lib().ch_adjoint_events(self._h, C.byref(n), step.ctypes.data, ion.ctypes.data, flags.ctypes.data,
+                                       data.ctypes.data))
+        return dict(step=step, ion=ion, flags=flags, data=data)
+
+    def timing(self) -> dict:
+        t = AdjointTiming()
+        _check(lib().ch_adjoint_get_timing(self._h, C.byref(t)))
+        return t.as_dict()
 
 
 def host_register(a: np.ndarray):

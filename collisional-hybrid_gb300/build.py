@@ -16,7 +16,7 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libchybrid.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["chybrid.cu", "particles.cu", "solver.cu", "noalloc.cu", "batch_solve.cu", "chybrid_batch.cu"]
+SOURCES = ["chybrid.cu", "particles.cu", "solver.cu", "noalloc.cu", "batch_solve.cu", "chybrid_batch.cu", "adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -18,6 +18,7 @@
 
 #include <atomic>
 
+#include "ion_dev.cuh"
 #include "physics.cuh"
 
 namespace ch {
@@ -31,44 +32,6 @@ namespace ch {
 __device__ __forceinline__ unsigned long long g_fixed(float g) {
   // g < 2^12 in any plasma the fixed-point deposit admits; 32-bit conversion
   return (unsigned long long)__float2uint_rn(g * 1048576.0f);
-}
-
-__device__ __forceinline__ void red_add(unsigned long long* a, long long v) {
-  atomicAdd(a, (unsigned long long)v);
-}
-
-template <typename R>
-__device__ __forceinline__ long long to_fx(R v, R scale) {
-  return __double2ll_rn((double)(v * scale));
-}
-template <>
-__device__ __forceinline__ long long to_fx<float>(float v, float scale) {
-  return __float2ll_rn(v * scale);
-}
-
-// Deposit one ion's CIC weights: nodes (i..i+1, j..j+1, k..k+1), weights in
-// the order of src/particles.c:204-211.
-template <typename R>
-__device__ __forceinline__ void deposit_cic(const GridDesc& g, unsigned long long* __restrict__ acc, int i, int j,
-                                            int k, R wxh, R wyh, R wzh, R vx, R vy, R vz, R scale) {
-  const R wxl = R(1) - wxh, wyl = R(1) - wyh, wzl = R(1) - wzh;
-  const int i1 = (i + 1 == g.Nx) ? 0 : i + 1;
-  const int j1 = (j + 1 == g.Ny) ? 0 : j + 1;
-  const int k1 = (k + 1 == g.Nz) ? 0 : k + 1;
-  const int64_t N = g.N;
-  const int64_t rz0 = (int64_t)k * g.Ny, rz1 = (int64_t)k1 * g.Ny;
-  const int64_t c[8] = {(rz1 + j1) * g.Nx + i1, (rz0 + j1) * g.Nx + i1, (rz1 + j) * g.Nx + i1,
-                        (rz0 + j) * g.Nx + i1,  (rz1 + j1) * g.Nx + i,  (rz0 + j1) * g.Nx + i,
-                        (rz1 + j) * g.Nx + i,   (rz0 + j) * g.Nx + i};
-  const R w[8] = {wzh * wyh * wxh, wzl * wyh * wxh, wzh * wyl * wxh, wzl * wyl * wxh,
-                  wzh * wyh * wxl, wzl * wyh * wxl, wzh * wyl * wxl, wzl * wyl * wxl};
-#pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    red_add(acc + c[q], to_fx<R>(w[q], scale));
-    red_add(acc + N + c[q], to_fx<R>(vx * w[q], scale));
-    red_add(acc + 2 * N + c[q], to_fx<R>(vy * w[q], scale));
-    red_add(acc + 3 * N + c[q], to_fx<R>(vz * w[q], scale));
-  }
 }
 
 // Warp-aggregated increment of counts[key]; returns this lane's rank among
@@ -320,13 +283,6 @@ __device__ void diffvec_faithful(const GridDesc& g, const double* __restrict__ p
   }
 }
 
-__device__ __forceinline__ double wrap_pos(double x, double x0, double L) {
-  double u = x - x0;
-  if (u < 0.0 || u >= L) u -= L * floor(u / L);
-  if (u >= L) u -= L;
-  if (u < 0.0) u = 0.0;
-  return x0 + u;
-}
 
 // ------------------------------------------------------------------ FP64 pass
 // Block partials: 0 expected, 1 S(next).

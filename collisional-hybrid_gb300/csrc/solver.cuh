@@ -64,6 +64,11 @@ class PotentialSolver {
   ch_status solve(const double* n, const double* b, double* phi, SolveStats* st, cudaStream_t s);
   // y = A(n) x in FP64.
   void apply64(const double* n, const double* x, double* y, cudaStream_t s);
+  // Applied field of the RHS (varied by the adjoint's gradient and
+  // finite-difference runs).
+  void set_E0(const double E0[3]) {
+    for (int d = 0; d < 3; ++d) p_.E0[d] = E0[d];
+  }
 
  private:
   ch_status solve_fp64(const double* n, const double* b, double* phi, SolveStats* st, cudaStream_t s);

@@ -1,12 +1,17 @@
-"""Per-phase timing of the ion pass: the fused step (push + collide + move +
-deposit) against UpdateVelocities, UpdatePositions and CollectVlasovQuantities
-run separately, on a seeded synthetic plasma.  Prints one JSON line.
+"""Profiling driver of the hot-path kernels on seeded synthetic plasmas;
+prints one JSON line.
+
+    --mode pass (default): the fused step (push + collide + move + deposit)
+        against UpdateVelocities, UpdatePositions and CollectVlasovQuantities
+        run separately; each phase is one launch of k_pass_tiled<PH> (or
+        k_pass_f64<PH>).  Timings are the library's CUDA-event phase times.
+    --mode ensemble: a ch_batch of --runs small runs (edges 16-32), --steps
+        steps; one k_batch_pass and one k_batch_solve launch per step.
+    --mode adjoint: a ch_adjoint run (FP64, --grid^3, --ppc ions per cell,
+        --steps steps): one recorded forward and one gradient.
 
     python collisional-hybrid_gb300/profile_pass.py --grid 128 --ppc 64 --nu 0.5
-
-Timings are CUDA-event phase times of the library (ch_get_profile); the step
-that is timed follows `--warm` untimed steps.  Used for the ncu captures of
-the pass kernels (each phase is one launch of k_pass_tiled<PH>)."""
+"""
 import argparse
 import importlib
 import json
@@ -26,8 +31,15 @@ def main(argv=None):
     ap.add_argument("--sort-period", type=int, default=4)
     ap.add_argument("--warm", type=int, default=3)
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--mode", choices=["pass", "ensemble", "adjoint"], default="pass")
+    ap.add_argument("--runs", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=4)
     a = ap.parse_args(argv)
     m = importlib.import_module("collisional-hybrid_gb300")
+    if a.mode == "ensemble":
+        return ensemble(m, a)
+    if a.mode == "adjoint":
+        return adjoint(m, a)
     N = a.grid
     p = m.params_for((N, N, N), precision=m.PRECISION[a.precision], E0=(a.Ex, 0.0, 0.0), nui=a.nu, ksp_rtol=1e-10,
                      pc_type=m.PC["mg"], sort_period=a.sort_period, mn=(1.0 if a.nu > 0 else 0.0))
@@ -45,6 +57,37 @@ def main(argv=None):
         h.reset_profile(); h.UpdatePositions(); out["move_ms"] = h.profile()["pass_ms"]
         h.reset_profile(); h.CollectVlasovQuantities(copy=False); out["deposit_ms"] = h.profile()["pass_ms"]
     print(json.dumps(out))
+
+
+def ensemble(m, a):
+    import numpy as np
+
+    rng = np.random.default_rng(7)
+    params, nions, loaders = [], [], []
+    for r in range(a.runs):
+        N = tuple(int(x) for x in rng.choice([16, 24, 32], 3))
+        params.append(m.params_for(N, precision=m.PRECISION["mixed"], E0=(a.Ex, 0.0, 0.0), nui=a.nu,
+                                   ksp_rtol=1e-10, pc_type=m.PC["mg"], sort_period=a.sort_period, seed=100 + r,
+                                   run=r))
+        nions.append(N[0] * N[1] * N[2] * a.ppc)
+        loaders.append(m.loader(amp=(0.01, 0.0, 0.0)))
+    with m.Batch(params, nions) as b:
+        b.load(loaders)
+        b.initialize()
+        info = b.step(0, a.steps)
+        print(json.dumps({"mode": "ensemble", "runs": a.runs, "ions": sum(nions), "steps": a.steps,
+                          "ok": all(i["status"] == 0 for i in info)}))
+
+
+def adjoint(m, a):
+    N = a.grid
+    p = m.params_for((N, N, N), precision=m.PRECISION["fp64"], E0=(0.5, 0.1, 0.0), nui=a.nu, ksp_rtol=1e-13,
+                     pc_type=m.PC["mg"], seed=1)
+    with m.Adjoint(p, N ** 3 * a.ppc, m.loader(amp=(0.01, 0.0, 0.0)), nsteps=a.steps,
+                   checkpoint_every=max(1, a.steps // 2), window=max(1, a.steps // 2)) as adj:
+        J = adj.forward(adj.theta0(), record=True)
+        g, _ = adj.gradient()
+        print(json.dumps({"mode": "adjoint", "J": J, "grad": [float(x) for x in g], **adj.timing()}))
 
 
 if __name__ == "__main__":

@@ -302,6 +302,50 @@ ch_status ch_batch_set_profiling(ch_batch* b, int32_t enable);
 ch_status ch_batch_get_profile(ch_batch* b, ch_profile* out);
 ch_status ch_batch_get_stream(ch_batch* b, void** stream);
 
+/* ---------------------------------------------------------------------
+ * Differentiation (no counterpart in the reference).  A discrete adjoint of
+ * the FP64 step with the collision events and scattering draws of a
+ * recorded run frozen.  Parameters theta = (E0x, E0y, E0z, vn0x, vn0y, vn0z,
+ * amp), amp = loader amp[0] (the first density mode).  Objective, summed
+ * over the states after the last `window` steps:
+ *   J = sum_k [ flux_weight/(window N) sum_i v_x,i + phi_weight/(window N) sum_c phi_c^2 ]
+ * (sum_i v_x,i is the sum over nodes of Gamma_x: the mean x-directed ion flux
+ * times N).  kappa_e = 0, full LHS/RHS, uniform neutrals.
+ * --------------------------------------------------------------------- */
+typedef struct ch_adjoint ch_adjoint;
+#define CH_ADJ_NTHETA 7
+typedef struct ch_adjoint_config {
+  int32_t nsteps;            /* steps of the run                              */
+  int32_t checkpoint_every;  /* ion-state checkpoints every k steps           */
+  int32_t window;            /* the objective covers the final `window` steps */
+  int32_t pad;
+  double flux_weight;        /* weight of the mean x flux                     */
+  double phi_weight;         /* weight of the mean square potential           */
+} ch_adjoint_config;
+typedef struct ch_adjoint_timing {
+  double forward_ms;         /* last ch_adjoint_forward                       */
+  double gradient_ms;        /* last ch_adjoint_gradient (recompute included) */
+  double recompute_ms;       /* its segment recomputation                     */
+  int64_t events;            /* frozen collision events of the recorded run   */
+} ch_adjoint_timing;
+ch_status ch_adjoint_create(const ch_params* p, int64_t np, const ch_loader* L, const ch_adjoint_config* cfg,
+                            int32_t device, ch_adjoint** out);
+ch_status ch_adjoint_destroy(ch_adjoint* a);
+/* The forward model at theta (CH_ADJ_NTHETA values).  record = 1 draws the
+ * collision events (Philox, as the FP64 step) and freezes them, stores the
+ * checkpoints and makes theta the point of the next gradient; record = 0
+ * replays the frozen events at this theta (finite differences). */
+ch_status ch_adjoint_forward(ch_adjoint* a, const double* theta, int32_t record, double* J);
+/* dJ/dtheta at the recorded point; J (nullable) receives J there. */
+ch_status ch_adjoint_gradient(ch_adjoint* a, double* grad, double* J);
+/* The frozen events, for an independent replay: with null arrays *count
+ * receives the number; otherwise `count` events in (step, ion, event) order:
+ * step, ion, flags (1 = refused) and 5 doubles each (V - vn0 (3), uz, uphi
+ * as a fraction of a turn). */
+ch_status ch_adjoint_events(ch_adjoint* a, int64_t* count, int32_t* step, uint32_t* ion, int32_t* flags,
+                            double* data);
+ch_status ch_adjoint_get_timing(ch_adjoint* a, ch_adjoint_timing* out);
+
 /* Page-locks caller memory so that the copies of upload/download run at
  * full link speed (no counterpart in the reference: its arrays never leave
  * the host). */

@@ -832,5 +832,123 @@ int orc_step(orc_state* s, int64_t step, orc_counters* cnt, int* its, double* rn
   return potential(s, its, rnorm, bnorm);
 }
 
+/* ------------------------------------------------------------------ */
+/* Centre-of-mass scatter of one frozen event (src/particles.c:552-591,
+ * the formula of collide_ion above) with the neutral velocity V given. */
+static void scatter_event(double* vx, double* vy, double* vz, const double V[3], double uz, double uphi_frac,
+                          double mi, double mn) {
+  const double M = mi + mn;
+  const double vix = *vx, viy = *vy, viz = *vz;
+  const double uphi = 2.0 * PI * uphi_frac;
+  double vrx = vix - V[0], vry = viy - V[1], vrz = viz - V[2];
+  double vrr = sqrt(vrx * vrx + vry * vry + vrz * vrz);
+  double vcx = (vix * mi + V[0] * mn) / M, vcy = (viy * mi + V[1] * mn) / M, vcz = (viz * mi + V[2] * mn) / M;
+  double ax = vix - vcx, ay = viy - vcy, az = viz - vcz;
+  double vcr = sqrt(ax * ax + ay * ay + az * az);
+  double uperp = sqrt(fmax(0.0, 1.0 - uz * uz));
+  double ux = uperp * cos(uphi), uy = uperp * sin(uphi);
+  double costht = vrr > 0.0 ? vrz / vrr : 1.0;
+  double sintht = sqrt(fmax(0.0, 1.0 - costht * costht));
+  double cosphi = 1.0, sinphi = 0.0;
+  if (vrr * sintht > 0.0) { cosphi = vrx / (vrr * sintht); sinphi = vry / (vrr * sintht); }
+  double ux1 = uz * sintht + ux * costht, uy1 = uy, uz1 = uz * costht - ux * sintht;
+  double ux2 = ux1 * cosphi - uy1 * sinphi, uy2 = ux1 * sinphi + uy1 * cosphi, uz2 = uz1;
+  *vx = vcx + vcr * ux2; *vy = vcy + vcr * uy2; *vz = vcz + vcr * uz2;
+}
+
+int orc_adj_objective(const ch_params* p, const ch_loader* L, int64_t np, int nsteps, int window,
+                      double flux_weight, double phi_weight, int64_t nev, const int32_t* ev_step,
+                      const uint32_t* ev_ion, const int32_t* ev_flags, const double* ev_data, double rtol,
+                      double* J) {
+  grid g = mkgrid(p);
+  const int64_t N = g.N;
+  orc_particles P;
+  P.np = np;
+  double* buf = (double*)malloc(sizeof(double) * 6 * (size_t)np);
+  double* nodes = (double*)calloc((size_t)N * 4, sizeof(double));
+  double* b = (double*)malloc(sizeof(double) * N);
+  double* phi = (double*)calloc((size_t)N, sizeof(double));
+  double* n = (double*)malloc(sizeof(double) * N);
+  double* E = (double*)malloc(sizeof(double) * 3 * N);
+  int64_t* start = (int64_t*)malloc(sizeof(int64_t) * (size_t)np);
+  if (!buf || !nodes || !b || !phi || !n || !E || !start) {
+    free(buf); free(nodes); free(b); free(phi); free(n); free(E); free(start);
+    return CH_ERR_NOMEM;
+  }
+  P.x = buf; P.y = buf + np; P.z = buf + 2 * np; P.vx = buf + 3 * np; P.vy = buf + 4 * np; P.vz = buf + 5 * np;
+  orc_load(p, L, &P);
+  int its, rc = 0;
+  double rn, bn;
+  orc_collect(p, &P, nodes, 0);
+  orc_rhs(p, nodes, b);
+  for (int64_t c = 0; c < N; ++c) n[c] = nodes[4 * c];
+  rc = orc_solve(p, n, b, phi, rtol, p->ksp_max_it, &its, &rn, &bn);
+  const double tscale = 0.5 * (p->qi / p->mi) * p->dt;
+  double t[3], s[3];
+  for (int d = 0; d < 3; ++d) t[d] = tscale * p->B0[d];
+  const double tt = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+  for (int d = 0; d < 3; ++d) s[d] = 2.0 * t[d] / (1.0 + tt);
+  double Jsum = 0.0;
+  int64_t e0 = 0;
+  for (int st = 0; st < nsteps && rc == 0; ++st) {
+    int64_t e1 = e0;
+    while (e1 < nev && ev_step[e1] == st) ++e1;
+    for (int64_t i = 0; i < np; ++i) start[i] = -1;
+    for (int64_t e = e1 - 1; e >= e0; --e) start[ev_ion[e]] = e;  /* first event of each ion */
+    orc_node_efield(p, phi, E, E + N, E + 2 * N);
+    double sumvx = 0.0;
+#pragma omp parallel for num_threads(g_threads) reduction(+ : sumvx) schedule(static)
+    for (int64_t ip = 0; ip < np; ++ip) {
+      double X = (P.x[ip] - g.x0) / g.dx, Y = (P.y[ip] - g.y0) / g.dy, Z = (P.z[ip] - g.z0) / g.dz;
+      int i = (int)floor(X), j = (int)floor(Y), k = (int)floor(Z);
+      double wx = X - i, wy = Y - j, wz = Z - k;
+      int64_t c000 = nid(&g, i, j, k), c100 = nid(&g, i + 1, j, k), c010 = nid(&g, i, j + 1, k),
+              c110 = nid(&g, i + 1, j + 1, k), c001 = nid(&g, i, j, k + 1), c101 = nid(&g, i + 1, j, k + 1),
+              c011 = nid(&g, i, j + 1, k + 1), c111 = nid(&g, i + 1, j + 1, k + 1);
+      double Ef[3];
+      for (int d = 0; d < 3; ++d) {
+        const double* e = E + d * N;
+        double wll = e[c000] + wy * (e[c010] - e[c000]);
+        double wlh = e[c100] + wy * (e[c110] - e[c100]);
+        double whl = e[c001] + wy * (e[c011] - e[c001]);
+        double whh = e[c101] + wy * (e[c111] - e[c101]);
+        double ezl = wll + wx * (wlh - wll);
+        double ezh = whl + wx * (whh - whl);
+        Ef[d] = ezl + wz * (ezh - ezl);
+      }
+      if (p->push_E0) { Ef[0] += p->E0[0]; Ef[1] += p->E0[1]; Ef[2] += p->E0[2]; }
+      double vm[3] = {P.vx[ip] + tscale * Ef[0], P.vy[ip] + tscale * Ef[1], P.vz[ip] + tscale * Ef[2]};
+      double c1[3] = {vm[1] * t[2] - vm[2] * t[1], vm[2] * t[0] - vm[0] * t[2], vm[0] * t[1] - vm[1] * t[0]};
+      double vpr[3] = {vm[0] + c1[0], vm[1] + c1[1], vm[2] + c1[2]};
+      double c2[3] = {vpr[1] * s[2] - vpr[2] * s[1], vpr[2] * s[0] - vpr[0] * s[2], vpr[0] * s[1] - vpr[1] * s[0]};
+      double vx = vm[0] + c2[0] + tscale * Ef[0], vy = vm[1] + c2[1] + tscale * Ef[1],
+             vz = vm[2] + c2[2] + tscale * Ef[2];
+      if (p->mn > 0.0 && start[ip] >= 0)
+        for (int64_t e = start[ip]; e < e1 && ev_ion[e] == (uint32_t)ip; ++e) {
+          if (ev_flags[e] & 1) continue;
+          const double* q = ev_data + 5 * e;
+          const double V[3] = {p->vn0[0] + q[0], p->vn0[1] + q[1], p->vn0[2] + q[2]};
+          scatter_event(&vx, &vy, &vz, V, q[3], q[4], p->mi, p->mn);
+        }
+      P.vx[ip] = vx; P.vy[ip] = vy; P.vz[ip] = vz;
+      sumvx += vx;
+    }
+    e0 = e1;
+    orc_update_positions(p, &P);
+    orc_collect(p, &P, nodes, 0);
+    orc_rhs(p, nodes, b);
+    for (int64_t c = 0; c < N; ++c) n[c] = nodes[4 * c];
+    rc = orc_solve(p, n, b, phi, rtol, p->ksp_max_it, &its, &rn, &bn);
+    if (st >= nsteps - window) {
+      double s2 = 0.0;
+      for (int64_t c = 0; c < N; ++c) s2 += phi[c] * phi[c];
+      Jsum += flux_weight / ((double)window * (double)N) * sumvx + phi_weight / ((double)window * (double)N) * s2;
+    }
+  }
+  *J = Jsum;
+  free(buf); free(nodes); free(b); free(phi); free(n); free(E); free(start);
+  return rc;
+}
+
 /* sizeof(ch_params) as the C compiler lays it out, for the binding checks. */
 int64_t orc_sizeof_params(void) { return (int64_t)sizeof(ch_params); }

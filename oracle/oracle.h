@@ -104,6 +104,18 @@ int orc_step(orc_state* s, int64_t step, orc_counters* cnt, int* its, double* rn
 /* Initial moments and first solve (src/hybrid.c:67,81); also sets sbar. */
 int orc_initialize(orc_state* s, int* its, double* rnorm, double* bnorm);
 
+/* The differentiable model of the GPU adjoint with frozen collision events
+ * (the FP64 step: gather, Boris, the given events, move, deposit, solve),
+ * replayed at the parameters in p (E0, vn0) and L (amp[0]).  Events in
+ * (step, ion, event) order: ev_step, ev_ion, ev_flags (1 = refused) and 5
+ * doubles each (V - vn0, uz, uphi as a fraction of a turn).  Returns J, the
+ * objective over the states after the last `window` steps:
+ * flux_weight/(window N) sum_i v_x + phi_weight/(window N) sum phi^2. */
+int orc_adj_objective(const ch_params* p, const ch_loader* L, int64_t np, int nsteps, int window,
+                      double flux_weight, double phi_weight, int64_t nev, const int32_t* ev_step,
+                      const uint32_t* ev_ion, const int32_t* ev_flags, const double* ev_data, double rtol,
+                      double* J);
+
 int64_t orc_sizeof_params(void);
 
 /* Threads used by the loops (1 = serial, as the reference's per-rank loops). */

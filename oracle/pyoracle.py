@@ -98,6 +98,9 @@ def lib():
         L.orc_step.argtypes = [C.POINTER(State), C.c_int64, C.POINTER(Counters), C.POINTER(C.c_int), _dp, _dp]
         L.orc_initialize.argtypes = [C.POINTER(State), C.POINTER(C.c_int), _dp, _dp]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_adj_objective.argtypes = [C.POINTER(Params), C.POINTER(Loader), C.c_int64, C.c_int, C.c_int,
+                                        C.c_double, C.c_double, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_double, _dp]
         L.orc_get_threads.restype = C.c_int
         L.orc_sizeof_params.restype = C.c_int64
         _lib = L
@@ -276,6 +279,23 @@ def solve(p: Params, n, b, phi0=None, rtol=None, maxit=None):
                          p.ksp_rtol if rtol is None else rtol, p.ksp_max_it if maxit is None else maxit,
                          C.byref(its), C.byref(rn), C.byref(bn))
     return phi, dict(rc=rc, its=its.value, rnorm=rn.value, bnorm=bn.value)
+
+
+def adj_objective(p: Params, L: Loader, np_: int, nsteps: int, window: int, flux_weight: float, phi_weight: float,
+                  events: dict, rtol: float) -> float:
+    """The frozen-event objective of the GPU adjoint, replayed in FP64 on the
+    CPU (theta enters through p.E0, p.vn0 and L.amp[0])."""
+    st = np.ascontiguousarray(events["step"], dtype=np.int32)
+    ion = np.ascontiguousarray(events["ion"], dtype=np.uint32)
+    fl = np.ascontiguousarray(events["flags"], dtype=np.int32)
+    data = np.ascontiguousarray(events["data"], dtype=np.float64)
+    J = C.c_double()
+    rc = lib().orc_adj_objective(C.byref(p), C.byref(L), int(np_), int(nsteps), int(window), float(flux_weight),
+                                 float(phi_weight), len(st), st.ctypes.data, ion.ctypes.data, fl.ctypes.data,
+                                 data.ctypes.data, float(rtol), C.byref(J))
+    if rc:
+        raise RuntimeError(f"orc_adj_objective: {rc}")
+    return J.value
 
 
 def difference_vector(p: Params, phi, X, Y, Z, faithful=0):
