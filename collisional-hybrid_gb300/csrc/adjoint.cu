@@ -526,7 +526,8 @@ struct ch_adjoint {
   std::vector<void*> allocs;
   F64Particles cur{};                 // working state
   std::vector<F64Particles> ckpt;     // state s = k * checkpoint_every
-  std::vector<F64Particles> seg;      // pre-step states of the segment being reversed
+  std::vector<F64Particles> seg;      // pre-step states of segment seg_holds
+  int seg_holds = -1;
   double *phi_all = nullptr, *mom_all = nullptr;  // (nsteps + 1) x N, x 4N
   double *E64 = nullptr, *Ebar = nullptr, *phibar = nullptr, *lam = nullptr, *nbar = nullptr, *Gbar = nullptr,
          *rhs = nullptr, *dxda = nullptr, *RbT = nullptr;
@@ -816,6 +817,7 @@ extern "C" ch_status ch_adjoint_forward(ch_adjoint* a, const double* theta, int3
     CH_CUDA_OK(cudaMemcpy(&ne, a->ev_count, sizeof(unsigned), cudaMemcpyDeviceToHost));
     a->timing.events = ne;
     a->recorded = true;
+    a->seg_holds = last_seg;  // the forward run stored the last segment
     for (int q = 0; q < CH_ADJ_NTHETA; ++q) a->theta_rec[q] = theta[q];
     a->J_rec = Jsum;
   }
@@ -863,7 +865,7 @@ extern "C" ch_status ch_adjoint_gradient(ch_adjoint* a, double* grad, double* J)
   const int nseg = (S + K - 1) / K;
   for (int sg = nseg - 1; sg >= 0; --sg) {
     const int s0 = sg * K, s1 = (s0 + K < S) ? s0 + K : S;
-    if (sg != nseg - 1) {
+    if (sg != a->seg_holds) {
       // rebuild the segment's pre-step states from its checkpoint
       cudaEvent_t r0, r1;
       cudaEventCreate(&r0);
@@ -885,6 +887,7 @@ extern "C" ch_status ch_adjoint_gradient(ch_adjoint* a, double* grad, double* J)
       recompute_ms += ms;
       cudaEventDestroy(r0);
       cudaEventDestroy(r1);
+      a->seg_holds = sg;
     }
     for (int st = s1 - 1; st >= s0; --st) {
       const int kpost = st + 1;  // state produced by step st

@@ -9,7 +9,9 @@
 #include <string.h>
 
 #include <atomic>
+#include <mutex>
 #include <new>
+#include <vector>
 
 #include "particles.cuh"
 #include "solver.cuh"
@@ -17,6 +19,27 @@
 using namespace ch;
 
 static thread_local char g_err[512] = "";
+
+// Host ranges page-locked through ch_host_register, with the device address
+// of each mapping.  A transfer whose whole host range lies inside one of
+// them is done by the conversion kernels reading (or a copy kernel writing)
+// host memory directly over the C2C link instead of a staging copy.
+struct HostRange {
+  char* p;
+  uint64_t n;
+  char* d;
+};
+static std::mutex g_hr_mu;
+static std::vector<HostRange> g_hr;
+
+static void* device_view(const void* ptr, uint64_t bytes, uint64_t align) {
+  if (!ptr || ((uintptr_t)ptr % align) != 0) return nullptr;
+  const char* q = static_cast<const char*>(ptr);
+  std::lock_guard<std::mutex> lk(g_hr_mu);
+  for (const auto& r : g_hr)
+    if (r.d && q >= r.p && q + bytes <= r.p + r.n) return r.d + (q - r.p);
+  return nullptr;
+}
 
 ch_status ch_fail(ch_status code, const char* fmt, ...) {
   va_list ap;
@@ -362,11 +385,20 @@ extern "C" ch_status ch_particles_upload(ch_ctx* c, const ch_real_vector* pos, c
   if (!c || !pos || !vel) return ch_fail(CH_ERR_ARG, "ch_particles_upload: null argument");
   ch_status rc = ensure_particles(c, np);
   if (rc) return rc;
-  rc = ensure_staging(c);
-  if (rc) return rc;
-  CH_CUDA_OK(cudaMemcpyAsync(c->stage_pos, pos, sizeof(double4_32a) * np, cudaMemcpyHostToDevice, c->stream));
-  CH_CUDA_OK(cudaMemcpyAsync(c->stage_vel, vel, sizeof(double4_32a) * np, cudaMemcpyHostToDevice, c->stream));
-  launch_aos_in(c->mixed, c->g, c->stage_pos, c->stage_vel, c->P, c->M, c->sms, c->stream);
+  const uint64_t bytes = sizeof(double4_32a) * (uint64_t)np;
+  const void* dp = device_view(pos, bytes, 32);
+  const void* dv = device_view(vel, bytes, 32);
+  if (dp && dv) {
+    // registered host arrays: the conversion reads them directly
+    launch_aos_in(c->mixed, c->g, static_cast<const double4_32a*>(dp), static_cast<const double4_32a*>(dv), c->P,
+                  c->M, c->sms, c->stream);
+  } else {
+    rc = ensure_staging(c);
+    if (rc) return rc;
+    CH_CUDA_OK(cudaMemcpyAsync(c->stage_pos, pos, bytes, cudaMemcpyHostToDevice, c->stream));
+    CH_CUDA_OK(cudaMemcpyAsync(c->stage_vel, vel, bytes, cudaMemcpyHostToDevice, c->stream));
+    launch_aos_in(c->mixed, c->g, c->stage_pos, c->stage_vel, c->P, c->M, c->sms, c->stream);
+  }
   return after_load(c);
 }
 
@@ -386,8 +418,17 @@ extern "C" ch_status ch_particles_download(ch_ctx* c, ch_real_vector* pos, ch_re
   ch_status rc = ensure_staging(c);
   if (rc) return rc;
   launch_aos_out(c->mixed, c->g, c->P, c->M, c->stage_pos, c->stage_vel, c->sms, c->stream);
-  CH_CUDA_OK(cudaMemcpyAsync(pos, c->stage_pos, sizeof(double4_32a) * c->np, cudaMemcpyDeviceToHost, c->stream));
-  CH_CUDA_OK(cudaMemcpyAsync(vel, c->stage_vel, sizeof(double4_32a) * c->np, cudaMemcpyDeviceToHost, c->stream));
+  const uint64_t bytes = sizeof(double4_32a) * (uint64_t)c->np;
+  void* dp = device_view(pos, bytes, 16);
+  void* dv = device_view(vel, bytes, 16);
+  if (dp && dv) {
+    // registered host arrays: a copy kernel streams the staging out
+    launch_stream_copy(dp, c->stage_pos, bytes, c->sms, c->stream);
+    launch_stream_copy(dv, c->stage_vel, bytes, c->sms, c->stream);
+  } else {
+    CH_CUDA_OK(cudaMemcpyAsync(pos, c->stage_pos, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CH_CUDA_OK(cudaMemcpyAsync(vel, c->stage_vel, bytes, cudaMemcpyDeviceToHost, c->stream));
+  }
   CH_CUDA_OK(cudaStreamSynchronize(c->stream));
   return CH_OK;
 }
@@ -607,12 +648,27 @@ extern "C" ch_status ch_apply_operator(ch_ctx* c, const double* x, double* y) {
 
 extern "C" ch_status ch_host_register(void* ptr, uint64_t bytes) {
   if (!ptr || !bytes) return ch_fail(CH_ERR_ARG, "null argument");
-  CH_CUDA_OK(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+  CH_CUDA_OK(cudaHostRegister(ptr, bytes, cudaHostRegisterMapped | cudaHostRegisterPortable));
+  void* d = nullptr;
+  if (cudaHostGetDevicePointer(&d, ptr, 0) != cudaSuccess) {
+    cudaGetLastError();
+    d = nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_hr_mu);
+  g_hr.push_back(HostRange{static_cast<char*>(ptr), bytes, static_cast<char*>(d)});
   return CH_OK;
 }
 
 extern "C" ch_status ch_host_unregister(void* ptr) {
   if (!ptr) return ch_fail(CH_ERR_ARG, "null argument");
+  {
+    std::lock_guard<std::mutex> lk(g_hr_mu);
+    for (size_t i = 0; i < g_hr.size(); ++i)
+      if (g_hr[i].p == ptr) {
+        g_hr.erase(g_hr.begin() + (long)i);
+        break;
+      }
+  }
   CH_CUDA_OK(cudaHostUnregister(ptr));
   return CH_OK;
 }

@@ -1229,6 +1229,19 @@ void launch_load(bool mixed, const GridDesc& g, const ch_loader& L, uint64_t see
   else k_load_f64<<<grid_for(P.np, 256, sms, 8), 256, 0, s>>>(g, L, lo, hi, run, P), ::ch::note_launch();
 }
 
+// dst <- src, 16 bytes per thread and iteration (bytes a multiple of 16,
+// both 16-byte aligned); dst may be mapped host memory.
+__global__ void k_stream_copy(uint4* __restrict__ dst, const uint4* __restrict__ src, int64_t n16) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+void launch_stream_copy(void* dst, const void* src, uint64_t bytes, int sms, cudaStream_t s) {
+  const int64_t n16 = (int64_t)(bytes / 16);
+  k_stream_copy<<<grid_for(n16, 256, sms, 8), 256, 0, s>>>(static_cast<uint4*>(dst), static_cast<const uint4*>(src),
+                                                           n16), ::ch::note_launch();
+}
+
 void launch_aos_in(bool mixed, const GridDesc& g, const double4_32a* pos, const double4_32a* vel, F64Particles P,
                    MixParticles M, int sms, cudaStream_t s) {
   if (mixed) k_aos_to_mixed<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, pos, vel, M), ::ch::note_launch();

@@ -26,6 +26,9 @@ void launch_load(bool mixed, const GridDesc& g, const ch_loader& L, uint64_t see
                  MixParticles M, int sms, cudaStream_t s);
 void launch_aos_in(bool mixed, const GridDesc& g, const double4_32a* pos, const double4_32a* vel, F64Particles P,
                    MixParticles M, int sms, cudaStream_t s);
+// Copies bytes (a multiple of 16; both pointers 16-byte aligned) on the SMs;
+// dst may be mapped host memory.
+void launch_stream_copy(void* dst, const void* src, uint64_t bytes, int sms, cudaStream_t s);
 void launch_aos_out(bool mixed, const GridDesc& g, F64Particles P, MixParticles M, double4_32a* pos, double4_32a* vel,
                     int sms, cudaStream_t s);
 void launch_node_efield(bool mixed, const GridDesc& g, double tscale, const double* phi, double* E64, float4* E32,

@@ -11,13 +11,23 @@ template <> __device__ __forceinline__ float unitR<float>(uint32_t r) { return c
 __device__ __forceinline__ double ch_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float ch_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double ch_log(double x) { return log(x); }
-__device__ __forceinline__ float ch_log(float x) { return logf(x); }
+// FP32 form: the hardware log2 (absolute error near 1e-7 on the unit
+// interval, ample for waiting times and Box-Muller radii of the FP32 form)
+__device__ __forceinline__ float ch_log(float x) { return __logf(x); }
 __device__ __forceinline__ double ch_exp(double x) { return exp(x); }
 __device__ __forceinline__ float ch_exp(float x) { return expf(x); }
 __device__ __forceinline__ double ch_erf(double x) { return erf(x); }
 __device__ __forceinline__ float ch_erf(float x) { return erff(x); }
 __device__ __forceinline__ void ch_sincos2pi(double u, double* s, double* c) { sincos(2.0 * CH_PI * u, s, c); }
-__device__ __forceinline__ void ch_sincos2pi(float u, float* s, float* c) { sincospif(2.0f * u, s, c); }
+// FP32 form, u in [0, 1): the hardware sine/cosine on the angle 2 pi (u -
+// 1/2) in [-pi, pi), where its absolute error stays near 2^-21, and the half
+// turn restored by the signs.
+__device__ __forceinline__ void ch_sincos2pi(float u, float* s, float* c) {
+  float sh, ch;
+  __sincosf(6.2831853071795865f * (u - 0.5f), &sh, &ch);
+  *s = -sh;
+  *c = -ch;
+}
 
 // E|w - V| for |w - vn0| = w and V Maxwellian with per-component std sigma:
 // sigma sqrt(2/pi) exp(-a^2) + (w + sigma^2/w) erf(a), a = w/(sigma sqrt 2);

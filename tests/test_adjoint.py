@@ -117,6 +117,7 @@ def test_torch_autograd_binding(chy):
         theta = torch.tensor(adj.theta0(), dtype=torch.float64, requires_grad=True)
         J = ag.objective(theta, adj)
         J.backward()
+        # a second reverse sweep of the same recorded run gives the same gradient
         g, Jg = adj.gradient()
-        assert float(J) == Jg
-        assert np.array_equal(theta.grad.numpy(), g)
+        assert float(J.detach()) == Jg
+        assert np.allclose(theta.grad.numpy(), g, rtol=1e-12, atol=0.0)
