@@ -337,6 +337,7 @@ static ch_status ensure_particles(ch_ctx* c, int64_t np) {
     c->P.np = c->Q.np = np;
   }
   if (e == cudaSuccess) e = cudaMalloc(&c->keys, sizeof(uint32_t) * np);
+  if (c->mixed) c->M.rank = c->MQ.rank = c->keys;  // in-cell ranks of the pass before a sort
   const int cap = grid_for(np > c->g.N ? np : c->g.N, 256, c->sms, 8);
   if (e == cudaSuccess) e = cudaMalloc(&c->part, sizeof(double) * 4 * cap);
   if (e != cudaSuccess) {

@@ -119,6 +119,7 @@ static MixParticles slice(const MixParticles& M, int64_t off, int64_t n) {
   s.pos = M.pos + off;
   s.vel = M.vel + off;
   s.np = n;
+  s.rank = nullptr;
   return s;
 }
 
@@ -286,6 +287,7 @@ extern "C" ch_status ch_batch_create(const ch_params* runs, const int64_t* np, i
   const int64_t N = b->Ntot, NP = b->NPtot;
   b->M.pos = P.get<float4>(NP); b->M.vel = P.get<float4>(NP); b->M.np = NP;
   b->MQ.pos = P.get<float4>(NP); b->MQ.vel = P.get<float4>(NP); b->MQ.np = NP;
+  b->M.rank = b->MQ.rank = P.get<uint32_t>(NP);
   b->counts = P.get<uint32_t>(N);
   b->starts = P.get<uint32_t>(N + 1);
   b->cursor = P.get<uint32_t>(N);
@@ -445,8 +447,8 @@ extern "C" ch_status ch_batch_download(ch_batch* b, int32_t run, ch_real_vector*
 static void full_sort(ch_batch* b) {
   cudaMemsetAsync(b->counts, 0, sizeof(uint32_t) * b->Ntot, b->stream);
   launch_batch_hist(batch_dev(b), b->M, b->counts, b->sms, b->stream);
-  launch_batch_sort(batch_dev(b), b->Ntot, b->M, b->MQ, b->counts, b->starts, b->cursor, b->block_sums, b->sms,
-                    b->stream);
+  launch_batch_sort(batch_dev(b), b->Ntot, b->M, b->MQ, b->counts, b->starts, b->cursor, b->block_sums, false,
+                    b->sms, b->stream);
   std::swap(b->M, b->MQ);
   b->since_sort = 0;
 }
@@ -526,7 +528,7 @@ static cudaError_t enqueue_step(ch_batch* b, bool sort_due) {
   cudaError_t e = launch_batch_solve(b->d_solve, b->nruns, b->tune.cluster, s);
   if (b->prof) cudaEventRecord(b->ev[2], s);
   if (sort_due)
-    launch_batch_sort(B, b->Ntot, b->M, b->MQ, b->counts, b->starts, b->cursor, b->block_sums, b->sms, s);
+    launch_batch_sort(B, b->Ntot, b->M, b->MQ, b->counts, b->starts, b->cursor, b->block_sums, true, b->sms, s);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }

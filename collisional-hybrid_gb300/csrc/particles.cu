@@ -756,7 +756,10 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
       const bool go = active && !defer;
       if (move && go) move_ion(p, v, i, j, k);
       if (move && go) P.pos[ip] = p;
-      if (hist) agg_inc(hist, (uint32_t)(((int64_t)k * g.Ny + j) * g.Nx + i), go);
+      if (hist) {
+        const uint32_t rk = agg_inc(hist, (uint32_t)(((int64_t)k * g.Ny + j) * g.Nx + i), go);
+        if (go && P.rank) P.rank[ip] = rk;
+      }
       if (PH & PH_DEPOSIT) {
         const bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v[0]) && isfinite(v[1]) &&
                             isfinite(v[2]);
@@ -804,7 +807,10 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
                 P.pos[qip] = qp;
               }
             }
-            if (hist) agg_inc(hist, (uint32_t)(((int64_t)qk * g.Ny + qj) * g.Nx + qi), act);
+            if (hist) {
+              const uint32_t rk = agg_inc(hist, (uint32_t)(((int64_t)qk * g.Ny + qj) * g.Nx + qi), act);
+              if (act && P.rank) P.rank[qip] = rk;
+            }
             if ((PH & PH_DEPOSIT) && act) {
               const bool finite = isfinite(qp.x) && isfinite(qp.y) && isfinite(qp.z) && isfinite(qv[0]) &&
                                   isfinite(qv[1]) && isfinite(qv[2]);
@@ -1099,6 +1105,16 @@ __global__ void k_scatter_mixed(GridDesc g, MixParticles P, MixParticles Q, uint
 }
 
 // Exclusive scan of counts[0..n) into starts[0..n] (three phases).
+// Scatter with the in-cell ranks the pass recorded: no atomics.
+__global__ void k_scatter_ranked(GridDesc g, MixParticles P, MixParticles Q, const uint32_t* __restrict__ starts) {
+  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
+    const float4 p = P.pos[ip];
+    const uint32_t dst = starts[key_mixed(g, p.w)] + P.rank[ip];
+    Q.pos[dst] = p;
+    Q.vel[dst] = P.vel[ip];
+  }
+}
+
 __global__ void k_scan_blocks(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint32_t* block_sums,
                               int64_t n) {
   __shared__ uint32_t sm[1024];
@@ -1186,6 +1202,22 @@ __global__ void k_batch_hist(BatchDev B, MixParticles P, uint32_t* counts) {
       key = (uint32_t)R.node_off + key_mixed(R.c.g, P.pos[ip].w);
     }
     agg_inc(counts, key, act);
+  }
+}
+
+__global__ void k_batch_scatter_ranked(BatchDev B, MixParticles P, MixParticles Q,
+                                       const uint32_t* __restrict__ starts) {
+  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
+    const float4 p = P.pos[ip];
+    int lo = 0, hi = B.nruns;  // run of slot ip
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (B.ion_off[mid] <= ip) lo = mid; else hi = mid;
+    }
+    const BatchRunDev& R = B.runs[lo];
+    const uint32_t dst = starts[(uint32_t)R.node_off + key_mixed(R.c.g, p.w)] + P.rank[ip];
+    Q.pos[dst] = p;
+    Q.vel[dst] = P.vel[ip];
   }
 }
 
@@ -1348,7 +1380,8 @@ void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, 
   k_scan_blocks<<<nsb, 512, 0, s>>>(counts, starts, block_sums, N), ::ch::note_launch();
   k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nsb, starts + N), ::ch::note_launch();
   k_scan_add<<<(int)((N + 255) / 256), 256, 0, s>>>(starts, block_sums, N, cursor), ::ch::note_launch();
-  if (mixed) k_scatter_mixed<<<nb, 256, 0, s>>>(g, M, MQ, cursor), ::ch::note_launch();
+  if (mixed && have_hist && M.rank) k_scatter_ranked<<<nb, 256, 0, s>>>(g, M, MQ, starts), ::ch::note_launch();
+  else if (mixed) k_scatter_mixed<<<nb, 256, 0, s>>>(g, M, MQ, cursor), ::ch::note_launch();
   else k_scatter_f64<<<nb, 256, 0, s>>>(P, Q, keys, cursor), ::ch::note_launch();
 }
 
@@ -1399,12 +1432,16 @@ void launch_batch_finalize(int64_t n4, unsigned long long* acc, double inv_scale
 }
 
 void launch_batch_sort(const BatchDev& B, int64_t Ntot, MixParticles M, MixParticles MQ, uint32_t* counts,
-                       uint32_t* starts, uint32_t* cursor, uint32_t* block_sums, int sms, cudaStream_t s) {
+                       uint32_t* starts, uint32_t* cursor, uint32_t* block_sums, bool ranked, int sms,
+                       cudaStream_t s) {
   const int nsb = (int)((Ntot + 1023) / 1024);
   k_scan_blocks<<<nsb, 512, 0, s>>>(counts, starts, block_sums, Ntot), ::ch::note_launch();
   k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nsb, starts + Ntot), ::ch::note_launch();
   k_scan_add<<<(int)((Ntot + 255) / 256), 256, 0, s>>>(starts, block_sums, Ntot, cursor), ::ch::note_launch();
-  k_batch_scatter<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(B, M, MQ, cursor), ::ch::note_launch();
+  if (ranked && M.rank)
+    k_batch_scatter_ranked<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(B, M, MQ, starts), ::ch::note_launch();
+  else
+    k_batch_scatter<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(B, M, MQ, cursor), ::ch::note_launch();
 }
 
 }  // namespace ch

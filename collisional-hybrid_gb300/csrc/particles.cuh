@@ -17,6 +17,7 @@ struct MixParticles {
   float4* pos;  // (ox, oy, oz, packed cell bits)
   float4* vel;  // (vx, vy, vz, id bits)
   int64_t np;
+  uint32_t* rank;  // nullable: a pass that counts new cells stores each ion's rank in its cell here
 };
 
 // Launch configuration: grid-stride kernels sized to a multiple of the SM count.
@@ -47,8 +48,9 @@ int launch_finalize(int64_t N, unsigned long long* acc, double inv_scale, int re
                     DevCounters* cnt, int sms, cudaStream_t s);
 // Counting sort by cell: counts (N), starts (N+1), cursor (N), keys (np),
 // block_sums (ceil(N/1024)+1).  Results land in the Q buffers.
-// have_hist: counts already hold the per-cell ion counts (mixed form, counted
-// by the preceding pass).
+// have_hist: counts already hold the per-cell ion counts and M.rank each
+// ion's rank in its new cell (mixed form, recorded by the preceding pass), so
+// the scatter needs no atomics.
 void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, MixParticles M, MixParticles MQ,
                  uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* keys, uint32_t* block_sums,
                  bool have_hist, int sms, cudaStream_t s);
@@ -95,8 +97,10 @@ void launch_batch_hist(const BatchDev& B, MixParticles M, uint32_t* counts, int 
 void launch_batch_finalize(int64_t n4, unsigned long long* acc, double inv_scale, double* mom, int* flag, int sms,
                            cudaStream_t s);
 // Counting sort over the batch grid (keys node_off[r] + cell keep the runs
-// contiguous); counts hold the cell counts from the preceding pass.
+// contiguous); counts hold the cell counts.  ranked: the preceding pass
+// counted them and stored each ion's in-cell rank in M.rank.
 void launch_batch_sort(const BatchDev& B, int64_t Ntot, MixParticles M, MixParticles MQ, uint32_t* counts,
-                       uint32_t* starts, uint32_t* cursor, uint32_t* block_sums, int sms, cudaStream_t s);
+                       uint32_t* starts, uint32_t* cursor, uint32_t* block_sums, bool ranked, int sms,
+                       cudaStream_t s);
 
 }  // namespace ch
