@@ -166,6 +166,9 @@ def lib():
             "ch_get_profile": [vp, C.POINTER(Profile)],
             "ch_reset_profile": [vp],
             "ch_get_stream": [vp, C.POINTER(vp)],
+            "ch_output_open": [vp, C.c_char_p],
+            "ch_output": [vp, C.c_char_p],
+            "ch_output_wait": [vp, C.POINTER(C.c_int64)],
             "ch_host_register": [vp, C.c_uint64],
             "ch_host_unregister": [vp],
             "ch_batch_create": [vp, vp, C.c_int32, C.c_int32, C.POINTER(vp)],
@@ -361,6 +364,20 @@ class Hybrid:
         _check(lib().ch_apply_operator(self._h, x.ctypes.data, y.ctypes.data))
         return y
 
+    # ---------------------------------------------------------------- output (OutputHDF5)
+    def output_open(self, stem: str):
+        _check(lib().ch_output_open(self._h, stem.encode()))
+
+    def output(self, insert: str):
+        """Queues the current fields for writing as <stem><insert>.*; returns
+        at once (the copy and the writes overlap the next steps)."""
+        _check(lib().ch_output(self._h, insert.encode()))
+
+    def output_wait(self) -> int:
+        n = C.c_int64()
+        _check(lib().ch_output_wait(self._h, C.byref(n)))
+        return n.value
+
     # ---------------------------------------------------------------- profiling
     def set_profiling(self, on: bool = True):
         _check(lib().ch_set_profiling(self._h, int(on)))
@@ -550,6 +567,19 @@ class Adjoint:
         t = AdjointTiming()
         _check(lib().ch_adjoint_get_timing(self._h, C.byref(t)))
         return t.as_dict()
+
+
+def read_output(path: str) -> dict:
+    """Reads one output written by Hybrid.output: path = <stem><insert>
+    (without extension); returns {dataset name: (Nz, Ny, Nx) array}."""
+    import json
+
+    with open(path + ".json") as f:
+        man = json.load(f)
+    g = man["grid"]
+    d = os.path.dirname(path)
+    return {name: np.fromfile(os.path.join(d, fn), dtype="<f8").reshape(g["Nz"], g["Ny"], g["Nx"])
+            for name, fn in man["datasets"].items()}
 
 
 def host_register(a: np.ndarray):

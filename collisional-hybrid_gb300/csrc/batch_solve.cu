@@ -27,7 +27,7 @@ namespace ch {
 namespace {
 
 constexpr float B_OMEGA = 0.8f;      // damped-Jacobi weight of the smoother
-constexpr int B_COARSE_SWEEPS = 64;  // Jacobi sweeps of the coarsest level
+constexpr int B_COARSE_SWEEPS_MAX = 64;  // Jacobi sweeps of the coarsest level: 4 per node of its longest edge
 constexpr double B_INNER_RTOL = 1e-4;
 constexpr int B_MAX_REFINE = 50;
 constexpr int B_MAX_INNER = 200;     // inner iterations per refinement (rtol 1e-4 takes ~10)
@@ -219,7 +219,9 @@ __global__ void __launch_bounds__(256) k_batch_solve(const BSolveRun* runs) {
       float* xb = sh.xb;
       for (int c = threadIdx.x; c < Nc; c += blockDim.x) xa[c] = w * V.dinv[c] * b[c];
       __syncthreads();
-      for (int sw = 1; sw < B_COARSE_SWEEPS; ++sw) {
+      const int emax = max(V.g.Nx, max(V.g.Ny, V.g.Nz));
+      const int sweeps = min(B_COARSE_SWEEPS_MAX, max(16, 4 * emax));
+      for (int sw = 1; sw < sweeps; ++sw) {
         for (int c = threadIdx.x; c < Nc; c += blockDim.x)
           xb[c] = xa[c] + w * V.dinv[c] * (b[c] - apply_row<float>(V.C, V.n, xa, neighbours(V.g, c)));
         __syncthreads();

@@ -9,8 +9,12 @@
 #include <string.h>
 
 #include <atomic>
+#include <condition_variable>
+#include <deque>
 #include <mutex>
 #include <new>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "particles.cuh"
@@ -59,7 +63,10 @@ void ch::note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void ch::note_launch_n(long long n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 unsigned long long ch::launches_now() { return g_launches.load(); }
 
+struct ChOutput;
+
 struct ch_ctx {
+  ChOutput* out = nullptr;  // asynchronous output (ch_output_*), created on demand
   ch_params p;
   GridDesc g;
   int device = 0;
@@ -199,9 +206,12 @@ static void free_particles(ch_ctx* c) {
   c->np = 0;
 }
 
+static void output_close(ch_ctx* c);
+
 extern "C" ch_status ch_destroy(ch_ctx* c) {
   if (!c) return CH_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  output_close(c);
   free_particles(c);
   void* v[] = {c->counts, c->starts, c->cursor, c->block_sums, c->phi, c->E64, c->mom, c->rhs, c->nfz,
                c->E32, c->acc, c->cnt, c->red};
@@ -387,12 +397,11 @@ extern "C" ch_status ch_particles_upload(ch_ctx* c, const ch_real_vector* pos, c
   ch_status rc = ensure_particles(c, np);
   if (rc) return rc;
   const uint64_t bytes = sizeof(double4_32a) * (uint64_t)np;
-  const void* dp = device_view(pos, bytes, 32);
-  const void* dv = device_view(vel, bytes, 32);
+  const void* dp = device_view(pos, bytes, 16);
+  const void* dv = device_view(vel, bytes, 16);
   if (dp && dv) {
     // registered host arrays: the conversion reads them directly
-    launch_aos_in(c->mixed, c->g, static_cast<const double4_32a*>(dp), static_cast<const double4_32a*>(dv), c->P,
-                  c->M, c->sms, c->stream);
+    launch_aos_in_u16(c->mixed, c->g, dp, dv, c->P, c->M, c->sms, c->stream);
   } else {
     rc = ensure_staging(c);
     if (rc) return rc;
@@ -585,7 +594,13 @@ extern "C" ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_s
   for (int32_t s = 0; s < nsteps; ++s) {
     memset(&local, 0, sizeof(local));
     const bool sort_due = c->p.sort_period > 0 && c->since_sort + 1 >= c->p.sort_period;
-    ch_status rc = run_pass(c, PH_PUSH | PH_MOVE | PH_DEPOSIT, first_step + s, &local, sort_due);
+    // Two launches: push + collide + move (with the new-cell histogram when
+    // a sort is due) at 4 CTAs per SM in a small shared footprint, then the
+    // deposit.  The pair is faster than one fused launch, whose shared
+    // memory and registers allow only 2 CTAs per SM; the results are the
+    // same bit for bit.
+    ch_status rc = run_pass(c, PH_PUSH | PH_MOVE, first_step + s, &local, sort_due);
+    if (!rc) rc = run_pass(c, PH_DEPOSIT, 0, nullptr);
     if (rc) return rc;
     rc = finalize_moments(c, &local);
     if (rc) return rc;
@@ -700,5 +715,195 @@ extern "C" ch_status ch_reset_profile(ch_ctx* c) {
 extern "C" ch_status ch_get_stream(ch_ctx* c, void** stream) {
   if (!c || !stream) return ch_fail(CH_ERR_ARG, "null argument");
   *stream = (void*)c->stream;
+  return CH_OK;
+}
+
+// ------------------------------------------------------------------ output
+// OutputHDF5 (src/fileio.c:73-126) without HDF5: the fields of one step --
+// density, x/y/z flux, rhs, potential, in the reference's dataset names --
+// are snapshot on the device, copied to pinned host memory on a second
+// stream while the next step runs, and written by a host thread as raw
+// little-endian FP64 files (DMDA natural order) with a JSON manifest.
+namespace {
+constexpr int OUT_SLOTS = 2;
+constexpr int OUT_FIELDS = 6;
+const char* const OUT_NAMES[OUT_FIELDS] = {"density", "x flux", "y flux", "z flux", "rhs", "potential"};
+const char* const OUT_FILES[OUT_FIELDS] = {"density", "x_flux", "y_flux", "z_flux", "rhs", "potential"};
+}  // namespace
+
+struct ChOutput {
+  std::string stem;
+  int device = 0;
+  GridDesc g{};
+  ch_params p{};
+  cudaStream_t stream = nullptr;
+  double* dev[OUT_SLOTS] = {nullptr, nullptr};
+  double* host[OUT_SLOTS] = {nullptr, nullptr};
+  cudaEvent_t snap[OUT_SLOTS] = {nullptr, nullptr};
+  cudaEvent_t ready[OUT_SLOTS] = {nullptr, nullptr};
+  bool busy[OUT_SLOTS] = {false, false};
+  int next = 0;
+  std::thread writer;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<std::pair<int, std::string>> jobs;
+  bool stop = false;
+  std::string error;
+  int64_t written = 0;
+};
+
+static void output_write(ChOutput* o, int slot, const std::string& insert) {
+  const int64_t N = o->g.N;
+  const std::string base = o->stem + insert;
+  std::string err;
+  for (int f = 0; f < OUT_FIELDS && err.empty(); ++f) {
+    const std::string name = base + "." + OUT_FILES[f] + ".f64";
+    FILE* fp = fopen(name.c_str(), "wb");
+    if (!fp) { err = "cannot open " + name; break; }
+    if (fwrite(o->host[slot] + (size_t)f * N, sizeof(double), (size_t)N, fp) != (size_t)N) err = "short write " + name;
+    if (fclose(fp) != 0 && err.empty()) err = "close " + name;
+  }
+  if (err.empty()) {
+    const std::string name = base + ".json";
+    FILE* fp = fopen(name.c_str(), "w");
+    if (!fp) {
+      err = "cannot open " + name;
+    } else {
+      fprintf(fp, "{\n  \"format\": \"raw little-endian float64, DMDA natural order (x fastest)\",\n");
+      fprintf(fp, "  \"grid\": {\"Nx\": %d, \"Ny\": %d, \"Nz\": %d, \"x0\": %.17g, \"x1\": %.17g, "
+                  "\"y0\": %.17g, \"y1\": %.17g, \"z0\": %.17g, \"z1\": %.17g},\n",
+              o->g.Nx, o->g.Ny, o->g.Nz, o->p.x0, o->p.x1, o->p.y0, o->p.y1, o->p.z0, o->p.z1);
+      fprintf(fp, "  \"datasets\": {");
+      for (int f = 0; f < OUT_FIELDS; ++f) {
+        const std::string file = base + "." + OUT_FILES[f] + ".f64";
+        const size_t cut = file.find_last_of('/');
+        fprintf(fp, "%s\n    \"%s\": \"%s\"", f ? "," : "", OUT_NAMES[f],
+                (cut == std::string::npos ? file : file.substr(cut + 1)).c_str());
+      }
+      fprintf(fp, "\n  }\n}\n");
+      if (fclose(fp) != 0) err = "close " + name;
+    }
+  }
+  std::lock_guard<std::mutex> lk(o->mu);
+  if (!err.empty() && o->error.empty()) o->error = err;
+  if (err.empty()) o->written++;
+}
+
+static void output_thread(ChOutput* o) {
+  cudaSetDevice(o->device);
+  for (;;) {
+    std::pair<int, std::string> job;
+    {
+      std::unique_lock<std::mutex> lk(o->mu);
+      o->cv.wait(lk, [&] { return o->stop || !o->jobs.empty(); });
+      if (o->jobs.empty()) return;
+      job = o->jobs.front();
+      o->jobs.pop_front();
+    }
+    const cudaError_t e = cudaEventSynchronize(o->ready[job.first]);
+    if (e != cudaSuccess) {
+      std::lock_guard<std::mutex> lk(o->mu);
+      if (o->error.empty()) o->error = std::string("output copy: ") + cudaGetErrorString(e);
+    } else {
+      output_write(o, job.first, job.second);
+    }
+    {
+      std::lock_guard<std::mutex> lk(o->mu);
+      o->busy[job.first] = false;
+    }
+    o->cv.notify_all();
+  }
+}
+
+static void output_close(ch_ctx* c) {
+  ChOutput* o = c->out;
+  if (!o) return;
+  {
+    std::lock_guard<std::mutex> lk(o->mu);
+    o->stop = true;
+  }
+  o->cv.notify_all();
+  if (o->writer.joinable()) o->writer.join();
+  for (int k = 0; k < OUT_SLOTS; ++k) {
+    if (o->dev[k]) cudaFree(o->dev[k]);
+    if (o->host[k]) cudaFreeHost(o->host[k]);
+    if (o->snap[k]) cudaEventDestroy(o->snap[k]);
+    if (o->ready[k]) cudaEventDestroy(o->ready[k]);
+  }
+  if (o->stream) cudaStreamDestroy(o->stream);
+  delete o;
+  c->out = nullptr;
+}
+
+extern "C" ch_status ch_output_open(ch_ctx* c, const char* stem) {
+  if (!c || !stem) return ch_fail(CH_ERR_ARG, "null argument");
+  output_close(c);
+  ChOutput* o = new (std::nothrow) ChOutput();
+  if (!o) return ch_fail(CH_ERR_NOMEM, "host allocation");
+  o->stem = stem;
+  o->device = c->device;
+  o->g = c->g;
+  o->p = c->p;
+  c->out = o;
+  const size_t b = sizeof(double) * OUT_FIELDS * (size_t)c->g.N;
+  cudaError_t e = cudaStreamCreateWithFlags(&o->stream, cudaStreamNonBlocking);
+  for (int k = 0; k < OUT_SLOTS && e == cudaSuccess; ++k) {
+    e = cudaMalloc(&o->dev[k], b);
+    if (e == cudaSuccess) e = cudaMallocHost(&o->host[k], b);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&o->snap[k], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&o->ready[k], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) {
+    output_close(c);
+    return ch_cuda_fail(e, "ch_output_open", __FILE__, __LINE__);
+  }
+  o->writer = std::thread(output_thread, o);
+  return CH_OK;
+}
+
+extern "C" ch_status ch_output(ch_ctx* c, const char* insert) {
+  if (!c || !insert) return ch_fail(CH_ERR_ARG, "null argument");
+  ChOutput* o = c->out;
+  if (!o) return ch_fail(CH_ERR_STATE, "ch_output_open first");
+  if (!c->moments_valid || !c->solved_once) return ch_fail(CH_ERR_STATE, "no moments or potential to output");
+  const int k = o->next;
+  o->next = (o->next + 1) % OUT_SLOTS;
+  {
+    std::unique_lock<std::mutex> lk(o->mu);
+    o->cv.wait(lk, [&] { return !o->busy[k]; });  // the slot's previous write is done
+    if (!o->error.empty()) return ch_fail(CH_ERR_CUDA, "output: %s", o->error.c_str());
+    o->busy[k] = true;
+  }
+  const int64_t N = c->g.N;
+  // snapshot on the compute stream (the next step overwrites the fields) ...
+  CH_CUDA_OK(cudaMemcpyAsync(o->dev[k], c->mom, sizeof(double) * 4 * N, cudaMemcpyDeviceToDevice, c->stream));
+  CH_CUDA_OK(cudaMemcpyAsync(o->dev[k] + 4 * N, c->rhs, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+  CH_CUDA_OK(cudaMemcpyAsync(o->dev[k] + 5 * N, c->phi, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+  CH_CUDA_OK(cudaEventRecord(o->snap[k], c->stream));
+  // ... and the copy to the host on the output stream, beside the next step
+  CH_CUDA_OK(cudaStreamWaitEvent(o->stream, o->snap[k], 0));
+  CH_CUDA_OK(cudaMemcpyAsync(o->host[k], o->dev[k], sizeof(double) * OUT_FIELDS * N, cudaMemcpyDeviceToHost,
+                             o->stream));
+  CH_CUDA_OK(cudaEventRecord(o->ready[k], o->stream));
+  {
+    std::lock_guard<std::mutex> lk(o->mu);
+    o->jobs.emplace_back(k, std::string(insert));
+  }
+  o->cv.notify_all();
+  return CH_OK;
+}
+
+extern "C" ch_status ch_output_wait(ch_ctx* c, int64_t* written) {
+  if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
+  ChOutput* o = c->out;
+  if (!o) return ch_fail(CH_ERR_STATE, "ch_output_open first");
+  std::unique_lock<std::mutex> lk(o->mu);
+  o->cv.wait(lk, [&] {
+    bool idle = o->jobs.empty();
+    for (int k = 0; k < OUT_SLOTS; ++k) idle = idle && !o->busy[k];
+    return idle;
+  });
+  if (written) *written = o->written;
+  if (!o->error.empty()) return ch_fail(CH_ERR_CUDA, "output: %s", o->error.c_str());
   return CH_OK;
 }

@@ -299,7 +299,7 @@ extern "C" ch_status ch_batch_create(const ch_params* runs, const int64_t* np, i
   b->r64 = P.get<double>(N);
   b->E32 = P.get<float4>(N);
   b->acc = P.get<unsigned long long>(4 * N);
-  b->tile_part = P.get<double>(4 * (size_t)b->total_tiles);
+  b->tile_part = P.get<double>(8 * (size_t)b->total_tiles);  // push partials, then the deposit's (unused)
   b->run_sums = P.get<double>(4 * (size_t)nruns);
   b->sbar = P.get<double>(nruns);
   b->part = P.get<double>((size_t)grid_for(NP, 256, b->sms, 8) * 4);
@@ -503,8 +503,8 @@ extern "C" ch_status ch_batch_initialize(ch_batch* b) {
     launch_reduce_partials(b->part, nb, 1, b->sbar + r, s);
   }
   CH_CUDA_OK(cudaMemsetAsync(b->flags, 0, sizeof(int) * (b->nruns + 1), s));
-  launch_batch_pass(true, batch_dev(b), b->dstep, b->M, b->E32, b->starts, b->acc, b->sbar, b->dep_log2, nullptr,
-                    b->tile_part, b->flags, b->tune.pass_ctas_per_sm, b->sms, s);
+  launch_batch_pass(PH_DEPOSIT, batch_dev(b), b->dstep, b->M, b->E32, b->starts, b->acc, b->sbar, b->dep_log2,
+                    nullptr, b->tile_part, b->flags, b->tune.pass_ctas_per_sm, b->sms, s);
   launch_batch_finalize(4 * b->Ntot, b->acc, 1.0 / b->dep_scale, b->mom, b->flags + b->nruns, b->sms, s);
   CH_CUDA_OK(launch_batch_solve(b->d_solve, b->nruns, b->tune.cluster, s));
   CH_CUDA_OK(cudaGetLastError());
@@ -520,8 +520,11 @@ static cudaError_t enqueue_step(ch_batch* b, bool sort_due) {
   const BatchDev B = batch_dev(b);
   if (b->prof) cudaEventRecord(b->ev[0], s);
   if (sort_due) cudaMemsetAsync(b->counts, 0, sizeof(uint32_t) * b->Ntot, s);
-  launch_batch_pass(false, B, b->dstep, b->M, b->E32, b->starts, b->acc, b->sbar, b->dep_log2,
+  // push + collide + move, then the deposit (two launches, as the single-run step)
+  launch_batch_pass(PH_PUSH | PH_MOVE, B, b->dstep, b->M, b->E32, b->starts, b->acc, b->sbar, b->dep_log2,
                     sort_due ? b->counts : nullptr, b->tile_part, b->flags, b->tune.pass_ctas_per_sm, b->sms, s);
+  launch_batch_pass(PH_DEPOSIT, B, b->dstep, b->M, b->E32, b->starts, b->acc, b->sbar, b->dep_log2, nullptr,
+                    b->tile_part + 4 * (size_t)b->total_tiles, b->flags, b->tune.pass_ctas_per_sm, b->sms, s);
   launch_batch_runsum(B, b->tile_part, b->run_sums, b->sbar, b->flags, b->dstep, s);
   launch_batch_finalize(4 * b->Ntot, b->acc, 1.0 / b->dep_scale, b->mom, b->flags + b->nruns, b->sms, s);
   if (b->prof) cudaEventRecord(b->ev[1], s);
@@ -689,8 +692,10 @@ extern "C" ch_status ch_batch_autotune(ch_batch* b, ch_batch_tuning* out) {
       cudaMemcpyAsync(b->M.pos, b->MQ.pos, sizeof(float4) * NP, cudaMemcpyDeviceToDevice, s);
       cudaMemcpyAsync(b->M.vel, b->MQ.vel, sizeof(float4) * NP, cudaMemcpyDeviceToDevice, s);
       t = timed([&] {
-        launch_batch_pass(false, batch_dev(b), b->dstep, b->M, b->E32, b->starts, b->acc, b->sbar, b->dep_log2,
-                          nullptr, b->tile_part, b->flags, k, b->sms, s);
+        launch_batch_pass(PH_PUSH | PH_MOVE, batch_dev(b), b->dstep, b->M, b->E32, b->starts, b->acc, b->sbar,
+                          b->dep_log2, nullptr, b->tile_part, b->flags, k, b->sms, s);
+        launch_batch_pass(PH_DEPOSIT, batch_dev(b), b->dstep, b->M, b->E32, b->starts, b->acc, b->sbar,
+                          b->dep_log2, nullptr, b->tile_part + 4 * (size_t)b->total_tiles, b->flags, k, b->sms, s);
       });
     }
     if (t < best_pass) { best_pass = t; best_k = k; }

@@ -17,6 +17,7 @@
 #include "particles.cuh"
 
 #include <atomic>
+#include <cstddef>
 
 #include "ion_dev.cuh"
 #include "physics.cuh"
@@ -399,14 +400,31 @@ __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, 
 __device__ __forceinline__ int rni_biased(float x) { return __float_as_int(__fadd_rn(x, 12582912.0f)); }
 __device__ __forceinline__ int rni(float x) { return rni_biased(x) - CH_RNI_BIAS; }
 
+#define CH_PUSH_CTAS 4          // CTAs per SM of a pass without the deposit
 #define CH_TILE_QCAP 512       // ring of deferred colliding ions (power of two, >= 2 x threads)
 #define CH_TILE_ROUNDS 3       // key groups a warp reduces before per-lane adds
 
 #define CH_TILE_K 4            // consecutive slots one thread deposits together
 #define CH_TILE_BATCH (256 * CH_TILE_K)
 
+// Shared memory of one CTA of the tiled pass.  The push part comes first:
+// a pass without the deposit launches with only that prefix
+// (tile_smem_bytes), the deposit part follows.
 struct TileShared {
-  float4 E[BNODES];
+  // ---- push part
+  uint32_t rowbeg[TY * TZ];
+  uint32_t pre[TY * TZ + 1];
+  unsigned qn;                  // enqueued in this brick (monotone; slot = qn mod CH_TILE_QCAP)
+  alignas(16) float4 E[BNODES];
+  // Ions whose first collision event falls inside the step are queued here
+  // after the Boris push and finished (collide, move, deposit) together, so
+  // the long collision code runs on full warps instead of one lane in 40.
+  float4 q_pos[CH_TILE_QCAP];   // offsets + packed cell, before the move
+  float4 q_vel[CH_TILE_QCAP];   // velocity after the push, rate scale in w
+  uint32_t q_ip[CH_TILE_QCAP];
+  uint32_t q_id[CH_TILE_QCAP];
+  // ---- deposit part
+  unsigned ov_n;
   // One batch of CH_TILE_BATCH ions staged between the push and the deposit:
   // box key of the ion's cell (-1: nothing to deposit here), offsets and
   // velocity.  Thread t deposits slots CH_TILE_K t .. CH_TILE_K t + K-1.
@@ -418,20 +436,14 @@ struct TileShared {
   alignas(16) float st_vy[CH_TILE_BATCH];
   alignas(16) float st_vz[CH_TILE_BATCH];
   uint16_t ov_idx[CH_TILE_BATCH];  // staged slots outside their thread's cell, added one per thread
-  unsigned ov_n;
   unsigned acc_lo[4][BNODES];  // 64-bit fixed-point sums at the tile scale as
   int acc_hi[4][BNODES];       // lo + hi * 2^32, carried exactly (order-free)
-  uint32_t rowbeg[TY * TZ];
-  uint32_t pre[TY * TZ + 1];
-  // Ions whose first collision event falls inside the step are queued here
-  // after the Boris push and finished (collide, move, deposit) together, so
-  // the long collision code runs on full warps instead of one lane in 40.
-  float4 q_pos[CH_TILE_QCAP];   // offsets + packed cell, before the move
-  float4 q_vel[CH_TILE_QCAP];   // velocity after the push, rate scale in w
-  uint32_t q_ip[CH_TILE_QCAP];
-  uint32_t q_id[CH_TILE_QCAP];
-  unsigned qn;                  // enqueued in this brick (monotone; slot = qn mod CH_TILE_QCAP)
 };
+
+template <int PH>
+constexpr size_t tile_smem_bytes() {
+  return (PH & PH_DEPOSIT) ? sizeof(TileShared) : offsetof(TileShared, ov_n);
+}
 
 // value += v for a 64-bit integer kept as (hi, lo) 32-bit words in shared
 // memory; the carry out of lo is detected from the returned old value, so
@@ -588,11 +600,13 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
   // Move one ion by v dt (cell units), wrap, repack the cell.
   auto move_ion = [&](float4& p, const float v[3], int& i, int& j, int& k) {
     float ox = p.x + v[0] * dtx, oy = p.y + v[1] * dty, oz = p.z + v[2] * dtz;
-    const float fx = floorf(ox), fy = floorf(oy), fz = floorf(oz);
+    float fx = floorf(ox), fy = floorf(oy), fz = floorf(oz);
     ox -= fx; oy -= fy; oz -= fz;
-    if (ox >= 1.0f) ox = 0.0f;
-    if (oy >= 1.0f) oy = 0.0f;
-    if (oz >= 1.0f) oz = 0.0f;
+    // a tiny negative offset rounds up to 1.0f: that point is the start of
+    // the next cell, so carry into it (as pack_mixed does)
+    if (ox >= 1.0f) { ox = 0.0f; fx += 1.0f; }
+    if (oy >= 1.0f) { oy = 0.0f; fy += 1.0f; }
+    if (oz >= 1.0f) { oz = 0.0f; fz += 1.0f; }
     if (isfinite(fx) && isfinite(fy) && isfinite(fz)) {
       i = ch_wrap(i + (int)fx, g.Nx); j = ch_wrap(j + (int)fy, g.Ny); k = ch_wrap(k + (int)fz, g.Nz);
     }
@@ -859,7 +873,7 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
 }
 
 template <int PH>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? 2 : CH_PUSH_CTAS)
     k_pass_tiled(StepConsts c, MixParticles P, const float4* __restrict__ E, const uint32_t* __restrict__ starts,
                  unsigned long long* __restrict__ acc, float pscale, int shift_d, int shift_f, DevCounters* cnt,
                  double* part, uint32_t* hist) {
@@ -885,7 +899,7 @@ __global__ void __launch_bounds__(256, 2)
 // run.  Brick partials are written per brick, so the run sums are formed in
 // a fixed order afterwards.
 template <int PH>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? 2 : CH_PUSH_CTAS)
     k_batch_pass(BatchDev B, const uint32_t* dstep, MixParticles P, const float4* __restrict__ E,
                  const uint32_t* __restrict__ starts, unsigned long long* __restrict__ acc,
                  const double* __restrict__ sbar, int shift_d, int shift_f, uint32_t* hist, double* tile_part,
@@ -1261,11 +1275,51 @@ void launch_load(bool mixed, const GridDesc& g, const ch_loader& L, uint64_t see
   else k_load_f64<<<grid_for(P.np, 256, sms, 8), 256, 0, s>>>(g, L, lo, hi, run, P), ::ch::note_launch();
 }
 
-// dst <- src, 16 bytes per thread and iteration (bytes a multiple of 16,
-// both 16-byte aligned); dst may be mapped host memory.
+// dst <- src in 16-byte words (bytes a multiple of 16, both 16-byte
+// aligned); dst may be mapped host memory.  Four independent words per
+// thread and iteration keep enough bytes in flight for the host link.
 __global__ void k_stream_copy(uint4* __restrict__ dst, const uint4* __restrict__ src, int64_t n16) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += (int64_t)gridDim.x * blockDim.x)
-    dst[i] = src[i];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n16; i += 4 * stride) {
+    const uint4 a = src[i], b = src[i + stride], c = src[i + 2 * stride], d = src[i + 3 * stride];
+    dst[i] = a;
+    dst[i + stride] = b;
+    dst[i + 2 * stride] = c;
+    dst[i + 3 * stride] = d;
+  }
+  for (; i < n16; i += stride) dst[i] = src[i];
+}
+
+// Host AoS (16-byte aligned, e.g. mapped host memory) -> mixed state:
+// 16-byte loads, two ions per thread and iteration in flight.
+__global__ void k_aos_to_mixed_u16(GridDesc g, const double2* __restrict__ pos, const double2* __restrict__ vel,
+                                   MixParticles P) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.np; i += stride) {
+    const double2 p0 = pos[2 * i], p1 = pos[2 * i + 1], v0 = vel[2 * i], v1 = vel[2 * i + 1];
+    const double s[3] = {p0.x, p0.y, p1.x};
+    P.pos[i] = pack_mixed(g, s);
+    P.vel[i] = make_float4((float)v0.x, (float)v0.y, (float)v1.x, __uint_as_float((uint32_t)i));
+  }
+}
+
+__global__ void k_aos_to_f64_u16(const double2* __restrict__ pos, const double2* __restrict__ vel, F64Particles P) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.np; i += stride) {
+    const double2 p0 = pos[2 * i], p1 = pos[2 * i + 1], v0 = vel[2 * i], v1 = vel[2 * i + 1];
+    P.x[i] = p0.x; P.y[i] = p0.y; P.z[i] = p1.x;
+    P.vx[i] = v0.x; P.vy[i] = v0.y; P.vz[i] = v1.x;
+    P.id[i] = (uint32_t)i;
+  }
+}
+
+void launch_aos_in_u16(bool mixed, const GridDesc& g, const void* pos, const void* vel, F64Particles P,
+                       MixParticles M, int sms, cudaStream_t s) {
+  const double2* p = static_cast<const double2*>(pos);
+  const double2* v = static_cast<const double2*>(vel);
+  if (mixed) k_aos_to_mixed_u16<<<grid_for(M.np, 256, sms, 16), 256, 0, s>>>(g, p, v, M), ::ch::note_launch();
+  else k_aos_to_f64_u16<<<grid_for(P.np, 256, sms, 16), 256, 0, s>>>(p, v, P), ::ch::note_launch();
 }
 
 void launch_stream_copy(void* dst, const void* src, uint64_t bytes, int sms, cudaStream_t s) {
@@ -1302,8 +1356,8 @@ static void tiled_smem_attr() {
   const uint32_t bit = 1u << (dev & 31);
   if (done.load() & bit) return;
   // a failure here surfaces as the launch error of the pass
-  if (cudaFuncSetAttribute(k_pass_tiled<PH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileShared)) ==
-      cudaSuccess)
+  if (cudaFuncSetAttribute(k_pass_tiled<PH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)tile_smem_bytes<PH>()) == cudaSuccess)
     done.fetch_or(bit);
 }
 
@@ -1317,10 +1371,11 @@ static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticle
   if (mixed) {
     const float pscale = sbar > 0.0 ? (float)(Nc / sbar) : 0.0f;
     const int ntiles = ((c.g.Nx + 15) / 16) * ((c.g.Ny + 3) / 4) * ((c.g.Nz + 3) / 4);
-    nb = ntiles < 2 * sms ? ntiles : 2 * sms;
+    const int per_sm = (PH & PH_DEPOSIT) ? 2 : CH_PUSH_CTAS;
+    nb = ntiles < per_sm * sms ? ntiles : per_sm * sms;
     const int s2 = (int)lround(log2(c.dep_scale));
     tiled_smem_attr<PH>();
-    k_pass_tiled<PH><<<nb, 256, sizeof(TileShared), s>>>(c, M, E32, starts, acc, pscale, s2 - CH_TILE_DLOG2,
+    k_pass_tiled<PH><<<nb, 256, tile_smem_bytes<PH>(), s>>>(c, M, E32, starts, acc, pscale, s2 - CH_TILE_DLOG2,
                                                          s2 - CH_TILE_FLOG2, cnt, part, hist),
         ::ch::note_launch();
   } else {
@@ -1338,6 +1393,7 @@ int launch_pass(bool mixed, int phases, const StepConsts& c, F64Particles P, Mix
     case PH_MOVE: return CH_PASS(PH_MOVE);
     case PH_DEPOSIT: return CH_PASS(PH_DEPOSIT);
     case PH_MOVE | PH_DEPOSIT: return CH_PASS(PH_MOVE | PH_DEPOSIT);
+    case PH_PUSH | PH_MOVE: return CH_PASS(PH_PUSH | PH_MOVE);
     default: return CH_PASS(PH_PUSH | PH_MOVE | PH_DEPOSIT);
   }
 #undef CH_PASS
@@ -1393,28 +1449,32 @@ static void batch_smem_attr() {
   cudaGetDevice(&dev);
   const uint32_t bit = 1u << (dev & 31);
   if (done.load() & bit) return;
-  if (cudaFuncSetAttribute(k_batch_pass<PH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileShared)) ==
-      cudaSuccess)
+  if (cudaFuncSetAttribute(k_batch_pass<PH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)tile_smem_bytes<PH>()) == cudaSuccess)
     done.fetch_or(bit);
 }
 
 void batch_pass_prepare() {
   batch_smem_attr<PH_PUSH | PH_MOVE | PH_DEPOSIT>();
+  batch_smem_attr<PH_PUSH | PH_MOVE>();
   batch_smem_attr<PH_DEPOSIT>();
 }
 
-void launch_batch_pass(bool deposit_only, const BatchDev& B, const uint32_t* dstep, MixParticles P, const float4* E,
+void launch_batch_pass(int phases, const BatchDev& B, const uint32_t* dstep, MixParticles P, const float4* E,
                        const uint32_t* starts, unsigned long long* acc, const double* sbar, int dep_log2,
                        uint32_t* hist, double* tile_part, int* flags, int ctas_per_sm, int sms, cudaStream_t s) {
-  const int cap = (ctas_per_sm < 1 ? 1 : ctas_per_sm) * sms;
+  const int per_sm = (phases & PH_DEPOSIT) ? (ctas_per_sm < 1 ? 1 : ctas_per_sm) : CH_PUSH_CTAS;
+  const int cap = per_sm * sms;
   const int nb = B.total_tiles < cap ? B.total_tiles : cap;
   const int sd = dep_log2 - CH_TILE_DLOG2, sf = dep_log2 - CH_TILE_FLOG2;
-  if (deposit_only)
-    k_batch_pass<PH_DEPOSIT><<<nb, 256, sizeof(TileShared), s>>>(B, dstep, P, E, starts, acc, sbar, sd, sf, hist,
-                                                                 tile_part, flags), ::ch::note_launch();
-  else
-    k_batch_pass<PH_PUSH | PH_MOVE | PH_DEPOSIT><<<nb, 256, sizeof(TileShared), s>>>(
-        B, dstep, P, E, starts, acc, sbar, sd, sf, hist, tile_part, flags), ::ch::note_launch();
+#define CH_BPASS(PHV)                                                                                            \
+  k_batch_pass<PHV><<<nb, 256, tile_smem_bytes<PHV>(), s>>>(B, dstep, P, E, starts, acc, sbar, sd, sf, hist, \
+                                                            tile_part, flags),                                 \
+      ::ch::note_launch()
+  if (phases == PH_DEPOSIT) CH_BPASS(PH_DEPOSIT);
+  else if (phases == (PH_PUSH | PH_MOVE)) CH_BPASS(PH_PUSH | PH_MOVE);
+  else CH_BPASS(PH_PUSH | PH_MOVE | PH_DEPOSIT);
+#undef CH_BPASS
 }
 
 void launch_batch_runsum(const BatchDev& B, const double* tile_part, double* sums, double* sbar, int* flags,

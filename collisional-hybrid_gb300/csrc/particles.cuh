@@ -30,6 +30,10 @@ void launch_aos_in(bool mixed, const GridDesc& g, const double4_32a* pos, const 
 // Copies bytes (a multiple of 16; both pointers 16-byte aligned) on the SMs;
 // dst may be mapped host memory.
 void launch_stream_copy(void* dst, const void* src, uint64_t bytes, int sms, cudaStream_t s);
+// AoS in from 16-byte aligned arrays that the device can read directly
+// (mapped host memory).
+void launch_aos_in_u16(bool mixed, const GridDesc& g, const void* pos, const void* vel, F64Particles P,
+                       MixParticles M, int sms, cudaStream_t s);
 void launch_aos_out(bool mixed, const GridDesc& g, F64Particles P, MixParticles M, double4_32a* pos, double4_32a* vel,
                     int sms, cudaStream_t s);
 void launch_node_efield(bool mixed, const GridDesc& g, double tscale, const double* phi, double* E64, float4* E32,
@@ -80,9 +84,10 @@ int tiles_of(const GridDesc& g);
 // tile_part; flags[r] |= 16 for a non-finite ion of run r.  hist (nullable)
 // counts the ions' new cells over the batch grid.
 // The step number is read from *dstep (device), so a captured step can be
-// replayed.  deposit_only: CollectVlasovQuantities alone (before the loop).
+// replayed.  phases: PH_DEPOSIT alone (CollectVlasovQuantities), PH_PUSH |
+// PH_MOVE, or all three.  Brick partials (tile_part) come from the push.
 void batch_pass_prepare();  // once, before any capture
-void launch_batch_pass(bool deposit_only, const BatchDev& B, const uint32_t* dstep, MixParticles P, const float4* E,
+void launch_batch_pass(int phases, const BatchDev& B, const uint32_t* dstep, MixParticles P, const float4* E,
                        const uint32_t* starts, unsigned long long* acc, const double* sbar, int dep_log2,
                        uint32_t* hist, double* tile_part, int* flags, int ctas_per_sm, int sms, cudaStream_t s);
 // sums[4r + q] = the run's brick partials summed in a fixed order; sbar[r] =

@@ -491,7 +491,15 @@ void PotentialSolver::release() {
 // ------------------------------------------------------------------ multigrid (host)
 static constexpr int MG_NU = 2;            // pre- and post-smoothing sweeps (even)
 static constexpr double MG_OMEGA = 0.8;    // Jacobi damping
-static constexpr int MG_COARSE_SWEEPS = 64;
+// Jacobi sweeps of the coarsest level: enough to reduce its smoothest mode
+// well below the V-cycle's own error (4 per node of its longest edge; 16 for
+// the 4^3 level of a 2^k grid, where 16 and 64 sweeps give the same Krylov
+// iteration counts).
+static int mg_coarse_sweeps(const GridDesc& g) {
+  const int e = g.Nx > g.Ny ? (g.Nx > g.Nz ? g.Nx : g.Nz) : (g.Ny > g.Nz ? g.Ny : g.Nz);
+  const int s = 4 * e;
+  return s < 16 ? 16 : (s > 64 ? 64 : s);
+}
 static constexpr int64_t MG_COARSE_MAX = 4096;
 
 template <typename T>
@@ -572,7 +580,7 @@ void PotentialSolver::mg_vcycle(MGHier<T>& h, int l, const T* b, T* x, cudaStrea
   const T w = (T)MG_OMEGA;
   if (l == h.L - 1) {
     const size_t sh = 2 * sizeof(T) * g.N;
-    k_coarse<T><<<1, 1024, sh, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, x, MG_COARSE_SWEEPS, w), ::ch::note_launch();
+    k_coarse<T><<<1, 1024, sh, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, x, mg_coarse_sweeps(g), w), ::ch::note_launch();
     return;
   }
   T* t = h.t[l];

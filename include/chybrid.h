@@ -212,6 +212,19 @@ ch_status ch_reset_profile(ch_ctx* c);
 /* The cudaStream_t every call of this context is ordered on. */
 ch_status ch_get_stream(ch_ctx* c, void** stream);
 
+/* OutputHDF5 (src/fileio.c:73-126) without HDF5.  ch_output_open sets the
+ * file stem (the reference's ctx->outstem); ch_output then writes the current
+ * density, x/y/z flux, rhs and potential -- the reference's dataset names --
+ * as <stem><insert>.<field>.f64 (raw little-endian FP64, DMDA natural order;
+ * spaces in names become '_') with a manifest <stem><insert>.json.  The fields
+ * are snapshot on the device at once; the copy to the host and the file
+ * writes run beside the following steps (a second stream and a host thread,
+ * two slots in flight).  ch_output_wait returns when every queued output is
+ * on disk (written: files-sets written so far; nullable). */
+ch_status ch_output_open(ch_ctx* c, const char* stem);
+ch_status ch_output(ch_ctx* c, const char* insert);
+ch_status ch_output_wait(ch_ctx* c, int64_t* written);
+
 /* CollectVlasovQuantities for callers that cannot allocate device memory
  * (no counterpart in the reference).  Hosts whose device memory belongs to
  * their own pool allocator, code that records its launches into a CUDA graph

@@ -419,3 +419,24 @@ def test_bad_arguments_are_rejected(chy):
     with pytest.raises(chy.HybridError) as e:
         chy.Hybrid(chy.params_for((8, 8, 8), precision=1, faithful=chy.FAITHFUL[3]))
     assert e.value.status == -10
+
+
+def test_mixed_move_a_hair_across_a_cell_face(chy):
+    """An ion on a cell face that moves left by far less than the FP32
+    spacing of the offset ends where it started, not a cell away: the offset
+    that rounds to 1.0 carries into the next cell (found at 128^3 x 64
+    ions/cell, 6 ions per step)."""
+    p = chy.params_for((8, 8, 8), precision=chy.PRECISION["mixed"], mn=0.0)
+    n = 64
+    pos = np.zeros((n, 4))
+    vel = np.zeros((n, 4))
+    pos[:, 0] = 5.0                      # on the face between cells 4 and 5
+    pos[:, 1] = 3.5
+    pos[:, 2] = 2.25 + np.arange(n) / 64.0
+    vel[:, 0] = -np.logspace(-12, -6, n) / p.dt   # moves left by 1e-12 .. 1e-6 cells
+    with chy.Hybrid(p) as h:
+        h.upload(pos, vel)
+        h.UpdatePositions()
+        out, _ = h.download()
+    expect = pos[:, 0] + vel[:, 0] * p.dt
+    assert np.abs(out[:, 0] - expect).max() < 1e-6, np.abs(out[:, 0] - expect).max()

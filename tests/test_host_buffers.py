@@ -2,7 +2,7 @@
 ch_host_register are read and written by the GPU directly (the conversion
 kernels read them, a copy kernel writes them); other arrays go through
 staging copies.  Both routes must give the same ions bit for bit, and a view
-that is not 32-byte aligned inside a registered range must take the staged
+that is not 16-byte aligned inside a registered range must take the staged
 route."""
 import numpy as np
 import pytest
