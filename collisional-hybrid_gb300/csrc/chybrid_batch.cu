@@ -96,7 +96,7 @@ struct ch_batch {
   std::vector<char> present;  // ions of run r loaded or uploaded
   bool loaded = false, initialized = false, parity = false;
   int since_sort = 0;
-  ch_batch_tuning tune{4, 2, 0.0, 0.0};
+  ch_batch_tuning tune{4, 3, 0.0, 0.0};
   cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [sort_due][parity]
   long long graph_nodes[2][2] = {{0, 0}, {0, 0}};
   bool prof = false;
@@ -629,7 +629,7 @@ extern "C" ch_status ch_batch_set_tuning(ch_batch* b, const ch_batch_tuning* t) 
   if (!b || !t) return ch_fail(CH_ERR_ARG, "null argument");
   if (!(t->cluster == 1 || t->cluster == 2 || t->cluster == 4 || t->cluster == 8))
     return ch_fail(CH_ERR_ARG, "cluster must be 1, 2, 4 or 8");
-  if (t->pass_ctas_per_sm < 1 || t->pass_ctas_per_sm > 2) return ch_fail(CH_ERR_ARG, "pass_ctas_per_sm: 1 or 2");
+  if (t->pass_ctas_per_sm < 1 || t->pass_ctas_per_sm > 3) return ch_fail(CH_ERR_ARG, "pass_ctas_per_sm: 1 to 3");
   b->tune.cluster = t->cluster;
   b->tune.pass_ctas_per_sm = t->pass_ctas_per_sm;
   drop_graphs(b);
@@ -644,7 +644,8 @@ extern "C" ch_status ch_batch_get_tuning(ch_batch* b, ch_batch_tuning* out) {
 
 // Times each launch shape on the current state.  The solve is timed from the
 // same phi (saved and restored); the pass from the same ions (saved in the
-// sort's spare buffers and restored), with the deposit discarded.
+// sort's spare buffers and restored), with the deposit discarded.  The
+// pass shape is the deposit launch's CTAs per SM.
 extern "C" ch_status ch_batch_autotune(ch_batch* b, ch_batch_tuning* out) {
   if (!b) return ch_fail(CH_ERR_ARG, "null batch");
   if (!b->initialized) return ch_fail(CH_ERR_STATE, "call ch_batch_initialize first");
@@ -686,7 +687,7 @@ extern "C" ch_status ch_batch_autotune(ch_batch* b, ch_batch_tuning* out) {
   cudaMemcpyAsync(b->MQ.vel, b->M.vel, sizeof(float4) * NP, cudaMemcpyDeviceToDevice, s);
   double best_pass = 1e30;
   int best_k = b->tune.pass_ctas_per_sm;
-  for (int k : {1, 2}) {
+  for (int k : {1, 2, 3}) {
     double t = 0.0;
     for (int rep = 0; rep < 2; ++rep) {
       cudaMemcpyAsync(b->M.pos, b->MQ.pos, sizeof(float4) * NP, cudaMemcpyDeviceToDevice, s);

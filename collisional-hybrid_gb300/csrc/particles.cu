@@ -401,20 +401,19 @@ __device__ __forceinline__ int rni_biased(float x) { return __float_as_int(__fad
 __device__ __forceinline__ int rni(float x) { return rni_biased(x) - CH_RNI_BIAS; }
 
 #define CH_PUSH_CTAS 4          // CTAs per SM of a pass without the deposit
+#define CH_DEP_CTAS 3           // CTAs per SM of a pass with the deposit (61 KB each when deposit-only)
 #define CH_TILE_QCAP 512       // ring of deferred colliding ions (power of two, >= 2 x threads)
 #define CH_TILE_ROUNDS 3       // key groups a warp reduces before per-lane adds
 
 #define CH_TILE_K 4            // consecutive slots one thread deposits together
 #define CH_TILE_BATCH (256 * CH_TILE_K)
 
-// Shared memory of one CTA of the tiled pass.  The push part comes first:
-// a pass without the deposit launches with only that prefix
-// (tile_smem_bytes), the deposit part follows.
+// Shared memory of one CTA of the tiled pass: [push part][header][deposit
+// part].  A pass with the push allocates from the start; a deposit-only pass
+// allocates from the header, so it needs no room for the field tile and the
+// collision queue (tile_smem_base / tile_smem_bytes).
 struct TileShared {
   // ---- push part
-  uint32_t rowbeg[TY * TZ];
-  uint32_t pre[TY * TZ + 1];
-  unsigned qn;                  // enqueued in this brick (monotone; slot = qn mod CH_TILE_QCAP)
   alignas(16) float4 E[BNODES];
   // Ions whose first collision event falls inside the step are queued here
   // after the Boris push and finished (collide, move, deposit) together, so
@@ -423,8 +422,14 @@ struct TileShared {
   float4 q_vel[CH_TILE_QCAP];   // velocity after the push, rate scale in w
   uint32_t q_ip[CH_TILE_QCAP];
   uint32_t q_id[CH_TILE_QCAP];
-  // ---- deposit part
+  float q_t[CH_TILE_QCAP];      // elapsed time of the event process (waiting times so far)
+  uint32_t q_st[CH_TILE_QCAP];  // event | proposal << 8
+  // ---- header
+  alignas(16) uint32_t rowbeg[TY * TZ];
+  uint32_t pre[TY * TZ + 1];
+  unsigned qn;                  // enqueued in this brick (monotone; slot = qn mod CH_TILE_QCAP)
   unsigned ov_n;
+  // ---- deposit part
   // One batch of CH_TILE_BATCH ions staged between the push and the deposit:
   // box key of the ion's cell (-1: nothing to deposit here), offsets and
   // velocity.  Thread t deposits slots CH_TILE_K t .. CH_TILE_K t + K-1.
@@ -441,8 +446,19 @@ struct TileShared {
 };
 
 template <int PH>
+constexpr size_t tile_smem_skip() {  // bytes of TileShared a launch of PH does not allocate
+  return (PH & (PH_PUSH | PH_MOVE)) ? 0 : offsetof(TileShared, rowbeg);
+}
+template <int PH>
 constexpr size_t tile_smem_bytes() {
-  return (PH & PH_DEPOSIT) ? sizeof(TileShared) : offsetof(TileShared, ov_n);
+  return (PH & PH_DEPOSIT) ? sizeof(TileShared) - tile_smem_skip<PH>() : offsetof(TileShared, st_key);
+}
+// The TileShared view of a launch's dynamic shared memory: for a
+// deposit-only launch the allocation starts at the header, and the push part
+// (never touched by such a launch) lies before it.
+template <int PH>
+__device__ __forceinline__ TileShared& tile_smem_base(unsigned char* smem) {
+  return *reinterpret_cast<TileShared*>(smem - tile_smem_skip<PH>());
 }
 
 // value += v for a 64-bit integer kept as (hi, lo) 32-bit words in shared
@@ -685,7 +701,7 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
         v[0] = vv.x; v[1] = vv.y; v[2] = vv.z;
       }
       bool defer = false;
-      float qscale = 0.0f;  // rate scale of a deferred ion
+      float qscale = 0.0f, qt0 = 0.0f;  // rate scale and first waiting time of a deferred ion
       if ((PH & PH_PUSH) && active) {
         bool near;
         const int q = box_key(g, i, j, k, bi0, bj0, bk0, &near);
@@ -738,13 +754,15 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
           tsum0 += lam;
           const uint32_t id = __float_as_uint(vv.w);
           const U4 r0 = ch_philox(id, c.step, CH_PURPOSE_COLLIDE << 24, c.run, c.seed_lo, c.seed_hi);
-          // first event inside the step: -log(u) < lam  <=>  u > exp(-lam)
-          if (lam > 0.0f && ch_unitf(r0.x) > __expf(-lam)) {
-            defer = true;
-            qscale = lscale;
-          } else {
-            gsum += g_fixed(gi);
+          // first event inside the step: -log(u) < lam  <=>  u > exp(-lam);
+          // the queue keeps its waiting time
+          const float u0 = ch_unitf(r0.x);
+          if (lam > 0.0f && u0 > __expf(-lam)) {
+            qt0 = -ch_log(u0) / lam;
+            defer = qt0 < 1.0f;
           }
+          if (defer) qscale = lscale;
+          else gsum += g_fixed(gi);
         }
         if (!defer) {
           vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
@@ -764,6 +782,8 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
             sh.q_vel[slot] = make_float4(v[0], v[1], v[2], qscale);
             sh.q_ip[slot] = (uint32_t)ip;
             sh.q_id[slot] = __float_as_uint(vv.w);
+            sh.q_t[slot] = qt0;
+            sh.q_st[slot] = 0u;
           }
         }
       }
@@ -792,56 +812,87 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
         // every enqueue of this iteration is visible after the barrier
         qtail += (unsigned)__syncthreads_count(defer);
         const bool last = base + (kk + 1) * blockDim.x >= total;
-        // drain full rounds of one queued ion per thread (the rest waits for
-        // the next iteration), and everything at the end of the brick:
-        // collide, move and deposit
+        // Drain in rounds: each round advances up to one queued ion per
+        // thread by one proposal of its current event (with the scatter and
+        // the next waiting time when the proposal is accepted); ions with
+        // further events go back to the tail.  Full rounds run as the queue
+        // fills, and the queue is emptied at the end of the brick.
         while (qtail - qhead >= blockDim.x || (last && qtail > qhead)) {
           const unsigned nq = min(qtail - qhead, blockDim.x);
+          const unsigned e = (qhead + threadIdx.x) & (CH_TILE_QCAP - 1);
+          const bool act = threadIdx.x < nq;
+          float4 qp = make_float4(0.f, 0.f, 0.f, 0.f);
+          float qv[3] = {0.f, 0.f, 0.f};
+          float qsc = 0.0f, qtm = 0.0f;
+          uint32_t qip = 0, qid = 0, qe = 0, qit = 0;
+          bool done = false;
+          if (act) {
+            qp = sh.q_pos[e];
+            const float4 q4 = sh.q_vel[e];
+            qip = sh.q_ip[e];
+            qid = sh.q_id[e];
+            qtm = sh.q_t[e];
+            const uint32_t st = sh.q_st[e];
+            qe = st & 0xFFu;
+            qit = st >> 8;
+            qv[0] = q4.x; qv[1] = q4.y; qv[2] = q4.z;
+            qsc = q4.w;
+            done = ch_collide_round<float>(c, qid, qsc, qv, qtm, qe, qit, &ncol, &nref);
+          }
+          __syncthreads();  // this round's entries are read before any re-queue reuses their slots
+          const bool requeue = act && !done;
           {
-            const unsigned e = (qhead + threadIdx.x) & (CH_TILE_QCAP - 1);
-            const bool act = threadIdx.x < nq;
-            float4 qp = make_float4(0.f, 0.f, 0.f, 0.f);
-            float qv[3] = {0.f, 0.f, 0.f};
-            int qi = 0, qj = 0, qk = 0;
-            uint32_t qip = 0;
-            if (act) {
-              qp = sh.q_pos[e];
-              const float4 q4 = sh.q_vel[e];
-              qip = sh.q_ip[e];
-              const uint32_t qid = sh.q_id[e];
-              qv[0] = q4.x; qv[1] = q4.y; qv[2] = q4.z;
-              ncol += ch_collide<float>(c, qid, q4.w, qv, &nref);
-              gsum += g_fixed(gmean_of(qv));
-              P.vel[qip] = make_float4(qv[0], qv[1], qv[2], __uint_as_float(qid));
-              const uint32_t cell = __float_as_uint(qp.w);
-              qi = cell & (CH_MAX_NX - 1); qj = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1);
-              qk = cell >> (CH_PACK_BX + CH_PACK_BY);
-              if (move) {
-                move_ion(qp, qv, qi, qj, qk);
-                P.pos[qip] = qp;
+            const unsigned rm = __ballot_sync(0xffffffffu, requeue);
+            if (rm) {
+              const int leader = __ffs(rm) - 1;
+              unsigned slot = 0;
+              if (lane == leader) slot = atomicAdd(&sh.qn, (unsigned)__popc(rm));
+              slot = (__shfl_sync(0xffffffffu, slot, leader) + __popc(rm & ((1u << lane) - 1u))) & (CH_TILE_QCAP - 1);
+              if (requeue) {
+                sh.q_pos[slot] = qp;
+                sh.q_vel[slot] = make_float4(qv[0], qv[1], qv[2], qsc);
+                sh.q_ip[slot] = qip;
+                sh.q_id[slot] = qid;
+                sh.q_t[slot] = qtm;
+                sh.q_st[slot] = qe | (qit << 8);
               }
             }
-            if (hist) {
-              const uint32_t rk = agg_inc(hist, (uint32_t)(((int64_t)qk * g.Ny + qj) * g.Nx + qi), act);
-              if (act && P.rank) P.rank[qip] = rk;
-            }
-            if ((PH & PH_DEPOSIT) && act) {
-              const bool finite = isfinite(qp.x) && isfinite(qp.y) && isfinite(qp.z) && isfinite(qv[0]) &&
-                                  isfinite(qv[1]) && isfinite(qv[2]);
-              bool inbox;
-              const int key = box_key(g, qi, qj, qk, bi0, bj0, bk0, &inbox);
-              const bool slow =
-                  fabsf(qv[0]) >= CH_TILE_VMAX || fabsf(qv[1]) >= CH_TILE_VMAX || fabsf(qv[2]) >= CH_TILE_VMAX;
-              if (!finite)
-                bad = 1;
-              else if (inbox && !slow)
-                tile_deposit_lane(sh, key, qp.x, qp.y, qp.z, qv[0], qv[1], qv[2]);
-              else
-                deposit_cic<float>(g, acc, qi, qj, qk, qp.x, qp.y, qp.z, qv[0], qv[1], qv[2], (float)c.dep_scale);
+          }
+          // ions whose event process ended: the velocity, the move, the cell count
+          const bool fin = act && done;
+          int qi = 0, qj = 0, qk = 0;
+          if (fin) {
+            gsum += g_fixed(gmean_of(qv));
+            P.vel[qip] = make_float4(qv[0], qv[1], qv[2], __uint_as_float(qid));
+            const uint32_t cell = __float_as_uint(qp.w);
+            qi = cell & (CH_MAX_NX - 1); qj = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1);
+            qk = cell >> (CH_PACK_BX + CH_PACK_BY);
+            if (move) {
+              move_ion(qp, qv, qi, qj, qk);
+              P.pos[qip] = qp;
             }
           }
+          if (hist) {
+            const uint32_t rk = agg_inc(hist, (uint32_t)(((int64_t)qk * g.Ny + qj) * g.Nx + qi), fin);
+            if (fin && P.rank) P.rank[qip] = rk;
+          }
+          if ((PH & PH_DEPOSIT) && fin) {
+            const bool finite = isfinite(qp.x) && isfinite(qp.y) && isfinite(qp.z) && isfinite(qv[0]) &&
+                                isfinite(qv[1]) && isfinite(qv[2]);
+            bool inbox;
+            const int key = box_key(g, qi, qj, qk, bi0, bj0, bk0, &inbox);
+            const bool slow =
+                fabsf(qv[0]) >= CH_TILE_VMAX || fabsf(qv[1]) >= CH_TILE_VMAX || fabsf(qv[2]) >= CH_TILE_VMAX;
+            if (!finite)
+              bad = 1;
+            else if (inbox && !slow)
+              tile_deposit_lane(sh, key, qp.x, qp.y, qp.z, qv[0], qv[1], qv[2]);
+            else
+              deposit_cic<float>(g, acc, qi, qj, qk, qp.x, qp.y, qp.z, qv[0], qv[1], qv[2], (float)c.dep_scale);
+          }
           qhead += nq;
-          __syncthreads();  // the queue is read before the next enqueue reuses its slots
+          // the re-queued entries are visible before the next round reads them
+          qtail += (unsigned)__syncthreads_count(requeue);
         }
       }
     }
@@ -873,12 +924,12 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
 }
 
 template <int PH>
-__global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? 2 : CH_PUSH_CTAS)
+__global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH_CTAS)
     k_pass_tiled(StepConsts c, MixParticles P, const float4* __restrict__ E, const uint32_t* __restrict__ starts,
                  unsigned long long* __restrict__ acc, float pscale, int shift_d, int shift_f, DevCounters* cnt,
                  double* part, uint32_t* hist) {
   extern __shared__ __align__(16) unsigned char smem_tiled[];
-  TileShared& sh = *reinterpret_cast<TileShared*>(smem_tiled);
+  TileShared& sh = tile_smem_base<PH>(smem_tiled);
   double vsum[2] = {0.0, 0.0};
   unsigned ncol = 0, nref = 0;
   int bad = 0;
@@ -899,13 +950,13 @@ __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? 2 : CH_PUSH_CTAS)
 // run.  Brick partials are written per brick, so the run sums are formed in
 // a fixed order afterwards.
 template <int PH>
-__global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? 2 : CH_PUSH_CTAS)
+__global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH_CTAS)
     k_batch_pass(BatchDev B, const uint32_t* dstep, MixParticles P, const float4* __restrict__ E,
                  const uint32_t* __restrict__ starts, unsigned long long* __restrict__ acc,
                  const double* __restrict__ sbar, int shift_d, int shift_f, uint32_t* hist, double* tile_part,
                  int* flags) {
   extern __shared__ __align__(16) unsigned char smem_tiled[];
-  TileShared& sh = *reinterpret_cast<TileShared*>(smem_tiled);
+  TileShared& sh = tile_smem_base<PH>(smem_tiled);
   __shared__ StepConsts sc;
   __shared__ int s_run;
   constexpr int W = (int)(sizeof(StepConsts) / sizeof(uint32_t));
@@ -1371,7 +1422,7 @@ static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticle
   if (mixed) {
     const float pscale = sbar > 0.0 ? (float)(Nc / sbar) : 0.0f;
     const int ntiles = ((c.g.Nx + 15) / 16) * ((c.g.Ny + 3) / 4) * ((c.g.Nz + 3) / 4);
-    const int per_sm = (PH & PH_DEPOSIT) ? 2 : CH_PUSH_CTAS;
+    const int per_sm = (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH_CTAS;
     nb = ntiles < per_sm * sms ? ntiles : per_sm * sms;
     const int s2 = (int)lround(log2(c.dep_scale));
     tiled_smem_attr<PH>();

@@ -181,3 +181,95 @@ __device__ __noinline__ int ch_collide(const StepConsts& c, uint32_t id, R lscal
   }
   return ncol;
 }
+
+// One round of the collision event process of one ion, for queues that
+// advance every queued ion by one proposal per round (so that a warp does
+// not wait on the unluckiest lane's rejection loop).  State: event e,
+// proposal it of that event, elapsed time t (the waiting time of event e is
+// already in t).  The round draws proposal it of event e from the same
+// Philox blocks as ch_collide; if it is accepted the scatter (or refusal) is
+// applied and the waiting time of event e + 1 is added.  Returns true when
+// the ion has no further event in this step.
+template <typename R>
+__device__ __forceinline__ bool ch_collide_round(const StepConsts& c, uint32_t id, R lscale, R v[3], R& t,
+                                                 uint32_t& e, uint32_t& it, unsigned* ncol, unsigned* refused) {
+  const R sig = R(c.vnT);
+  const R vn0x = R(c.vn0[0]), vn0y = R(c.vn0[1]), vn0z = R(c.vn0[2]);
+  const R m1 = R(c.m1);
+  const R mi = R(c.mi), mn = R(c.mn), M = mn + mi;
+  const R vix = v[0], viy = v[1], viz = v[2];
+  const R wx = vix - vn0x, wy = viy - vn0y, wz = viz - vn0z;
+  const R w = ch_sqrt(wx * wx + wy * wy + wz * wz);
+  const U4 a = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (e << 8) | (1 + 2 * it), c.run, c.seed_lo, c.seed_hi);
+  const U4 b = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (e << 8) | (2 + 2 * it), c.run, c.seed_lo, c.seed_hi);
+  R nx, ny, nz;
+  if (unitR<R>(a.x) * (w + m1) < w) {
+    R s1, c1, s2, c2;
+    const R r1 = ch_sqrt(R(-2) * ch_log(unitR<R>(a.y)));
+    ch_sincos2pi(unitR<R>(a.z), &s1, &c1);
+    const R r2 = ch_sqrt(R(-2) * ch_log(unitR<R>(a.w)));
+    ch_sincos2pi(unitR<R>(b.x), &s2, &c2);
+    nx = sig * (r1 * c1); ny = sig * (r1 * s1); nz = sig * (r2 * c2);
+  } else {
+    const R sp = sig * ch_sqrt(R(-2) * ch_log(unitR<R>(a.y) * unitR<R>(a.z)));
+    const R ct = R(2) * unitR<R>(a.w) - R(1);
+    R st = R(1) - ct * ct;
+    st = ch_sqrt(st > R(0) ? st : R(0));
+    R sph, cph;
+    ch_sincos2pi(unitR<R>(b.x), &sph, &cph);
+    nx = sp * st * cph; ny = sp * st * sph; nz = sp * ct;
+  }
+  const R Vx = vn0x + nx, Vy = vn0y + ny, Vz = vn0z + nz;
+  const R dV = ch_sqrt(nx * nx + ny * ny + nz * nz);
+  const R rx = vix - Vx, ry = viy - Vy, rz = viz - Vz;
+  const R D = ch_sqrt(rx * rx + ry * ry + rz * rz);
+  const bool accept = unitR<R>(b.y) * (w + dV) < D;
+  if (!accept && it + 1 < 64) {
+    ++it;
+    return false;
+  }
+  if (accept) {
+    // centre-of-mass scatter (src/particles.c:552-591)
+    const R uz = R(2) * unitR<R>(b.z) - R(1);
+    const R vrr = D;
+    const R vcx = (vix * mi + Vx * mn) / M, vcy = (viy * mi + Vy * mn) / M, vcz = (viz * mi + Vz * mn) / M;
+    const R ax = vix - vcx, ay = viy - vcy, az = viz - vcz;
+    const R vcr = ch_sqrt(ax * ax + ay * ay + az * az);
+    R up = R(1) - uz * uz;
+    const R uperp = ch_sqrt(up > R(0) ? up : R(0));
+    R sph, cph;
+    ch_sincos2pi(unitR<R>(b.w), &sph, &cph);
+    const R ux = uperp * cph, uy = uperp * sph;
+    const R costht = vrr > R(0) ? rz / vrr : R(1);
+    R st2 = R(1) - costht * costht;
+    const R sintht = ch_sqrt(st2 > R(0) ? st2 : R(0));
+    R cosphi = R(1), sinphi = R(0);
+    if (vrr * sintht > R(0)) {
+      cosphi = rx / (vrr * sintht);
+      sinphi = ry / (vrr * sintht);
+    }
+    const R ux1 = uz * sintht + ux * costht, uy1 = uy, uz1 = uz * costht - ux * sintht;
+    const R ux2 = ux1 * cosphi - uy1 * sinphi, uy2 = ux1 * sinphi + uy1 * cosphi, uz2 = uz1;
+    const R vfx = vcx + vcr * ux2, vfy = vcy + vcr * uy2, vfz = vcz + vcr * uz2;
+    const R vfr = ch_sqrt(vfx * vfx + vfy * vfy + vfz * vfz);
+    if (vfr / R(c.viTr) > R(10)) {
+      ++*refused;  // src/particles.c:597-606
+    } else {
+      v[0] = vfx; v[1] = vfy; v[2] = vfz;
+      ++*ncol;
+    }
+  } else {
+    ++*refused;  // 64 proposals without acceptance
+  }
+  // the next event's waiting time
+  ++e;
+  it = 0;
+  if (e >= CH_MAX_EVENTS) return true;
+  const R qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
+  const R lam = lscale * ch_gmean<R>(ch_sqrt(qx * qx + qy * qy + qz * qz), sig);
+  if (!(lam > R(0))) return true;
+  const U4 r0 = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (e << 8), c.run, c.seed_lo, c.seed_hi);
+  t += -ch_log(unitR<R>(r0.x)) / lam;
+  return !(t < R(1));
+}
+

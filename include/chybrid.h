@@ -276,7 +276,7 @@ typedef struct ch_run_info {
 /* Launch shape of the ensemble step; ch_batch_autotune picks it by timing. */
 typedef struct ch_batch_tuning {
   int32_t cluster;           /* CTAs per run in the potential solve: 1, 2, 4, 8 */
-  int32_t pass_ctas_per_sm;  /* persistent CTAs per SM of the ion pass: 1, 2  */
+  int32_t pass_ctas_per_sm;  /* persistent CTAs per SM of the deposit: 1 to 3 */
   double pass_ms;            /* measured for the chosen shape (autotune)      */
   double solve_ms;
 } ch_batch_tuning;

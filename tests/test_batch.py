@@ -95,7 +95,7 @@ def test_batch_autotune_restores_state(chy):
         b.step(0, 2)
         before = [(b.phi(r), b.download(r)) for r in range(len(params))]
         t = b.autotune()
-        assert t["cluster"] in (1, 2, 4, 8) and t["pass_ctas_per_sm"] in (1, 2)
+        assert t["cluster"] in (1, 2, 4, 8) and t["pass_ctas_per_sm"] in (1, 2, 3)
         assert t["pass_ms"] > 0 and t["solve_ms"] > 0
         after = [(b.phi(r), b.download(r)) for r in range(len(params))]
         for (pa, (xa, va)), (pb, (xb, vb)) in zip(before, after):
