@@ -126,7 +126,8 @@ class AdjointTiming(C.Structure):
 class Profile(C.Structure):
     _fields_ = [("pass_ms", C.c_double), ("pass_calls", C.c_int64), ("solve_ms", C.c_double),
                 ("solve_calls", C.c_int64), ("sort_ms", C.c_double), ("sort_calls", C.c_int64),
-                ("moments_ms", C.c_double), ("moments_calls", C.c_int64), ("launches", C.c_int64)]
+                ("moments_ms", C.c_double), ("moments_calls", C.c_int64), ("launches", C.c_int64),
+                ("deposit_ms", C.c_double), ("deposit_calls", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -619,7 +619,7 @@ extern "C" ch_status ch_adjoint_create(const ch_params* p, int64_t np, const ch_
   if (e == cudaSuccess) e = cudaEventCreate(&a->e1);
   GridDesc& g = a->g;
   g.Nx = p->Nx; g.Ny = p->Ny; g.Nz = p->Nz;
-  g.N = (int64_t)p->Nx * p->Ny * p->Nz;
+  ch_grid_finish(g);
   g.x0 = p->x0; g.y0 = p->y0; g.z0 = p->z0;
   g.Lx = p->x1 - p->x0; g.Ly = p->y1 - p->y0; g.Lz = p->z1 - p->z0;
   g.dx = g.Lx / p->Nx; g.dy = g.Ly / p->Ny; g.dz = g.Lz / p->Nz;

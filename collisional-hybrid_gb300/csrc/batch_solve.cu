@@ -88,7 +88,8 @@ __device__ __forceinline__ void own_range(int64_t N, int rank, int C, int64_t* l
 // Full weighting (see k_restrict) of fine vector `in` at coarse node c.
 __device__ __forceinline__ float restrict_at(const GridDesc& gf, const GridDesc& gc, int hx, int hy, int hz,
                                              const float* in, int64_t c) {
-  const int I = (int)(c % gc.Nx), J = (int)((c / gc.Nx) % gc.Ny), K = (int)(c / ((int64_t)gc.Nx * gc.Ny));
+  int I, J, K;
+  ch_ijk(gc, c, I, J, K);
   const int i0 = hx ? 2 * I : I, j0 = hy ? 2 * J : J, k0 = hz ? 2 * K : K;
   float acc = 0.0f;
   for (int dk = -hz; dk <= hz; ++dk) {
@@ -110,7 +111,8 @@ __device__ __forceinline__ float restrict_at(const GridDesc& gf, const GridDesc&
 // Trilinear prolongation (see k_prolong_add) of coarse `ec` at fine node c.
 __device__ __forceinline__ float prolong_at(const GridDesc& gf, const GridDesc& gc, int hx, int hy, int hz,
                                             const float* ec, int64_t c) {
-  const int i = (int)(c % gf.Nx), j = (int)((c / gf.Nx) % gf.Ny), k = (int)(c / ((int64_t)gf.Nx * gf.Ny));
+  int i, j, k;
+  ch_ijk(gf, c, i, j, k);
   int I0, I1, J0, J1, K0, K1;
   float wi1, wj1, wk1;
   if (hx) { I0 = i >> 1; I1 = (i & 1) ? ch_wrap(I0 + 1, gc.Nx) : I0; wi1 = (i & 1) ? 0.5f : 0.0f; }
@@ -330,7 +332,8 @@ __global__ void __launch_bounds__(256) k_batch_solve(const BSolveRun* runs) {
   // ---- node field of the next push, premultiplied by (q/m) dt/2
   OWN(ce, N) {
     const int64_t c = ce;
-    const int i = (int)(c % g.Nx), j = (int)((c / g.Nx) % g.Ny), k = (int)(c / ((int64_t)g.Nx * g.Ny));
+    int i, j, k;
+    ch_ijk(g, c, i, j, k);
     const int ip = i + 1 == g.Nx ? 0 : i + 1, im = i == 0 ? g.Nx - 1 : i - 1;
     const int jp = j + 1 == g.Ny ? 0 : j + 1, jm = j == 0 ? g.Ny - 1 : j - 1;
     const int kp = k + 1 == g.Nz ? 0 : k + 1, km = k == 0 ? g.Nz - 1 : k - 1;

@@ -155,6 +155,8 @@ static ch_status validate(const ch_params* p) {
   if (p->Nx < 3 || p->Ny < 3 || p->Nz < 3)
     return ch_fail(CH_ERR_ARG, "grid %dx%dx%d: each axis needs at least 3 nodes for the 19-point stencil", p->Nx,
                    p->Ny, p->Nz);
+  if ((int64_t)p->Nx * p->Ny * p->Nz >= (1LL << 31))
+    return ch_fail(CH_ERR_ARG, "grid %dx%dx%d: at most 2^31-1 nodes", p->Nx, p->Ny, p->Nz);
   if (p->Nx > CH_MAX_NX || p->Ny > CH_MAX_NY || p->Nz > CH_MAX_NZ)
     return ch_fail(CH_ERR_ARG, "grid %dx%dx%d exceeds %dx%dx%d", p->Nx, p->Ny, p->Nz, CH_MAX_NX, CH_MAX_NY,
                    CH_MAX_NZ);
@@ -182,7 +184,7 @@ static ch_status validate(const ch_params* p) {
 static GridDesc make_grid(const ch_params& p) {
   GridDesc g;
   g.Nx = p.Nx; g.Ny = p.Ny; g.Nz = p.Nz;
-  g.N = (int64_t)p.Nx * p.Ny * p.Nz;
+  ch_grid_finish(g);
   g.x0 = p.x0; g.y0 = p.y0; g.z0 = p.z0;
   g.Lx = p.x1 - p.x0; g.Ly = p.y1 - p.y0; g.Lz = p.z1 - p.z0;
   g.dx = g.Lx / p.Nx; g.dy = g.Ly / p.Ny; g.dz = g.Lz / p.Nz;
@@ -462,7 +464,12 @@ static ch_status run_pass(ch_ctx* c, int phases, int64_t step, ch_step_info* inf
   }
   const int nb = launch_pass(c->mixed, phases, k, c->P, c->M, c->E64, c->E32, c->phi, c->acc, (double)Nc, c->sbar,
                              c->cnt, c->part, c->starts, hist, c->sms, c->stream);
+  const double before = c->pr.pass_ms;
   prof_end(c, &c->pr.pass_ms, &c->pr.pass_calls);
+  if (phases == PH_DEPOSIT && c->prof) {
+    c->pr.deposit_ms += c->pr.pass_ms - before;
+    c->pr.deposit_calls += 1;
+  }
   if (push) {
     launch_reduce_partials(c->part, nb, 2, c->red, c->stream);
     CH_CUDA_OK(cudaMemcpyAsync(c->hred, c->red, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));

@@ -211,7 +211,7 @@ static ch_status build_levels(ch_batch* b, int r, BSolveRun& S) {
     GridDesc c = f;
     c.Nx = ax ? f.Nx / 2 : f.Nx; c.Ny = ay ? f.Ny / 2 : f.Ny; c.Nz = az ? f.Nz / 2 : f.Nz;
     c.dx = ax ? 2 * f.dx : f.dx; c.dy = ay ? 2 * f.dy : f.dy; c.dz = az ? 2 * f.dz : f.dz;
-    c.N = (int64_t)c.Nx * c.Ny * c.Nz;
+    ch_grid_finish(c);
     hx[L - 1] = ax; hy[L - 1] = ay; hz[L - 1] = az;
     gl[L++] = c;
   }
@@ -266,7 +266,7 @@ extern "C" ch_status ch_batch_create(const ch_params* runs, const int64_t* np, i
     const ch_params& q = runs[r];
     GridDesc g;
     g.Nx = q.Nx; g.Ny = q.Ny; g.Nz = q.Nz;
-    g.N = (int64_t)q.Nx * q.Ny * q.Nz;
+    ch_grid_finish(g);
     g.x0 = q.x0; g.y0 = q.y0; g.z0 = q.z0;
     g.Lx = q.x1 - q.x0; g.Ly = q.y1 - q.y0; g.Lz = q.z1 - q.z0;
     g.dx = g.Lx / q.Nx; g.dy = g.Ly / q.Ny; g.dz = g.Lz / q.Nz;

@@ -30,9 +30,49 @@ struct GridDesc {
   double x0, y0, z0;
   double Lx, Ly, Lz;
   double dx, dy, dz;
+  // exact division of node indices by Nx and Nx*Ny (see ch_ijk)
+  uint32_t mx, sx1, sx2, mxy, sxy1, sxy2;
 };
 
+// Multiplier and shifts for the exact unsigned division n / d of any 32-bit
+// n by a constant d (Granlund & Montgomery, "Division by invariant integers
+// using multiplication", PLDI 1994, Fig. 4.1): l = ceil(log2 d),
+// m = floor(2^32 (2^l - d) / d) + 1, t = mulhi(m, n),
+// n / d = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0).
+__host__ inline void ch_magic(uint32_t d, uint32_t* m, uint32_t* s1, uint32_t* s2) {
+  uint32_t l = 0;
+  while (l < 32 && (1ull << l) < d) ++l;
+  *m = (uint32_t)((((1ull << l) - d) << 32) / d + 1);
+  *s1 = l < 1 ? l : 1;
+  *s2 = l > 0 ? l - 1 : 0;
+}
+__device__ __forceinline__ uint32_t ch_divu(uint32_t n, uint32_t m, uint32_t s1, uint32_t s2) {
+  const uint32_t t = __umulhi(m, n);
+  return (t + ((n - t) >> s1)) >> s2;
+}
+
+// Node count and division constants of a grid whose Nx, Ny, Nz are set.
+__host__ inline void ch_grid_finish(GridDesc& g) {
+  g.N = (int64_t)g.Nx * g.Ny * g.Nz;
+  ch_magic((uint32_t)g.Nx, &g.mx, &g.sx1, &g.sx2);
+  ch_magic((uint32_t)g.Nx * (uint32_t)g.Ny, &g.mxy, &g.sxy1, &g.sxy2);
+}
+
+// (i, j, k) of natural index c (N < 2^32).
+__device__ __forceinline__ void ch_ijk(const GridDesc& g, int64_t c, int& i, int& j, int& k) {
+  const uint32_t u = (uint32_t)c;
+  const uint32_t q = ch_divu(u, g.mx, g.sx1, g.sx2);
+  const uint32_t r = ch_divu(u, g.mxy, g.sxy1, g.sxy2);
+  i = (int)(u - q * (uint32_t)g.Nx);
+  k = (int)r;
+  j = (int)(q - r * (uint32_t)g.Ny);
+}
+
+// i mod n in [0, n); one compare for the usual |i| < 2n.
 __host__ __device__ inline int ch_wrap(int i, int n) {
+  if (i >= 0 && i < n) return i;
+  if (i < 0 && i >= -n) return i + n;
+  if (i >= n && i < 2 * n) return i - n;
   i %= n;
   return i < 0 ? i + n : i;
 }

@@ -111,7 +111,7 @@ extern "C" ch_status ch_collect_moments_noalloc(const ch_params* p, const double
   if (rc) return rc;
   GridDesc g;
   g.Nx = p->Nx; g.Ny = p->Ny; g.Nz = p->Nz;
-  g.N = N;
+  ch_grid_finish(g);
   g.x0 = p->x0; g.y0 = p->y0; g.z0 = p->z0;
   g.Lx = p->x1 - p->x0; g.Ly = p->y1 - p->y0; g.Lz = p->z1 - p->z0;
   g.dx = g.Lx / p->Nx; g.dy = g.Ly / p->Ny; g.dz = g.Lz / p->Nz;

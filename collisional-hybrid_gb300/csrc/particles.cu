@@ -219,7 +219,8 @@ __global__ void k_mixed_to_aos(GridDesc g, MixParticles P, double4_32a* __restri
 __global__ void k_node_efield_f64(GridDesc g, const double* __restrict__ phi, double* __restrict__ E) {
   const int64_t N = g.N;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(c % g.Nx), j = (int)((c / g.Nx) % g.Ny), k = (int)(c / ((int64_t)g.Nx * g.Ny));
+    int i, j, k;
+    ch_ijk(g, c, i, j, k);
     const int ip = i + 1 == g.Nx ? 0 : i + 1, im = i == 0 ? g.Nx - 1 : i - 1;
     const int jp = j + 1 == g.Ny ? 0 : j + 1, jm = j == 0 ? g.Ny - 1 : j - 1;
     const int kp = k + 1 == g.Nz ? 0 : k + 1, km = k == 0 ? g.Nz - 1 : k - 1;
@@ -234,7 +235,8 @@ __global__ void k_node_efield_f64(GridDesc g, const double* __restrict__ phi, do
 __global__ void k_node_efield_mixed(GridDesc g, float tscale, const double* __restrict__ phi, float4* __restrict__ E) {
   const int64_t N = g.N;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(c % g.Nx), j = (int)((c / g.Nx) % g.Ny), k = (int)(c / ((int64_t)g.Nx * g.Ny));
+    int i, j, k;
+    ch_ijk(g, c, i, j, k);
     const int ip = i + 1 == g.Nx ? 0 : i + 1, im = i == 0 ? g.Nx - 1 : i - 1;
     const int jp = j + 1 == g.Ny ? 0 : j + 1, jm = j == 0 ? g.Ny - 1 : j - 1;
     const int kp = k + 1 == g.Nz ? 0 : k + 1, km = k == 0 ? g.Nz - 1 : k - 1;

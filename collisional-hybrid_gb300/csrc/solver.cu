@@ -317,7 +317,8 @@ __global__ void k_rhs(GridDesc g, int rhs_type, double R00, double R01, double R
       b[c] = scal[S_MEAN] * (2.0 * g.dx * g.dy * g.dz / det);
       continue;
     }
-    const int i = (int)(c % g.Nx), j = (int)((c / g.Nx) % g.Ny), k = (int)(c / ((int64_t)g.Nx * g.Ny));
+    int i, j, k;
+    ch_ijk(g, c, i, j, k);
     if (rhs_type == CH_RHS_SINUSOIDAL) {
       const double x = ((double)i + 0.5) * g.dx, y = ((double)j + 0.5) * g.dy, z = ((double)k + 0.5) * g.dz;
       const double val = cos(2 * CH_PI * x) * cos(2 * CH_PI * y) * cos(2 * CH_PI * z);
@@ -361,7 +362,8 @@ template <typename T>
 __global__ void k_restrict(GridDesc gf, GridDesc gc, int hx, int hy, int hz, const T* __restrict__ in,
                            T* __restrict__ out, T scale) {
   GRID_LOOP(c, gc.N) {
-    const int I = (int)(c % gc.Nx), J = (int)((c / gc.Nx) % gc.Ny), K = (int)(c / ((int64_t)gc.Nx * gc.Ny));
+    int I, J, K;
+    ch_ijk(gc, c, I, J, K);
     const int i0 = hx ? 2 * I : I, j0 = hy ? 2 * J : J, k0 = hz ? 2 * K : K;
     T acc = T(0);
     for (int dk = -hz; dk <= hz; ++dk) {
@@ -386,7 +388,8 @@ template <typename T>
 __global__ void k_prolong_add(GridDesc gf, GridDesc gc, int hx, int hy, int hz, const T* __restrict__ ec,
                               T* __restrict__ xf) {
   GRID_LOOP(c, gf.N) {
-    const int i = (int)(c % gf.Nx), j = (int)((c / gf.Nx) % gf.Ny), k = (int)(c / ((int64_t)gf.Nx * gf.Ny));
+    int i, j, k;
+    ch_ijk(gf, c, i, j, k);
     int I0, I1, J0, J1, K0, K1;
     T wi1, wj1, wk1;
     if (hx) { I0 = i >> 1; I1 = (i & 1) ? ch_wrap(I0 + 1, gc.Nx) : I0; wi1 = (i & 1) ? T(0.5) : T(0); }
@@ -515,7 +518,7 @@ ch_status PotentialSolver::mg_build(MGHier<T>& h) {
     GridDesc c = f;
     c.Nx = hx ? f.Nx / 2 : f.Nx; c.Ny = hy ? f.Ny / 2 : f.Ny; c.Nz = hz ? f.Nz / 2 : f.Nz;
     c.dx = hx ? 2 * f.dx : f.dx; c.dy = hy ? 2 * f.dy : f.dy; c.dz = hz ? 2 * f.dz : f.dz;
-    c.N = (int64_t)c.Nx * c.Ny * c.Nz;
+    ch_grid_finish(c);
     h.hx[L - 1] = hx; h.hy[L - 1] = hy; h.hz[L - 1] = hz;
     // the full operator is finite-difference scaled (averaged residuals);
     // the Laplacian of src/lhs.c:205-207 is finite-volume scaled

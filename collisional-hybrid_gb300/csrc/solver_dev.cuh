@@ -13,9 +13,8 @@ struct Nb {
 };
 
 __device__ __forceinline__ Nb neighbours(const GridDesc& g, int64_t c) {
-  const int i = (int)(c % g.Nx);
-  const int j = (int)((c / g.Nx) % g.Ny);
-  const int k = (int)(c / ((int64_t)g.Nx * g.Ny));
+  int i, j, k;
+  ch_ijk(g, c, i, j, k);
   const int ip = i + 1 == g.Nx ? 0 : i + 1, im = i == 0 ? g.Nx - 1 : i - 1;
   const int jp = j + 1 == g.Ny ? 0 : j + 1, jm = j == 0 ? g.Ny - 1 : j - 1;
   const int kp = k + 1 == g.Nz ? 0 : k + 1, km = k == 0 ? g.Nz - 1 : k - 1;

@@ -205,6 +205,8 @@ typedef struct ch_profile {
   double moments_ms;   /* fixed-point -> FP64 moment conversion */
   int64_t moments_calls;
   int64_t launches;    /* kernels launched by this library, all contexts */
+  double deposit_ms;   /* the deposit-only passes among pass_ms */
+  int64_t deposit_calls;
 } ch_profile;
 ch_status ch_set_profiling(ch_ctx* c, int32_t enable);
 ch_status ch_get_profile(ch_ctx* c, ch_profile* out);
