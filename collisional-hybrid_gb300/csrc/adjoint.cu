@@ -693,6 +693,7 @@ static StepConsts adj_consts(const ch_adjoint* a, const double* theta, int64_t s
   // stays far below the changes of a finite-difference step; densities up to
   // 8192 per node keep within the int64 range
   k.dep_scale = ldexp(1.0, 50);
+  ch_consts_finish(k);
   return k;
 }
 

@@ -309,6 +309,7 @@ static StepConsts consts(const ch_ctx* c, int64_t step) {
   k.run = p.run;
   k.step = (uint32_t)step;
   k.dep_scale = c->dep_scale;
+  ch_consts_finish(k);
   return k;
 }
 

@@ -171,6 +171,7 @@ static StepConsts run_consts(const ch_params& p, const GridDesc& g, double dep_s
   k.seed_hi = (uint32_t)(p.seed >> 32);
   k.run = p.run;
   k.dep_scale = dep_scale;
+  ch_consts_finish(k);
   return k;
 }
 

@@ -121,7 +121,46 @@ struct StepConsts {
   uint32_t seed_lo, seed_hi, run, step;
   // deposit
   double dep_scale;     // fixed-point scale 2^s
+  // FP32 copies of the constants above (ch_consts_finish), rounded once on
+  // the host: the FP32 kernels read them as they are, so no FP64 arithmetic
+  // or conversion (a slow pipe on this part) runs inside their loops
+  struct {
+    float dtx, dty, dtz;        // dt / dx: cells per unit velocity
+    float t[3], s[3], pE0[3];   // pE0 = E0 tscale
+    float vnT, vn0[3], mi, mn, viTr, m1;
+    float nn_center, nn_sigma, nn_floor, dep_scale;
+  } f;
 };
+
+// Fills StepConsts::f from the FP64 fields; called after every change of them.
+inline void ch_consts_finish(StepConsts& k) {
+  k.f.dtx = (float)(k.dt / k.g.dx);
+  k.f.dty = (float)(k.dt / k.g.dy);
+  k.f.dtz = (float)(k.dt / k.g.dz);
+  for (int d = 0; d < 3; ++d) {
+    k.f.t[d] = (float)k.t[d];
+    k.f.s[d] = (float)k.s[d];
+    k.f.pE0[d] = (float)(k.E0[d] * k.tscale);
+    k.f.vn0[d] = (float)k.vn0[d];
+  }
+  k.f.vnT = (float)k.vnT;
+  k.f.mi = (float)k.mi;
+  k.f.mn = (float)k.mn;
+  k.f.viTr = (float)k.viTr;
+  k.f.m1 = (float)k.m1;
+  k.f.nn_center = (float)k.nn_center;
+  k.f.nn_sigma = (float)k.nn_sigma;
+  k.f.nn_floor = (float)k.nn_floor;
+  k.f.dep_scale = (float)k.dep_scale;
+}
+
+// The constant in the kernel's precision: the FP64 field, or its FP32 copy.
+template <typename R>
+__host__ __device__ __forceinline__ R ch_pick(double d, float f);
+template <>
+__host__ __device__ __forceinline__ double ch_pick<double>(double d, float) { return d; }
+template <>
+__host__ __device__ __forceinline__ float ch_pick<float>(double, float f) { return f; }
 
 // Device-side counters; every sum is integer so the result does not depend
 // on the order in which blocks finish.

@@ -605,12 +605,11 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
                                           unsigned& nref, int& bad) {
   const GridDesc& g = c.g;
   const int lane = threadIdx.x & 31;
-  const float dtx = (float)(c.dt / g.dx), dty = (float)(c.dt / g.dy), dtz = (float)(c.dt / g.dz);
-  const float vnTf = (float)c.vnT, vn0x = (float)c.vn0[0], vn0y = (float)c.vn0[1], vn0z = (float)c.vn0[2];
-  const float t0 = (float)c.t[0], t1 = (float)c.t[1], t2 = (float)c.t[2];
-  const float s0 = (float)c.s[0], s1 = (float)c.s[1], s2 = (float)c.s[2];
-  const float pE0x = (float)(c.E0[0] * c.tscale), pE0y = (float)(c.E0[1] * c.tscale),
-              pE0z = (float)(c.E0[2] * c.tscale);
+  const float dtx = c.f.dtx, dty = c.f.dty, dtz = c.f.dtz;
+  const float vnTf = c.f.vnT, vn0x = c.f.vn0[0], vn0y = c.f.vn0[1], vn0z = c.f.vn0[2];
+  const float t0 = c.f.t[0], t1 = c.f.t[1], t2 = c.f.t[2];
+  const float s0 = c.f.s[0], s1 = c.f.s[1], s2 = c.f.s[2];
+  const float pE0x = c.f.pE0[0], pE0y = c.f.pE0[1], pE0z = c.f.pE0[2];
   const bool cross = !(c.faithful & CH_FAITHFUL_D2);
   const bool move = (PH & PH_MOVE) && !(c.faithful & CH_FAITHFUL_D5);
   const bool collide = (PH & PH_PUSH) && c.collide;
@@ -805,7 +804,7 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
         const bool slow = fabsf(v[0]) >= CH_TILE_VMAX || fabsf(v[1]) >= CH_TILE_VMAX || fabsf(v[2]) >= CH_TILE_VMAX;
         const bool valid = go && finite && inbox && !slow;
         if (go && finite && !valid)
-          deposit_cic<float>(g, acc, i, j, k, p.x, p.y, p.z, v[0], v[1], v[2], (float)c.dep_scale);
+          deposit_cic<float>(g, acc, i, j, k, p.x, p.y, p.z, v[0], v[1], v[2], c.f.dep_scale);
         sh.st_key[sidx] = valid ? key0 : -1;
         sh.st_ox[sidx] = p.x; sh.st_oy[sidx] = p.y; sh.st_oz[sidx] = p.z;
         sh.st_vx[sidx] = v[0]; sh.st_vy[sidx] = v[1]; sh.st_vz[sidx] = v[2];
@@ -890,7 +889,7 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
             else if (inbox && !slow)
               tile_deposit_lane(sh, key, qp.x, qp.y, qp.z, qv[0], qv[1], qv[2]);
             else
-              deposit_cic<float>(g, acc, qi, qj, qk, qp.x, qp.y, qp.z, qv[0], qv[1], qv[2], (float)c.dep_scale);
+              deposit_cic<float>(g, acc, qi, qj, qk, qp.x, qp.y, qp.z, qv[0], qv[1], qv[2], c.f.dep_scale);
           }
           qhead += nq;
           // the re-queued entries are visible before the next round reads them

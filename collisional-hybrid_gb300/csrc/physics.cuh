@@ -62,9 +62,10 @@ __device__ __forceinline__ float ch_gmean<float>(float w, float sigma) {
 template <typename R>
 __device__ __forceinline__ R ch_neutral_density(const StepConsts& c, R x_abs) {
   if (c.nn_profile != CH_NN_GAUSSIAN_X) return R(1);
-  const R u = (x_abs - R(c.nn_center)) / R(c.nn_sigma);
+  const R u = (x_abs - ch_pick<R>(c.nn_center, c.f.nn_center)) / ch_pick<R>(c.nn_sigma, c.f.nn_sigma);
   const R v = ch_exp(R(-0.5) * u * u);
-  return v > R(c.nn_floor) ? v : R(c.nn_floor);
+  const R fl = ch_pick<R>(c.nn_floor, c.f.nn_floor);
+  return v > fl ? v : fl;
 }
 
 // Boris push (src/particles.c:374-447), E already includes the push scale.
@@ -100,10 +101,11 @@ __device__ __forceinline__ void ch_boris(const StepConsts& c, const R E[3], R v[
 #define CH_MAX_EVENTS 32
 template <typename R>
 __device__ __noinline__ int ch_collide(const StepConsts& c, uint32_t id, R lscale, R v[3], unsigned* refused) {
-  const R sig = R(c.vnT);
-  const R vn0x = R(c.vn0[0]), vn0y = R(c.vn0[1]), vn0z = R(c.vn0[2]);
-  const R m1 = R(c.m1);
-  const R mi = R(c.mi), mn = R(c.mn), M = mn + mi;
+  const R sig = ch_pick<R>(c.vnT, c.f.vnT);
+  const R vn0x = ch_pick<R>(c.vn0[0], c.f.vn0[0]), vn0y = ch_pick<R>(c.vn0[1], c.f.vn0[1]),
+          vn0z = ch_pick<R>(c.vn0[2], c.f.vn0[2]);
+  const R m1 = ch_pick<R>(c.m1, c.f.m1);
+  const R mi = ch_pick<R>(c.mi, c.f.mi), mn = ch_pick<R>(c.mn, c.f.mn), M = mn + mi;
   R t = R(0);
   int ncol = 0;
   for (uint32_t e = 0; e < CH_MAX_EVENTS; ++e) {
@@ -175,7 +177,7 @@ __device__ __noinline__ int ch_collide(const StepConsts& c, uint32_t id, R lscal
     const R ux2 = ux1 * cosphi - uy1 * sinphi, uy2 = ux1 * sinphi + uy1 * cosphi, uz2 = uz1;
     const R vfx = vcx + vcr * ux2, vfy = vcy + vcr * uy2, vfz = vcz + vcr * uz2;
     const R vfr = ch_sqrt(vfx * vfx + vfy * vfy + vfz * vfz);
-    if (vfr / R(c.viTr) > R(10)) { ++*refused; continue; }
+    if (vfr / ch_pick<R>(c.viTr, c.f.viTr) > R(10)) { ++*refused; continue; }
     v[0] = vfx; v[1] = vfy; v[2] = vfz;
     ++ncol;
   }
@@ -193,10 +195,11 @@ __device__ __noinline__ int ch_collide(const StepConsts& c, uint32_t id, R lscal
 template <typename R>
 __device__ __forceinline__ bool ch_collide_round(const StepConsts& c, uint32_t id, R lscale, R v[3], R& t,
                                                  uint32_t& e, uint32_t& it, unsigned* ncol, unsigned* refused) {
-  const R sig = R(c.vnT);
-  const R vn0x = R(c.vn0[0]), vn0y = R(c.vn0[1]), vn0z = R(c.vn0[2]);
-  const R m1 = R(c.m1);
-  const R mi = R(c.mi), mn = R(c.mn), M = mn + mi;
+  const R sig = ch_pick<R>(c.vnT, c.f.vnT);
+  const R vn0x = ch_pick<R>(c.vn0[0], c.f.vn0[0]), vn0y = ch_pick<R>(c.vn0[1], c.f.vn0[1]),
+          vn0z = ch_pick<R>(c.vn0[2], c.f.vn0[2]);
+  const R m1 = ch_pick<R>(c.m1, c.f.m1);
+  const R mi = ch_pick<R>(c.mi, c.f.mi), mn = ch_pick<R>(c.mn, c.f.mn), M = mn + mi;
   const R vix = v[0], viy = v[1], viz = v[2];
   const R wx = vix - vn0x, wy = viy - vn0y, wz = viz - vn0z;
   const R w = ch_sqrt(wx * wx + wy * wy + wz * wz);
@@ -252,7 +255,7 @@ __device__ __forceinline__ bool ch_collide_round(const StepConsts& c, uint32_t i
     const R ux2 = ux1 * cosphi - uy1 * sinphi, uy2 = ux1 * sinphi + uy1 * cosphi, uz2 = uz1;
     const R vfx = vcx + vcr * ux2, vfy = vcy + vcr * uy2, vfz = vcz + vcr * uz2;
     const R vfr = ch_sqrt(vfx * vfx + vfy * vfy + vfz * vfz);
-    if (vfr / R(c.viTr) > R(10)) {
+    if (vfr / ch_pick<R>(c.viTr, c.f.viTr) > R(10)) {
       ++*refused;  // src/particles.c:597-606
     } else {
       v[0] = vfx; v[1] = vfy; v[2] = vfz;
