@@ -399,16 +399,22 @@ __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, 
 // in [2^23, 2^24), where floats are the integers, so the bits of the sum are
 // rint(x) + CH_RNI_BIAS (the conversion unit runs at a fraction of the rate).
 #define CH_RNI_BIAS 0x4B400000
+// rni_fma(a, b): the same for the exact product a b, rounded once (one FMA).
 __device__ __forceinline__ int rni_biased(float x) { return __float_as_int(__fadd_rn(x, 12582912.0f)); }
 __device__ __forceinline__ int rni(float x) { return rni_biased(x) - CH_RNI_BIAS; }
+__device__ __forceinline__ int rni_fma(float a, float b) { return __float_as_int(__fmaf_rn(a, b, 12582912.0f)); }
 
 #define CH_PUSH_CTAS 4          // CTAs per SM of a pass without the deposit
 #define CH_DEP_CTAS 3           // CTAs per SM of a pass with the deposit (61 KB each when deposit-only)
-#define CH_TILE_QCAP 512       // ring of deferred colliding ions (power of two, >= 2 x threads)
+#define CH_TILE_QCAP 512       // deferred colliding ions: one ring of CH_TILE_QW per warp
+#define CH_TILE_QW (CH_TILE_QCAP / 8)
+static_assert(CH_TILE_QW >= 64 && (CH_TILE_QW & (CH_TILE_QW - 1)) == 0,
+              "a warp ring holds 31 pending + 32 new entries and is indexed modulo its size");
 #define CH_TILE_ROUNDS 3       // key groups a warp reduces before per-lane adds
 
 #define CH_TILE_K 4            // consecutive slots one thread deposits together
 #define CH_TILE_BATCH (256 * CH_TILE_K)
+#define CH_DEP_RW 256          // ring of displaced ions per warp (31 waiting + 128 of a chunk fit)
 
 // Shared memory of one CTA of the tiled pass: [push part][header][deposit
 // part].  A pass with the push allocates from the start; a deposit-only pass
@@ -420,6 +426,7 @@ struct TileShared {
   // Ions whose first collision event falls inside the step are queued here
   // after the Boris push and finished (collide, move, deposit) together, so
   // the long collision code runs on full warps instead of one lane in 40.
+  // Warp w owns entries [w CH_TILE_QW, (w + 1) CH_TILE_QW) as a ring.
   float4 q_pos[CH_TILE_QCAP];   // offsets + packed cell, before the move
   float4 q_vel[CH_TILE_QCAP];   // velocity after the push, rate scale in w
   uint32_t q_ip[CH_TILE_QCAP];
@@ -429,22 +436,10 @@ struct TileShared {
   // ---- header
   alignas(16) uint32_t rowbeg[TY * TZ];
   uint32_t pre[TY * TZ + 1];
-  unsigned qn;                  // enqueued in this brick (monotone; slot = qn mod CH_TILE_QCAP)
-  unsigned ov_n;
   // ---- deposit part
-  // One batch of CH_TILE_BATCH ions staged between the push and the deposit:
-  // box key of the ion's cell (-1: nothing to deposit here), offsets and
-  // velocity.  Thread t deposits slots CH_TILE_K t .. CH_TILE_K t + K-1.
-  alignas(16) int st_key[CH_TILE_BATCH];
-  alignas(16) float st_ox[CH_TILE_BATCH];
-  alignas(16) float st_oy[CH_TILE_BATCH];
-  alignas(16) float st_oz[CH_TILE_BATCH];
-  alignas(16) float st_vx[CH_TILE_BATCH];
-  alignas(16) float st_vy[CH_TILE_BATCH];
-  alignas(16) float st_vz[CH_TILE_BATCH];
-  uint16_t ov_idx[CH_TILE_BATCH];  // staged slots outside their thread's cell, added one per thread
-  unsigned acc_lo[4][BNODES];  // 64-bit fixed-point sums at the tile scale as
-  int acc_hi[4][BNODES];       // lo + hi * 2^32, carried exactly (order-free)
+  uint32_t d_ip[8 * CH_DEP_RW];  // per warp: ring of displaced ions (indices into the ion arrays)
+  unsigned acc_lo[4][BNODES];    // 64-bit fixed-point sums at the tile scale as
+  int acc_hi[4][BNODES];         // lo + hi * 2^32, carried exactly (order-free)
 };
 
 template <int PH>
@@ -453,7 +448,7 @@ constexpr size_t tile_smem_skip() {  // bytes of TileShared a launch of PH does 
 }
 template <int PH>
 constexpr size_t tile_smem_bytes() {
-  return (PH & PH_DEPOSIT) ? sizeof(TileShared) - tile_smem_skip<PH>() : offsetof(TileShared, st_key);
+  return (PH & PH_DEPOSIT) ? sizeof(TileShared) - tile_smem_skip<PH>() : offsetof(TileShared, d_ip);
 }
 // The TileShared view of a launch's dynamic shared memory: for a
 // deposit-only launch the allocation starts at the header, and the push part
@@ -484,102 +479,12 @@ __device__ __forceinline__ void tile_deposit_lane(TileShared& sh, int node, floa
 #pragma unroll
   for (int cn = 0; cn < 8; ++cn) {
     const int nd = node + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
+    // (v 2^19) w is v (w 2^19) exactly: the scale is a power of two
     const float wf = w[cn] * CH_TILE_FSCALE;
-    shared_add64(&sh.acc_lo[0][nd], &sh.acc_hi[0][nd], rni(w[cn] * CH_TILE_DSCALE));
-    shared_add64(&sh.acc_lo[1][nd], &sh.acc_hi[1][nd], rni(vx * wf));
-    shared_add64(&sh.acc_lo[2][nd], &sh.acc_hi[2][nd], rni(vy * wf));
-    shared_add64(&sh.acc_lo[3][nd], &sh.acc_hi[3][nd], rni(vz * wf));
-  }
-}
-
-// Deposit of one staged batch.  Thread t sums the 32 fixed-point
-// contributions of its CH_TILE_K consecutive slots that share the cell of its
-// first valid slot (in cell-sorted ions, usually all of them) in registers;
-// a slot in another cell is added lane by lane.  The threads of a warp whose
-// first cells agree (one or two groups per sorted warp, up to
-// CH_TILE_ROUNDS) are then summed with integer warp reductions, lane q adding
-// sum q; the rest add their own sums.  Every contribution is rounded to an
-// integer before any addition, so the result does not depend on the order.
-__device__ __forceinline__ void tile_deposit_batch(TileShared& sh, int lane) {
-  const int t = threadIdx.x;
-  const int4 kq = reinterpret_cast<const int4*>(sh.st_key)[t];
-  const float4 X = reinterpret_cast<const float4*>(sh.st_ox)[t], Y = reinterpret_cast<const float4*>(sh.st_oy)[t],
-               Z = reinterpret_cast<const float4*>(sh.st_oz)[t], VX = reinterpret_cast<const float4*>(sh.st_vx)[t],
-               VY = reinterpret_cast<const float4*>(sh.st_vy)[t], VZ = reinterpret_cast<const float4*>(sh.st_vz)[t];
-  const int keys[4] = {kq.x, kq.y, kq.z, kq.w};
-  const float ox[4] = {X.x, X.y, X.z, X.w}, oy[4] = {Y.x, Y.y, Y.z, Y.w}, oz[4] = {Z.x, Z.y, Z.z, Z.w};
-  const float vx[4] = {VX.x, VX.y, VX.z, VX.w}, vy[4] = {VY.x, VY.y, VY.z, VY.w}, vz[4] = {VZ.x, VZ.y, VZ.z, VZ.w};
-  // the cell most of the thread's slots share (ties: the earliest)
-  int akey = -1, best = 0;
-#pragma unroll
-  for (int k = 0; k < CH_TILE_K; ++k) {
-    int n = 0;
-#pragma unroll
-    for (int q = 0; q < CH_TILE_K; ++q) n += (keys[q] == keys[k]) ? 1 : 0;
-    if (keys[k] >= 0 && n > best) { best = n; akey = keys[k]; }
-  }
-  unsigned a[32];
-#pragma unroll
-  for (int q = 0; q < 32; ++q) a[q] = 0u;
-  unsigned cnt = 0;
-#pragma unroll
-  for (int k = 0; k < CH_TILE_K; ++k) {
-    if (keys[k] < 0) continue;
-    if (keys[k] != akey) {
-      sh.ov_idx[atomicAdd(&sh.ov_n, 1u)] = (uint16_t)(CH_TILE_K * t + k);
-      continue;
-    }
-    ++cnt;
-    const float wxh = ox[k], wyh = oy[k], wzh = oz[k];
-    const float wxl = 1.0f - wxh, wyl = 1.0f - wyh, wzl = 1.0f - wzh;
-    const float w[8] = {wzl * wyl * wxl, wzl * wyl * wxh, wzl * wyh * wxl, wzl * wyh * wxh,
-                        wzh * wyl * wxl, wzh * wyl * wxh, wzh * wyh * wxl, wzh * wyh * wxh};
-    // (v 2^19) w equals v (w 2^19) exactly: the scale is a power of two
-    const float fx = vx[k] * CH_TILE_FSCALE, fy = vy[k] * CH_TILE_FSCALE, fz = vz[k] * CH_TILE_FSCALE;
-#pragma unroll
-    for (int cn = 0; cn < 8; ++cn) {
-      a[cn] += (unsigned)rni_biased(w[cn] * CH_TILE_DSCALE);
-      a[8 + cn] += (unsigned)rni_biased(fx * w[cn]);
-      a[16 + cn] += (unsigned)rni_biased(fy * w[cn]);
-      a[24 + cn] += (unsigned)rni_biased(fz * w[cn]);
-    }
-  }
-  const unsigned unbias = cnt * (unsigned)CH_RNI_BIAS;
-#pragma unroll
-  for (int q = 0; q < 32; ++q) a[q] -= unbias;  // exact sums, |sum| < 2^25
-  unsigned rem = __ballot_sync(0xffffffffu, akey >= 0);
-#pragma unroll 1
-  for (int round = 0; rem && round < CH_TILE_ROUNDS; ++round) {
-    const int leader = __ffs(rem) - 1;
-    const int lkey = __shfl_sync(0xffffffffu, akey, leader);
-    const bool mine = ((rem >> lane) & 1u) && akey == lkey;
-    rem &= ~__ballot_sync(0xffffffffu, mine);
-    int myval = 0;
-#pragma unroll
-    for (int q = 0; q < 32; ++q) {
-      const int sq = (int)__reduce_add_sync(0xffffffffu, mine ? a[q] : 0u);
-      myval = lane == q ? sq : myval;
-    }
-    const int cn = lane & 7, m = lane >> 3;
-    const int node = lkey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
-    if (myval != 0)
-      shared_add64(&sh.acc_lo[m][node], &sh.acc_hi[m][node], myval);
-  }
-  if ((rem >> lane) & 1u) {
-#pragma unroll
-    for (int q = 0; q < 32; ++q) {
-      const int cn = q & 7, m = q >> 3;
-      const int node = akey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
-      if (a[q] != 0u)
-        shared_add64(&sh.acc_lo[m][node], &sh.acc_hi[m][node], (long long)(int)a[q]);
-    }
-  }
-  __syncthreads();  // the overflow list is complete
-  const unsigned nov = sh.ov_n;
-  for (unsigned e = t; e < nov; e += blockDim.x) {
-    const int q = sh.ov_idx[e];
-    tile_deposit_lane(sh, sh.st_key[q], sh.st_ox[q], sh.st_oy[q], sh.st_oz[q], sh.st_vx[q], sh.st_vy[q],
-                      sh.st_vz[q]);
+    shared_add64(&sh.acc_lo[0][nd], &sh.acc_hi[0][nd], rni_fma(w[cn], CH_TILE_DSCALE) - CH_RNI_BIAS);
+    shared_add64(&sh.acc_lo[1][nd], &sh.acc_hi[1][nd], rni_fma(vx, wf) - CH_RNI_BIAS);
+    shared_add64(&sh.acc_lo[2][nd], &sh.acc_hi[2][nd], rni_fma(vy, wf) - CH_RNI_BIAS);
+    shared_add64(&sh.acc_lo[3][nd], &sh.acc_hi[3][nd], rni_fma(vz, wf) - CH_RNI_BIAS);
   }
 }
 
@@ -594,46 +499,268 @@ __device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, i
   return (dk * BY + dj) * BX + di;
 }
 
+// Deposit of one brick whose ions' cells are current (a deposit-only pass).
+// Warp w takes the chunks of 128 consecutive slots w, w + 8, ...; lane l the
+// 4 slots 4l .. 4l+3 of a chunk, read straight from global memory (the ions
+// of a cell are contiguous after a sort and mostly stay together between
+// sorts, so the 4 usually share a cell).  A lane sums the 32 fixed-point
+// contributions of its slots in the cell most of them share in registers;
+// the lanes of the warp whose cells agree (up to CH_TILE_ROUNDS groups) are
+// then summed with integer warp reductions, lane q adding sum q to the
+// brick.  Slots in another cell ("displaced": they moved since the last
+// sort) go to the warp's ring and are added lane by lane, 32 at a time.
+// Every contribution is rounded to an integer before any addition, so the
+// result does not depend on the order; no block barrier is needed.
+__device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepConsts& c, MixParticles P,
+                                                    unsigned long long* __restrict__ acc, uint32_t total, int bi0,
+                                                    int bj0, int bk0, int& bad) {
+  const GridDesc& g = c.g;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t* ring = sh.d_ip + warp * CH_DEP_RW;
+  const unsigned lt = (1u << lane) - 1u;
+  unsigned dh = 0, dt = 0;  // warp-uniform ring head / tail
+  // lanes l < n add the ring's next n displaced ions
+  auto drain = [&](unsigned n) {
+    if ((unsigned)lane < n) {
+      const uint32_t ip = ring[(dh + lane) & (CH_DEP_RW - 1)];
+      const float4 p = P.pos[ip], v = P.vel[ip];
+      const uint32_t cell = __float_as_uint(p.w);
+      bool inbox;  // checked when the ion was put in the ring
+      const int key = box_key(g, cell & (CH_MAX_NX - 1), (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
+                              cell >> (CH_PACK_BX + CH_PACK_BY), bi0, bj0, bk0, &inbox);
+      tile_deposit_lane(sh, key, p.x, p.y, p.z, v.x, v.y, v.z);
+    }
+    dh += n;
+    __syncwarp();  // the entries are read before later appends reuse them
+  };
+  for (uint32_t cb = (uint32_t)warp * 128u; cb < total; cb += (blockDim.x >> 5) * 128u) {
+    const uint32_t s0 = cb + 4u * (uint32_t)lane;
+    int r = 0;
+#pragma unroll
+    for (int st = 8; st > 0; st >>= 1)
+      if (r + st < TY * TZ && sh.pre[r + st] <= s0) r += st;
+    int keys[CH_TILE_K];
+    uint32_t ips[CH_TILE_K];
+    float ox[CH_TILE_K], oy[CH_TILE_K], oz[CH_TILE_K], vx[CH_TILE_K], vy[CH_TILE_K], vz[CH_TILE_K];
+#pragma unroll
+    for (int k = 0; k < CH_TILE_K; ++k) {
+      const uint32_t idx = s0 + k;
+      keys[k] = -1;
+      ips[k] = 0;
+      ox[k] = oy[k] = oz[k] = vx[k] = vy[k] = vz[k] = 0.0f;
+      if (idx < total) {
+        while (r + 1 < TY * TZ && sh.pre[r + 1] <= idx) ++r;  // rows may be empty
+        const uint32_t ip = sh.rowbeg[r] + (idx - sh.pre[r]);
+        const float4 p = P.pos[ip], v = P.vel[ip];
+        const uint32_t cell = __float_as_uint(p.w);
+        const int i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
+                  kz = cell >> (CH_PACK_BX + CH_PACK_BY);
+        const bool finite =
+            isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
+        bool inbox;
+        const int key = box_key(g, i, j, kz, bi0, bj0, bk0, &inbox);
+        const bool slow = fabsf(v.x) >= CH_TILE_VMAX || fabsf(v.y) >= CH_TILE_VMAX || fabsf(v.z) >= CH_TILE_VMAX;
+        if (!finite) {
+          bad = 1;
+        } else if (inbox && !slow) {
+          keys[k] = key;
+          ips[k] = ip;
+          ox[k] = p.x; oy[k] = p.y; oz[k] = p.z; vx[k] = v.x; vy[k] = v.y; vz[k] = v.z;
+        } else {
+          deposit_cic<float>(g, acc, i, j, kz, p.x, p.y, p.z, v.x, v.y, v.z, c.f.dep_scale);
+        }
+      }
+    }
+    // the cell most of the lane's slots share (ties: the earliest)
+    int akey = -1, best = 0;
+#pragma unroll
+    for (int k = 0; k < CH_TILE_K; ++k) {
+      int n = 0;
+#pragma unroll
+      for (int q = 0; q < CH_TILE_K; ++q) n += (keys[q] == keys[k]) ? 1 : 0;
+      if (keys[k] >= 0 && n > best) { best = n; akey = keys[k]; }
+    }
+    // displaced slots to the ring (at most 31 wait there, so 128 more fit)
+#pragma unroll
+    for (int k = 0; k < CH_TILE_K; ++k) {
+      const bool dsp = keys[k] >= 0 && keys[k] != akey;
+      const unsigned m = __ballot_sync(0xffffffffu, dsp);
+      if (dsp) ring[(dt + __popc(m & lt)) & (CH_DEP_RW - 1)] = ips[k];
+      dt += (unsigned)__popc(m);
+    }
+    unsigned a[32];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) a[q] = 0u;
+    unsigned cnt = 0;
+#pragma unroll
+    for (int k = 0; k < CH_TILE_K; ++k) {
+      if (keys[k] < 0 || keys[k] != akey) continue;
+      ++cnt;
+      const float wxh = ox[k], wyh = oy[k], wzh = oz[k];
+      const float wxl = 1.0f - wxh, wyl = 1.0f - wyh, wzl = 1.0f - wzh;
+      const float w[8] = {wzl * wyl * wxl, wzl * wyl * wxh, wzl * wyh * wxl, wzl * wyh * wxh,
+                          wzh * wyl * wxl, wzh * wyl * wxh, wzh * wyh * wxl, wzh * wyh * wxh};
+      // (v 2^19) w is v (w 2^19) exactly: the scale is a power of two
+      const float fx = vx[k] * CH_TILE_FSCALE, fy = vy[k] * CH_TILE_FSCALE, fz = vz[k] * CH_TILE_FSCALE;
+#pragma unroll
+      for (int cn = 0; cn < 8; ++cn) {
+        a[cn] += (unsigned)rni_fma(w[cn], CH_TILE_DSCALE);
+        a[8 + cn] += (unsigned)rni_fma(fx, w[cn]);
+        a[16 + cn] += (unsigned)rni_fma(fy, w[cn]);
+        a[24 + cn] += (unsigned)rni_fma(fz, w[cn]);
+      }
+    }
+    const unsigned unbias = cnt * (unsigned)CH_RNI_BIAS;
+#pragma unroll
+    for (int q = 0; q < 32; ++q) a[q] -= unbias;  // exact sums, |sum| < 2^25
+    unsigned rem = __ballot_sync(0xffffffffu, akey >= 0);
+#pragma unroll 1
+    for (int round = 0; rem && round < CH_TILE_ROUNDS; ++round) {
+      const int leader = __ffs(rem) - 1;
+      const int lkey = __shfl_sync(0xffffffffu, akey, leader);
+      const bool mine = ((rem >> lane) & 1u) && akey == lkey;
+      rem &= ~__ballot_sync(0xffffffffu, mine);
+      int myval = 0;
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const int sq = (int)__reduce_add_sync(0xffffffffu, mine ? a[q] : 0u);
+        myval = lane == q ? sq : myval;
+      }
+      const int cn = lane & 7, m = lane >> 3;
+      const int node = lkey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
+      if (myval != 0) shared_add64(&sh.acc_lo[m][node], &sh.acc_hi[m][node], myval);
+    }
+    if ((rem >> lane) & 1u) {
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const int cn = q & 7, m = q >> 3;
+        const int node = akey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
+        if (a[q] != 0u) shared_add64(&sh.acc_lo[m][node], &sh.acc_hi[m][node], (long long)(int)a[q]);
+      }
+    }
+    __syncwarp();  // the appended entries are visible to every lane
+    while (dt - dh >= 32u) drain(32u);
+  }
+  if (dt != dh) drain(dt - dh);
+}
+
+// Moves one ion by v dt (cell units), wraps it into the grid and repacks the
+// cell word.
+__device__ __forceinline__ void tile_move_ion(const StepConsts& c, float4& p, const float v[3], int& i, int& j,
+                                              int& k) {
+  const GridDesc& g = c.g;
+  float ox = p.x + v[0] * c.f.dtx, oy = p.y + v[1] * c.f.dty, oz = p.z + v[2] * c.f.dtz;
+  float fx = floorf(ox), fy = floorf(oy), fz = floorf(oz);
+  ox -= fx; oy -= fy; oz -= fz;
+  // a tiny negative offset rounds up to 1.0f: that point is the start of
+  // the next cell, so carry into it (as pack_mixed does)
+  if (ox >= 1.0f) { ox = 0.0f; fx += 1.0f; }
+  if (oy >= 1.0f) { oy = 0.0f; fy += 1.0f; }
+  if (oz >= 1.0f) { oz = 0.0f; fz += 1.0f; }
+  if (isfinite(fx) && isfinite(fy) && isfinite(fz)) {
+    i = ch_wrap(i + (int)fx, g.Nx); j = ch_wrap(j + (int)fy, g.Ny); k = ch_wrap(k + (int)fz, g.Nz);
+  }
+  const uint32_t cell = (uint32_t)i | ((uint32_t)j << CH_PACK_BX) | ((uint32_t)k << (CH_PACK_BX + CH_PACK_BY));
+  p = make_float4(ox, oy, oz, __uint_as_float(cell));
+}
+
+__device__ __forceinline__ float tile_gmean(const StepConsts& c, const float v[3]) {
+  const float qx = v[0] - c.f.vn0[0], qy = v[1] - c.f.vn0[1], qz = v[2] - c.f.vn0[2];
+  return ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), c.f.vnT);
+}
+
+// One drain round of the calling warp's ring of deferred ions (warp-uniform
+// head, tail and n <= 32): lane l < n advances entry head + l by one proposal
+// of its current collision event (with the scatter and the next waiting time
+// when the proposal is accepted).  Ions with further events go back to the
+// tail; the others are finished: velocity stored, moved and counted in the
+// new cell.  Needs no block barrier: only the warp touches its ring.
+template <int PH>
+__device__ __forceinline__ void tile_queue_round(TileShared& sh, const StepConsts& c, MixParticles P, uint32_t* hist,
+                                                 unsigned& head, unsigned& tail, unsigned n, unsigned long long& gsum,
+                                                 unsigned& ncol, unsigned& nref) {
+  const GridDesc& g = c.g;
+  const int lane = threadIdx.x & 31;
+  const unsigned wbase = (threadIdx.x >> 5) * CH_TILE_QW;
+  const bool move = (PH & PH_MOVE) && !(c.faithful & CH_FAITHFUL_D5);
+  const bool act = (unsigned)lane < n;
+  float4 qp = make_float4(0.f, 0.f, 0.f, 0.f), q4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  uint32_t qip = 0, qid = 0, st = 0;
+  float qtm = 0.0f;
+  if (act) {
+    const unsigned e = wbase + ((head + lane) & (CH_TILE_QW - 1));
+    qp = sh.q_pos[e];
+    q4 = sh.q_vel[e];
+    qip = sh.q_ip[e];
+    qid = sh.q_id[e];
+    qtm = sh.q_t[e];
+    st = sh.q_st[e];
+  }
+  __syncwarp();  // this round's entries are read before a re-queue reuses their slots
+  float qv[3] = {q4.x, q4.y, q4.z};
+  const float qsc = q4.w;
+  uint32_t qe = st & 0xFFu, qit = st >> 8;
+  bool done = false;
+  if (act) done = ch_collide_round<float>(c, qid, qsc, qv, qtm, qe, qit, &ncol, &nref);
+  const bool requeue = act && !done;
+  const unsigned rm = __ballot_sync(0xffffffffu, requeue);
+  if (requeue) {
+    const unsigned e = wbase + ((tail + __popc(rm & ((1u << lane) - 1u))) & (CH_TILE_QW - 1));
+    sh.q_pos[e] = qp;
+    sh.q_vel[e] = make_float4(qv[0], qv[1], qv[2], qsc);
+    sh.q_ip[e] = qip;
+    sh.q_id[e] = qid;
+    sh.q_t[e] = qtm;
+    sh.q_st[e] = qe | (qit << 8);
+  }
+  tail += (unsigned)__popc(rm);
+  head += n;
+  __syncwarp();  // re-queued entries are visible to the lanes that read them next
+  const bool fin = act && done;
+  int qi = 0, qj = 0, qk = 0;
+  if (fin) {
+    gsum += g_fixed(tile_gmean(c, qv));
+    P.vel[qip] = make_float4(qv[0], qv[1], qv[2], __uint_as_float(qid));
+    const uint32_t cell = __float_as_uint(qp.w);
+    qi = cell & (CH_MAX_NX - 1); qj = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1);
+    qk = cell >> (CH_PACK_BX + CH_PACK_BY);
+    if (move) {
+      tile_move_ion(c, qp, qv, qi, qj, qk);
+      P.pos[qip] = qp;
+    }
+  }
+  if (hist) {
+    const uint32_t rk = agg_inc(hist, (uint32_t)(((int64_t)qk * g.Ny + qj) * g.Nx + qi), fin);
+    if (fin && P.rank) P.rank[qip] = rk;
+  }
+}
+
 // One brick of the tiled pass: tile index `tile` of the run described by c
 // (starts, E, acc and hist are the run's own arrays; starts holds indices
-// into P).  Per-thread sums go to vsum / ncol / nref / bad.
-template <int PH>
+// into P).  Per-thread sums go to vsum / gsum / ncol / nref / bad.  Deferred
+// colliding ions wait in the warp's ring (head, tail); with CARRY the ring is
+// left as it is at the end of the brick (the caller drains it after its last
+// brick: possible when the finish of an ion does not use the brick, i.e.
+// without the deposit, and the run's constants do not change between
+// bricks), otherwise it is drained here.
+template <int PH, bool CARRY>
 __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, MixParticles P,
                                           const float4* __restrict__ E, const uint32_t* __restrict__ starts,
                                           unsigned long long* __restrict__ acc, float pscale, int shift_d,
-                                          int shift_f, uint32_t* hist, int tile, double (&vsum)[2], unsigned& ncol,
+                                          int shift_f, uint32_t* hist, int tile, double (&vsum)[2],
+                                          unsigned long long& gsum, unsigned& qhead, unsigned& qtail, unsigned& ncol,
                                           unsigned& nref, int& bad) {
+  static_assert(PH == PH_DEPOSIT || !(PH & PH_DEPOSIT), "the deposit has a launch of its own");
+  static_assert(!(CARRY && (PH & PH_DEPOSIT)), "a deposit pass has no deferred ions to carry");
   const GridDesc& g = c.g;
   const int lane = threadIdx.x & 31;
-  const float dtx = c.f.dtx, dty = c.f.dty, dtz = c.f.dtz;
-  const float vnTf = c.f.vnT, vn0x = c.f.vn0[0], vn0y = c.f.vn0[1], vn0z = c.f.vn0[2];
+  const unsigned wbase = (threadIdx.x >> 5) * CH_TILE_QW;
   const float t0 = c.f.t[0], t1 = c.f.t[1], t2 = c.f.t[2];
   const float s0 = c.f.s[0], s1 = c.f.s[1], s2 = c.f.s[2];
-  const float pE0x = c.f.pE0[0], pE0y = c.f.pE0[1], pE0z = c.f.pE0[2];
   const bool cross = !(c.faithful & CH_FAITHFUL_D2);
   const bool move = (PH & PH_MOVE) && !(c.faithful & CH_FAITHFUL_D5);
   const bool collide = (PH & PH_PUSH) && c.collide;
   const int ntx = (g.Nx + TX - 1) / TX, nty = (g.Ny + TY - 1) / TY;
-  // Move one ion by v dt (cell units), wrap, repack the cell.
-  auto move_ion = [&](float4& p, const float v[3], int& i, int& j, int& k) {
-    float ox = p.x + v[0] * dtx, oy = p.y + v[1] * dty, oz = p.z + v[2] * dtz;
-    float fx = floorf(ox), fy = floorf(oy), fz = floorf(oz);
-    ox -= fx; oy -= fy; oz -= fz;
-    // a tiny negative offset rounds up to 1.0f: that point is the start of
-    // the next cell, so carry into it (as pack_mixed does)
-    if (ox >= 1.0f) { ox = 0.0f; fx += 1.0f; }
-    if (oy >= 1.0f) { oy = 0.0f; fy += 1.0f; }
-    if (oz >= 1.0f) { oz = 0.0f; fz += 1.0f; }
-    if (isfinite(fx) && isfinite(fy) && isfinite(fz)) {
-      i = ch_wrap(i + (int)fx, g.Nx); j = ch_wrap(j + (int)fy, g.Ny); k = ch_wrap(k + (int)fz, g.Nz);
-    }
-    const uint32_t cell = (uint32_t)i | ((uint32_t)j << CH_PACK_BX) | ((uint32_t)k << (CH_PACK_BX + CH_PACK_BY));
-    p = make_float4(ox, oy, oz, __uint_as_float(cell));
-  };
-  auto gmean_of = [&](const float v[3]) {
-    const float qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
-    return ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), vnTf);
-  };
 
   const int i0 = (tile % ntx) * TX, j0 = ((tile / ntx) % nty) * TY, k0 = (tile / (ntx * nty)) * TZ;
   const int i1 = min(i0 + TX, g.Nx), j1 = min(j0 + TY, g.Ny), k1 = min(k0 + TZ, g.Nz);
@@ -667,245 +794,140 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
         }
       }
     sh.pre[TY * TZ] = tot;
-    sh.qn = 0;
   }
   __syncthreads();
   const uint32_t total = sh.pre[TY * TZ];
-  unsigned qhead = 0, qtail = 0;  // block-uniform: drained / enqueued entries of this brick
-  // Per-brick sums: tsum0 (expected events, reported only) in FP32; the
+  // Per-brick sum of the expected events (reported only) in FP32; the
   // post-step mean relative speeds, which normalise the next step's rates,
-  // as integers of 2^-20 so that S is exact whatever the ion order.
+  // go to gsum as integers of 2^-20 so that S is exact whatever the ion order.
   float tsum0 = 0.0f;
-  unsigned long long gsum = 0ull;
-  for (uint32_t base = 0; base < total; base += CH_TILE_BATCH) {
+  if (PH == PH_DEPOSIT) tile_deposit_direct(sh, c, P, acc, total, bi0, bj0, bk0, bad);
+  const uint32_t ptotal = total * (PH == PH_DEPOSIT ? 0u : 1u);  // ions the push / move loop visits
 #pragma unroll 1
-    for (int kk = 0; kk < CH_TILE_K; ++kk) {
-      const uint32_t sidx = kk * blockDim.x + threadIdx.x;  // slot within the batch
-      const uint32_t idx = base + sidx;
-      const bool active = idx < total;
-      int64_t ip = 0;
-      if (active) {
-        int r = 0;
-  #pragma unroll
-        for (int st = 8; st > 0; st >>= 1)
-          if (r + st < TY * TZ && sh.pre[r + st] <= idx) r += st;
-        ip = (int64_t)sh.rowbeg[r] + (idx - sh.pre[r]);
+  for (uint32_t base = 0; base < ptotal; base += blockDim.x) {
+    const uint32_t idx = base + threadIdx.x;
+    const bool active = idx < ptotal;
+    int64_t ip = 0;
+    if (active) {
+      int r = 0;
+#pragma unroll
+      for (int st = 8; st > 0; st >>= 1)
+        if (r + st < TY * TZ && sh.pre[r + st] <= idx) r += st;
+      ip = (int64_t)sh.rowbeg[r] + (idx - sh.pre[r]);
+    }
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f), vv = make_float4(0.f, 0.f, 0.f, 0.f);
+    int i = 0, j = 0, k = 0;
+    float v[3] = {0.f, 0.f, 0.f};
+    if (active) {
+      p = P.pos[ip];
+      vv = P.vel[ip];
+      const uint32_t cell = __float_as_uint(p.w);
+      i = cell & (CH_MAX_NX - 1); j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1); k = cell >> (CH_PACK_BX + CH_PACK_BY);
+      v[0] = vv.x; v[1] = vv.y; v[2] = vv.z;
+    }
+    bool defer = false;
+    float qscale = 0.0f, qt0 = 0.0f;  // rate scale and first waiting time of a deferred ion
+    if ((PH & PH_PUSH) && active) {
+      bool near;
+      const int q = box_key(g, i, j, k, bi0, bj0, bk0, &near);
+      float4 e000, e100, e010, e110, e001, e101, e011, e111;
+      if (near) {
+        e000 = sh.E[q]; e100 = sh.E[q + 1]; e010 = sh.E[q + BX]; e110 = sh.E[q + BX + 1];
+        e001 = sh.E[q + BX * BY]; e101 = sh.E[q + BX * BY + 1]; e011 = sh.E[q + BX * BY + BX];
+        e111 = sh.E[q + BX * BY + BX + 1];
+      } else {
+        const int ii1 = i + 1 == g.Nx ? 0 : i + 1, jj1 = j + 1 == g.Ny ? 0 : j + 1, kk1 = k + 1 == g.Nz ? 0 : k + 1;
+        const int64_t r00 = ((int64_t)k * g.Ny + j) * g.Nx, r10 = ((int64_t)k * g.Ny + jj1) * g.Nx,
+                      r01 = ((int64_t)kk1 * g.Ny + j) * g.Nx, r11 = ((int64_t)kk1 * g.Ny + jj1) * g.Nx;
+        e000 = __ldg(E + r00 + i); e100 = __ldg(E + r00 + ii1); e010 = __ldg(E + r10 + i);
+        e110 = __ldg(E + r10 + ii1); e001 = __ldg(E + r01 + i); e101 = __ldg(E + r01 + ii1);
+        e011 = __ldg(E + r11 + i); e111 = __ldg(E + r11 + ii1);
       }
-      float4 p = make_float4(0.f, 0.f, 0.f, 0.f), vv = make_float4(0.f, 0.f, 0.f, 0.f);
-      int i = 0, j = 0, k = 0;
-      float v[3] = {0.f, 0.f, 0.f};
-      if (active) {
-        p = P.pos[ip];
-        vv = P.vel[ip];
-        const uint32_t cell = __float_as_uint(p.w);
-        i = cell & (CH_MAX_NX - 1); j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1); k = cell >> (CH_PACK_BX + CH_PACK_BY);
-        v[0] = vv.x; v[1] = vv.y; v[2] = vv.z;
+      const float wx = p.x, wy = p.y, wz = p.z;
+      float Ef[3];
+#define LERP3(f, d)                                                                \
+{                                                                                \
+  const float wll = e000.f + wy * (e010.f - e000.f);                             \
+  const float wlh = e100.f + wy * (e110.f - e100.f);                             \
+  const float whl = e001.f + wy * (e011.f - e001.f);                             \
+  const float whh = e101.f + wy * (e111.f - e101.f);                             \
+  const float ezl = wll + wx * (wlh - wll), ezh = whl + wx * (whh - whl);        \
+  Ef[d] = ezl + wz * (ezh - ezl);                                                \
+}
+      LERP3(x, 0) LERP3(y, 1) LERP3(z, 2)
+#undef LERP3
+      if (c.push_E0) { Ef[0] += c.f.pE0[0]; Ef[1] += c.f.pE0[1]; Ef[2] += c.f.pE0[2]; }
+      // Boris (src/particles.c:374-447) with E premultiplied by (q/m) dt/2
+      const float vm0 = v[0] + Ef[0], vm1 = v[1] + Ef[1], vm2 = v[2] + Ef[2];
+      float vp0 = vm0, vp1 = vm1, vp2 = vm2;
+      if (cross) {
+        const float q0 = vm0 + (vm1 * t2 - vm2 * t1);
+        const float q1 = vm1 + (vm2 * t0 - vm0 * t2);
+        const float q2 = vm2 + (vm0 * t1 - vm1 * t0);
+        vp0 = vm0 + (q1 * s2 - q2 * s1);
+        vp1 = vm1 + (q2 * s0 - q0 * s2);
+        vp2 = vm2 + (q0 * s1 - q1 * s0);
       }
-      bool defer = false;
-      float qscale = 0.0f, qt0 = 0.0f;  // rate scale and first waiting time of a deferred ion
-      if ((PH & PH_PUSH) && active) {
-        bool near;
-        const int q = box_key(g, i, j, k, bi0, bj0, bk0, &near);
-        float4 e000, e100, e010, e110, e001, e101, e011, e111;
-        if (near) {
-          e000 = sh.E[q]; e100 = sh.E[q + 1]; e010 = sh.E[q + BX]; e110 = sh.E[q + BX + 1];
-          e001 = sh.E[q + BX * BY]; e101 = sh.E[q + BX * BY + 1]; e011 = sh.E[q + BX * BY + BX];
-          e111 = sh.E[q + BX * BY + BX + 1];
-        } else {
-          const int ii1 = i + 1 == g.Nx ? 0 : i + 1, jj1 = j + 1 == g.Ny ? 0 : j + 1, kk1 = k + 1 == g.Nz ? 0 : k + 1;
-          const int64_t r00 = ((int64_t)k * g.Ny + j) * g.Nx, r10 = ((int64_t)k * g.Ny + jj1) * g.Nx,
-                        r01 = ((int64_t)kk1 * g.Ny + j) * g.Nx, r11 = ((int64_t)kk1 * g.Ny + jj1) * g.Nx;
-          e000 = __ldg(E + r00 + i); e100 = __ldg(E + r00 + ii1); e010 = __ldg(E + r10 + i);
-          e110 = __ldg(E + r10 + ii1); e001 = __ldg(E + r01 + i); e101 = __ldg(E + r01 + ii1);
-          e011 = __ldg(E + r11 + i); e111 = __ldg(E + r11 + ii1);
+      v[0] = vp0 + Ef[0]; v[1] = vp1 + Ef[1]; v[2] = vp2 + Ef[2];
+      if (collide) {
+        const float gi = tile_gmean(c, v);
+        float nd = 1.0f;
+        if (c.nn_profile == CH_NN_GAUSSIAN_X)
+          nd = ch_neutral_density<float>(c, (float)(g.x0 + ((double)i + (double)p.x) * g.dx));
+        const float lscale = pscale * nd;
+        const float lam = lscale * gi;
+        tsum0 += lam;
+        const uint32_t id = __float_as_uint(vv.w);
+        const U4 r0 = ch_philox(id, c.step, CH_PURPOSE_COLLIDE << 24, c.run, c.seed_lo, c.seed_hi);
+        // first event inside the step: -log(u) < lam  <=>  u > exp(-lam);
+        // the queue keeps its waiting time
+        const float u0 = ch_unitf(r0.x);
+        if (lam > 0.0f && u0 > __expf(-lam)) {
+          qt0 = -ch_log(u0) / lam;
+          defer = qt0 < 1.0f;
         }
-        const float wx = p.x, wy = p.y, wz = p.z;
-        float Ef[3];
-  #define LERP3(f, d)                                                                \
-  {                                                                                \
-    const float wll = e000.f + wy * (e010.f - e000.f);                             \
-    const float wlh = e100.f + wy * (e110.f - e100.f);                             \
-    const float whl = e001.f + wy * (e011.f - e001.f);                             \
-    const float whh = e101.f + wy * (e111.f - e101.f);                             \
-    const float ezl = wll + wx * (wlh - wll), ezh = whl + wx * (whh - whl);        \
-    Ef[d] = ezl + wz * (ezh - ezl);                                                \
+        if (defer) qscale = lscale;
+        else gsum += g_fixed(gi);
+      }
+      if (!defer) {
+        vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
+        P.vel[ip] = vv;
+      }
+    }
+    if (collide) {
+      // append the deferred ions to the warp's ring (at most 31 entries
+      // wait there between iterations, so 32 more fit)
+      const unsigned dm = __ballot_sync(0xffffffffu, defer);
+      if (defer) {
+        const unsigned e = wbase + ((qtail + __popc(dm & ((1u << lane) - 1u))) & (CH_TILE_QW - 1));
+        sh.q_pos[e] = p;
+        sh.q_vel[e] = make_float4(v[0], v[1], v[2], qscale);
+        sh.q_ip[e] = (uint32_t)ip;
+        sh.q_id[e] = __float_as_uint(vv.w);
+        sh.q_t[e] = qt0;
+        sh.q_st[e] = 0u;
+      }
+      qtail += (unsigned)__popc(dm);
+    }
+    const bool go = active && !defer;
+    if (move && go) tile_move_ion(c, p, v, i, j, k);
+    if (move && go) P.pos[ip] = p;
+    if (hist) {
+      const uint32_t rk = agg_inc(hist, (uint32_t)(((int64_t)k * g.Ny + j) * g.Nx + i), go);
+      if (go && P.rank) P.rank[ip] = rk;
+    }
+    if (collide) {
+      __syncwarp();  // the appended entries are visible to every lane
+      // full rounds as the ring fills (each advances 32 ions by one proposal)
+      while (qtail - qhead >= 32u)
+        tile_queue_round<PH>(sh, c, P, hist, qhead, qtail, 32u, gsum, ncol, nref);
+    }
   }
-        LERP3(x, 0) LERP3(y, 1) LERP3(z, 2)
-  #undef LERP3
-        if (c.push_E0) { Ef[0] += pE0x; Ef[1] += pE0y; Ef[2] += pE0z; }
-        // Boris (src/particles.c:374-447) with E premultiplied by (q/m) dt/2
-        const float vm0 = v[0] + Ef[0], vm1 = v[1] + Ef[1], vm2 = v[2] + Ef[2];
-        float vp0 = vm0, vp1 = vm1, vp2 = vm2;
-        if (cross) {
-          const float q0 = vm0 + (vm1 * t2 - vm2 * t1);
-          const float q1 = vm1 + (vm2 * t0 - vm0 * t2);
-          const float q2 = vm2 + (vm0 * t1 - vm1 * t0);
-          vp0 = vm0 + (q1 * s2 - q2 * s1);
-          vp1 = vm1 + (q2 * s0 - q0 * s2);
-          vp2 = vm2 + (q0 * s1 - q1 * s0);
-        }
-        v[0] = vp0 + Ef[0]; v[1] = vp1 + Ef[1]; v[2] = vp2 + Ef[2];
-        if (collide) {
-          const float gi = gmean_of(v);
-          float nd = 1.0f;
-          if (c.nn_profile == CH_NN_GAUSSIAN_X)
-            nd = ch_neutral_density<float>(c, (float)(g.x0 + ((double)i + (double)p.x) * g.dx));
-          const float lscale = pscale * nd;
-          const float lam = lscale * gi;
-          tsum0 += lam;
-          const uint32_t id = __float_as_uint(vv.w);
-          const U4 r0 = ch_philox(id, c.step, CH_PURPOSE_COLLIDE << 24, c.run, c.seed_lo, c.seed_hi);
-          // first event inside the step: -log(u) < lam  <=>  u > exp(-lam);
-          // the queue keeps its waiting time
-          const float u0 = ch_unitf(r0.x);
-          if (lam > 0.0f && u0 > __expf(-lam)) {
-            qt0 = -ch_log(u0) / lam;
-            defer = qt0 < 1.0f;
-          }
-          if (defer) qscale = lscale;
-          else gsum += g_fixed(gi);
-        }
-        if (!defer) {
-          vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
-          P.vel[ip] = vv;
-        }
-      }
-      if (collide) {
-        // warp-aggregated enqueue of the deferred ions
-        const unsigned dm = __ballot_sync(0xffffffffu, defer);
-        if (dm) {
-          const int leader = __ffs(dm) - 1;
-          unsigned slot = 0;
-          if (lane == leader) slot = atomicAdd(&sh.qn, (unsigned)__popc(dm));
-          slot = (__shfl_sync(0xffffffffu, slot, leader) + __popc(dm & ((1u << lane) - 1u))) & (CH_TILE_QCAP - 1);
-          if (defer) {
-            sh.q_pos[slot] = p;
-            sh.q_vel[slot] = make_float4(v[0], v[1], v[2], qscale);
-            sh.q_ip[slot] = (uint32_t)ip;
-            sh.q_id[slot] = __float_as_uint(vv.w);
-            sh.q_t[slot] = qt0;
-            sh.q_st[slot] = 0u;
-          }
-        }
-      }
-      const bool go = active && !defer;
-      if (move && go) move_ion(p, v, i, j, k);
-      if (move && go) P.pos[ip] = p;
-      if (hist) {
-        const uint32_t rk = agg_inc(hist, (uint32_t)(((int64_t)k * g.Ny + j) * g.Nx + i), go);
-        if (go && P.rank) P.rank[ip] = rk;
-      }
-      if (PH & PH_DEPOSIT) {
-        const bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v[0]) && isfinite(v[1]) &&
-                            isfinite(v[2]);
-        if (go && !finite) bad = 1;
-        bool inbox;
-        const int key0 = box_key(g, i, j, k, bi0, bj0, bk0, &inbox);
-        const bool slow = fabsf(v[0]) >= CH_TILE_VMAX || fabsf(v[1]) >= CH_TILE_VMAX || fabsf(v[2]) >= CH_TILE_VMAX;
-        const bool valid = go && finite && inbox && !slow;
-        if (go && finite && !valid)
-          deposit_cic<float>(g, acc, i, j, k, p.x, p.y, p.z, v[0], v[1], v[2], c.f.dep_scale);
-        sh.st_key[sidx] = valid ? key0 : -1;
-        sh.st_ox[sidx] = p.x; sh.st_oy[sidx] = p.y; sh.st_oz[sidx] = p.z;
-        sh.st_vx[sidx] = v[0]; sh.st_vy[sidx] = v[1]; sh.st_vz[sidx] = v[2];
-      }
-      if (collide) {
-        // every enqueue of this iteration is visible after the barrier
-        qtail += (unsigned)__syncthreads_count(defer);
-        const bool last = base + (kk + 1) * blockDim.x >= total;
-        // Drain in rounds: each round advances up to one queued ion per
-        // thread by one proposal of its current event (with the scatter and
-        // the next waiting time when the proposal is accepted); ions with
-        // further events go back to the tail.  Full rounds run as the queue
-        // fills, and the queue is emptied at the end of the brick.
-        while (qtail - qhead >= blockDim.x || (last && qtail > qhead)) {
-          const unsigned nq = min(qtail - qhead, blockDim.x);
-          const unsigned e = (qhead + threadIdx.x) & (CH_TILE_QCAP - 1);
-          const bool act = threadIdx.x < nq;
-          float4 qp = make_float4(0.f, 0.f, 0.f, 0.f);
-          float qv[3] = {0.f, 0.f, 0.f};
-          float qsc = 0.0f, qtm = 0.0f;
-          uint32_t qip = 0, qid = 0, qe = 0, qit = 0;
-          bool done = false;
-          if (act) {
-            qp = sh.q_pos[e];
-            const float4 q4 = sh.q_vel[e];
-            qip = sh.q_ip[e];
-            qid = sh.q_id[e];
-            qtm = sh.q_t[e];
-            const uint32_t st = sh.q_st[e];
-            qe = st & 0xFFu;
-            qit = st >> 8;
-            qv[0] = q4.x; qv[1] = q4.y; qv[2] = q4.z;
-            qsc = q4.w;
-            done = ch_collide_round<float>(c, qid, qsc, qv, qtm, qe, qit, &ncol, &nref);
-          }
-          __syncthreads();  // this round's entries are read before any re-queue reuses their slots
-          const bool requeue = act && !done;
-          {
-            const unsigned rm = __ballot_sync(0xffffffffu, requeue);
-            if (rm) {
-              const int leader = __ffs(rm) - 1;
-              unsigned slot = 0;
-              if (lane == leader) slot = atomicAdd(&sh.qn, (unsigned)__popc(rm));
-              slot = (__shfl_sync(0xffffffffu, slot, leader) + __popc(rm & ((1u << lane) - 1u))) & (CH_TILE_QCAP - 1);
-              if (requeue) {
-                sh.q_pos[slot] = qp;
-                sh.q_vel[slot] = make_float4(qv[0], qv[1], qv[2], qsc);
-                sh.q_ip[slot] = qip;
-                sh.q_id[slot] = qid;
-                sh.q_t[slot] = qtm;
-                sh.q_st[slot] = qe | (qit << 8);
-              }
-            }
-          }
-          // ions whose event process ended: the velocity, the move, the cell count
-          const bool fin = act && done;
-          int qi = 0, qj = 0, qk = 0;
-          if (fin) {
-            gsum += g_fixed(gmean_of(qv));
-            P.vel[qip] = make_float4(qv[0], qv[1], qv[2], __uint_as_float(qid));
-            const uint32_t cell = __float_as_uint(qp.w);
-            qi = cell & (CH_MAX_NX - 1); qj = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1);
-            qk = cell >> (CH_PACK_BX + CH_PACK_BY);
-            if (move) {
-              move_ion(qp, qv, qi, qj, qk);
-              P.pos[qip] = qp;
-            }
-          }
-          if (hist) {
-            const uint32_t rk = agg_inc(hist, (uint32_t)(((int64_t)qk * g.Ny + qj) * g.Nx + qi), fin);
-            if (fin && P.rank) P.rank[qip] = rk;
-          }
-          if ((PH & PH_DEPOSIT) && fin) {
-            const bool finite = isfinite(qp.x) && isfinite(qp.y) && isfinite(qp.z) && isfinite(qv[0]) &&
-                                isfinite(qv[1]) && isfinite(qv[2]);
-            bool inbox;
-            const int key = box_key(g, qi, qj, qk, bi0, bj0, bk0, &inbox);
-            const bool slow =
-                fabsf(qv[0]) >= CH_TILE_VMAX || fabsf(qv[1]) >= CH_TILE_VMAX || fabsf(qv[2]) >= CH_TILE_VMAX;
-            if (!finite)
-              bad = 1;
-            else if (inbox && !slow)
-              tile_deposit_lane(sh, key, qp.x, qp.y, qp.z, qv[0], qv[1], qv[2]);
-            else
-              deposit_cic<float>(g, acc, qi, qj, qk, qp.x, qp.y, qp.z, qv[0], qv[1], qv[2], c.f.dep_scale);
-          }
-          qhead += nq;
-          // the re-queued entries are visible before the next round reads them
-          qtail += (unsigned)__syncthreads_count(requeue);
-        }
-      }
-    }
-    if (PH & PH_DEPOSIT) {
-      if (threadIdx.x == 0) sh.ov_n = 0u;
-      __syncthreads();  // the batch is staged
-      tile_deposit_batch(sh, lane);
-      __syncthreads();  // staging is read before the next batch overwrites it
-    }
+  if (!CARRY) {
+    while (qtail != qhead)
+      tile_queue_round<PH>(sh, c, P, hist, qhead, qtail, min(qtail - qhead, 32u), gsum, ncol, nref);
   }
   vsum[0] += (double)tsum0;
-  vsum[1] += (double)gsum * CH_G_UNIT;
   if (PH & PH_DEPOSIT) {
     __syncthreads();
     for (int q = threadIdx.x; q < 4 * BNODES; q += blockDim.x) {
@@ -924,22 +946,32 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
   }
 }
 
+// A pass without the deposit carries deferred ions from brick to brick and
+// drains the rings once, after the CTA's last brick.
 template <int PH>
 __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH_CTAS)
     k_pass_tiled(StepConsts c, MixParticles P, const float4* __restrict__ E, const uint32_t* __restrict__ starts,
                  unsigned long long* __restrict__ acc, float pscale, int shift_d, int shift_f, DevCounters* cnt,
                  double* part, uint32_t* hist) {
+  constexpr bool CARRY = !(PH & PH_DEPOSIT);
   extern __shared__ __align__(16) unsigned char smem_tiled[];
   TileShared& sh = tile_smem_base<PH>(smem_tiled);
   double vsum[2] = {0.0, 0.0};
-  unsigned ncol = 0, nref = 0;
+  unsigned long long gsum = 0ull;
+  unsigned qhead = 0, qtail = 0, ncol = 0, nref = 0;
   int bad = 0;
   const GridDesc& g = c.g;
   const int ntiles = ((g.Nx + TX - 1) / TX) * ((g.Ny + TY - 1) / TY) * ((g.Nz + TZ - 1) / TZ);
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
-    tile_pass<PH>(sh, c, P, E, starts, acc, pscale, shift_d, shift_f, hist, tile, vsum, ncol, nref, bad);
+    tile_pass<PH, CARRY>(sh, c, P, E, starts, acc, pscale, shift_d, shift_f, hist, tile, vsum, gsum, qhead, qtail,
+                         ncol, nref, bad);
+  if (CARRY) {
+    while (qtail != qhead)
+      tile_queue_round<PH>(sh, c, P, hist, qhead, qtail, min(qtail - qhead, 32u), gsum, ncol, nref);
+  }
   if (bad) atomicOr(&cnt->range_error, 2);
   if (PH & PH_PUSH) {
+    vsum[1] = (double)gsum * CH_G_UNIT;
     count_add(cnt, ncol, nref);
     block_partials<2>(vsum, part);
   }
@@ -948,8 +980,9 @@ __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH
 // Every run's bricks in one persistent launch: brick t belongs to the run r
 // with tile_off[r] <= t < tile_off[r + 1]; the run's constants are staged in
 // shared memory and the brick is processed by the same tile_pass as a single
-// run.  Brick partials are written per brick, so the run sums are formed in
-// a fixed order afterwards.
+// run (its deferred ions finished inside the brick, as the next brick may
+// belong to another run).  Brick partials are written per brick, so the run
+// sums are formed in a fixed order afterwards.
 template <int PH>
 __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH_CTAS)
     k_batch_pass(BatchDev B, const uint32_t* dstep, MixParticles P, const float4* __restrict__ E,
@@ -984,13 +1017,14 @@ __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH
     const float pscale = S > 0.0 ? (float)(R.Nc / S) : 0.0f;
     double vsum[4] = {0.0, 0.0, 0.0, 0.0};
     double v2[2] = {0.0, 0.0};
-    unsigned ncol = 0, nref = 0;
+    unsigned long long gsum = 0ull;
+    unsigned qhead = 0, qtail = 0, ncol = 0, nref = 0;
     int bad = 0;
     // tile_pass starts with a barrier, after which sc.step is visible
-    tile_pass<PH>(sh, sc, P, E + no, starts + no, acc + 4 * no, pscale, shift_d, shift_f, hist ? hist + no : nullptr,
-                  t - R.tile_off, v2, ncol, nref, bad);
+    tile_pass<PH, false>(sh, sc, P, E + no, starts + no, acc + 4 * no, pscale, shift_d, shift_f,
+                         hist ? hist + no : nullptr, t - R.tile_off, v2, gsum, qhead, qtail, ncol, nref, bad);
     if (bad) atomicOr(flags + r, 16);  // non-finite ion
-    vsum[0] = v2[0]; vsum[1] = v2[1]; vsum[2] = (double)ncol; vsum[3] = (double)nref;
+    vsum[0] = v2[0]; vsum[1] = (double)gsum * CH_G_UNIT; vsum[2] = (double)ncol; vsum[3] = (double)nref;
     block_partials<4>(vsum, tile_part, t);
   }
 }
@@ -1421,6 +1455,7 @@ static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticle
   const int64_t np = mixed ? M.np : P.np;
   int nb = grid_for(np, 256, sms, 8);
   if (mixed) {
+    if constexpr (PH == PH_DEPOSIT || !(PH & PH_DEPOSIT)) {  // launch_pass splits the rest
     const float pscale = sbar > 0.0 ? (float)(Nc / sbar) : 0.0f;
     const int ntiles = ((c.g.Nx + 15) / 16) * ((c.g.Ny + 3) / 4) * ((c.g.Nz + 3) / 4);
     const int per_sm = (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH_CTAS;
@@ -1430,6 +1465,7 @@ static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticle
     k_pass_tiled<PH><<<nb, 256, tile_smem_bytes<PH>(), s>>>(c, M, E32, starts, acc, pscale, s2 - CH_TILE_DLOG2,
                                                          s2 - CH_TILE_FLOG2, cnt, part, hist),
         ::ch::note_launch();
+    }
   } else {
     k_pass_f64<PH><<<nb, 256, 0, s>>>(c, P, E64, phi, acc, Nc, sbar, cnt, part), ::ch::note_launch();
   }
@@ -1439,6 +1475,14 @@ static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticle
 int launch_pass(bool mixed, int phases, const StepConsts& c, F64Particles P, MixParticles M, const double* E64,
                 const float4* E32, const double* phi, unsigned long long* acc, double Nc, double sbar,
                 DevCounters* cnt, double* part, const uint32_t* starts, uint32_t* hist, int sms, cudaStream_t s) {
+  // the mixed pass deposits in a launch of its own (the push / move launch
+  // writes the block partials, so its grid size is returned)
+  if (mixed && (phases & PH_DEPOSIT) && (phases & (PH_PUSH | PH_MOVE))) {
+    const int nb = launch_pass(mixed, phases & (PH_PUSH | PH_MOVE), c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part,
+                               starts, hist, sms, s);
+    launch_pass(mixed, PH_DEPOSIT, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, starts, nullptr, sms, s);
+    return nb;
+  }
 #define CH_PASS(PHV) pass_one<PHV>(mixed, c, P, M, E64, E32, phi, acc, Nc, sbar, cnt, part, starts, hist, sms, s)
   switch (phases) {
     case PH_PUSH: return CH_PASS(PH_PUSH);
@@ -1507,7 +1551,6 @@ static void batch_smem_attr() {
 }
 
 void batch_pass_prepare() {
-  batch_smem_attr<PH_PUSH | PH_MOVE | PH_DEPOSIT>();
   batch_smem_attr<PH_PUSH | PH_MOVE>();
   batch_smem_attr<PH_DEPOSIT>();
 }
@@ -1515,18 +1558,19 @@ void batch_pass_prepare() {
 void launch_batch_pass(int phases, const BatchDev& B, const uint32_t* dstep, MixParticles P, const float4* E,
                        const uint32_t* starts, unsigned long long* acc, const double* sbar, int dep_log2,
                        uint32_t* hist, double* tile_part, int* flags, int ctas_per_sm, int sms, cudaStream_t s) {
-  const int per_sm = (phases & PH_DEPOSIT) ? (ctas_per_sm < 1 ? 1 : ctas_per_sm) : CH_PUSH_CTAS;
-  const int cap = per_sm * sms;
-  const int nb = B.total_tiles < cap ? B.total_tiles : cap;
   const int sd = dep_log2 - CH_TILE_DLOG2, sf = dep_log2 - CH_TILE_FLOG2;
-#define CH_BPASS(PHV)                                                                                            \
-  k_batch_pass<PHV><<<nb, 256, tile_smem_bytes<PHV>(), s>>>(B, dstep, P, E, starts, acc, sbar, sd, sf, hist, \
-                                                            tile_part, flags),                                 \
-      ::ch::note_launch()
-  if (phases == PH_DEPOSIT) CH_BPASS(PH_DEPOSIT);
-  else if (phases == (PH_PUSH | PH_MOVE)) CH_BPASS(PH_PUSH | PH_MOVE);
-  else CH_BPASS(PH_PUSH | PH_MOVE | PH_DEPOSIT);
-#undef CH_BPASS
+  auto grid = [&](int per_sm) { return B.total_tiles < per_sm * sms ? B.total_tiles : per_sm * sms; };
+  // the deposit is a launch of its own
+  if (phases & (PH_PUSH | PH_MOVE)) {
+    k_batch_pass<PH_PUSH | PH_MOVE><<<grid(CH_PUSH_CTAS), 256, tile_smem_bytes<PH_PUSH | PH_MOVE>(), s>>>(
+        B, dstep, P, E, starts, acc, sbar, sd, sf, hist, tile_part, flags),
+        ::ch::note_launch();
+  }
+  if (phases & PH_DEPOSIT) {
+    k_batch_pass<PH_DEPOSIT><<<grid(ctas_per_sm < 1 ? 1 : ctas_per_sm), 256, tile_smem_bytes<PH_DEPOSIT>(), s>>>(
+        B, dstep, P, E, starts, acc, sbar, sd, sf, nullptr, tile_part, flags),
+        ::ch::note_launch();
+  }
 }
 
 void launch_batch_runsum(const BatchDev& B, const double* tile_part, double* sums, double* sbar, int* flags,
