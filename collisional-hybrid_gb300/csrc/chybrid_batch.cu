@@ -343,12 +343,8 @@ extern "C" ch_status ch_batch_create(const ch_params* runs, const int64_t* np, i
     S.C64 = dev_coefs<double>(op_coefs(runs[r], b->g[r]));
     // R = I + kappa kappa^T + [kappa]x with kappa_e = 0: the identity
     const double Rm[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-    for (int q = 0; q < 9; ++q) S.K.R[q] = Rm[q];
-    S.K.det = 1.0;
-    for (int d = 0; d < 3; ++d) S.K.E0[d] = runs[r].E0[d];
-    S.K.cth = runs[r].cth;
-    S.K.cG = runs[r].cG;
-    S.K.d8 = (runs[r].faithful & CH_FAITHFUL_D8) != 0;
+    S.K = rhs_coefs(Rm, 1.0, runs[r].E0, runs[r].cth, runs[r].cG, (runs[r].faithful & CH_FAITHFUL_D8) != 0,
+                    b->g[r].dx, b->g[r].dy, b->g[r].dz);
     S.rtol = runs[r].ksp_rtol;
     S.atol = runs[r].ksp_atol;
     S.maxit = runs[r].ksp_max_it;

@@ -51,14 +51,17 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_apply(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
                                                const T* __restrict__ x, T* __restrict__ y, const T* __restrict__ w,
                                                double* part) {
-  double d[1] = {0.0};
+  T d0 = T(0);
   GRID_LOOP(c, g.N) {
     const Nb b = neighbours(g, c);
     const T v = apply_row<T>(C, n, x, b);
     y[c] = v;
-    if (w) d[0] += (double)w[c] * (double)v;
+    if (w) d0 += w[c] * v;
   }
-  if (part) partials<1>(d, part);
+  if (part) {
+    double d[1] = {(double)d0};
+    partials<1>(d, part);
+  }
 }
 
 // t = A x; partials (t.s, t.t).
@@ -66,14 +69,15 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_apply_dot2(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
                                                     const T* __restrict__ x, T* __restrict__ t,
                                                     const T* __restrict__ s, double* part) {
-  double d[2] = {0.0, 0.0};
+  T d0 = T(0), d1 = T(0);
   GRID_LOOP(c, g.N) {
     const Nb b = neighbours(g, c);
     const T v = apply_row<T>(C, n, x, b);
     t[c] = v;
-    d[0] += (double)v * (double)s[c];
-    d[1] += (double)v * (double)v;
+    d0 += v * s[c];
+    d1 += v * v;
   }
+  double d[2] = {(double)d0, (double)d1};
   partials<2>(d, part);
 }
 
@@ -82,13 +86,14 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_residual(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
                                                   const T* __restrict__ b, const T* __restrict__ x,
                                                   T* __restrict__ r, double* part) {
-  double d[1] = {0.0};
+  T d0 = T(0);
   GRID_LOOP(c, g.N) {
     const Nb nb = neighbours(g, c);
     const T v = b[c] - apply_row<T>(C, n, x, nb);
     r[c] = v;
-    d[0] += (double)v * (double)v;
+    d0 += v * v;
   }
+  double d[1] = {(double)d0};
   partials<1>(d, part);
 }
 
@@ -104,14 +109,15 @@ __global__ void k_jacobi(GridDesc g, DevCoefs<T> C, const T* __restrict__ n, T* 
 template <typename T>
 __global__ void k_prec_dot(int64_t N, const T* __restrict__ dinv, const T* __restrict__ r, T* __restrict__ z,
                            double* part) {
-  double d[2] = {0.0, 0.0};
+  T d0 = T(0), d1 = T(0);
   GRID_LOOP(c, N) {
     const T rv = r[c];
     const T zv = dinv[c] * rv;
     z[c] = zv;
-    d[0] += (double)rv * (double)zv;
-    d[1] += (double)rv * (double)rv;
+    d0 += rv * zv;
+    d1 += rv * rv;
   }
+  double d[2] = {(double)d0, (double)d1};
   partials<2>(d, part);
 }
 
@@ -180,16 +186,17 @@ __global__ void k_cg_xr(int64_t N, const double* __restrict__ scal, T* __restric
                         const T* __restrict__ p, const T* __restrict__ q, const T* __restrict__ dinv,
                         T* __restrict__ z, double* part) {
   const T a = (T)scal[S_ALPHA];
-  double d[2] = {0.0, 0.0};
+  T d0 = T(0), d1 = T(0);
   GRID_LOOP(c, N) {
     x[c] += a * p[c];
     const T rv = r[c] - a * q[c];
     r[c] = rv;
     const T zv = dinv[c] * rv;
     z[c] = zv;
-    d[0] += (double)rv * (double)zv;
-    d[1] += (double)rv * (double)rv;
+    d0 += rv * zv;
+    d1 += rv * rv;
   }
+  double d[2] = {(double)d0, (double)d1};
   partials<2>(d, part);
 }
 
@@ -228,13 +235,14 @@ template <typename T>
 __global__ void k_bi_s(int64_t N, const double* __restrict__ scal, const T* __restrict__ r, const T* __restrict__ v,
                        const T* __restrict__ dinv, T* __restrict__ s, T* __restrict__ sh, double* part) {
   const T a = (T)scal[S_ALPHA];
-  double d[1] = {0.0};
+  T d0 = T(0);
   GRID_LOOP(c, N) {
     const T sv = r[c] - a * v[c];
     s[c] = sv;
     if (dinv) sh[c] = dinv[c] * sv;
-    d[0] += (double)sv * (double)sv;
+    d0 += sv * sv;
   }
+  double d[1] = {(double)d0};
   partials<1>(d, part);
 }
 
@@ -244,14 +252,15 @@ __global__ void k_bi_xr(int64_t N, const double* __restrict__ scal, T* __restric
                         const T* __restrict__ sh, T* __restrict__ r, const T* __restrict__ s, const T* __restrict__ t,
                         const T* __restrict__ rh, double* part) {
   const T a = (T)scal[S_ALPHA], w = (T)scal[S_OMEGA];
-  double d[2] = {0.0, 0.0};
+  T d0 = T(0), d1 = T(0);
   GRID_LOOP(c, N) {
     x[c] += a * y[c] + w * sh[c];
     const T rv = s[c] - w * t[c];
     r[c] = rv;
-    d[0] += (double)rv * (double)rv;
-    d[1] += (double)rh[c] * (double)rv;
+    d0 += rv * rv;
+    d1 += rh[c] * rv;
   }
+  double d[2] = {(double)d0, (double)d1};
   partials<2>(d, part);
 }
 
@@ -283,8 +292,9 @@ __global__ void k_sub_mean(int64_t N, double* __restrict__ a, const double* __re
 }
 template <typename T>
 __global__ void k_dot(int64_t N, const T* __restrict__ a, const T* __restrict__ b, double* part) {
-  double d[1] = {0.0};
-  GRID_LOOP(c, N) d[0] += (double)a[c] * (double)b[c];
+  T d0 = T(0);
+  GRID_LOOP(c, N) d0 += a[c] * b[c];
+  double d[1] = {(double)d0};
   partials<1>(d, part);
 }
 __global__ void k_dot64(int64_t N, const double* __restrict__ a, const double* __restrict__ b, double* part) {
@@ -302,11 +312,10 @@ __global__ void k_up_add(int64_t N, const float* __restrict__ a, double s, doubl
 }
 
 // ComputeFullRHS (src/rhs.c:244-283) with the FD helpers of src/calculus.c;
-// ComputeConstantRHS / ComputeSinusoidalRHS for the other --rhs-type values.
-__global__ void k_rhs(GridDesc g, int rhs_type, double R00, double R01, double R02, double R10, double R11,
-                      double R12, double R20, double R21, double R22, double det, double E0x, double E0y, double E0z,
-                      double cth, double cG, int d8, const double* __restrict__ mom, const double* __restrict__ scal,
-                      double* __restrict__ b) {
+// ComputeConstantRHS / ComputeSinusoidalRHS for the other --rhs-type values
+// (cscale = 2 dx dy dz / det, the factor of both).
+__global__ void k_rhs(GridDesc g, int rhs_type, RhsCoefs K, double cscale, const double* __restrict__ mom,
+                      const double* __restrict__ scal, double* __restrict__ b) {
   const int64_t N = g.N;
   const double* n = mom;
   const double* Gx = mom + N;
@@ -314,18 +323,17 @@ __global__ void k_rhs(GridDesc g, int rhs_type, double R00, double R01, double R
   const double* Gz = mom + 3 * N;
   GRID_LOOP(c, N) {
     if (rhs_type == CH_RHS_CONSTANT) {
-      b[c] = scal[S_MEAN] * (2.0 * g.dx * g.dy * g.dz / det);
+      b[c] = scal[S_MEAN] * cscale;
       continue;
     }
-    int i, j, k;
-    ch_ijk(g, c, i, j, k);
     if (rhs_type == CH_RHS_SINUSOIDAL) {
+      int i, j, k;
+      ch_ijk(g, c, i, j, k);
       const double x = ((double)i + 0.5) * g.dx, y = ((double)j + 0.5) * g.dy, z = ((double)k + 0.5) * g.dz;
       const double val = cos(2 * CH_PI * x) * cos(2 * CH_PI * y) * cos(2 * CH_PI * z);
-      b[c] = scal[S_MEAN] * val * (2.0 * g.dx * g.dy * g.dz / det);
+      b[c] = scal[S_MEAN] * val * cscale;
       continue;
     }
-    const RhsCoefs K{{R00, R01, R02, R10, R11, R12, R20, R21, R22}, det, {E0x, E0y, E0z}, cth, cG, d8};
     b[c] = rhs_full_row(g, K, n, Gx, Gy, Gz, neighbours(g, c));
   }
 }
@@ -345,6 +353,16 @@ __global__ void __launch_bounds__(256) k_smooth(GridDesc g, DevCoefs<T> C, const
       y[c] = x[c] + w * dinv[c] * (b[c] - apply_row<T>(C, n, x, nb));
     }
   }
+}
+
+// Two damped-Jacobi sweeps from x = 0: the first iterate t = w dinv b is
+// formed wherever the second sweep reads it, so it is never stored.
+template <typename T>
+__global__ void __launch_bounds__(256) k_smooth_zero2(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
+                                                      const T* __restrict__ dinv, const T* __restrict__ b,
+                                                      T* __restrict__ y, T w) {
+  auto t = [&](int64_t i) { return w * dinv[i] * b[i]; };
+  GRID_LOOP(c, g.N) y[c] = t(c) + w * dinv[c] * (b[c] - apply_row_at<T>(C, n, t, neighbours(g, c)));
 }
 
 // r = b - A x without a norm (MG levels).
@@ -431,12 +449,32 @@ __global__ void __launch_bounds__(1024) k_coarse(GridDesc g, DevCoefs<T> C, cons
 // partials (r.z, r.r) after a multigrid preconditioner application
 template <typename T>
 __global__ void k_dot_rz_rr(int64_t N, const T* __restrict__ r, const T* __restrict__ z, double* part) {
-  double d[2] = {0.0, 0.0};
+  T d0 = T(0), d1 = T(0);
   GRID_LOOP(c, N) {
-    const double rv = (double)r[c];
-    d[0] += rv * (double)z[c];
-    d[1] += rv * rv;
+    const T rv = r[c];
+    d0 += rv * z[c];
+    d1 += rv * rv;
   }
+  double d[2] = {(double)d0, (double)d1};
+  partials<2>(d, part);
+}
+
+// The last post-smoothing sweep of the finest level, with the preconditioned
+// CG's partials (r.z, r.r) of r = b and z = y.
+template <typename T>
+__global__ void __launch_bounds__(256) k_smooth_dot(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
+                                                    const T* __restrict__ dinv, const T* __restrict__ b,
+                                                    const T* __restrict__ x, T* __restrict__ y, T w, double* part) {
+  T d0 = T(0), d1 = T(0);
+  GRID_LOOP(c, g.N) {
+    const Nb nb = neighbours(g, c);
+    const T rv = b[c];
+    const T z = x[c] + w * dinv[c] * (rv - apply_row<T>(C, n, x, nb));
+    y[c] = z;
+    d0 += rv * z;
+    d1 += rv * rv;
+  }
+  double d[2] = {(double)d0, (double)d1};
   partials<2>(d, part);
 }
 
@@ -575,21 +613,23 @@ void PotentialSolver::mg_update(MGHier<T>& h, const T* n_fine, cudaStream_t s) {
   }
 }
 
-// One V(2,2) cycle from a zero guess: x ~= A_l^{-1} b.
+// One V(2,2) cycle from a zero guess: x ~= A_l^{-1} b.  With part (finest
+// level only) the partials (b.x, b.b) of the result are written to part by
+// the last sweep, over the Krylov grid nb_.
 template <typename T>
-void PotentialSolver::mg_vcycle(MGHier<T>& h, int l, const T* b, T* x, cudaStream_t s) {
+void PotentialSolver::mg_vcycle(MGHier<T>& h, int l, const T* b, T* x, cudaStream_t s, double* part) {
   const GridDesc& g = h.g[l];
   const int nb = grid_n(g.N, sms_);
   const T w = (T)MG_OMEGA;
   if (l == h.L - 1) {
     const size_t sh = 2 * sizeof(T) * g.N;
     k_coarse<T><<<1, 1024, sh, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, x, mg_coarse_sweeps(g), w), ::ch::note_launch();
+    if (part) k_dot_rz_rr<T><<<nb_, 256, 0, s>>>(g.N, b, x, part), ::ch::note_launch();
     return;
   }
-  T* t = h.t[l];
-  // pre-smoothing (MG_NU = 2 sweeps): zero -> t -> x
-  k_smooth<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, (const T*)nullptr, t, w), ::ch::note_launch();
-  k_smooth<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, t, x, w), ::ch::note_launch();
+  // pre-smoothing (MG_NU = 2 sweeps from zero, in one pass)
+  static_assert(MG_NU == 2, "the pre-smoothing pass fuses exactly two sweeps");
+  k_smooth_zero2<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, x, w), ::ch::note_launch();
   // residual, restriction, coarse correction, prolongation
   k_resid<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], b, x, h.r[l]), ::ch::note_launch();
   k_restrict<T><<<grid_n(h.g[l + 1].N, sms_), 256, 0, s>>>(g, h.g[l + 1], h.hx[l], h.hy[l], h.hz[l], h.r[l],
@@ -600,7 +640,10 @@ void PotentialSolver::mg_vcycle(MGHier<T>& h, int l, const T* b, T* x, cudaStrea
   for (int k = 0; k < MG_NU; ++k) {
     T* src = (k % 2 == 0) ? x : h.t[l];
     T* dst = (k % 2 == 0) ? h.t[l] : x;
-    k_smooth<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, src, dst, w), ::ch::note_launch();
+    if (part && k == MG_NU - 1)
+      k_smooth_dot<T><<<nb_, 256, 0, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, src, dst, w, part), ::ch::note_launch();
+    else
+      k_smooth<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, src, dst, w), ::ch::note_launch();
   }
 }
 
@@ -629,8 +672,9 @@ void PotentialSolver::build_rhs(const double* mom, double* b, cudaStream_t s) {
     k_sum<double><<<nb_, 256, 0, s>>>(N_, mom, part_), ::ch::note_launch();
     k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_MEAN, scal_, 1.0 / (double)N_), ::ch::note_launch();
   }
-  k_rhs<<<nb_, 256, 0, s>>>(g_, p_.rhs_type, R00, R01, R02, R10, R11, R12, R20, R21, R22, det, p_.E0[0], p_.E0[1],
-                            p_.E0[2], p_.cth, p_.cG, (p_.faithful & CH_FAITHFUL_D8) != 0, mom, scal_, b), ::ch::note_launch();
+  const double R[9] = {R00, R01, R02, R10, R11, R12, R20, R21, R22};
+  const RhsCoefs K = rhs_coefs(R, det, p_.E0, p_.cth, p_.cG, (p_.faithful & CH_FAITHFUL_D8) != 0, g_.dx, g_.dy, g_.dz);
+  k_rhs<<<nb_, 256, 0, s>>>(g_, p_.rhs_type, K, 2.0 * g_.dx * g_.dy * g_.dz / det, mom, scal_, b), ::ch::note_launch();
   if (p_.rhs_type != CH_RHS_CONSTANT) remove_mean64(b, s);  // MatNullSpaceRemove (src/rhs.c:294-296)
 }
 
@@ -642,7 +686,8 @@ void PotentialSolver::apply64(const double* n, const double* x, double* y, cudaS
 // Converged when ||r||_2 <= rtol ||b||_2 (recurrence residual).
 template <typename T>
 ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* x, double rtol, int maxit,
-                                  bool zero_guess, int* its, double* rnorm_out, MGHier<T>* mg, cudaStream_t s) {
+                                  bool zero_guess, int* its, double* rnorm_out, MGHier<T>* mg, cudaStream_t s,
+                                  double bnorm_known) {
   const DevCoefs<T> C = dev_coefs<T>(c_);
   const int64_t N = g.N;
   const bool f64 = sizeof(T) == 8;
@@ -660,8 +705,7 @@ ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* 
   // z = M r with M = Jacobi (fused) or one multigrid V-cycle
   auto precond = [&](const T* rr_, T* zz_) {
     if (mg) {
-      mg_vcycle<T>(*mg, 0, rr_, zz_, s);
-      k_dot_rz_rr<T><<<nb, 256, 0, s>>>(N, rr_, zz_, part_), ::ch::note_launch();
+      mg_vcycle<T>(*mg, 0, rr_, zz_, s, part_);  // with the partials (r.z, r.r)
     } else {
       k_prec_dot<T><<<nb, 256, 0, s>>>(N, dinv, rr_, zz_, part_), ::ch::note_launch();
     }
@@ -674,15 +718,20 @@ ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* 
   }
   precond(r, z);
   k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_SET_RZ_RR, scal_, 0.0), ::ch::note_launch();
-  k_dot<T><<<nb, 256, 0, s>>>(N, b, b, part_), ::ch::note_launch();
-  k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_TMP, scal_, 0.0), ::ch::note_launch();
-  CH_CUDA_OK(cudaMemcpyAsync(hscal_, scal_, sizeof(double) * S_NSLOT, cudaMemcpyDeviceToHost, s));
-  CH_CUDA_OK(cudaStreamSynchronize(s));
-  const double bnorm = sqrt(hscal_[S_TMP]);
-  double rr = hscal_[S_RR];
+  // ||b||: given by the caller (no host round trip; the first iterations
+  // then run even when the start is already converged), or measured
+  double bnorm = bnorm_known, rr = 0.0;
+  if (!(bnorm_known >= 0.0)) {
+    k_dot<T><<<nb, 256, 0, s>>>(N, b, b, part_), ::ch::note_launch();
+    k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_TMP, scal_, 0.0), ::ch::note_launch();
+    CH_CUDA_OK(cudaMemcpyAsync(hscal_, scal_, sizeof(double) * S_NSLOT, cudaMemcpyDeviceToHost, s));
+    CH_CUDA_OK(cudaStreamSynchronize(s));
+    bnorm = sqrt(hscal_[S_TMP]);
+    rr = hscal_[S_RR];
+  }
   const double tol = rtol * bnorm;
   int it = 0;
-  if (sqrt(rr) <= tol || bnorm == 0.0) {
+  if (bnorm == 0.0 || (!(bnorm_known >= 0.0) && sqrt(rr) <= tol)) {
     *its = 0;
     *rnorm_out = sqrt(rr);
     return CH_OK;
@@ -839,7 +888,8 @@ ch_status PotentialSolver::solve_mixed(const double* n, const double* b, double*
     k_down<<<nb_, 256, 0, s>>>(N_, r_, sc, b32_), ::ch::note_launch();
     int its = 0;
     double rin = 0.0;
-    ch_status rc = krylov<float>(g_, n32_, b32_, x32_, inner_rtol, p_.ksp_max_it, true, &its, &rin, mg, s);
+    // b32 = r / ||r|| has unit norm up to its FP32 rounding
+    ch_status rc = krylov<float>(g_, n32_, b32_, x32_, inner_rtol, p_.ksp_max_it, true, &its, &rin, mg, s, 1.0);
     if (rc) return rc;
     total += its;
     k_up_add<<<nb_, 256, 0, s>>>(N_, x32_, rn, phi), ::ch::note_launch();

@@ -75,14 +75,15 @@ class PotentialSolver {
   ch_status solve_mixed(const double* n, const double* b, double* phi, SolveStats* st, cudaStream_t s);
   template <typename T>
   ch_status krylov(const GridDesc& g, const T* n, const T* b, T* x, double rtol, int maxit, bool zero_guess,
-                   int* its, double* rnorm_out, MGHier<T>* mg, cudaStream_t s);
+                   int* its, double* rnorm_out, MGHier<T>* mg, cudaStream_t s,
+                   double bnorm_known = -1.0);
   double dot64(const double* a, const double* b, cudaStream_t s);
   template <typename T>
   ch_status mg_build(MGHier<T>& h);
   template <typename T>
   void mg_update(MGHier<T>& h, const T* n_fine, cudaStream_t s);
   template <typename T>
-  void mg_vcycle(MGHier<T>& h, int l, const T* b, T* x, cudaStream_t s);
+  void mg_vcycle(MGHier<T>& h, int l, const T* b, T* x, cudaStream_t s, double* part = nullptr);
   template <typename T>
   void mg_release(MGHier<T>& h);
   void remove_mean64(double* v, cudaStream_t s);

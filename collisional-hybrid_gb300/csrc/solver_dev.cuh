@@ -44,43 +44,47 @@ DevCoefs<T> dev_coefs(const OpCoefs& c) {
 }
 
 // One row of A(n) x.  Values follow src/lhs.c:488-511 (f[...] assignments)
-// and src/lhs.c:7-106 (stencil order).
-template <typename T>
-__device__ __forceinline__ T apply_row(const DevCoefs<T>& C, const T* n, const T* x, const Nb& b) {
-  if (C.type == CH_LHS_IDENTITY) return x[b.c];
-  const T xc = x[b.c];
+// and src/lhs.c:7-106 (stencil order).  xat(i) gives x at node i (an array
+// read, or a value formed on the fly).
+template <typename T, typename X>
+__device__ __forceinline__ T apply_row_at(const DevCoefs<T>& C, const T* n, X xat, const Nb& b) {
+  if (C.type == CH_LHS_IDENTITY) return xat(b.c);
+  const T xc = xat(b.c), xe = xat(b.e), xw = xat(b.w), xn = xat(b.n), xs = xat(b.s), xu = xat(b.u), xd = xat(b.d);
   if (C.type == CH_LHS_LAPLACIAN)
-    return C.sxx * (x[b.e] + x[b.w]) + C.syy * (x[b.n] + x[b.s]) + C.szz * (x[b.u] + x[b.d]) -
-           T(2) * (C.sxx + C.syy + C.szz) * xc;
+    return C.sxx * (xe + xw) + C.syy * (xn + xs) + C.szz * (xu + xd) - T(2) * (C.sxx + C.syy + C.szz) * xc;
   const T nijk = n[b.c], npjk = n[b.e], nmjk = n[b.w], nipk = n[b.n], nimk = n[b.s], nijp = n[b.u], nijm = n[b.d];
   // star terms: sum of f_face (x_face - x_c) over the six faces reproduces
   // the diagonal value -(sum of the star values) exactly in exact arithmetic
-  T acc = C.sxx * ((npjk + nijk) * (x[b.e] - xc) + (nijk + nmjk) * (x[b.w] - xc)) +
-          C.syy * ((nipk + nijk) * (x[b.n] - xc) + (nijk + nimk) * (x[b.s] - xc)) +
-          C.szz * ((nijp + nijk) * (x[b.u] - xc) + (nijk + nijm) * (x[b.d] - xc));
+  T acc = C.sxx * ((npjk + nijk) * (xe - xc) + (nijk + nmjk) * (xw - xc)) +
+          C.syy * ((nipk + nijk) * (xn - xc) + (nijk + nimk) * (xs - xc)) +
+          C.szz * ((nijp + nijk) * (xu - xc) + (nijk + nijm) * (xd - xc));
   if (C.cross) {
     const T sxy = C.sxy, sxz = C.sxz, syz = C.syz, syx = C.syx, szx = C.szx, szy = C.szy;
     // cross parts of the six star values
-    acc += (syx * (nipk - nimk) + szx * (nijp - nijm)) * (x[b.e] - x[b.w]);
-    acc += (sxy * (npjk - nmjk) + szy * (nijp - nijm)) * (x[b.n] - x[b.s]);
-    acc += (sxz * (npjk - nmjk) + syz * (nipk - nimk)) * (x[b.u] - x[b.d]);
+    acc += (syx * (nipk - nimk) + szx * (nijp - nijm)) * (xe - xw);
+    acc += (sxy * (npjk - nmjk) + szy * (nijp - nijm)) * (xn - xs);
+    acc += (sxz * (npjk - nmjk) + syz * (nipk - nimk)) * (xu - xd);
     // x-y corners
-    acc += (sxy * (npjk + nijk) + syx * (nipk + nijk)) * x[b.en];
-    acc += (-sxy * (npjk + nijk) - syx * (nijk + nimk)) * x[b.es];
-    acc += (-sxy * (nijk + nmjk) - syx * (nipk + nijk)) * x[b.wn];
-    acc += (sxy * (nijk + nmjk) + syx * (nijk + nimk)) * x[b.ws];
+    acc += (sxy * (npjk + nijk) + syx * (nipk + nijk)) * xat(b.en);
+    acc += (-sxy * (npjk + nijk) - syx * (nijk + nimk)) * xat(b.es);
+    acc += (-sxy * (nijk + nmjk) - syx * (nipk + nijk)) * xat(b.wn);
+    acc += (sxy * (nijk + nmjk) + syx * (nijk + nimk)) * xat(b.ws);
     // x-z corners
-    acc += (sxz * (npjk + nijk) + szx * (nijp + nijk)) * x[b.eu];
-    acc += (-sxz * (npjk + nijk) - szx * (nijk + nijm)) * x[b.ed];
-    acc += (-sxz * (nijk + nmjk) - szx * (nijp + nijk)) * x[b.wu];
-    acc += (sxz * (nijk + nmjk) + szx * (nijk + nijm)) * x[b.wd];
+    acc += (sxz * (npjk + nijk) + szx * (nijp + nijk)) * xat(b.eu);
+    acc += (-sxz * (npjk + nijk) - szx * (nijk + nijm)) * xat(b.ed);
+    acc += (-sxz * (nijk + nmjk) - szx * (nijp + nijk)) * xat(b.wu);
+    acc += (sxz * (nijk + nmjk) + szx * (nijk + nijm)) * xat(b.wd);
     // y-z corners
-    acc += (syz * (nipk + nijk) + szy * (nijp + nijk)) * x[b.nu];
-    acc += (-syz * (nipk + nijk) - szy * (nijk + nijm)) * x[b.nd];
-    acc += (-syz * (nijk + nimk) - szy * (nijp + nijk)) * x[b.su];
-    acc += (syz * (nijk + nimk) + szy * (nijk + nijm)) * x[b.sd];
+    acc += (syz * (nipk + nijk) + szy * (nijp + nijk)) * xat(b.nu);
+    acc += (-syz * (nipk + nijk) - szy * (nijk + nijm)) * xat(b.nd);
+    acc += (-syz * (nijk + nimk) - szy * (nijp + nijk)) * xat(b.su);
+    acc += (syz * (nijk + nimk) + szy * (nijk + nijm)) * xat(b.sd);
   }
   return acc;
+}
+template <typename T>
+__device__ __forceinline__ T apply_row(const DevCoefs<T>& C, const T* n, const T* x, const Nb& b) {
+  return apply_row_at<T>(C, n, [x](int64_t i) { return x[i]; }, b);
 }
 
 template <typename T>
@@ -94,38 +98,51 @@ __device__ __forceinline__ T diag_row(const DevCoefs<T>& C, const T* n, const Nb
 
 // ComputeFullRHS at one node (src/rhs.c:133-303, src/calculus.c:21-520):
 // b = (1/det)[(R E0).grad n + c_th sum R_ab d_a d_b n + det c_G div Gamma].
-// d8 selects the as-written d2Fdyz (x-z stencil, src/calculus.c:464).
+// The differences of n and Gamma are formed as the reference forms them;
+// every constant factor (1/(2 dx), 1/dx^2, 1/det, R, E0, c_th, c_G) is folded
+// on the host into one coefficient per difference (rhs_coefs), so the row is
+// a dozen FP64 products and no divisions.  d8 selects the as-written d2Fdyz
+// (x-z stencil, src/calculus.c:464).
 struct RhsCoefs {
-  double R[9];
-  double det;
-  double E0[3];
-  double cth, cG;
+  double ex, ey, ez;     // (R E0)_a / (2 d_a det)
+  double pxx, pyy, pzz;  // c_th R_aa / (d_a^2 det)
+  double pxy, pxz, pyz;  // c_th (R_ab + R_ba) / (4 d_a d_b det)
+  double gx, gy, gz;     // c_G / (2 d_a)
   int d8;
 };
+inline RhsCoefs rhs_coefs(const double R[9], double det, const double E0[3], double cth, double cG, bool d8,
+                          double dx, double dy, double dz) {
+  RhsCoefs K;
+  const double a[3] = {R[0] * E0[0] + R[1] * E0[1] + R[2] * E0[2], R[3] * E0[0] + R[4] * E0[1] + R[5] * E0[2],
+                       R[6] * E0[0] + R[7] * E0[1] + R[8] * E0[2]};
+  K.ex = a[0] / (2.0 * dx * det);
+  K.ey = a[1] / (2.0 * dy * det);
+  K.ez = a[2] / (2.0 * dz * det);
+  K.pxx = cth * R[0] / (dx * dx * det);
+  K.pyy = cth * R[4] / (dy * dy * det);
+  K.pzz = cth * R[8] / (dz * dz * det);
+  K.pxy = cth * (R[1] + R[3]) / (4.0 * dx * dy * det);
+  K.pxz = cth * (R[2] + R[6]) / (4.0 * dx * dz * det);
+  K.pyz = cth * (R[5] + R[7]) / (4.0 * dy * dz * det);
+  K.gx = cG / (2.0 * dx);
+  K.gy = cG / (2.0 * dy);
+  K.gz = cG / (2.0 * dz);
+  K.d8 = d8 ? 1 : 0;
+  return K;
+}
 __device__ __forceinline__ double rhs_full_row(const GridDesc& g, const RhsCoefs& K, const double* n, const double* Gx,
                                                const double* Gy, const double* Gz, const Nb& q) {
-  const double dx = g.dx, dy = g.dy, dz = g.dz;
-  const double dndx = (n[q.e] - n[q.w]) / (2.0 * dx);
-  const double dndy = (n[q.n] - n[q.s]) / (2.0 * dy);
-  const double dndz = (n[q.u] - n[q.d]) / (2.0 * dz);
-  const double dGxdx = (Gx[q.e] - Gx[q.w]) / (2.0 * dx);
-  const double dGydy = (Gy[q.n] - Gy[q.s]) / (2.0 * dy);
-  const double dGzdz = (Gz[q.u] - Gz[q.d]) / (2.0 * dz);
-  const double d2ndxx = (n[q.e] - 2.0 * n[q.c] + n[q.w]) / (dx * dx);
-  const double d2ndyy = (n[q.n] - 2.0 * n[q.c] + n[q.s]) / (dy * dy);
-  const double d2ndzz = (n[q.u] - 2.0 * n[q.c] + n[q.d]) / (dz * dz);
-  const double d2ndxy = (n[q.en] - n[q.wn] - n[q.es] + n[q.ws]) / (4.0 * dx * dy);
-  const double d2ndxz = (n[q.eu] - n[q.wu] - n[q.ed] + n[q.wd]) / (4.0 * dx * dz);
-  const double vyz = K.d8 ? (n[q.eu] - n[q.wu] - n[q.ed] + n[q.wd]) : (n[q.nu] - n[q.su] - n[q.nd] + n[q.sd]);
-  const double d2ndyz = vyz / (4.0 * dy * dz);
-  const double* R = K.R;
-  const double Eterm = (R[0] * K.E0[0] + R[1] * K.E0[1] + R[2] * K.E0[2]) * dndx +
-                       (R[3] * K.E0[0] + R[4] * K.E0[1] + R[5] * K.E0[2]) * dndy +
-                       (R[6] * K.E0[0] + R[7] * K.E0[1] + R[8] * K.E0[2]) * dndz;
-  const double Pterm = K.cth * (R[0] * d2ndxx + R[1] * d2ndxy + R[2] * d2ndxz + R[3] * d2ndxy + R[4] * d2ndyy +
-                                R[5] * d2ndyz + R[6] * d2ndxz + R[7] * d2ndyz + R[8] * d2ndzz);
-  const double Gterm = K.det * K.cG * (dGxdx + dGydy + dGzdz);
-  return (1.0 / K.det) * (Eterm + Pterm + Gterm);
+  (void)g;
+  const double dnx = n[q.e] - n[q.w], dny = n[q.n] - n[q.s], dnz = n[q.u] - n[q.d];
+  const double lxx = n[q.e] - 2.0 * n[q.c] + n[q.w];
+  const double lyy = n[q.n] - 2.0 * n[q.c] + n[q.s];
+  const double lzz = n[q.u] - 2.0 * n[q.c] + n[q.d];
+  const double lxy = n[q.en] - n[q.wn] - n[q.es] + n[q.ws];
+  const double lxz = n[q.eu] - n[q.wu] - n[q.ed] + n[q.wd];
+  const double lyz = K.d8 ? lxz : (n[q.nu] - n[q.su] - n[q.nd] + n[q.sd]);
+  return K.ex * dnx + K.ey * dny + K.ez * dnz + K.pxx * lxx + K.pyy * lyy + K.pzz * lzz + K.pxy * lxy +
+         K.pxz * lxz + K.pyz * lyz + K.gx * (Gx[q.e] - Gx[q.w]) + K.gy * (Gy[q.n] - Gy[q.s]) +
+         K.gz * (Gz[q.u] - Gz[q.d]);
 }
 
 // Block partial sums of K doubles (fixed order).
