@@ -405,12 +405,11 @@ __device__ __forceinline__ int rni(float x) { return rni_biased(x) - CH_RNI_BIAS
 __device__ __forceinline__ int rni_fma(float a, float b) { return __float_as_int(__fmaf_rn(a, b, 12582912.0f)); }
 
 #define CH_PUSH_CTAS 4          // CTAs per SM of a pass without the deposit
-#define CH_DEP_CTAS 3           // CTAs per SM of a pass with the deposit (61 KB each when deposit-only)
+#define CH_DEP_CTAS 3           // CTAs per SM of a deposit pass (72 KB of shared memory each)
 #define CH_TILE_QCAP 512       // deferred colliding ions: one ring of CH_TILE_QW per warp
 #define CH_TILE_QW (CH_TILE_QCAP / 8)
 static_assert(CH_TILE_QW >= 64 && (CH_TILE_QW & (CH_TILE_QW - 1)) == 0,
               "a warp ring holds 31 pending + 32 new entries and is indexed modulo its size");
-#define CH_TILE_ROUNDS 3       // key groups a warp reduces before per-lane adds
 
 #define CH_TILE_K 4            // consecutive slots one thread deposits together
 #define CH_TILE_BATCH (256 * CH_TILE_K)
@@ -438,6 +437,7 @@ struct TileShared {
   uint32_t pre[TY * TZ + 1];
   // ---- deposit part
   uint32_t d_ip[8 * CH_DEP_RW];  // per warp: ring of displaced ions (indices into the ion arrays)
+  unsigned d_sum[8][32 * 33];    // per warp: lane l's 32 sums in row l (33 words: no bank conflicts)
   unsigned acc_lo[4][BNODES];    // 64-bit fixed-point sums at the tile scale as
   int acc_hi[4][BNODES];         // lo + hi * 2^32, carried exactly (order-free)
 };
@@ -505,10 +505,11 @@ __device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, i
 // of a cell are contiguous after a sort and mostly stay together between
 // sorts, so the 4 usually share a cell).  A lane sums the 32 fixed-point
 // contributions of its slots in the cell most of them share in registers;
-// the lanes of the warp whose cells agree (up to CH_TILE_ROUNDS groups) are
-// then summed with integer warp reductions, lane q adding sum q to the
-// brick.  Slots in another cell ("displaced": they moved since the last
-// sort) go to the warp's ring and are added lane by lane, 32 at a time.
+// the sums of lanes whose cells agree are then added up through a matrix in
+// shared memory (lane q sums entry q of each run of equal cells) and added to
+// the brick once per run.  Slots in another cell ("displaced": they moved
+// since the last sort) go to the warp's ring and are added lane by lane, 32
+// at a time.
 // Every contribution is rounded to an integer before any addition, so the
 // result does not depend on the order; no block barrier is needed.
 __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepConsts& c, MixParticles P,
@@ -613,32 +614,31 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
     const unsigned unbias = cnt * (unsigned)CH_RNI_BIAS;
 #pragma unroll
     for (int q = 0; q < 32; ++q) a[q] -= unbias;  // exact sums, |sum| < 2^25
-    unsigned rem = __ballot_sync(0xffffffffu, akey >= 0);
-#pragma unroll 1
-    for (int round = 0; rem && round < CH_TILE_ROUNDS; ++round) {
-      const int leader = __ffs(rem) - 1;
-      const int lkey = __shfl_sync(0xffffffffu, akey, leader);
-      const bool mine = ((rem >> lane) & 1u) && akey == lkey;
-      rem &= ~__ballot_sync(0xffffffffu, mine);
-      int myval = 0;
+    // Sums of lanes whose cells agree: lane l's 32 sums become row l of the
+    // warp's matrix, and lane q walks column q down the rows, adding one sum
+    // per run of equal cells (consecutive in sorted order) to node q & 7 of
+    // that cell, moment q >> 3.
+    unsigned* M = sh.d_sum[warp];
 #pragma unroll
-      for (int q = 0; q < 32; ++q) {
-        const int sq = (int)__reduce_add_sync(0xffffffffu, mine ? a[q] : 0u);
-        myval = lane == q ? sq : myval;
-      }
+    for (int q = 0; q < 32; ++q) M[lane * 33 + q] = a[q];
+    __syncwarp();
+    {
       const int cn = lane & 7, m = lane >> 3;
-      const int node = lkey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
-      if (myval != 0) shared_add64(&sh.acc_lo[m][node], &sh.acc_hi[m][node], myval);
-    }
-    if ((rem >> lane) & 1u) {
-#pragma unroll
-      for (int q = 0; q < 32; ++q) {
-        const int cn = q & 7, m = q >> 3;
-        const int node = akey + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
-        if (a[q] != 0u) shared_add64(&sh.acc_lo[m][node], &sh.acc_hi[m][node], (long long)(int)a[q]);
+      const int off = (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
+      int cur = -1, sum = 0;  // |sum| < 32 x 2^25
+#pragma unroll 8
+      for (int l = 0; l < 32; ++l) {
+        const int kl = __shfl_sync(0xffffffffu, akey, l);
+        if (kl != cur) {  // warp-uniform
+          if (cur >= 0 && sum != 0) shared_add64(&sh.acc_lo[m][cur + off], &sh.acc_hi[m][cur + off], sum);
+          cur = kl;
+          sum = 0;
+        }
+        sum += (int)M[l * 33 + lane];  // a lane without a cell holds zeros
       }
+      if (cur >= 0 && sum != 0) shared_add64(&sh.acc_lo[m][cur + off], &sh.acc_hi[m][cur + off], sum);
     }
-    __syncwarp();  // the appended entries are visible to every lane
+    __syncwarp();  // ring entries visible, matrix read before the next chunk rewrites it
     while (dt - dh >= 32u) drain(32u);
   }
   if (dt != dh) drain(dt - dh);
