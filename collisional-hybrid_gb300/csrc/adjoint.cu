@@ -602,6 +602,8 @@ extern "C" ch_status ch_adjoint_create(const ch_params* p, int64_t np, const ch_
     return ch_fail(CH_ERR_UNSUPPORTED, "adjoint: full LHS/RHS, no as-written defects");
   if (p->nn_profile != CH_NN_UNIFORM) return ch_fail(CH_ERR_UNSUPPORTED, "adjoint: uniform neutral density");
   if (np > 0xFFFFFFFFll) return ch_fail(CH_ERR_ARG, "at most 2^32-1 ions");
+  if (p->Nx < 3 || p->Ny < 3 || p->Nz < 3 || (int64_t)p->Nx * p->Ny * p->Nz >= (1LL << 31))
+    return ch_fail(CH_ERR_ARG, "adjoint: grid %dx%dx%d (at least 3 and at most 2^31-1 nodes)", p->Nx, p->Ny, p->Nz);
   if (device >= 0) CH_CUDA_OK(cudaSetDevice(device));
   ch_adjoint* a = new (std::nothrow) ch_adjoint();
   if (!a) return ch_fail(CH_ERR_NOMEM, "host allocation");

@@ -185,7 +185,8 @@ static ch_status check_run(const ch_params& p, int r, const ch_params& p0) {
     return ch_fail(CH_ERR_UNSUPPORTED, "batch run %d: kappa_e != 0 makes A non-symmetric (CG needs kappa_e = 0)", r);
   if (p.faithful & ~(uint32_t)(CH_FAITHFUL_D2 | CH_FAITHFUL_D8))
     return ch_fail(CH_ERR_UNSUPPORTED, "batch run %d: faithful bits other than D2/D8", r);
-  if (p.Nx < 3 || p.Ny < 3 || p.Nz < 3 || p.Nx > CH_MAX_NX || p.Ny > CH_MAX_NY || p.Nz > CH_MAX_NZ)
+  if (p.Nx < 3 || p.Ny < 3 || p.Nz < 3 || p.Nx > CH_MAX_NX || p.Ny > CH_MAX_NY || p.Nz > CH_MAX_NZ ||
+      (int64_t)p.Nx * p.Ny * p.Nz >= (1LL << 31))
     return ch_fail(CH_ERR_ARG, "batch run %d: grid %dx%dx%d", r, p.Nx, p.Ny, p.Nz);
   if (!(p.x1 > p.x0) || !(p.y1 > p.y0) || !(p.z1 > p.z0) || !(p.mi > 0.0) || !(p.dt > 0.0))
     return ch_fail(CH_ERR_ARG, "batch run %d: empty domain, mass or dt", r);

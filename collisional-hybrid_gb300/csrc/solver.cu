@@ -390,7 +390,7 @@ __global__ void k_restrict(GridDesc gf, GridDesc gc, int hx, int hy, int hz, con
       for (int dj = -hy; dj <= hy; ++dj) {
         const T wj = hy ? (dj == 0 ? T(0.5) : T(0.25)) : T(1);
         const int j = ch_wrap(j0 + dj, gf.Ny);
-        const int64_t row = ((int64_t)k * gf.Ny + j) * gf.Nx;
+        const int row = (k * gf.Ny + j) * gf.Nx;  // grids have < 2^31 nodes
         for (int di = -hx; di <= hx; ++di) {
           const T wi = hx ? (di == 0 ? T(0.5) : T(0.25)) : T(1);
           acc += wk * wj * wi * in[row + ch_wrap(i0 + di, gf.Nx)];
@@ -417,7 +417,7 @@ __global__ void k_prolong_add(GridDesc gf, GridDesc gc, int hx, int hy, int hz, 
     if (hz) { K0 = k >> 1; K1 = (k & 1) ? ch_wrap(K0 + 1, gc.Nz) : K0; wk1 = (k & 1) ? T(0.5) : T(0); }
     else { K0 = K1 = k; wk1 = T(0); }
     const T wi0 = T(1) - wi1, wj0 = T(1) - wj1, wk0 = T(1) - wk1;
-    auto at = [&](int I, int J, int K) { return ec[((int64_t)K * gc.Ny + J) * gc.Nx + I]; };
+    auto at = [&](int I, int J, int K) { return ec[(K * gc.Ny + J) * gc.Nx + I]; };  // < 2^31 nodes
     const T v = wk0 * (wj0 * (wi0 * at(I0, J0, K0) + wi1 * at(I1, J0, K0)) +
                        wj1 * (wi0 * at(I0, J1, K0) + wi1 * at(I1, J1, K0))) +
                 wk1 * (wj0 * (wi0 * at(I0, J0, K1) + wi1 * at(I1, J0, K1)) +

@@ -7,28 +7,29 @@
 namespace ch {
 
 // ------------------------------------------------------------------ device helpers
+// Node indices of the 19-point stencil around a node.  Every grid has fewer
+// than 2^31 nodes, so the indices are 32-bit: each is the centre plus a sum
+// of per-axis steps, the periodic wrap folded into the step.
 struct Nb {
-  int64_t c, e, w, n, s, u, d;       // centre and faces (x+, x-, y+, y-, z+, z-)
-  int64_t en, es, wn, ws, eu, ed, wu, wd, nu, nd, su, sd;  // 12 edges
+  int c, e, w, n, s, u, d;       // centre and faces (x+, x-, y+, y-, z+, z-)
+  int en, es, wn, ws, eu, ed, wu, wd, nu, nd, su, sd;  // 12 edges
 };
 
-__device__ __forceinline__ Nb neighbours(const GridDesc& g, int64_t c) {
+__device__ __forceinline__ Nb neighbours(const GridDesc& g, int64_t c64) {
   int i, j, k;
-  ch_ijk(g, c, i, j, k);
-  const int ip = i + 1 == g.Nx ? 0 : i + 1, im = i == 0 ? g.Nx - 1 : i - 1;
-  const int jp = j + 1 == g.Ny ? 0 : j + 1, jm = j == 0 ? g.Ny - 1 : j - 1;
-  const int kp = k + 1 == g.Nz ? 0 : k + 1, km = k == 0 ? g.Nz - 1 : k - 1;
-  const int64_t X = g.Nx, XY = (int64_t)g.Nx * g.Ny;
-  const int64_t r0 = k * XY, rp = kp * XY, rm = km * XY;
-  const int64_t y0 = j * X, yp = jp * X, ym = jm * X;
+  ch_ijk(g, c64, i, j, k);
+  const int X = g.Nx, XY = g.Nx * g.Ny;
+  const int xp = i + 1 == g.Nx ? 1 - X : 1, xm = i == 0 ? X - 1 : -1;
+  const int yp = j + 1 == g.Ny ? X - XY : X, ym = j == 0 ? XY - X : -X;
+  const int zp = k + 1 == g.Nz ? XY - (int)g.N : XY, zm = k == 0 ? (int)g.N - XY : -XY;
   Nb b;
-  b.c = r0 + y0 + i;
-  b.e = r0 + y0 + ip; b.w = r0 + y0 + im;
-  b.n = r0 + yp + i;  b.s = r0 + ym + i;
-  b.u = rp + y0 + i;  b.d = rm + y0 + i;
-  b.en = r0 + yp + ip; b.es = r0 + ym + ip; b.wn = r0 + yp + im; b.ws = r0 + ym + im;
-  b.eu = rp + y0 + ip; b.ed = rm + y0 + ip; b.wu = rp + y0 + im; b.wd = rm + y0 + im;
-  b.nu = rp + yp + i;  b.nd = rm + yp + i;  b.su = rp + ym + i;  b.sd = rm + ym + i;
+  b.c = (int)c64;
+  b.e = b.c + xp; b.w = b.c + xm;
+  b.n = b.c + yp; b.s = b.c + ym;
+  b.u = b.c + zp; b.d = b.c + zm;
+  b.en = b.e + yp; b.es = b.e + ym; b.wn = b.w + yp; b.ws = b.w + ym;
+  b.eu = b.e + zp; b.ed = b.e + zm; b.wu = b.w + zp; b.wd = b.w + zm;
+  b.nu = b.n + zp; b.nd = b.n + zm; b.su = b.s + zp; b.sd = b.s + zm;
   return b;
 }
 
