@@ -45,12 +45,42 @@ OpCoefs op_coefs(const ch_params& p, const GridDesc& g) {
 
 #define GRID_LOOP(c, N) for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < (N); c += (int64_t)gridDim.x * blockDim.x)
 
+// Programmatic dependent launch.  The solver is a chain of short dependent
+// kernels, so each one is launched with programmatic stream serialization:
+// it may be scheduled while the kernel before it finishes, waits in
+// pdl_enter (griddepcontrol.wait: the previous grid has completed and its
+// writes are visible) before its first read, and then lets the next kernel be
+// scheduled.  The next kernel is released only when every block of this one
+// has done so, so blocks waiting there never hold back a grid still running.
+// Launched without the attribute, the wait returns at once.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+template <typename... KP, typename... A>
+static void launch(void (*k)(KP...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A... args) {
+  static_assert(sizeof...(KP) == sizeof...(A), "kernel arguments");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, (KP)args...);  // errors surface at the stream's next check, as with <<<>>>
+  ::ch::note_launch();
+}
+
 // ------------------------------------------------------------------ kernels
 // y = A x; partial w.y (w may be null).
 template <typename T>
 __global__ void __launch_bounds__(256) k_apply(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
                                                const T* __restrict__ x, T* __restrict__ y, const T* __restrict__ w,
                                                double* part) {
+  pdl_enter();
   T d0 = T(0);
   GRID_LOOP(c, g.N) {
     const Nb b = neighbours(g, c);
@@ -69,6 +99,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_apply_dot2(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
                                                     const T* __restrict__ x, T* __restrict__ t,
                                                     const T* __restrict__ s, double* part) {
+  pdl_enter();
   T d0 = T(0), d1 = T(0);
   GRID_LOOP(c, g.N) {
     const Nb b = neighbours(g, c);
@@ -86,6 +117,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_residual(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
                                                   const T* __restrict__ b, const T* __restrict__ x,
                                                   T* __restrict__ r, double* part) {
+  pdl_enter();
   T d0 = T(0);
   GRID_LOOP(c, g.N) {
     const Nb nb = neighbours(g, c);
@@ -99,6 +131,7 @@ __global__ void __launch_bounds__(256) k_residual(GridDesc g, DevCoefs<T> C, con
 
 template <typename T>
 __global__ void k_jacobi(GridDesc g, DevCoefs<T> C, const T* __restrict__ n, T* __restrict__ dinv, int jacobi) {
+  pdl_enter();
   GRID_LOOP(c, g.N) {
     const T d = jacobi ? diag_row<T>(C, n, neighbours(g, c)) : T(1);
     dinv[c] = d != T(0) ? T(1) / d : T(1);
@@ -109,6 +142,7 @@ __global__ void k_jacobi(GridDesc g, DevCoefs<T> C, const T* __restrict__ n, T* 
 template <typename T>
 __global__ void k_prec_dot(int64_t N, const T* __restrict__ dinv, const T* __restrict__ r, T* __restrict__ z,
                            double* part) {
+  pdl_enter();
   T d0 = T(0), d1 = T(0);
   GRID_LOOP(c, N) {
     const T rv = r[c];
@@ -130,6 +164,7 @@ enum { OP_SET_RZ_RR = 0, OP_CG_ALPHA, OP_CG_BETA, OP_RR, OP_BI_ALPHA, OP_BI_OMEG
 
 // Fixed-order reduction of K partials and the scalar update of one step.
 __global__ void k_scalar(const double* __restrict__ part, int nb, int K, int op, double* scal, double invN) {
+  pdl_enter();
   __shared__ double sm[3][32];
   __shared__ double red[3];
   for (int q = 0; q < K; ++q) {
@@ -185,6 +220,7 @@ template <typename T>
 __global__ void k_cg_xr(int64_t N, const double* __restrict__ scal, T* __restrict__ x, T* __restrict__ r,
                         const T* __restrict__ p, const T* __restrict__ q, const T* __restrict__ dinv,
                         T* __restrict__ z, double* part) {
+  pdl_enter();
   const T a = (T)scal[S_ALPHA];
   T d0 = T(0), d1 = T(0);
   GRID_LOOP(c, N) {
@@ -204,6 +240,7 @@ __global__ void k_cg_xr(int64_t N, const double* __restrict__ scal, T* __restric
 template <typename T>
 __global__ void k_cg_xr_plain(int64_t N, const double* __restrict__ scal, T* __restrict__ x, T* __restrict__ r,
                               const T* __restrict__ p, const T* __restrict__ q) {
+  pdl_enter();
   const T a = (T)scal[S_ALPHA];
   GRID_LOOP(c, N) {
     x[c] += a * p[c];
@@ -214,6 +251,7 @@ __global__ void k_cg_xr_plain(int64_t N, const double* __restrict__ scal, T* __r
 template <typename T>
 __global__ void k_cg_p(int64_t N, const double* __restrict__ scal, const T* __restrict__ z, T* __restrict__ p,
                        int first) {
+  pdl_enter();
   const T b = first ? T(0) : (T)scal[S_BETA];
   GRID_LOOP(c, N) p[c] = z[c] + b * p[c];
 }
@@ -222,6 +260,7 @@ __global__ void k_cg_p(int64_t N, const double* __restrict__ scal, const T* __re
 template <typename T>
 __global__ void k_bi_p(int64_t N, const double* __restrict__ scal, const T* __restrict__ r, T* __restrict__ p,
                        const T* __restrict__ v, const T* __restrict__ dinv, T* __restrict__ y, int first) {
+  pdl_enter();
   const T b = first ? T(0) : (T)scal[S_BETA], w = first ? T(0) : (T)scal[S_OMEGA];
   GRID_LOOP(c, N) {
     const T pv = r[c] + b * (p[c] - w * v[c]);
@@ -234,6 +273,7 @@ __global__ void k_bi_p(int64_t N, const double* __restrict__ scal, const T* __re
 template <typename T>
 __global__ void k_bi_s(int64_t N, const double* __restrict__ scal, const T* __restrict__ r, const T* __restrict__ v,
                        const T* __restrict__ dinv, T* __restrict__ s, T* __restrict__ sh, double* part) {
+  pdl_enter();
   const T a = (T)scal[S_ALPHA];
   T d0 = T(0);
   GRID_LOOP(c, N) {
@@ -251,6 +291,7 @@ template <typename T>
 __global__ void k_bi_xr(int64_t N, const double* __restrict__ scal, T* __restrict__ x, const T* __restrict__ y,
                         const T* __restrict__ sh, T* __restrict__ r, const T* __restrict__ s, const T* __restrict__ t,
                         const T* __restrict__ rh, double* part) {
+  pdl_enter();
   const T a = (T)scal[S_ALPHA], w = (T)scal[S_OMEGA];
   T d0 = T(0), d1 = T(0);
   GRID_LOOP(c, N) {
@@ -268,6 +309,7 @@ __global__ void k_bi_xr(int64_t N, const double* __restrict__ scal, T* __restric
 template <typename T>
 __global__ void k_bi_half(int64_t N, const double* __restrict__ scal, T* __restrict__ x, const T* __restrict__ y,
                           T* __restrict__ r, const T* __restrict__ s) {
+  pdl_enter();
   const T a = (T)scal[S_ALPHA];
   GRID_LOOP(c, N) {
     x[c] += a * y[c];
@@ -276,38 +318,46 @@ __global__ void k_bi_half(int64_t N, const double* __restrict__ scal, T* __restr
 }
 
 template <typename T>
-__global__ void k_copy(int64_t N, const T* __restrict__ a, T* __restrict__ b) { GRID_LOOP(c, N) b[c] = a[c]; }
+__global__ void k_copy(int64_t N, const T* __restrict__ a, T* __restrict__ b) {
+  pdl_enter(); GRID_LOOP(c, N) b[c] = a[c]; }
 template <typename T>
-__global__ void k_zero(int64_t N, T* __restrict__ a) { GRID_LOOP(c, N) a[c] = T(0); }
+__global__ void k_zero(int64_t N, T* __restrict__ a) {
+  pdl_enter(); GRID_LOOP(c, N) a[c] = T(0); }
 
 template <typename T>
 __global__ void k_sum(int64_t N, const T* __restrict__ a, double* part) {
+  pdl_enter();
   double d[1] = {0.0};
   GRID_LOOP(c, N) d[0] += (double)a[c];
   partials<1>(d, part);
 }
 __global__ void k_sub_mean(int64_t N, double* __restrict__ a, const double* __restrict__ scal) {
+  pdl_enter();
   const double m = scal[S_MEAN];
   GRID_LOOP(c, N) a[c] -= m;
 }
 template <typename T>
 __global__ void k_dot(int64_t N, const T* __restrict__ a, const T* __restrict__ b, double* part) {
+  pdl_enter();
   T d0 = T(0);
   GRID_LOOP(c, N) d0 += a[c] * b[c];
   double d[1] = {(double)d0};
   partials<1>(d, part);
 }
 __global__ void k_dot64(int64_t N, const double* __restrict__ a, const double* __restrict__ b, double* part) {
+  pdl_enter();
   double d[1] = {0.0};
   GRID_LOOP(c, N) d[0] += a[c] * b[c];
   partials<1>(d, part);
 }
 // r32 = (float)(r64 * s)
 __global__ void k_down(int64_t N, const double* __restrict__ a, double s, float* __restrict__ b) {
+  pdl_enter();
   GRID_LOOP(c, N) b[c] = (float)(a[c] * s);
 }
 // x64 += (double)x32 * s
 __global__ void k_up_add(int64_t N, const float* __restrict__ a, double s, double* __restrict__ x) {
+  pdl_enter();
   GRID_LOOP(c, N) x[c] += (double)a[c] * s;
 }
 
@@ -316,6 +366,7 @@ __global__ void k_up_add(int64_t N, const float* __restrict__ a, double s, doubl
 // (cscale = 2 dx dy dz / det, the factor of both).
 __global__ void k_rhs(GridDesc g, int rhs_type, RhsCoefs K, double cscale, const double* __restrict__ mom,
                       const double* __restrict__ scal, double* __restrict__ b) {
+  pdl_enter();
   const int64_t N = g.N;
   const double* n = mom;
   const double* Gx = mom + N;
@@ -345,6 +396,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_smooth(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
                                                 const T* __restrict__ dinv, const T* __restrict__ b,
                                                 const T* __restrict__ x, T* __restrict__ y, T w) {
+  pdl_enter();
   GRID_LOOP(c, g.N) {
     if (!x) {
       y[c] = w * dinv[c] * b[c];
@@ -361,6 +413,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_smooth_zero2(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
                                                       const T* __restrict__ dinv, const T* __restrict__ b,
                                                       T* __restrict__ y, T w) {
+  pdl_enter();
   auto t = [&](int64_t i) { return w * dinv[i] * b[i]; };
   GRID_LOOP(c, g.N) y[c] = t(c) + w * dinv[c] * (b[c] - apply_row_at<T>(C, n, t, neighbours(g, c)));
 }
@@ -370,6 +423,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_resid(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
                                                const T* __restrict__ b, const T* __restrict__ x,
                                                T* __restrict__ r) {
+  pdl_enter();
   GRID_LOOP(c, g.N) r[c] = b[c] - apply_row<T>(C, n, x, neighbours(g, c));
 }
 
@@ -379,6 +433,7 @@ __global__ void __launch_bounds__(256) k_resid(GridDesc g, DevCoefs<T> C, const 
 template <typename T>
 __global__ void k_restrict(GridDesc gf, GridDesc gc, int hx, int hy, int hz, const T* __restrict__ in,
                            T* __restrict__ out, T scale) {
+  pdl_enter();
   GRID_LOOP(c, gc.N) {
     int I, J, K;
     ch_ijk(gc, c, I, J, K);
@@ -405,6 +460,7 @@ __global__ void k_restrict(GridDesc gf, GridDesc gc, int hx, int hy, int hz, con
 template <typename T>
 __global__ void k_prolong_add(GridDesc gf, GridDesc gc, int hx, int hy, int hz, const T* __restrict__ ec,
                               T* __restrict__ xf) {
+  pdl_enter();
   GRID_LOOP(c, gf.N) {
     int i, j, k;
     ch_ijk(gf, c, i, j, k);
@@ -432,6 +488,7 @@ template <typename T>
 __global__ void __launch_bounds__(1024) k_coarse(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
                                                  const T* __restrict__ dinv, const T* __restrict__ b,
                                                  T* __restrict__ x, int sweeps, T w) {
+  pdl_enter();
   extern __shared__ unsigned char smem_raw[];
   T* xa = reinterpret_cast<T*>(smem_raw);
   T* xb = xa + g.N;
@@ -449,6 +506,7 @@ __global__ void __launch_bounds__(1024) k_coarse(GridDesc g, DevCoefs<T> C, cons
 // partials (r.z, r.r) after a multigrid preconditioner application
 template <typename T>
 __global__ void k_dot_rz_rr(int64_t N, const T* __restrict__ r, const T* __restrict__ z, double* part) {
+  pdl_enter();
   T d0 = T(0), d1 = T(0);
   GRID_LOOP(c, N) {
     const T rv = r[c];
@@ -465,6 +523,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_smooth_dot(GridDesc g, DevCoefs<T> C, const T* __restrict__ n,
                                                     const T* __restrict__ dinv, const T* __restrict__ b,
                                                     const T* __restrict__ x, T* __restrict__ y, T w, double* part) {
+  pdl_enter();
   T d0 = T(0), d1 = T(0);
   GRID_LOOP(c, g.N) {
     const Nb nb = neighbours(g, c);
@@ -607,9 +666,9 @@ void PotentialSolver::mg_update(MGHier<T>& h, const T* n_fine, cudaStream_t s) {
   h.n[0] = const_cast<T*>(n_fine);
   for (int l = 0; l < h.L; ++l) {
     if (l > 0)
-      k_restrict<T><<<grid_n(h.g[l].N, sms_), 256, 0, s>>>(h.g[l - 1], h.g[l], h.hx[l - 1], h.hy[l - 1], h.hz[l - 1],
-                                                          h.n[l - 1], h.n[l], T(1)), ::ch::note_launch();
-    k_jacobi<T><<<grid_n(h.g[l].N, sms_), 256, 0, s>>>(h.g[l], h.C[l], h.n[l], h.dinv[l], 1), ::ch::note_launch();
+      launch(k_restrict<T>, grid_n(h.g[l].N, sms_), 256, 0, s, h.g[l - 1], h.g[l], h.hx[l - 1], h.hy[l - 1], h.hz[l - 1],
+                                                          h.n[l - 1], h.n[l], T(1));
+    launch(k_jacobi<T>, grid_n(h.g[l].N, sms_), 256, 0, s, h.g[l], h.C[l], h.n[l], h.dinv[l], 1);
   }
 }
 
@@ -623,42 +682,42 @@ void PotentialSolver::mg_vcycle(MGHier<T>& h, int l, const T* b, T* x, cudaStrea
   const T w = (T)MG_OMEGA;
   if (l == h.L - 1) {
     const size_t sh = 2 * sizeof(T) * g.N;
-    k_coarse<T><<<1, 1024, sh, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, x, mg_coarse_sweeps(g), w), ::ch::note_launch();
-    if (part) k_dot_rz_rr<T><<<nb_, 256, 0, s>>>(g.N, b, x, part), ::ch::note_launch();
+    launch(k_coarse<T>, 1, 1024, sh, s, g, h.C[l], h.n[l], h.dinv[l], b, x, mg_coarse_sweeps(g), w);
+    if (part) launch(k_dot_rz_rr<T>, nb_, 256, 0, s, g.N, b, x, part);
     return;
   }
   // pre-smoothing (MG_NU = 2 sweeps from zero, in one pass)
   static_assert(MG_NU == 2, "the pre-smoothing pass fuses exactly two sweeps");
-  k_smooth_zero2<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, x, w), ::ch::note_launch();
+  launch(k_smooth_zero2<T>, nb, 256, 0, s, g, h.C[l], h.n[l], h.dinv[l], b, x, w);
   // residual, restriction, coarse correction, prolongation
-  k_resid<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], b, x, h.r[l]), ::ch::note_launch();
-  k_restrict<T><<<grid_n(h.g[l + 1].N, sms_), 256, 0, s>>>(g, h.g[l + 1], h.hx[l], h.hy[l], h.hz[l], h.r[l],
-                                                          h.b[l + 1], (T)h.sR[l]), ::ch::note_launch();
+  launch(k_resid<T>, nb, 256, 0, s, g, h.C[l], h.n[l], b, x, h.r[l]);
+  launch(k_restrict<T>, grid_n(h.g[l + 1].N, sms_), 256, 0, s, g, h.g[l + 1], h.hx[l], h.hy[l], h.hz[l], h.r[l],
+                                                          h.b[l + 1], (T)h.sR[l]);
   mg_vcycle<T>(h, l + 1, h.b[l + 1], h.x[l + 1], s);
-  k_prolong_add<T><<<nb, 256, 0, s>>>(g, h.g[l + 1], h.hx[l], h.hy[l], h.hz[l], h.x[l + 1], x), ::ch::note_launch();
+  launch(k_prolong_add<T>, nb, 256, 0, s, g, h.g[l + 1], h.hx[l], h.hy[l], h.hz[l], h.x[l + 1], x);
   // post-smoothing: x -> t -> x
   for (int k = 0; k < MG_NU; ++k) {
     T* src = (k % 2 == 0) ? x : h.t[l];
     T* dst = (k % 2 == 0) ? h.t[l] : x;
     if (part && k == MG_NU - 1)
-      k_smooth_dot<T><<<nb_, 256, 0, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, src, dst, w, part), ::ch::note_launch();
+      launch(k_smooth_dot<T>, nb_, 256, 0, s, g, h.C[l], h.n[l], h.dinv[l], b, src, dst, w, part);
     else
-      k_smooth<T><<<nb, 256, 0, s>>>(g, h.C[l], h.n[l], h.dinv[l], b, src, dst, w), ::ch::note_launch();
+      launch(k_smooth<T>, nb, 256, 0, s, g, h.C[l], h.n[l], h.dinv[l], b, src, dst, w);
   }
 }
 
 double PotentialSolver::dot64(const double* a, const double* b, cudaStream_t s) {
-  k_dot64<<<nb_, 256, 0, s>>>(N_, a, b, part_), ::ch::note_launch();
-  k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_RR, scal_, 0.0), ::ch::note_launch();
+  launch(k_dot64, nb_, 256, 0, s, N_, a, b, part_);
+  launch(k_scalar, 1, 256, 0, s, part_, nb_, 1, OP_RR, scal_, 0.0);
   cudaMemcpyAsync(hscal_, scal_, sizeof(double) * S_NSLOT, cudaMemcpyDeviceToHost, s);
   cudaStreamSynchronize(s);
   return hscal_[S_RR];
 }
 
 void PotentialSolver::remove_mean64(double* v, cudaStream_t s) {
-  k_sum<double><<<nb_, 256, 0, s>>>(N_, v, part_), ::ch::note_launch();
-  k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_MEAN, scal_, 1.0 / (double)N_), ::ch::note_launch();
-  k_sub_mean<<<nb_, 256, 0, s>>>(N_, v, scal_), ::ch::note_launch();
+  launch(k_sum<double>, nb_, 256, 0, s, N_, v, part_);
+  launch(k_scalar, 1, 256, 0, s, part_, nb_, 1, OP_MEAN, scal_, 1.0 / (double)N_);
+  launch(k_sub_mean, nb_, 256, 0, s, N_, v, scal_);
 }
 
 void PotentialSolver::build_rhs(const double* mom, double* b, cudaStream_t s) {
@@ -669,17 +728,17 @@ void PotentialSolver::build_rhs(const double* mom, double* b, cudaStream_t s) {
   const double R20 = Kx * Kz - Ky, R21 = Ky * Kz + Kx, R22 = 1 + Kz * Kz;
   if (p_.rhs_type != CH_RHS_FULL) {
     // mean density (VecMean, src/rhs.c:34,93)
-    k_sum<double><<<nb_, 256, 0, s>>>(N_, mom, part_), ::ch::note_launch();
-    k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_MEAN, scal_, 1.0 / (double)N_), ::ch::note_launch();
+    launch(k_sum<double>, nb_, 256, 0, s, N_, mom, part_);
+    launch(k_scalar, 1, 256, 0, s, part_, nb_, 1, OP_MEAN, scal_, 1.0 / (double)N_);
   }
   const double R[9] = {R00, R01, R02, R10, R11, R12, R20, R21, R22};
   const RhsCoefs K = rhs_coefs(R, det, p_.E0, p_.cth, p_.cG, (p_.faithful & CH_FAITHFUL_D8) != 0, g_.dx, g_.dy, g_.dz);
-  k_rhs<<<nb_, 256, 0, s>>>(g_, p_.rhs_type, K, 2.0 * g_.dx * g_.dy * g_.dz / det, mom, scal_, b), ::ch::note_launch();
+  launch(k_rhs, nb_, 256, 0, s, g_, p_.rhs_type, K, 2.0 * g_.dx * g_.dy * g_.dz / det, mom, scal_, b);
   if (p_.rhs_type != CH_RHS_CONSTANT) remove_mean64(b, s);  // MatNullSpaceRemove (src/rhs.c:294-296)
 }
 
 void PotentialSolver::apply64(const double* n, const double* x, double* y, cudaStream_t s) {
-  k_apply<double><<<nb_, 256, 0, s>>>(g_, dev_coefs<double>(c_), n, x, y, nullptr, nullptr), ::ch::note_launch();
+  launch(k_apply<double>, nb_, 256, 0, s, g_, dev_coefs<double>(c_), n, x, y, nullptr, nullptr);
 }
 
 // Preconditioned Krylov solve of A x = b in precision T (x holds the start).
@@ -701,29 +760,29 @@ ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* 
   T* sh = f64 ? (T*)sh_ : (T*)sh32_;
   T* dinv = f64 ? (T*)dinv_ : (T*)dinv32_;
   const int nb = nb_;
-  if (!mg) k_jacobi<T><<<nb, 256, 0, s>>>(g, C, n, dinv, p_.pc_type == CH_PC_JACOBI), ::ch::note_launch();
+  if (!mg) launch(k_jacobi<T>, nb, 256, 0, s, g, C, n, dinv, p_.pc_type == CH_PC_JACOBI);
   // z = M r with M = Jacobi (fused) or one multigrid V-cycle
   auto precond = [&](const T* rr_, T* zz_) {
     if (mg) {
       mg_vcycle<T>(*mg, 0, rr_, zz_, s, part_);  // with the partials (r.z, r.r)
     } else {
-      k_prec_dot<T><<<nb, 256, 0, s>>>(N, dinv, rr_, zz_, part_), ::ch::note_launch();
+      launch(k_prec_dot<T>, nb, 256, 0, s, N, dinv, rr_, zz_, part_);
     }
   };
   if (zero_guess) {
-    k_zero<T><<<nb, 256, 0, s>>>(N, x), ::ch::note_launch();
-    k_copy<T><<<nb, 256, 0, s>>>(N, b, r), ::ch::note_launch();
+    launch(k_zero<T>, nb, 256, 0, s, N, x);
+    launch(k_copy<T>, nb, 256, 0, s, N, b, r);
   } else {
-    k_residual<T><<<nb, 256, 0, s>>>(g, C, n, b, x, r, part_), ::ch::note_launch();
+    launch(k_residual<T>, nb, 256, 0, s, g, C, n, b, x, r, part_);
   }
   precond(r, z);
-  k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_SET_RZ_RR, scal_, 0.0), ::ch::note_launch();
+  launch(k_scalar, 1, 256, 0, s, part_, nb, 2, OP_SET_RZ_RR, scal_, 0.0);
   // ||b||: given by the caller (no host round trip; the first iterations
   // then run even when the start is already converged), or measured
   double bnorm = bnorm_known, rr = 0.0;
   if (!(bnorm_known >= 0.0)) {
-    k_dot<T><<<nb, 256, 0, s>>>(N, b, b, part_), ::ch::note_launch();
-    k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_TMP, scal_, 0.0), ::ch::note_launch();
+    launch(k_dot<T>, nb, 256, 0, s, N, b, b, part_);
+    launch(k_scalar, 1, 256, 0, s, part_, nb, 1, OP_TMP, scal_, 0.0);
     CH_CUDA_OK(cudaMemcpyAsync(hscal_, scal_, sizeof(double) * S_NSLOT, cudaMemcpyDeviceToHost, s));
     CH_CUDA_OK(cudaStreamSynchronize(s));
     bnorm = sqrt(hscal_[S_TMP]);
@@ -739,41 +798,39 @@ ch_status PotentialSolver::krylov(const GridDesc& g, const T* n, const T* b, T* 
   // One iteration, enqueued on s directly or under graph capture.  Scalars
   // stay on the device, so an iteration has no host dependency.
   auto cg_body = [&]() {
-    k_apply<T><<<nb, 256, 0, s>>>(g, C, n, pp, q, pp, part_), ::ch::note_launch();
-    k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_CG_ALPHA, scal_, 0.0), ::ch::note_launch();
+    launch(k_apply<T>, nb, 256, 0, s, g, C, n, pp, q, pp, part_);
+    launch(k_scalar, 1, 256, 0, s, part_, nb, 1, OP_CG_ALPHA, scal_, 0.0);
     if (mg) {
-      k_cg_xr_plain<T><<<nb, 256, 0, s>>>(N, scal_, x, r, pp, q), ::ch::note_launch();
+      launch(k_cg_xr_plain<T>, nb, 256, 0, s, N, scal_, x, r, pp, q);
       precond(r, z);
     } else {
-      k_cg_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, r, pp, q, dinv, z, part_), ::ch::note_launch();
+      launch(k_cg_xr<T>, nb, 256, 0, s, N, scal_, x, r, pp, q, dinv, z, part_);
     }
-    k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_CG_BETA, scal_, 0.0), ::ch::note_launch();
-    k_cg_p<T><<<nb, 256, 0, s>>>(N, scal_, z, pp, 0), ::ch::note_launch();
+    launch(k_scalar, 1, 256, 0, s, part_, nb, 2, OP_CG_BETA, scal_, 0.0);
+    launch(k_cg_p<T>, nb, 256, 0, s, N, scal_, z, pp, 0);
   };
   // BiCGStab, right preconditioned (van der Vorst 1992); p = v = 0 at the
   // start makes the first p = r whatever beta and omega hold.
   auto bi_body = [&]() {
-    k_bi_p<T><<<nb, 256, 0, s>>>(N, scal_, r, pp, q, mg ? (const T*)nullptr : dinv, z, 0),
-        ::ch::note_launch();  // z = y = M p
+    launch(k_bi_p<T>, nb, 256, 0, s, N, scal_, r, pp, q, mg ? (const T*)nullptr : dinv, z, 0);  // z = y = M p
     if (mg) mg_vcycle<T>(*mg, 0, pp, z, s);
-    k_apply<T><<<nb, 256, 0, s>>>(g, C, n, z, q, rh, part_), ::ch::note_launch();  // v = A y; rh.v
-    k_scalar<<<1, 256, 0, s>>>(part_, nb, 1, OP_BI_ALPHA, scal_, 0.0), ::ch::note_launch();
-    k_bi_s<T><<<nb, 256, 0, s>>>(N, scal_, r, q, mg ? (const T*)nullptr : dinv, sv, sh, part_),
-        ::ch::note_launch();
+    launch(k_apply<T>, nb, 256, 0, s, g, C, n, z, q, rh, part_);  // v = A y; rh.v
+    launch(k_scalar, 1, 256, 0, s, part_, nb, 1, OP_BI_ALPHA, scal_, 0.0);
+    launch(k_bi_s<T>, nb, 256, 0, s, N, scal_, r, q, mg ? (const T*)nullptr : dinv, sv, sh, part_);
     if (mg) mg_vcycle<T>(*mg, 0, sv, sh, s);
-    k_apply_dot2<T><<<nb, 256, 0, s>>>(g, C, n, sh, tv, sv, part_), ::ch::note_launch();
-    k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_OMEGA, scal_, 0.0), ::ch::note_launch();
-    k_bi_xr<T><<<nb, 256, 0, s>>>(N, scal_, x, z, sh, r, sv, tv, rh, part_), ::ch::note_launch();
-    k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_BI_BETA, scal_, 0.0), ::ch::note_launch();
+    launch(k_apply_dot2<T>, nb, 256, 0, s, g, C, n, sh, tv, sv, part_);
+    launch(k_scalar, 1, 256, 0, s, part_, nb, 2, OP_BI_OMEGA, scal_, 0.0);
+    launch(k_bi_xr<T>, nb, 256, 0, s, N, scal_, x, z, sh, r, sv, tv, rh, part_);
+    launch(k_scalar, 1, 256, 0, s, part_, nb, 2, OP_BI_BETA, scal_, 0.0);
   };
   const bool cg = p_.ksp_type == CH_KSP_CG;
   if (cg) {
-    k_cg_p<T><<<nb, 256, 0, s>>>(N, scal_, z, pp, 1), ::ch::note_launch();
+    launch(k_cg_p<T>, nb, 256, 0, s, N, scal_, z, pp, 1);
   } else {
-    k_copy<T><<<nb, 256, 0, s>>>(N, r, rh), ::ch::note_launch();
-    k_zero<T><<<nb, 256, 0, s>>>(N, pp), ::ch::note_launch();
-    k_zero<T><<<nb, 256, 0, s>>>(N, q), ::ch::note_launch();  // v
-    k_scalar<<<1, 256, 0, s>>>(part_, nb, 2, OP_SET_BICG, scal_, 0.0), ::ch::note_launch();
+    launch(k_copy<T>, nb, 256, 0, s, N, r, rh);
+    launch(k_zero<T>, nb, 256, 0, s, N, pp);
+    launch(k_zero<T>, nb, 256, 0, s, N, q);  // v
+    launch(k_scalar, 1, 256, 0, s, part_, nb, 2, OP_SET_BICG, scal_, 0.0);
   }
   // the iteration as one CUDA graph (captured once per buffer set)
   GraphKey key{(int)sizeof(T), (int)p_.ksp_type, (const void*)mg, (const void*)n, (const void*)b, (const void*)x};
@@ -846,8 +903,8 @@ ch_status PotentialSolver::solve_fp64(const double* n, const double* b, double* 
   if (rc) return rc;
   if (singular) remove_mean64(phi, s);
   // true residual
-  k_residual<double><<<nb_, 256, 0, s>>>(g_, dev_coefs<double>(c_), n, b, phi, r_, part_), ::ch::note_launch();
-  k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_RR, scal_, 0.0), ::ch::note_launch();
+  launch(k_residual<double>, nb_, 256, 0, s, g_, dev_coefs<double>(c_), n, b, phi, r_, part_);
+  launch(k_scalar, 1, 256, 0, s, part_, nb_, 1, OP_RR, scal_, 0.0);
   CH_CUDA_OK(cudaMemcpyAsync(hscal_, scal_, sizeof(double) * S_NSLOT, cudaMemcpyDeviceToHost, s));
   CH_CUDA_OK(cudaStreamSynchronize(s));
   st->iterations = its;
@@ -862,7 +919,7 @@ ch_status PotentialSolver::solve_fp64(const double* n, const double* b, double* 
 ch_status PotentialSolver::solve_mixed(const double* n, const double* b, double* phi, SolveStats* st,
                                        cudaStream_t s) {
   const DevCoefs<double> C64 = dev_coefs<double>(c_);
-  k_down<<<nb_, 256, 0, s>>>(N_, n, 1.0, n32_), ::ch::note_launch();
+  launch(k_down, nb_, 256, 0, s, N_, n, 1.0, n32_);
   MGHier<float>* mg = nullptr;
   if (p_.pc_type == CH_PC_MG) {
     ch_status rm = mg_build<float>(mg32_);
@@ -878,21 +935,21 @@ ch_status PotentialSolver::solve_mixed(const double* n, const double* b, double*
   int total = 0, ref = 0;
   double rn = 0.0;
   for (; ref < 50; ++ref) {
-    k_residual<double><<<nb_, 256, 0, s>>>(g_, C64, n, b, phi, r_, part_), ::ch::note_launch();
-    k_scalar<<<1, 256, 0, s>>>(part_, nb_, 1, OP_RR, scal_, 0.0), ::ch::note_launch();
+    launch(k_residual<double>, nb_, 256, 0, s, g_, C64, n, b, phi, r_, part_);
+    launch(k_scalar, 1, 256, 0, s, part_, nb_, 1, OP_RR, scal_, 0.0);
     CH_CUDA_OK(cudaMemcpyAsync(hscal_ + S_RR, scal_ + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s));
     CH_CUDA_OK(cudaStreamSynchronize(s));
     rn = sqrt(hscal_[S_RR]);
     if (rn <= tol || rn == 0.0) break;
     const double sc = 1.0 / rn;
-    k_down<<<nb_, 256, 0, s>>>(N_, r_, sc, b32_), ::ch::note_launch();
+    launch(k_down, nb_, 256, 0, s, N_, r_, sc, b32_);
     int its = 0;
     double rin = 0.0;
     // b32 = r / ||r|| has unit norm up to its FP32 rounding
     ch_status rc = krylov<float>(g_, n32_, b32_, x32_, inner_rtol, p_.ksp_max_it, true, &its, &rin, mg, s, 1.0);
     if (rc) return rc;
     total += its;
-    k_up_add<<<nb_, 256, 0, s>>>(N_, x32_, rn, phi), ::ch::note_launch();
+    launch(k_up_add, nb_, 256, 0, s, N_, x32_, rn, phi);
     remove_mean64(phi, s);
   }
   st->iterations = total;

@@ -9,6 +9,9 @@ prints one JSON line.
         steps; one k_batch_pass and one k_batch_solve launch per step.
     --mode adjoint: a ch_adjoint run (FP64, --grid^3, --ppc ions per cell,
         --steps steps): one recorded forward and one gradient.
+    --mode solve: --steps steps of the plasma of the pass mode; the solves
+        inside them (warm start from the previous step's potential) are the
+        ones a run makes; prints the solve time, iterations and refinements.
 
     python collisional-hybrid_gb300/profile_pass.py --grid 128 --ppc 64 --nu 0.5
 """
@@ -31,7 +34,7 @@ def main(argv=None):
     ap.add_argument("--sort-period", type=int, default=4)
     ap.add_argument("--warm", type=int, default=3)
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
-    ap.add_argument("--mode", choices=["pass", "ensemble", "adjoint"], default="pass")
+    ap.add_argument("--mode", choices=["pass", "ensemble", "adjoint", "solve"], default="pass")
     ap.add_argument("--runs", type=int, default=8)
     ap.add_argument("--steps", type=int, default=4)
     a = ap.parse_args(argv)
@@ -40,6 +43,8 @@ def main(argv=None):
         return ensemble(m, a)
     if a.mode == "adjoint":
         return adjoint(m, a)
+    if a.mode == "solve":
+        return solve(m, a)
     N = a.grid
     p = m.params_for((N, N, N), precision=m.PRECISION[a.precision], E0=(a.Ex, 0.0, 0.0), nui=a.nu, ksp_rtol=1e-10,
                      pc_type=m.PC["mg"], sort_period=a.sort_period, mn=(1.0 if a.nu > 0 else 0.0))
@@ -57,6 +62,23 @@ def main(argv=None):
         h.reset_profile(); h.UpdatePositions(); out["move_ms"] = h.profile()["pass_ms"]
         h.reset_profile(); h.CollectVlasovQuantities(copy=False); out["deposit_ms"] = h.profile()["pass_ms"]
     print(json.dumps(out))
+
+
+def solve(m, a):
+    N = a.grid
+    p = m.params_for((N, N, N), precision=m.PRECISION[a.precision], E0=(a.Ex, 0.0, 0.0), nui=a.nu, ksp_rtol=1e-10,
+                     pc_type=m.PC["mg"], sort_period=a.sort_period, mn=(1.0 if a.nu > 0 else 0.0))
+    with m.Hybrid(p) as h:
+        h.load(N ** 3 * a.ppc, m.loader(amp=(0.02, 0.02, 0.02), phase=tuple(m.mode_phases(1))))
+        h.CollectVlasovQuantities(copy=False)
+        h.ComputePotential(copy=False)
+        h.set_profiling(True)
+        rows = []
+        for s in range(a.steps):
+            h.reset_profile()
+            info = h.step(s, 1)
+            rows.append([round(h.profile()["solve_ms"], 3), info["iterations"], info["refinements"]])
+        print(json.dumps({"mode": "solve", "grid": N, "ppc": a.ppc, "steps[solve_ms, iterations, refinements]": rows}))
 
 
 def ensemble(m, a):
