@@ -535,6 +535,7 @@ def main():
         kname = "k_pass_f64<PUSH|MOVE>"
     achieved = alg / (push_ms / 1e3) / 1e9
     tr = committed_traffic(kname)
+    tr_dep = committed_traffic("k_pass_tiled<DEPOSIT>") if w["precision"] == "mixed" else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -546,7 +547,9 @@ def main():
                      "peak_kind": peak_kind, "kernel": kname, "algorithmic_bytes_per_launch": alg,
                      "avg_launch_ms": push_ms,
                      "deposit_kernel": {"algorithmic_bytes_per_launch": alg_dep, "avg_launch_ms": dep_ms,
-                                        "achieved": alg_dep / (dep_ms / 1e3) / 1e9 if dep_ms > 0 else None},
+                                        "achieved": alg_dep / (dep_ms / 1e3) / 1e9 if dep_ms > 0 else None,
+                                        "traffic": (tr_dep["dram_bytes_per_launch"] * r["np"] / tr_dep["ions"]
+                                                    if isinstance(tr_dep, dict) else None)},
                      "traffic": (tr["dram_bytes_per_launch"] * r["np"] / tr["ions"]
                                  if isinstance(tr, dict) and "dram_bytes_per_launch" in tr else None),
                      "traffic_source": (f"ncu capture of {tr['ions']:,} ions scaled by the ion count"
