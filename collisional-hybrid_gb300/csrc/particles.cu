@@ -432,6 +432,10 @@ struct TileShared {
   uint32_t q_id[CH_TILE_QCAP];
   float q_t[CH_TILE_QCAP];      // elapsed time of the event process (waiting times so far)
   uint32_t q_st[CH_TILE_QCAP];  // event | proposal << 8
+  // Thread t's next ion (position, velocity), copied in by cp.async while
+  // the current one is pushed.
+  alignas(16) float4 pf_pos[256];
+  alignas(16) float4 pf_vel[256];
   // ---- header
   alignas(16) uint32_t rowbeg[TY * TZ];
   uint32_t pre[TY * TZ + 1];
@@ -644,6 +648,14 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
   if (dt != dh) drain(dt - dh);
 }
 
+// 16-byte asynchronous copy global -> shared (L2 only), and its group fences.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 // Moves one ion by v dt (cell units), wraps it into the grid and repacks the
 // cell word.
 __device__ __forceinline__ void tile_move_ion(const StepConsts& c, float4& p, const float v[3], int& i, int& j,
@@ -803,24 +815,44 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
   float tsum0 = 0.0f;
   if (PH == PH_DEPOSIT) tile_deposit_direct(sh, c, P, acc, total, bi0, bj0, bk0, bad);
   const uint32_t ptotal = total * (PH == PH_DEPOSIT ? 0u : 1u);  // ions the push / move loop visits
+  // index of slot idx in the ion arrays (rows of the brick are contiguous)
+  auto slot_ip = [&](uint32_t idx) -> uint32_t {
+    int r = 0;
+#pragma unroll
+    for (int st = 8; st > 0; st >>= 1)
+      if (r + st < TY * TZ && sh.pre[r + st] <= idx) r += st;
+    return sh.rowbeg[r] + (idx - sh.pre[r]);
+  };
+  // Thread t's ions are slots t, t + 256, ...; the next one is copied into
+  // the thread's own prefetch slot by cp.async while this one is pushed (only
+  // thread t touches slot t, and it has read the slot before refilling it).
+  uint32_t next_ip = 0;
+  if (threadIdx.x < ptotal) {
+    next_ip = slot_ip(threadIdx.x);
+    cp_async16(&sh.pf_pos[threadIdx.x], P.pos + next_ip);
+    cp_async16(&sh.pf_vel[threadIdx.x], P.vel + next_ip);
+  }
+  cp_async_commit();
 #pragma unroll 1
   for (uint32_t base = 0; base < ptotal; base += blockDim.x) {
     const uint32_t idx = base + threadIdx.x;
     const bool active = idx < ptotal;
-    int64_t ip = 0;
-    if (active) {
-      int r = 0;
-#pragma unroll
-      for (int st = 8; st > 0; st >>= 1)
-        if (r + st < TY * TZ && sh.pre[r + st] <= idx) r += st;
-      ip = (int64_t)sh.rowbeg[r] + (idx - sh.pre[r]);
-    }
+    const int64_t ip = next_ip;
     float4 p = make_float4(0.f, 0.f, 0.f, 0.f), vv = make_float4(0.f, 0.f, 0.f, 0.f);
+    cp_async_wait_all();
+    if (active) {
+      p = sh.pf_pos[threadIdx.x];
+      vv = sh.pf_vel[threadIdx.x];
+    }
+    if (idx + blockDim.x < ptotal) {
+      next_ip = slot_ip(idx + blockDim.x);
+      cp_async16(&sh.pf_pos[threadIdx.x], P.pos + next_ip);
+      cp_async16(&sh.pf_vel[threadIdx.x], P.vel + next_ip);
+    }
+    cp_async_commit();
     int i = 0, j = 0, k = 0;
     float v[3] = {0.f, 0.f, 0.f};
     if (active) {
-      p = P.pos[ip];
-      vv = P.vel[ip];
       const uint32_t cell = __float_as_uint(p.w);
       i = cell & (CH_MAX_NX - 1); j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1); k = cell >> (CH_PACK_BX + CH_PACK_BY);
       v[0] = vv.x; v[1] = vv.y; v[2] = vv.z;
@@ -1206,12 +1238,38 @@ __global__ void k_scatter_mixed(GridDesc g, MixParticles P, MixParticles Q, uint
 
 // Exclusive scan of counts[0..n) into starts[0..n] (three phases).
 // Scatter with the in-cell ranks the pass recorded: no atomics.
+// P and Q are different buffers.  A thread moves 4 ions per iteration (each
+// of the 4 a coalesced slot of its warp) and issues all their loads before
+// any store, so that 4 ions' memory latency overlaps.
 __global__ void k_scatter_ranked(GridDesc g, MixParticles P, MixParticles Q, const uint32_t* __restrict__ starts) {
-  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
-    const float4 p = P.pos[ip];
-    const uint32_t dst = starts[key_mixed(g, p.w)] + P.rank[ip];
-    Q.pos[dst] = p;
-    Q.vel[dst] = P.vel[ip];
+  const float4* __restrict__ ppos = P.pos;
+  const float4* __restrict__ pvel = P.vel;
+  const uint32_t* __restrict__ prank = P.rank;
+  float4* __restrict__ qpos = Q.pos;
+  float4* __restrict__ qvel = Q.vel;
+  const int64_t T = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < P.np; i0 += 4 * T) {
+    float4 p[4], v[4];
+    uint32_t rk[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t ip = i0 + u * T;
+      if (ip < P.np) {
+        p[u] = ppos[ip];
+        v[u] = pvel[ip];
+        rk[u] = prank[ip];
+      }
+    }
+    uint32_t dst[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (i0 + u * T < P.np) dst[u] = starts[key_mixed(g, p[u].w)] + rk[u];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (i0 + u * T < P.np) {
+        qpos[dst[u]] = p[u];
+        qvel[dst[u]] = v[u];
+      }
   }
 }
 
