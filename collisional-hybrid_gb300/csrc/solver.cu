@@ -429,57 +429,151 @@ __global__ void __launch_bounds__(256) k_resid(GridDesc g, DevCoefs<T> C, const 
 
 // Full weighting onto the coarse vertex grid (coarse node I = fine node 2I
 // along each halved axis): 1D weights 1/4, 1/2, 1/4; axes that are not
-// halved take the fine value.  out = scale * R in.
+// halved take the fine value.  Returns (R in) at coarse node c.
+template <typename T>
+__device__ __forceinline__ T restrict_node(const GridDesc& gf, const GridDesc& gc, int hx, int hy, int hz,
+                                           const T* in, int64_t c) {
+  int I, J, K;
+  ch_ijk(gc, c, I, J, K);
+  const int i0 = hx ? 2 * I : I, j0 = hy ? 2 * J : J, k0 = hz ? 2 * K : K;
+  T acc = T(0);
+  for (int dk = -hz; dk <= hz; ++dk) {
+    const T wk = hz ? (dk == 0 ? T(0.5) : T(0.25)) : T(1);
+    const int k = ch_wrap(k0 + dk, gf.Nz);
+    for (int dj = -hy; dj <= hy; ++dj) {
+      const T wj = hy ? (dj == 0 ? T(0.5) : T(0.25)) : T(1);
+      const int j = ch_wrap(j0 + dj, gf.Ny);
+      const int row = (k * gf.Ny + j) * gf.Nx;  // grids have < 2^31 nodes
+      for (int di = -hx; di <= hx; ++di) {
+        const T wi = hx ? (di == 0 ? T(0.5) : T(0.25)) : T(1);
+        acc += wk * wj * wi * in[row + ch_wrap(i0 + di, gf.Nx)];
+      }
+    }
+  }
+  return acc;
+}
+// out = scale * R in.
 template <typename T>
 __global__ void k_restrict(GridDesc gf, GridDesc gc, int hx, int hy, int hz, const T* __restrict__ in,
                            T* __restrict__ out, T scale) {
   pdl_enter();
-  GRID_LOOP(c, gc.N) {
-    int I, J, K;
-    ch_ijk(gc, c, I, J, K);
-    const int i0 = hx ? 2 * I : I, j0 = hy ? 2 * J : J, k0 = hz ? 2 * K : K;
-    T acc = T(0);
-    for (int dk = -hz; dk <= hz; ++dk) {
-      const T wk = hz ? (dk == 0 ? T(0.5) : T(0.25)) : T(1);
-      const int k = ch_wrap(k0 + dk, gf.Nz);
-      for (int dj = -hy; dj <= hy; ++dj) {
-        const T wj = hy ? (dj == 0 ? T(0.5) : T(0.25)) : T(1);
-        const int j = ch_wrap(j0 + dj, gf.Ny);
-        const int row = (k * gf.Ny + j) * gf.Nx;  // grids have < 2^31 nodes
-        for (int di = -hx; di <= hx; ++di) {
-          const T wi = hx ? (di == 0 ? T(0.5) : T(0.25)) : T(1);
-          acc += wk * wj * wi * in[row + ch_wrap(i0 + di, gf.Nx)];
-        }
-      }
-    }
-    out[c] = scale * acc;
-  }
+  GRID_LOOP(c, gc.N) out[c] = scale * restrict_node<T>(gf, gc, hx, hy, hz, in, c);
 }
 
-// Trilinear prolongation, added: xf += P ec.
+// Trilinear prolongation of ec to fine node c.
+template <typename T>
+__device__ __forceinline__ T prolong_node(const GridDesc& gf, const GridDesc& gc, int hx, int hy, int hz, const T* ec,
+                                          int64_t c) {
+  int i, j, k;
+  ch_ijk(gf, c, i, j, k);
+  int I0, I1, J0, J1, K0, K1;
+  T wi1, wj1, wk1;
+  if (hx) { I0 = i >> 1; I1 = (i & 1) ? ch_wrap(I0 + 1, gc.Nx) : I0; wi1 = (i & 1) ? T(0.5) : T(0); }
+  else { I0 = I1 = i; wi1 = T(0); }
+  if (hy) { J0 = j >> 1; J1 = (j & 1) ? ch_wrap(J0 + 1, gc.Ny) : J0; wj1 = (j & 1) ? T(0.5) : T(0); }
+  else { J0 = J1 = j; wj1 = T(0); }
+  if (hz) { K0 = k >> 1; K1 = (k & 1) ? ch_wrap(K0 + 1, gc.Nz) : K0; wk1 = (k & 1) ? T(0.5) : T(0); }
+  else { K0 = K1 = k; wk1 = T(0); }
+  const T wi0 = T(1) - wi1, wj0 = T(1) - wj1, wk0 = T(1) - wk1;
+  auto at = [&](int I, int J, int K) { return ec[(K * gc.Ny + J) * gc.Nx + I]; };  // < 2^31 nodes
+  return wk0 * (wj0 * (wi0 * at(I0, J0, K0) + wi1 * at(I1, J0, K0)) +
+                wj1 * (wi0 * at(I0, J1, K0) + wi1 * at(I1, J1, K0))) +
+         wk1 * (wj0 * (wi0 * at(I0, J0, K1) + wi1 * at(I1, J0, K1)) +
+                wj1 * (wi0 * at(I0, J1, K1) + wi1 * at(I1, J1, K1)));
+}
+// xf += P ec.
 template <typename T>
 __global__ void k_prolong_add(GridDesc gf, GridDesc gc, int hx, int hy, int hz, const T* __restrict__ ec,
                               T* __restrict__ xf) {
   pdl_enter();
-  GRID_LOOP(c, gf.N) {
-    int i, j, k;
-    ch_ijk(gf, c, i, j, k);
-    int I0, I1, J0, J1, K0, K1;
-    T wi1, wj1, wk1;
-    if (hx) { I0 = i >> 1; I1 = (i & 1) ? ch_wrap(I0 + 1, gc.Nx) : I0; wi1 = (i & 1) ? T(0.5) : T(0); }
-    else { I0 = I1 = i; wi1 = T(0); }
-    if (hy) { J0 = j >> 1; J1 = (j & 1) ? ch_wrap(J0 + 1, gc.Ny) : J0; wj1 = (j & 1) ? T(0.5) : T(0); }
-    else { J0 = J1 = j; wj1 = T(0); }
-    if (hz) { K0 = k >> 1; K1 = (k & 1) ? ch_wrap(K0 + 1, gc.Nz) : K0; wk1 = (k & 1) ? T(0.5) : T(0); }
-    else { K0 = K1 = k; wk1 = T(0); }
-    const T wi0 = T(1) - wi1, wj0 = T(1) - wj1, wk0 = T(1) - wk1;
-    auto at = [&](int I, int J, int K) { return ec[(K * gc.Ny + J) * gc.Nx + I]; };  // < 2^31 nodes
-    const T v = wk0 * (wj0 * (wi0 * at(I0, J0, K0) + wi1 * at(I1, J0, K0)) +
-                       wj1 * (wi0 * at(I0, J1, K0) + wi1 * at(I1, J1, K0))) +
-                wk1 * (wj0 * (wi0 * at(I0, J0, K1) + wi1 * at(I1, J0, K1)) +
-                       wj1 * (wi0 * at(I0, J1, K1) + wi1 * at(I1, J1, K1)));
-    xf[c] += v;
+  GRID_LOOP(c, gf.N) xf[c] += prolong_node<T>(gf, gc, hx, hy, hz, ec, c);
+}
+
+// The lower part of a V(2,2) cycle in one CTA: levels q = 0 .. L-1 of the
+// tail (level 0 of the tail has at most MG_TAIL_MAX nodes), every array in
+// shared memory.  The node arithmetic is that of k_smooth_zero2, k_resid,
+// k_restrict, k_coarse, k_prolong_add and k_smooth, so the result is the
+// one of those kernels; the levels' launches become barriers.
+constexpr int MG_TAIL_LEVELS = 8;
+template <typename T>
+struct TailLevels {
+  GridDesc g[MG_TAIL_LEVELS];
+  DevCoefs<T> C[MG_TAIL_LEVELS];
+  const T* n[MG_TAIL_LEVELS];
+  const T* dinv[MG_TAIL_LEVELS];
+  int hx[MG_TAIL_LEVELS], hy[MG_TAIL_LEVELS], hz[MG_TAIL_LEVELS];  // halving from q to q + 1
+  T sR[MG_TAIL_LEVELS];
+  int off[MG_TAIL_LEVELS];  // level q's five arrays (n, dinv, b, x, t) start at element off[q]
+  int L, sweeps;
+};
+// threads of the tail CTA (FP64 rows need more registers)
+template <typename T>
+constexpr int mg_tail_threads() { return sizeof(T) == 4 ? 1024 : 512; }
+template <typename T>
+__global__ void __launch_bounds__(mg_tail_threads<T>()) k_mg_tail(TailLevels<T> V, const T* __restrict__ b_in,
+                                                                  T* __restrict__ x_out, T w) {
+  pdl_enter();
+  extern __shared__ __align__(16) unsigned char smem_tail[];
+  T* const base = reinterpret_cast<T*>(smem_tail);
+  auto arr = [&](int q, int a) { return base + V.off[q] + (int64_t)a * V.g[q].N; };  // a: n dinv b x t
+  for (int q = 0; q < V.L; ++q)
+    for (int64_t c = threadIdx.x; c < V.g[q].N; c += blockDim.x) {
+      arr(q, 0)[c] = V.n[q][c];
+      arr(q, 1)[c] = V.dinv[q][c];
+    }
+  for (int64_t c = threadIdx.x; c < V.g[0].N; c += blockDim.x) arr(0, 2)[c] = b_in[c];
+  __syncthreads();
+  // down: two sweeps from zero, residual (into t), restriction
+  for (int q = 0; q + 1 < V.L; ++q) {
+    const GridDesc& g = V.g[q];
+    const T *n = arr(q, 0), *dinv = arr(q, 1), *b = arr(q, 2);
+    T *x = arr(q, 3), *r = arr(q, 4);
+    auto t = [&](int64_t i) { return w * dinv[i] * b[i]; };
+    for (int64_t c = threadIdx.x; c < g.N; c += blockDim.x)
+      x[c] = t(c) + w * dinv[c] * (b[c] - apply_row_at<T>(V.C[q], n, t, neighbours(g, c)));
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < g.N; c += blockDim.x) r[c] = b[c] - apply_row<T>(V.C[q], n, x, neighbours(g, c));
+    __syncthreads();
+    T* b1 = arr(q + 1, 2);
+    for (int64_t c = threadIdx.x; c < V.g[q + 1].N; c += blockDim.x)
+      b1[c] = V.sR[q] * restrict_node<T>(g, V.g[q + 1], V.hx[q], V.hy[q], V.hz[q], r, c);
+    __syncthreads();
   }
+  // coarsest: sweeps from zero, x and t in turn
+  const int qc = V.L - 1;
+  {
+    const GridDesc& g = V.g[qc];
+    const T *n = arr(qc, 0), *dinv = arr(qc, 1), *b = arr(qc, 2);
+    T *xa = arr(qc, 3), *xb = arr(qc, 4);
+    for (int64_t c = threadIdx.x; c < g.N; c += blockDim.x) xa[c] = w * dinv[c] * b[c];
+    __syncthreads();
+    for (int s = 1; s < V.sweeps; ++s) {
+      for (int64_t c = threadIdx.x; c < g.N; c += blockDim.x)
+        xb[c] = xa[c] + w * dinv[c] * (b[c] - apply_row<T>(V.C[qc], n, xa, neighbours(g, c)));
+      __syncthreads();
+      T* tmp = xa; xa = xb; xb = tmp;
+    }
+    if (xa != arr(qc, 3)) {
+      for (int64_t c = threadIdx.x; c < g.N; c += blockDim.x) arr(qc, 3)[c] = xa[c];
+      __syncthreads();
+    }
+  }
+  // up: prolongation, two sweeps (x -> t -> x)
+  for (int q = V.L - 2; q >= 0; --q) {
+    const GridDesc& g = V.g[q];
+    const T *n = arr(q, 0), *dinv = arr(q, 1), *b = arr(q, 2), *ec = arr(q + 1, 3);
+    T *x = arr(q, 3), *t = arr(q, 4);
+    for (int64_t c = threadIdx.x; c < g.N; c += blockDim.x)
+      x[c] += prolong_node<T>(g, V.g[q + 1], V.hx[q], V.hy[q], V.hz[q], ec, c);
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < g.N; c += blockDim.x)
+      t[c] = x[c] + w * dinv[c] * (b[c] - apply_row<T>(V.C[q], n, x, neighbours(g, c)));
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < g.N; c += blockDim.x)
+      x[c] = t[c] + w * dinv[c] * (b[c] - apply_row<T>(V.C[q], n, t, neighbours(g, c)));
+    __syncthreads();
+  }
+  for (int64_t c = threadIdx.x; c < V.g[0].N; c += blockDim.x) x_out[c] = arr(0, 3)[c];
 }
 
 // Coarsest level: `sweeps` damped-Jacobi sweeps from zero in one block,
@@ -601,6 +695,8 @@ static int mg_coarse_sweeps(const GridDesc& g) {
   return s < 16 ? 16 : (s > 64 ? 64 : s);
 }
 static constexpr int64_t MG_COARSE_MAX = 4096;
+static constexpr int64_t MG_TAIL_MAX = 512;          // top level of the one-CTA tail
+static constexpr size_t MG_TAIL_SMEM = 200 * 1024;   // its shared memory at most
 
 template <typename T>
 ch_status PotentialSolver::mg_build(MGHier<T>& h) {
@@ -641,9 +737,27 @@ ch_status PotentialSolver::mg_build(MGHier<T>& h) {
       CH_CUDA_OK(cudaMalloc(&h.b[l], b));
     }
   }
-  const size_t sh = 2 * sizeof(T) * h.g[L - 1].N;
-  if (sh > 48 * 1024) CH_CUDA_OK(cudaFuncSetAttribute(k_coarse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      (int)sh));
+  // (per kernel, not per hierarchy: the largest coarse grid of any solver)
+  CH_CUDA_OK(cudaFuncSetAttribute(k_coarse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(2 * sizeof(T) * MG_COARSE_MAX)));
+  // the one-CTA tail: from the first level of at most MG_TAIL_MAX nodes,
+  // when its levels' five arrays fit in shared memory
+  h.tail = -1;
+  h.tail_smem = 0;
+  for (int l = 0; l + 1 < L; ++l) {
+    if (h.g[l].N > MG_TAIL_MAX) continue;
+    size_t bytes = 0;
+    for (int q = l; q < L; ++q) bytes += 5 * sizeof(T) * (size_t)h.g[q].N;
+    if (L - l <= MG_TAIL_LEVELS && bytes <= MG_TAIL_SMEM) {
+      // the attribute belongs to the kernel, not to this hierarchy: the fixed
+      // maximum serves every solver on the device
+      CH_CUDA_OK(cudaFuncSetAttribute(k_mg_tail<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)MG_TAIL_SMEM));
+      h.tail = l;
+      h.tail_smem = bytes;
+    }
+    break;
+  }
   h.built = true;
   return CH_OK;
 }
@@ -683,6 +797,25 @@ void PotentialSolver::mg_vcycle(MGHier<T>& h, int l, const T* b, T* x, cudaStrea
   if (l == h.L - 1) {
     const size_t sh = 2 * sizeof(T) * g.N;
     launch(k_coarse<T>, 1, 1024, sh, s, g, h.C[l], h.n[l], h.dinv[l], b, x, mg_coarse_sweeps(g), w);
+    if (part) launch(k_dot_rz_rr<T>, nb_, 256, 0, s, g.N, b, x, part);
+    return;
+  }
+  if (l == h.tail) {
+    TailLevels<T> V;
+    V.L = h.L - l;
+    V.sweeps = mg_coarse_sweeps(h.g[h.L - 1]);
+    int off = 0;
+    for (int q = 0; q < V.L; ++q) {
+      V.g[q] = h.g[l + q];
+      V.C[q] = h.C[l + q];
+      V.n[q] = h.n[l + q];
+      V.dinv[q] = h.dinv[l + q];
+      V.hx[q] = h.hx[l + q]; V.hy[q] = h.hy[l + q]; V.hz[q] = h.hz[l + q];
+      V.sR[q] = (T)h.sR[l + q];
+      V.off[q] = off;
+      off += 5 * (int)h.g[l + q].N;
+    }
+    launch(k_mg_tail<T>, 1, mg_tail_threads<T>(), h.tail_smem, s, V, b, x, w);
     if (part) launch(k_dot_rz_rr<T>, nb_, 256, 0, s, g.N, b, x, part);
     return;
   }

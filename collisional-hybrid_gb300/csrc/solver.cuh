@@ -50,6 +50,8 @@ struct MGHier {
   double sR[CH_MG_MAX_LEVELS];                                           // residual scale into l+1
   T *n[CH_MG_MAX_LEVELS], *dinv[CH_MG_MAX_LEVELS], *x[CH_MG_MAX_LEVELS], *b[CH_MG_MAX_LEVELS],
       *r[CH_MG_MAX_LEVELS], *t[CH_MG_MAX_LEVELS];
+  int tail = -1;          // first level of the one-CTA tail cycle (k_mg_tail), or -1
+  size_t tail_smem = 0;   // its shared memory
   bool built = false;
 };
 
