@@ -92,6 +92,10 @@ struct ch_ctx {
   double* hred = nullptr;
   // staging for AoS transfers
   double4_32a *stage_pos = nullptr, *stage_vel = nullptr;
+  // slot of each ion id in the current order (mixed form), made by a download
+  // into mapped host arrays; valid until the order changes (sort, load)
+  uint32_t* slot_of_id = nullptr;
+  bool slot_map_valid = false;
   // state
   double sbar = 0.0;
   double dep_scale = 0.0;
@@ -194,9 +198,11 @@ static GridDesc make_grid(const ch_params& p) {
 static void free_particles(ch_ctx* c) {
   void* v[] = {c->P.x, c->P.y, c->P.z, c->P.vx, c->P.vy, c->P.vz, c->P.id, c->Q.x, c->Q.y, c->Q.z, c->Q.vx,
                c->Q.vy, c->Q.vz, c->Q.id, c->M.pos, c->M.vel, c->MQ.pos, c->MQ.vel, c->keys, c->stage_pos,
-               c->stage_vel, c->part};
+               c->stage_vel, c->part, c->slot_of_id};
   for (void* q : v)
     if (q) cudaFree(q);
+  c->slot_of_id = nullptr;
+  c->slot_map_valid = false;
   c->P = F64Particles{};
   c->Q = F64Particles{};
   c->M = MixParticles{};
@@ -371,6 +377,7 @@ static ch_status ensure_staging(ch_ctx* c) {
 }
 
 static void do_sort(ch_ctx* c, bool have_hist = false) {
+  c->slot_map_valid = false;
   prof_begin(c);
   launch_sort(c->mixed, c->g, c->P, c->Q, c->M, c->MQ, c->counts, c->starts, c->cursor, c->keys, c->block_sums,
               have_hist, c->sms, c->stream);
@@ -380,8 +387,10 @@ static void do_sort(ch_ctx* c, bool have_hist = false) {
   c->since_sort = 0;
 }
 
-static ch_status after_load(ch_ctx* c) {
-  do_sort(c);
+// keep_order: the ions were put back into the slots of the current order,
+// whose brick ranges stay valid, so no sort is needed.
+static ch_status after_load(ch_ctx* c, bool keep_order = false) {
+  if (!keep_order) do_sort(c);
   if (c->p.mn > 0.0) {
     StepConsts k = consts(c, 0);
     const int nb = launch_sbar(c->mixed, k, c->P, c->M, c->part, c->sms, c->stream);
@@ -402,6 +411,12 @@ extern "C" ch_status ch_particles_upload(ch_ctx* c, const ch_real_vector* pos, c
   const uint64_t bytes = sizeof(double4_32a) * (uint64_t)np;
   const void* dp = device_view(pos, bytes, 16);
   const void* dv = device_view(vel, bytes, 16);
+  if (dp && dv && c->mixed && c->slot_map_valid) {
+    // registered host arrays in the id order of the last download: every ion
+    // goes back into its slot (one pass over the link, no sort)
+    launch_host_to_mixed(c->g, dp, dv, c->slot_of_id, c->M, c->sms, c->stream);
+    return after_load(c, true);
+  }
   if (dp && dv) {
     // registered host arrays: the conversion reads them directly
     launch_aos_in_u16(c->mixed, c->g, dp, dv, c->P, c->M, c->sms, c->stream);
@@ -428,12 +443,22 @@ extern "C" ch_status ch_particles_load(ch_ctx* c, int64_t np, const ch_loader* L
 extern "C" ch_status ch_particles_download(ch_ctx* c, ch_real_vector* pos, ch_real_vector* vel) {
   if (!c || !pos || !vel) return ch_fail(CH_ERR_ARG, "ch_particles_download: null argument");
   if (c->np == 0) return ch_fail(CH_ERR_STATE, "no ions");
-  ch_status rc = ensure_staging(c);
-  if (rc) return rc;
-  launch_aos_out(c->mixed, c->g, c->P, c->M, c->stage_pos, c->stage_vel, c->sms, c->stream);
   const uint64_t bytes = sizeof(double4_32a) * (uint64_t)c->np;
   void* dp = device_view(pos, bytes, 16);
   void* dv = device_view(vel, bytes, 16);
+  if (dp && dv && c->mixed) {
+    // registered host arrays: convert and write them in id order in one pass
+    // (the slot map also lets the next upload keep the order)
+    if (!c->slot_of_id) CH_CUDA_OK(cudaMalloc(&c->slot_of_id, sizeof(uint32_t) * c->np));
+    launch_slot_map(c->M, c->slot_of_id, c->sms, c->stream);
+    launch_mixed_to_host(c->g, c->M, c->slot_of_id, dp, dv, c->sms, c->stream);
+    CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+    c->slot_map_valid = true;
+    return CH_OK;
+  }
+  ch_status rc = ensure_staging(c);
+  if (rc) return rc;
+  launch_aos_out(c->mixed, c->g, c->P, c->M, c->stage_pos, c->stage_vel, c->sms, c->stream);
   if (dp && dv) {
     // registered host arrays: a copy kernel streams the staging out
     launch_stream_copy(dp, c->stage_pos, bytes, c->sms, c->stream);

@@ -1458,6 +1458,100 @@ __global__ void k_aos_to_f64_u16(const double2* __restrict__ pos, const double2*
   }
 }
 
+// ------------------------------------------------------------------ host arrays in ion-id order
+// slot_of_id[id] = the slot that holds ion id.
+__global__ void k_slot_map(MixParticles P, uint32_t* __restrict__ slot_of_id) {
+  const float* vw = reinterpret_cast<const float*>(P.vel) + 3;
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < P.np; s += (int64_t)gridDim.x * blockDim.x)
+    slot_of_id[__float_as_uint(vw[4 * s])] = (uint32_t)s;
+}
+
+// Mixed state -> host AoS arrays (4 doubles per ion, mapped host memory) in
+// id order, in one pass: warp w converts ions i0 .. i0+31 (read from their
+// slots) into shared memory and then writes them out as 512 contiguous bytes
+// per instruction, which is what keeps the host link at its rate.
+__global__ void __launch_bounds__(256) k_mixed_to_host(GridDesc g, MixParticles P,
+                                                       const uint32_t* __restrict__ slot_of_id,
+                                                       double2* __restrict__ pos, double2* __restrict__ vel) {
+  __shared__ double2 bp[8][64], bv[8][64];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i0 = (blockIdx.x * (int64_t)(blockDim.x >> 5) + w) * 32; i0 < P.np; i0 += nw * 32) {
+    const int64_t i = i0 + lane;
+    if (i < P.np) {
+      const uint32_t s = slot_of_id[i];
+      const float4 p = P.pos[s], v = P.vel[s];
+      const uint32_t cell = __float_as_uint(p.w);
+      const int ci = cell & (CH_MAX_NX - 1), cj = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
+                ck = cell >> (CH_PACK_BX + CH_PACK_BY);
+      bp[w][2 * lane] = make_double2(g.x0 + ((double)ci + (double)p.x) * g.dx, g.y0 + ((double)cj + (double)p.y) * g.dy);
+      bp[w][2 * lane + 1] = make_double2(g.z0 + ((double)ck + (double)p.z) * g.dz, 0.0);
+      bv[w][2 * lane] = make_double2((double)v.x, (double)v.y);
+      bv[w][2 * lane + 1] = make_double2((double)v.z, 0.0);
+    }
+    __syncwarp();
+    const int64_t n2 = 2 * (P.np - i0 < 32 ? P.np - i0 : 32);  // 16-byte words of this chunk
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int q = lane + 32 * h;
+      if (q < n2) {
+        pos[2 * i0 + q] = bp[w][q];
+        vel[2 * i0 + q] = bv[w][q];
+      }
+    }
+    __syncwarp();  // the buffers are written out before the next chunk refills them
+  }
+}
+
+// Host AoS arrays in id order -> mixed state, each ion back into the slot it
+// had (slot_of_id), so that the order of the ions, and with it the brick
+// ranges of the last sort, stay as they were.  Reads as k_mixed_to_host
+// writes: 512 contiguous bytes per warp instruction.
+__global__ void __launch_bounds__(256) k_host_to_mixed(GridDesc g, const double2* __restrict__ pos,
+                                                       const double2* __restrict__ vel,
+                                                       const uint32_t* __restrict__ slot_of_id, MixParticles P) {
+  __shared__ double2 bp[8][64], bv[8][64];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i0 = (blockIdx.x * (int64_t)(blockDim.x >> 5) + w) * 32; i0 < P.np; i0 += nw * 32) {
+    const int64_t n2 = 2 * (P.np - i0 < 32 ? P.np - i0 : 32);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int q = lane + 32 * h;
+      if (q < n2) {
+        bp[w][q] = pos[2 * i0 + q];
+        bv[w][q] = vel[2 * i0 + q];
+      }
+    }
+    __syncwarp();
+    const int64_t i = i0 + lane;
+    if (i < P.np) {
+      const double2 p0 = bp[w][2 * lane], p1 = bp[w][2 * lane + 1], v0 = bv[w][2 * lane], v1 = bv[w][2 * lane + 1];
+      const double sx[3] = {p0.x, p0.y, p1.x};
+      const uint32_t s = slot_of_id[i];
+      P.pos[s] = pack_mixed(g, sx);
+      P.vel[s] = make_float4((float)v0.x, (float)v0.y, (float)v1.x, __uint_as_float((uint32_t)i));
+    }
+    __syncwarp();
+  }
+}
+
+void launch_slot_map(MixParticles M, uint32_t* slot_of_id, int sms, cudaStream_t s) {
+  k_slot_map<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(M, slot_of_id), ::ch::note_launch();
+}
+void launch_mixed_to_host(const GridDesc& g, MixParticles M, const uint32_t* slot_of_id, void* pos, void* vel, int sms,
+                          cudaStream_t s) {
+  k_mixed_to_host<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, M, slot_of_id, static_cast<double2*>(pos),
+                                                                      static_cast<double2*>(vel)),
+      ::ch::note_launch();
+}
+void launch_host_to_mixed(const GridDesc& g, const void* pos, const void* vel, const uint32_t* slot_of_id,
+                          MixParticles M, int sms, cudaStream_t s) {
+  k_host_to_mixed<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, static_cast<const double2*>(pos),
+                                                                      static_cast<const double2*>(vel), slot_of_id, M),
+      ::ch::note_launch();
+}
+
 void launch_aos_in_u16(bool mixed, const GridDesc& g, const void* pos, const void* vel, F64Particles P,
                        MixParticles M, int sms, cudaStream_t s) {
   const double2* p = static_cast<const double2*>(pos);

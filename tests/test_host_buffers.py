@@ -66,3 +66,36 @@ def test_misaligned_view_of_a_registered_range_is_staged(chy):
         assert np.array_equal(a, pos) and np.array_equal(b, vel)
     finally:
         chy.host_unregister(big)
+
+
+def test_round_trip_through_registered_arrays_keeps_the_run(chy):
+    """A download into registered arrays followed by an upload of the same
+    arrays puts every ion back into its slot (no sort); a plain round trip
+    re-sorts.  The order of the ions does not enter any result (integer
+    deposit sums, per-ion draws), so both runs stay identical bit for bit."""
+    p = chy.params_for((16, 12, 20), precision=chy.PRECISION["mixed"], nui=0.4, sort_period=3)
+    n = 16 * 12 * 20 * 8
+    outs = []
+    for registered in (False, True):
+        with chy.Hybrid(p) as h:
+            h.load(n, chy.loader(amp=(0.05, 0.02, 0.0)))
+            h.CollectVlasovQuantities(copy=False)
+            h.ComputePotential(copy=False)
+            h.step(0, 2)
+            pos, vel = np.zeros((n, 4)), np.zeros((n, 4))
+            if registered:
+                chy.host_register(pos)
+                chy.host_register(vel)
+            try:
+                for s in range(2, 6):
+                    h.download(pos, vel)
+                    h.upload(pos, vel)
+                    h.step(s, 1)
+                h.download(pos, vel)
+                outs.append((pos.copy(), vel.copy(), h.CollectVlasovQuantities(), h.phi()))
+            finally:
+                if registered:
+                    chy.host_unregister(pos)
+                    chy.host_unregister(vel)
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
