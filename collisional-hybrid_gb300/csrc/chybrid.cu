@@ -96,6 +96,10 @@ struct ch_ctx {
   // into mapped host arrays; valid until the order changes (sort, load)
   uint32_t* slot_of_id = nullptr;
   bool slot_map_valid = false;
+  // download of registered arrays: conversion chunks on `stream`, their
+  // copies to the host on copy_stream
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ev = nullptr;
   // state
   double sbar = 0.0;
   double dep_scale = 0.0;
@@ -230,6 +234,8 @@ extern "C" ch_status ch_destroy(ch_ctx* c) {
   c->solver.release();
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
+  if (c->copy_ev) cudaEventDestroy(c->copy_ev);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return CH_OK;
@@ -447,12 +453,31 @@ extern "C" ch_status ch_particles_download(ch_ctx* c, ch_real_vector* pos, ch_re
   void* dp = device_view(pos, bytes, 16);
   void* dv = device_view(vel, bytes, 16);
   if (dp && dv && c->mixed) {
-    // registered host arrays: convert and write them in id order in one pass
-    // (the slot map also lets the next upload keep the order)
+    // registered host arrays: chunks of ids converted into the staging arrays
+    // in id order while the previous chunk is copied out over the host link,
+    // which then runs without gaps (the slot map also lets the next upload
+    // keep the order)
     if (!c->slot_of_id) CH_CUDA_OK(cudaMalloc(&c->slot_of_id, sizeof(uint32_t) * c->np));
+    ch_status rs = ensure_staging(c);
+    if (rs) return rs;
+    if (!c->copy_stream) {
+      CH_CUDA_OK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+      CH_CUDA_OK(cudaEventCreateWithFlags(&c->copy_ev, cudaEventDisableTiming));
+    }
     launch_slot_map(c->M, c->slot_of_id, c->sms, c->stream);
-    launch_mixed_to_host(c->g, c->M, c->slot_of_id, dp, dv, c->sms, c->stream);
-    CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+    const int64_t chunks = 8, per = ((c->np + chunks - 1) / chunks + 31) / 32 * 32;
+    for (int64_t a = 0; a < c->np; a += per) {
+      const int64_t b = a + per < c->np ? a + per : c->np;
+      launch_mixed_to_host(c->g, c->M, c->slot_of_id, c->stage_pos, c->stage_vel, a, b, c->sms, c->stream);
+      CH_CUDA_OK(cudaEventRecord(c->copy_ev, c->stream));
+      CH_CUDA_OK(cudaStreamWaitEvent(c->copy_stream, c->copy_ev, 0));
+      const size_t off = sizeof(double4_32a) * (size_t)a, len = sizeof(double4_32a) * (size_t)(b - a);
+      CH_CUDA_OK(cudaMemcpyAsync(reinterpret_cast<char*>(pos) + off, reinterpret_cast<char*>(c->stage_pos) + off, len,
+                                 cudaMemcpyDeviceToHost, c->copy_stream));
+      CH_CUDA_OK(cudaMemcpyAsync(reinterpret_cast<char*>(vel) + off, reinterpret_cast<char*>(c->stage_vel) + off, len,
+                                 cudaMemcpyDeviceToHost, c->copy_stream));
+    }
+    CH_CUDA_OK(cudaStreamSynchronize(c->copy_stream));
     c->slot_map_valid = true;
     return CH_OK;
   }

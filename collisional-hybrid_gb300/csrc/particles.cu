@@ -1466,19 +1466,20 @@ __global__ void k_slot_map(MixParticles P, uint32_t* __restrict__ slot_of_id) {
     slot_of_id[__float_as_uint(vw[4 * s])] = (uint32_t)s;
 }
 
-// Mixed state -> host AoS arrays (4 doubles per ion, mapped host memory) in
-// id order, in one pass: warp w converts ions i0 .. i0+31 (read from their
-// slots) into shared memory and then writes them out as 512 contiguous bytes
-// per instruction, which is what keeps the host link at its rate.
+// Mixed state -> AoS arrays (4 doubles per ion) in id order, ids
+// [i_begin, i_end): warp w converts ions i0 .. i0+31 (read from their slots)
+// into shared memory and then writes them out as 512 contiguous bytes per
+// instruction.
 __global__ void __launch_bounds__(256) k_mixed_to_host(GridDesc g, MixParticles P,
                                                        const uint32_t* __restrict__ slot_of_id,
-                                                       double2* __restrict__ pos, double2* __restrict__ vel) {
+                                                       double2* __restrict__ pos, double2* __restrict__ vel,
+                                                       int64_t i_begin, int64_t i_end) {
   __shared__ double2 bp[8][64], bv[8][64];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t i0 = (blockIdx.x * (int64_t)(blockDim.x >> 5) + w) * 32; i0 < P.np; i0 += nw * 32) {
+  for (int64_t i0 = i_begin + (blockIdx.x * (int64_t)(blockDim.x >> 5) + w) * 32; i0 < i_end; i0 += nw * 32) {
     const int64_t i = i0 + lane;
-    if (i < P.np) {
+    if (i < i_end) {
       const uint32_t s = slot_of_id[i];
       const float4 p = P.pos[s], v = P.vel[s];
       const uint32_t cell = __float_as_uint(p.w);
@@ -1490,7 +1491,7 @@ __global__ void __launch_bounds__(256) k_mixed_to_host(GridDesc g, MixParticles 
       bv[w][2 * lane + 1] = make_double2((double)v.z, 0.0);
     }
     __syncwarp();
-    const int64_t n2 = 2 * (P.np - i0 < 32 ? P.np - i0 : 32);  // 16-byte words of this chunk
+    const int64_t n2 = 2 * (i_end - i0 < 32 ? i_end - i0 : 32);  // 16-byte words of this chunk
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int q = lane + 32 * h;
@@ -1539,10 +1540,10 @@ __global__ void __launch_bounds__(256) k_host_to_mixed(GridDesc g, const double2
 void launch_slot_map(MixParticles M, uint32_t* slot_of_id, int sms, cudaStream_t s) {
   k_slot_map<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(M, slot_of_id), ::ch::note_launch();
 }
-void launch_mixed_to_host(const GridDesc& g, MixParticles M, const uint32_t* slot_of_id, void* pos, void* vel, int sms,
-                          cudaStream_t s) {
-  k_mixed_to_host<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(g, M, slot_of_id, static_cast<double2*>(pos),
-                                                                      static_cast<double2*>(vel)),
+void launch_mixed_to_host(const GridDesc& g, MixParticles M, const uint32_t* slot_of_id, void* pos, void* vel,
+                          int64_t i_begin, int64_t i_end, int sms, cudaStream_t s) {
+  k_mixed_to_host<<<grid_for(i_end - i_begin, 256, sms, 8), 256, 0, s>>>(
+      g, M, slot_of_id, static_cast<double2*>(pos), static_cast<double2*>(vel), i_begin, i_end),
       ::ch::note_launch();
 }
 void launch_host_to_mixed(const GridDesc& g, const void* pos, const void* vel, const uint32_t* slot_of_id,

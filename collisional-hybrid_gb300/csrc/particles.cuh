@@ -29,12 +29,12 @@ void launch_aos_in(bool mixed, const GridDesc& g, const double4_32a* pos, const 
                    MixParticles M, int sms, cudaStream_t s);
 // Copies bytes (a multiple of 16; both pointers 16-byte aligned) on the SMs;
 // dst may be mapped host memory.
-// Host AoS arrays (mapped, 16-byte aligned) in ion-id order: the slot map of
-// the current order, the one-pass download, and the upload that puts every
-// ion back into its slot.
+// AoS arrays (16-byte aligned; mapped host memory for the upload) in ion-id
+// order: the slot map of the current order, the conversion of an id range,
+// and the upload that puts every ion back into its slot.
 void launch_slot_map(MixParticles M, uint32_t* slot_of_id, int sms, cudaStream_t s);
-void launch_mixed_to_host(const GridDesc& g, MixParticles M, const uint32_t* slot_of_id, void* pos, void* vel, int sms,
-                          cudaStream_t s);
+void launch_mixed_to_host(const GridDesc& g, MixParticles M, const uint32_t* slot_of_id, void* pos, void* vel,
+                          int64_t i_begin, int64_t i_end, int sms, cudaStream_t s);
 void launch_host_to_mixed(const GridDesc& g, const void* pos, const void* vel, const uint32_t* slot_of_id,
                           MixParticles M, int sms, cudaStream_t s);
 void launch_stream_copy(void* dst, const void* src, uint64_t bytes, int sms, cudaStream_t s);
