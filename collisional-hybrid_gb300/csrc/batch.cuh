@@ -46,5 +46,7 @@ constexpr int BATCH_COARSE_MAX = 2048;
 // One launch: run r is solved by the cluster of `cluster` CTAs starting at
 // block r * cluster.
 cudaError_t launch_batch_solve(const BSolveRun* runs, int nruns, int cluster, cudaStream_t s);
+// Allows clusters of 16 CTAs for the solve on the current device (false if refused).
+bool batch_solve_allow_wide();
 
 }  // namespace ch

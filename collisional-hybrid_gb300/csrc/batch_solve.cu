@@ -18,6 +18,8 @@
 // read-only path), because other CTAs of the cluster write them.
 #include <cooperative_groups.h>
 
+#include <atomic>
+
 #include "batch.cuh"
 
 namespace cg = cooperative_groups;
@@ -362,6 +364,23 @@ __global__ void __launch_bounds__(256) k_batch_solve(const BSolveRun* runs) {
 }
 
 #undef OWN
+
+// Clusters of 16 CTAs (beyond the portable 8) are allowed once per device;
+// false when the device refuses them.
+bool batch_solve_allow_wide() {
+  static std::atomic<uint32_t> ok{0}, tried{0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint32_t bit = 1u << (dev & 31);
+  if (!(tried.load() & bit)) {
+    if (cudaFuncSetAttribute(k_batch_solve, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
+      ok.fetch_or(bit);
+    else
+      cudaGetLastError();
+    tried.fetch_or(bit);
+  }
+  return (ok.load() & bit) != 0;
+}
 
 cudaError_t launch_batch_solve(const BSolveRun* runs, int nruns, int cluster, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};

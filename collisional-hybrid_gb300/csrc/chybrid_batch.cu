@@ -13,6 +13,7 @@
 #include <string.h>
 
 #include <new>
+#include <algorithm>
 #include <vector>
 
 #include "batch.cuh"
@@ -89,6 +90,8 @@ struct ch_batch {
   // host mirrors
   std::vector<BatchRunDev> runs;
   std::vector<BSolveRun> solve;
+  // the solve records in the device order: largest grid first (see below)
+  std::vector<BSolveRun> solve_order;
   BSolveOut* h_out = nullptr;
   double* h_sums = nullptr;
   int* h_flags = nullptr;
@@ -102,7 +105,35 @@ struct ch_batch {
   bool prof = false;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   ch_profile pr{};
+  // Runs of at least twice the mean node count ("large": the first nbig
+  // solve records) may be solved by clusters of cluster_big CTAs in a launch
+  // of their own, beside the others' launch on stream s2 (cluster_big 0: one
+  // launch for all).
+  int nbig = 0, cluster_big = 0;
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
 };
+
+// The cluster solve of every run: one launch, or the large runs with
+// clusters of Cbig CTAs on s and the others with C on s2, joined back to s
+// (graph-capturable).
+__global__ void k_scaled_copy(int64_t n, const double* __restrict__ a, double f, double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = f * a[i];
+}
+
+static cudaError_t solve_launch(ch_batch* b, int C, int Cbig, cudaStream_t s) {
+  if (Cbig > 0 && b->nbig > 0 && b->nbig < b->nruns) {
+    cudaEventRecord(b->fork_ev, s);
+    cudaStreamWaitEvent(b->s2, b->fork_ev, 0);
+    const cudaError_t e1 = launch_batch_solve(b->d_solve, b->nbig, Cbig, s);
+    const cudaError_t e2 = launch_batch_solve(b->d_solve + b->nbig, b->nruns - b->nbig, C, b->s2);
+    cudaEventRecord(b->join_ev, b->s2);
+    cudaStreamWaitEvent(s, b->join_ev, 0);
+    return e1 != cudaSuccess ? e1 : e2;
+  }
+  return launch_batch_solve(b->d_solve, b->nruns, C, s);
+}
 
 static BatchDev batch_dev(const ch_batch* b) {
   BatchDev B;
@@ -139,6 +170,9 @@ extern "C" ch_status ch_batch_destroy(ch_batch* b) {
   if (b->h_flags) cudaFreeHost(b->h_flags);
   for (auto& e : b->ev)
     if (e) cudaEventDestroy(e);
+  if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+  if (b->join_ev) cudaEventDestroy(b->join_ev);
+  if (b->s2) cudaStreamDestroy(b->s2);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return CH_OK;
@@ -253,6 +287,9 @@ extern "C" ch_status ch_batch_create(const ch_params* runs, const int64_t* np, i
   CH_CUDA_OK(cudaGetDevice(&b->device));
   CH_CUDA_OK(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device));
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->s2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming);
   if (e != cudaSuccess) { ch_batch_destroy(b); return ch_cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__); }
   b->nruns = nruns;
   b->p.assign(runs, runs + nruns);
@@ -363,7 +400,21 @@ extern "C" ch_status ch_batch_create(const ch_params* runs, const int64_t* np, i
   }
   cudaStream_t s = b->stream;
   CH_CUDA_OK(cudaMemcpyAsync(b->d_runs, b->runs.data(), sizeof(BatchRunDev) * nruns, cudaMemcpyHostToDevice, s));
-  CH_CUDA_OK(cudaMemcpyAsync(b->d_solve, b->solve.data(), sizeof(BSolveRun) * nruns, cudaMemcpyHostToDevice, s));
+  // The cluster solve runs the largest grids first: the CTAs of one launch do
+  // not all fit at once, and a large run left to the last wave sets the
+  // time of the whole launch.  Each record carries its own arrays and output,
+  // so the order is free.
+  b->solve_order = b->solve;
+  std::stable_sort(b->solve_order.begin(), b->solve_order.end(),
+                   [](const BSolveRun& a, const BSolveRun& c) { return a.g.N > c.g.N; });
+  {
+    double mean = 0.0;
+    for (const BSolveRun& R : b->solve_order) mean += (double)R.g.N / nruns;
+    b->nbig = 0;
+    while (b->nbig < nruns && (double)b->solve_order[b->nbig].g.N >= 2.0 * mean) ++b->nbig;
+  }
+  CH_CUDA_OK(cudaMemcpyAsync(b->d_solve, b->solve_order.data(), sizeof(BSolveRun) * nruns, cudaMemcpyHostToDevice,
+                             s));
   CH_CUDA_OK(cudaMemcpyAsync(b->d_tile_off, b->tile_off.data(), sizeof(int) * (nruns + 1), cudaMemcpyHostToDevice, s));
   CH_CUDA_OK(cudaMemcpyAsync(b->d_ion_off, b->ion_off.data(), sizeof(int64_t) * (nruns + 1), cudaMemcpyHostToDevice,
                              s));
@@ -504,7 +555,7 @@ extern "C" ch_status ch_batch_initialize(ch_batch* b) {
   launch_batch_pass(PH_DEPOSIT, batch_dev(b), b->dstep, b->M, b->E32, b->starts, b->acc, b->sbar, b->dep_log2,
                     nullptr, b->tile_part, b->flags, b->tune.pass_ctas_per_sm, b->sms, s);
   launch_batch_finalize(4 * b->Ntot, b->acc, 1.0 / b->dep_scale, b->mom, b->flags + b->nruns, b->sms, s);
-  CH_CUDA_OK(launch_batch_solve(b->d_solve, b->nruns, b->tune.cluster, s));
+  CH_CUDA_OK(solve_launch(b, b->tune.cluster, b->cluster_big, s));
   CH_CUDA_OK(cudaGetLastError());
   ch_status rc = read_status(b, nullptr);
   if (rc) return rc;
@@ -526,7 +577,7 @@ static cudaError_t enqueue_step(ch_batch* b, bool sort_due) {
   launch_batch_runsum(B, b->tile_part, b->run_sums, b->sbar, b->flags, b->dstep, s);
   launch_batch_finalize(4 * b->Ntot, b->acc, 1.0 / b->dep_scale, b->mom, b->flags + b->nruns, b->sms, s);
   if (b->prof) cudaEventRecord(b->ev[1], s);
-  cudaError_t e = launch_batch_solve(b->d_solve, b->nruns, b->tune.cluster, s);
+  cudaError_t e = solve_launch(b, b->tune.cluster, b->cluster_big, s);
   if (b->prof) cudaEventRecord(b->ev[2], s);
   if (sort_due)
     launch_batch_sort(B, b->Ntot, b->M, b->MQ, b->counts, b->starts, b->cursor, b->block_sums, true, b->sms, s);
@@ -630,6 +681,7 @@ extern "C" ch_status ch_batch_set_tuning(ch_batch* b, const ch_batch_tuning* t) 
   if (t->pass_ctas_per_sm < 1 || t->pass_ctas_per_sm > 3) return ch_fail(CH_ERR_ARG, "pass_ctas_per_sm: 1 to 3");
   b->tune.cluster = t->cluster;
   b->tune.pass_ctas_per_sm = t->pass_ctas_per_sm;
+  b->cluster_big = 0;  // one launch shape for every run, as set
   drop_graphs(b);
   return CH_OK;
 }
@@ -667,17 +719,28 @@ extern "C" ch_status ch_batch_autotune(ch_batch* b, ch_batch_tuning* out) {
   uint32_t step_now = 0;
   cudaMemcpyAsync(&step_now, b->dstep, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
   cudaMemcpyAsync(phi0, b->phi, sizeof(double) * N, cudaMemcpyDeviceToDevice, s);
-  // solve: clusters of 1, 2, 4, 8 CTAs
+  // solve: clusters of 1, 2, 4, 8 CTAs for every run, or the large runs with
+  // clusters of 8 or 16 beside the others.  Each shape starts from the saved
+  // phi scaled by 0.999 (a residual of about 1e-3 of b, as a step's warm
+  // start), not from the converged phi, which would time a solve of a few
+  // iterations.
+  const bool wide = batch_solve_allow_wide();
   double best_solve = 1e30;
-  int best_c = b->tune.cluster;
-  for (int C : {1, 2, 4, 8}) {
+  int best_c = b->tune.cluster, best_big = 0;
+  const int shapes[][2] = {{1, 0}, {2, 0}, {4, 0}, {8, 0}, {1, 8}, {2, 8}, {4, 8}, {2, 16}, {4, 16}, {8, 16}};
+  for (const auto& sh : shapes) {
+    const int C = sh[0], Cb = sh[1];
+    if (Cb > 0 && (b->nbig == 0 || b->nbig == b->nruns)) continue;
+    if (Cb > 8 && !wide) continue;
     double t = 0.0;
-    for (int rep = 0; rep < 2; ++rep) {  // the first launch of a shape warms up
-      cudaMemcpyAsync(b->phi, phi0, sizeof(double) * N, cudaMemcpyDeviceToDevice, s);
-      t = timed([&] { launch_batch_solve(b->d_solve, b->nruns, C, s); });
+    bool ok = true;
+    for (int rep = 0; rep < 2 && ok; ++rep) {  // the first launch of a shape warms up
+      k_scaled_copy<<<grid_for(N, 256, b->sms, 4), 256, 0, s>>>(N, phi0, 0.999, b->phi);
+      ::ch::note_launch();
+      t = timed([&] { ok = solve_launch(b, C, Cb, s) == cudaSuccess; });
     }
-    if (cudaGetLastError() != cudaSuccess) continue;
-    if (t < best_solve) { best_solve = t; best_c = C; }
+    if (cudaGetLastError() != cudaSuccess || !ok) continue;
+    if (t < best_solve) { best_solve = t; best_c = C; best_big = Cb; }
   }
   cudaMemcpyAsync(b->phi, phi0, sizeof(double) * N, cudaMemcpyDeviceToDevice, s);
   // pass: 1 or 2 persistent CTAs per SM, from the same ions each time
@@ -710,6 +773,7 @@ extern "C" ch_status ch_batch_autotune(ch_batch* b, ch_batch_tuning* out) {
   cudaEventDestroy(e1);
   if (err != cudaSuccess) return ch_cuda_fail(err, "ch_batch_autotune", __FILE__, __LINE__);
   b->tune.cluster = best_c;
+  b->cluster_big = best_big;
   b->tune.pass_ctas_per_sm = best_k;
   b->tune.solve_ms = best_solve;
   b->tune.pass_ms = best_pass;
