@@ -104,7 +104,7 @@ class RunInfo(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("cluster", C.c_int32), ("pass_ctas_per_sm", C.c_int32), ("pass_ms", C.c_double),
-                ("solve_ms", C.c_double)]
+                ("solve_ms", C.c_double), ("cluster_big", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -485,8 +485,8 @@ class Batch:
         _check(lib().ch_batch_get_tuning(self._h, C.byref(t)))
         return t.as_dict()
 
-    def set_tuning(self, cluster: int, pass_ctas_per_sm: int = 2):
-        t = Tuning(cluster, pass_ctas_per_sm, 0.0, 0.0)
+    def set_tuning(self, cluster: int, pass_ctas_per_sm: int = 2, cluster_big: int = 0):
+        t = Tuning(cluster, pass_ctas_per_sm, 0.0, 0.0, cluster_big)
         _check(lib().ch_batch_set_tuning(self._h, C.byref(t)))
 
     def set_profiling(self, on: bool = True):

@@ -99,17 +99,17 @@ struct ch_batch {
   std::vector<char> present;  // ions of run r loaded or uploaded
   bool loaded = false, initialized = false, parity = false;
   int since_sort = 0;
-  ch_batch_tuning tune{4, 3, 0.0, 0.0};
+  ch_batch_tuning tune{4, 3, 0.0, 0.0, 0};
   cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [sort_due][parity]
   long long graph_nodes[2][2] = {{0, 0}, {0, 0}};
   bool prof = false;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   ch_profile pr{};
   // Runs of at least twice the mean node count ("large": the first nbig
-  // solve records) may be solved by clusters of cluster_big CTAs in a launch
-  // of their own, beside the others' launch on stream s2 (cluster_big 0: one
-  // launch for all).
-  int nbig = 0, cluster_big = 0;
+  // solve records) may be solved by clusters of tune.cluster_big CTAs in a
+  // launch of their own, beside the others' launch on stream s2
+  // (tune.cluster_big 0: one launch for all).
+  int nbig = 0;
   cudaStream_t s2 = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
 };
@@ -555,7 +555,7 @@ extern "C" ch_status ch_batch_initialize(ch_batch* b) {
   launch_batch_pass(PH_DEPOSIT, batch_dev(b), b->dstep, b->M, b->E32, b->starts, b->acc, b->sbar, b->dep_log2,
                     nullptr, b->tile_part, b->flags, b->tune.pass_ctas_per_sm, b->sms, s);
   launch_batch_finalize(4 * b->Ntot, b->acc, 1.0 / b->dep_scale, b->mom, b->flags + b->nruns, b->sms, s);
-  CH_CUDA_OK(solve_launch(b, b->tune.cluster, b->cluster_big, s));
+  CH_CUDA_OK(solve_launch(b, b->tune.cluster, b->tune.cluster_big, s));
   CH_CUDA_OK(cudaGetLastError());
   ch_status rc = read_status(b, nullptr);
   if (rc) return rc;
@@ -577,7 +577,7 @@ static cudaError_t enqueue_step(ch_batch* b, bool sort_due) {
   launch_batch_runsum(B, b->tile_part, b->run_sums, b->sbar, b->flags, b->dstep, s);
   launch_batch_finalize(4 * b->Ntot, b->acc, 1.0 / b->dep_scale, b->mom, b->flags + b->nruns, b->sms, s);
   if (b->prof) cudaEventRecord(b->ev[1], s);
-  cudaError_t e = solve_launch(b, b->tune.cluster, b->cluster_big, s);
+  cudaError_t e = solve_launch(b, b->tune.cluster, b->tune.cluster_big, s);
   if (b->prof) cudaEventRecord(b->ev[2], s);
   if (sort_due)
     launch_batch_sort(B, b->Ntot, b->M, b->MQ, b->counts, b->starts, b->cursor, b->block_sums, true, b->sms, s);
@@ -680,8 +680,12 @@ extern "C" ch_status ch_batch_set_tuning(ch_batch* b, const ch_batch_tuning* t) 
     return ch_fail(CH_ERR_ARG, "cluster must be 1, 2, 4 or 8");
   if (t->pass_ctas_per_sm < 1 || t->pass_ctas_per_sm > 3) return ch_fail(CH_ERR_ARG, "pass_ctas_per_sm: 1 to 3");
   b->tune.cluster = t->cluster;
+  if (!(t->cluster_big == 0 || t->cluster_big == 8 || t->cluster_big == 16))
+    return ch_fail(CH_ERR_ARG, "cluster_big must be 0, 8 or 16");
+  if (t->cluster_big == 16 && !batch_solve_allow_wide())
+    return ch_fail(CH_ERR_UNSUPPORTED, "clusters of 16 CTAs are not available on this device");
   b->tune.pass_ctas_per_sm = t->pass_ctas_per_sm;
-  b->cluster_big = 0;  // one launch shape for every run, as set
+  b->tune.cluster_big = t->cluster_big;
   drop_graphs(b);
   return CH_OK;
 }
@@ -773,7 +777,7 @@ extern "C" ch_status ch_batch_autotune(ch_batch* b, ch_batch_tuning* out) {
   cudaEventDestroy(e1);
   if (err != cudaSuccess) return ch_cuda_fail(err, "ch_batch_autotune", __FILE__, __LINE__);
   b->tune.cluster = best_c;
-  b->cluster_big = best_big;
+  b->tune.cluster_big = best_big;
   b->tune.pass_ctas_per_sm = best_k;
   b->tune.solve_ms = best_solve;
   b->tune.pass_ms = best_pass;

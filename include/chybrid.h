@@ -281,6 +281,9 @@ typedef struct ch_batch_tuning {
   int32_t pass_ctas_per_sm;  /* persistent CTAs per SM of the deposit: 1 to 3 */
   double pass_ms;            /* measured for the chosen shape (autotune)      */
   double solve_ms;
+  int32_t cluster_big;       /* CTAs per large run (node count >= twice the
+                                mean) solved in a launch of their own beside
+                                the others: 0 (no such launch), 8 or 16      */
 } ch_batch_tuning;
 
 /* Creates the device state of nruns runs (all CH_MIXED, lhs/rhs full,

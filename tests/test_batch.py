@@ -96,6 +96,7 @@ def test_batch_autotune_restores_state(chy):
         before = [(b.phi(r), b.download(r)) for r in range(len(params))]
         t = b.autotune()
         assert t["cluster"] in (1, 2, 4, 8) and t["pass_ctas_per_sm"] in (1, 2, 3)
+        assert t["cluster_big"] in (0, 8, 16) and b.tuning() == t
         assert t["pass_ms"] > 0 and t["solve_ms"] > 0
         after = [(b.phi(r), b.download(r)) for r in range(len(params))]
         for (pa, (xa, va)), (pb, (xb, vb)) in zip(before, after):
