@@ -1025,6 +1025,7 @@ __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH
   TileShared& sh = tile_smem_base<PH>(smem_tiled);
   __shared__ StepConsts sc;
   __shared__ int s_run;
+  __shared__ float s_pscale;
   constexpr int W = (int)(sizeof(StepConsts) / sizeof(uint32_t));
   static_assert(sizeof(StepConsts) % sizeof(uint32_t) == 0, "StepConsts is copied as words");
   for (int t = blockIdx.x; t < B.total_tiles; t += gridDim.x) {
@@ -1042,11 +1043,14 @@ __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH
     const BatchRunDev& R = B.runs[r];
     for (int w = threadIdx.x; w < W; w += blockDim.x)
       reinterpret_cast<uint32_t*>(&sc)[w] = reinterpret_cast<const uint32_t*>(&R.c)[w];
+    if (threadIdx.x == 0) {  // one FP64 division per brick, not per thread
+      const double S = sbar[r];
+      s_pscale = S > 0.0 ? (float)(R.Nc / S) : 0.0f;
+    }
     __syncthreads();
     if (threadIdx.x == 0) sc.step = *dstep;
     const int64_t no = R.node_off;
-    const double S = sbar[r];
-    const float pscale = S > 0.0 ? (float)(R.Nc / S) : 0.0f;
+    const float pscale = s_pscale;
     double vsum[4] = {0.0, 0.0, 0.0, 0.0};
     double v2[2] = {0.0, 0.0};
     unsigned long long gsum = 0ull;
