@@ -395,13 +395,11 @@ __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, 
 #define CH_TILE_VMAX 8.0f
 #define CH_TILE_DLOG2 22
 #define CH_TILE_FLOG2 19
-// Round-to-nearest-even of |x| <= 2^22 on the FP32 pipe: x + 1.5 * 2^23 lies
-// in [2^23, 2^24), where floats are the integers, so the bits of the sum are
-// rint(x) + CH_RNI_BIAS (the conversion unit runs at a fraction of the rate).
+// Round-to-nearest-even of a b, |a b| <= 2^22, on the FP32 pipe: the exact
+// product plus 1.5 * 2^23 lies in [2^23, 2^24), where floats are the
+// integers, so the bits of fma(a, b, 1.5 * 2^23) are rint(a b) + CH_RNI_BIAS
+// (the conversion unit runs at a fraction of the rate).
 #define CH_RNI_BIAS 0x4B400000
-// rni_fma(a, b): the same for the exact product a b, rounded once (one FMA).
-__device__ __forceinline__ int rni_biased(float x) { return __float_as_int(__fadd_rn(x, 12582912.0f)); }
-__device__ __forceinline__ int rni(float x) { return rni_biased(x) - CH_RNI_BIAS; }
 __device__ __forceinline__ int rni_fma(float a, float b) { return __float_as_int(__fmaf_rn(a, b, 12582912.0f)); }
 
 #define CH_PUSH_CTAS 4          // CTAs per SM of a pass without the deposit
@@ -412,7 +410,6 @@ static_assert(CH_TILE_QW >= 64 && (CH_TILE_QW & (CH_TILE_QW - 1)) == 0,
               "a warp ring holds 31 pending + 32 new entries and is indexed modulo its size");
 
 #define CH_TILE_K 4            // consecutive slots one thread deposits together
-#define CH_TILE_BATCH (256 * CH_TILE_K)
 #define CH_DEP_RW 256          // ring of displaced ions per warp (31 waiting + 128 of a chunk fit)
 
 // Shared memory of one CTA of the tiled pass: [push part][header][deposit
