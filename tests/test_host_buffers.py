@@ -68,13 +68,14 @@ def test_misaligned_view_of_a_registered_range_is_staged(chy):
         chy.host_unregister(big)
 
 
-def test_round_trip_through_registered_arrays_keeps_the_run(chy):
+@pytest.mark.parametrize("extra", [0, 7])  # 7: a last warp chunk and copy chunk that are partial
+def test_round_trip_through_registered_arrays_keeps_the_run(chy, extra):
     """A download into registered arrays followed by an upload of the same
     arrays puts every ion back into its slot (no sort); a plain round trip
     re-sorts.  The order of the ions does not enter any result (integer
     deposit sums, per-ion draws), so both runs stay identical bit for bit."""
     p = chy.params_for((16, 12, 20), precision=chy.PRECISION["mixed"], nui=0.4, sort_period=3)
-    n = 16 * 12 * 20 * 8
+    n = 16 * 12 * 20 * 8 + extra
     outs = []
     for registered in (False, True):
         with chy.Hybrid(p) as h:
