@@ -80,6 +80,7 @@ struct ch_ctx {
   uint32_t* keys = nullptr;
   // grid
   uint32_t *counts = nullptr, *starts = nullptr, *cursor = nullptr, *block_sums = nullptr;
+  uint32_t* starts_next = nullptr;  // the order a step's fused deposit + scatter writes (mixed form)
   double *phi = nullptr, *E64 = nullptr, *mom = nullptr, *rhs = nullptr, *nfz = nullptr;
   float4* E32 = nullptr;
   unsigned long long* acc = nullptr;
@@ -225,7 +226,7 @@ extern "C" ch_status ch_destroy(ch_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   output_close(c);
   free_particles(c);
-  void* v[] = {c->counts, c->starts, c->cursor, c->block_sums, c->phi, c->E64, c->mom, c->rhs, c->nfz,
+  void* v[] = {c->counts, c->starts, c->starts_next, c->cursor, c->block_sums, c->phi, c->E64, c->mom, c->rhs, c->nfz,
                c->E32, c->acc, c->cnt, c->red};
   for (void* q : v)
     if (q) cudaFree(q);
@@ -263,6 +264,7 @@ extern "C" ch_status ch_create(const ch_params* p, int32_t device, ch_ctx** out)
   const int nsb = (int)((N + 1023) / 1024) + 1;
   struct { void** p; size_t b; } allocs[] = {
       {(void**)&c->counts, sizeof(uint32_t) * N},       {(void**)&c->starts, sizeof(uint32_t) * (N + 1)},
+      {(void**)&c->starts_next, sizeof(uint32_t) * (N + 1)},
       {(void**)&c->cursor, sizeof(uint32_t) * N},       {(void**)&c->block_sums, sizeof(uint32_t) * nsb},
       {(void**)&c->phi, sizeof(double) * N},            {(void**)&c->mom, sizeof(double) * 4 * N},
       {(void**)&c->rhs, sizeof(double) * N},            {(void**)&c->nfz, sizeof(double) * N},
@@ -643,6 +645,25 @@ extern "C" ch_status ch_compute_potential(ch_ctx* c, double* phi_out, ch_solve_i
   return CH_OK;
 }
 
+// Scan of the push's cell count into starts_next, then the deposit fused
+// with the scatter of M into MQ in that order (mixed form).
+static ch_status run_deposit_sort(ch_ctx* c) {
+  StepConsts k = consts(c, 0);
+  CH_CUDA_OK(cudaMemsetAsync(&c->cnt->range_error, 0, sizeof(int), c->stream));
+  prof_begin(c);
+  launch_scan(c->g, c->counts, c->starts_next, c->cursor, c->block_sums, c->stream);
+  prof_end(c, &c->pr.sort_ms, &c->pr.sort_calls);
+  prof_begin(c);
+  launch_deposit_sort(k, c->M, c->MQ, c->starts, c->starts_next, c->acc, c->cnt, c->sms, c->stream);
+  const double before = c->pr.pass_ms;
+  prof_end(c, &c->pr.pass_ms, &c->pr.pass_calls);
+  if (c->prof) {
+    c->pr.deposit_ms += c->pr.pass_ms - before;
+    c->pr.deposit_calls += 1;
+  }
+  return CH_OK;
+}
+
 extern "C" ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_step_info* info) {
   if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
   if (c->np == 0) return ch_fail(CH_ERR_STATE, "no ions");
@@ -658,13 +679,25 @@ extern "C" ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_s
     // memory and registers allow only 2 CTAs per SM; the results are the
     // same bit for bit.
     ch_status rc = run_pass(c, PH_PUSH | PH_MOVE, first_step + s, &local, sort_due);
-    if (!rc) rc = run_pass(c, PH_DEPOSIT, 0, nullptr);
+    // Mixed form, sort due: the push counted every ion's new cell and rank;
+    // the scan gives the new order, and the deposit, which reads every ion
+    // anyway, also writes it there (the counting sort's scatter).
+    const bool fused_sort = sort_due && c->mixed;
+    if (!rc && fused_sort) rc = run_deposit_sort(c);
+    else if (!rc) rc = run_pass(c, PH_DEPOSIT, 0, nullptr);
     if (rc) return rc;
     rc = finalize_moments(c, &local);
     if (rc) return rc;
     rc = potential(c, &local.solve);
     if (rc) return rc;
-    if (sort_due) do_sort(c, c->mixed);
+    if (fused_sort) {
+      std::swap(c->M, c->MQ);
+      std::swap(c->starts, c->starts_next);
+      c->since_sort = 0;
+      c->slot_map_valid = false;
+    } else if (sort_due) {
+      do_sort(c, c->mixed);
+    }
   }
   CH_CUDA_OK(cudaStreamSynchronize(c->stream));
   if (info) *info = local;

@@ -513,9 +513,16 @@ __device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, i
 // at a time.
 // Every contribution is rounded to an integer before any addition, so the
 // result does not depend on the order; no block barrier is needed.
+// SCAT (a step that ends with a sort): every ion read is also written to
+// slot dst_starts[its cell] + its rank of Q (the ranks come from the push's
+// cell count), which is the counting sort's scatter; the deposit reads each
+// ion anyway.  A separate instantiation, so that the plain deposit keeps
+// its registers.
+template <bool SCAT>
 __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepConsts& c, MixParticles P,
                                                     unsigned long long* __restrict__ acc, uint32_t total, int bi0,
-                                                    int bj0, int bk0, int& bad) {
+                                                    int bj0, int bk0, int& bad, MixParticles Q,
+                                                    const uint32_t* __restrict__ dst_starts) {
   const GridDesc& g = c.g;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t* ring = sh.d_ip + warp * CH_DEP_RW;
@@ -557,6 +564,11 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
         const uint32_t cell = __float_as_uint(p.w);
         const int i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
                   kz = cell >> (CH_PACK_BX + CH_PACK_BY);
+        if constexpr (SCAT) {  // every ion, whether or not it is deposited here
+          const uint32_t d = dst_starts[(kz * g.Ny + j) * g.Nx + i] + P.rank[ip];
+          Q.pos[d] = p;
+          Q.vel[d] = v;
+        }
         const bool finite =
             isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
         bool inbox;
@@ -752,13 +764,14 @@ __device__ __forceinline__ void tile_queue_round(TileShared& sh, const StepConst
 // brick: possible when the finish of an ion does not use the brick, i.e.
 // without the deposit, and the run's constants do not change between
 // bricks), otherwise it is drained here.
-template <int PH, bool CARRY>
+template <int PH, bool CARRY, bool SCAT = false>
 __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, MixParticles P,
                                           const float4* __restrict__ E, const uint32_t* __restrict__ starts,
                                           unsigned long long* __restrict__ acc, float pscale, int shift_d,
                                           int shift_f, uint32_t* hist, int tile, double (&vsum)[2],
                                           unsigned long long& gsum, unsigned& qhead, unsigned& qtail, unsigned& ncol,
-                                          unsigned& nref, int& bad) {
+                                          unsigned& nref, int& bad, MixParticles Q = MixParticles{},
+                                          const uint32_t* dst_starts = nullptr) {
   static_assert(PH == PH_DEPOSIT || !(PH & PH_DEPOSIT), "the deposit has a launch of its own");
   static_assert(!(CARRY && (PH & PH_DEPOSIT)), "a deposit pass has no deferred ions to carry");
   const GridDesc& g = c.g;
@@ -810,7 +823,7 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
   // post-step mean relative speeds, which normalise the next step's rates,
   // go to gsum as integers of 2^-20 so that S is exact whatever the ion order.
   float tsum0 = 0.0f;
-  if (PH == PH_DEPOSIT) tile_deposit_direct(sh, c, P, acc, total, bi0, bj0, bk0, bad);
+  if (PH == PH_DEPOSIT) tile_deposit_direct<SCAT>(sh, c, P, acc, total, bi0, bj0, bk0, bad, Q, dst_starts);
   const uint32_t ptotal = total * (PH == PH_DEPOSIT ? 0u : 1u);  // ions the push / move loop visits
   // index of slot idx in the ion arrays (rows of the brick are contiguous)
   auto slot_ip = [&](uint32_t idx) -> uint32_t {
@@ -976,12 +989,13 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
 }
 
 // A pass without the deposit carries deferred ions from brick to brick and
-// drains the rings once, after the CTA's last brick.
-template <int PH>
+// drains the rings once, after the CTA's last brick.  SCAT: the deposit
+// also scatters the ions into Q in the order of dst_starts.
+template <int PH, bool SCAT = false>
 __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH_CTAS)
     k_pass_tiled(StepConsts c, MixParticles P, const float4* __restrict__ E, const uint32_t* __restrict__ starts,
                  unsigned long long* __restrict__ acc, float pscale, int shift_d, int shift_f, DevCounters* cnt,
-                 double* part, uint32_t* hist) {
+                 double* part, uint32_t* hist, MixParticles Q, const uint32_t* dst_starts) {
   constexpr bool CARRY = !(PH & PH_DEPOSIT);
   extern __shared__ __align__(16) unsigned char smem_tiled[];
   TileShared& sh = tile_smem_base<PH>(smem_tiled);
@@ -992,8 +1006,8 @@ __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH
   const GridDesc& g = c.g;
   const int ntiles = ((g.Nx + TX - 1) / TX) * ((g.Ny + TY - 1) / TY) * ((g.Nz + TZ - 1) / TZ);
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
-    tile_pass<PH, CARRY>(sh, c, P, E, starts, acc, pscale, shift_d, shift_f, hist, tile, vsum, gsum, qhead, qtail,
-                         ncol, nref, bad);
+    tile_pass<PH, CARRY, SCAT>(sh, c, P, E, starts, acc, pscale, shift_d, shift_f, hist, tile, vsum, gsum, qhead,
+                               qtail, ncol, nref, bad, Q, dst_starts);
   if (CARRY) {
     while (qtail != qhead)
       tile_queue_round<PH>(sh, c, P, hist, qhead, qtail, min(qtail - qhead, 32u), gsum, ncol, nref);
@@ -1588,7 +1602,7 @@ void launch_node_efield(bool mixed, const GridDesc& g, double tscale, const doub
 
 // The tiled pass needs more than the default 48 KB of dynamic shared memory;
 // the attribute is set once per device and instantiation.
-template <int PH>
+template <int PH, bool SCAT = false>
 static void tiled_smem_attr() {
   static std::atomic<uint32_t> done{0};
   int dev = 0;
@@ -1596,7 +1610,7 @@ static void tiled_smem_attr() {
   const uint32_t bit = 1u << (dev & 31);
   if (done.load() & bit) return;
   // a failure here surfaces as the launch error of the pass
-  if (cudaFuncSetAttribute(k_pass_tiled<PH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (cudaFuncSetAttribute(k_pass_tiled<PH, SCAT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)tile_smem_bytes<PH>()) == cudaSuccess)
     done.fetch_or(bit);
 }
@@ -1617,7 +1631,8 @@ static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticle
     const int s2 = (int)lround(log2(c.dep_scale));
     tiled_smem_attr<PH>();
     k_pass_tiled<PH><<<nb, 256, tile_smem_bytes<PH>(), s>>>(c, M, E32, starts, acc, pscale, s2 - CH_TILE_DLOG2,
-                                                         s2 - CH_TILE_FLOG2, cnt, part, hist),
+                                                         s2 - CH_TILE_FLOG2, cnt, part, hist, MixParticles{},
+                                                         (const uint32_t*)nullptr),
         ::ch::note_launch();
     }
   } else {
@@ -1669,6 +1684,33 @@ int launch_finalize(int64_t N, unsigned long long* acc, double inv_scale, int re
   const int nb = grid_for(N, 256, sms, 4);
   k_finalize_moments<<<nb, 256, 0, s>>>(N, acc, inv_scale, reset, mom, part, cnt), ::ch::note_launch();
   return nb;
+}
+
+// Exclusive scan of counts into starts (starts[N] = total); cursor gets a
+// copy of starts.
+void launch_scan(const GridDesc& g, const uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* block_sums,
+                 cudaStream_t s) {
+  const int64_t N = g.N;
+  const int nsb = (int)((N + 1023) / 1024);
+  k_scan_blocks<<<nsb, 512, 0, s>>>(counts, starts, block_sums, N), ::ch::note_launch();
+  k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nsb, starts + N), ::ch::note_launch();
+  k_scan_add<<<(int)((N + 255) / 256), 256, 0, s>>>(starts, block_sums, N, cursor), ::ch::note_launch();
+}
+
+// The deposit of a step that ends with a sort: ions read in the order of
+// `starts` are deposited and written to Q in the order of dst_starts (the
+// scan of the push's cell count, with the ions' ranks in M.rank).
+void launch_deposit_sort(const StepConsts& c, MixParticles M, MixParticles MQ, const uint32_t* starts,
+                         const uint32_t* dst_starts, unsigned long long* acc, DevCounters* cnt, int sms,
+                         cudaStream_t s) {
+  const int ntiles = ((c.g.Nx + 15) / 16) * ((c.g.Ny + 3) / 4) * ((c.g.Nz + 3) / 4);
+  const int nb = ntiles < CH_DEP_CTAS * sms ? ntiles : CH_DEP_CTAS * sms;
+  const int s2 = (int)lround(log2(c.dep_scale));
+  tiled_smem_attr<PH_DEPOSIT, true>();
+  k_pass_tiled<PH_DEPOSIT, true><<<nb, 256, tile_smem_bytes<PH_DEPOSIT>(), s>>>(
+      c, M, (const float4*)nullptr, starts, acc, 0.0f, s2 - CH_TILE_DLOG2, s2 - CH_TILE_FLOG2, cnt, (double*)nullptr,
+      (uint32_t*)nullptr, MQ, dst_starts),
+      ::ch::note_launch();
 }
 
 void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, MixParticles M, MixParticles MQ,

@@ -63,6 +63,14 @@ int launch_finalize(int64_t N, unsigned long long* acc, double inv_scale, int re
 // have_hist: counts already hold the per-cell ion counts and M.rank each
 // ion's rank in its new cell (mixed form, recorded by the preceding pass), so
 // the scatter needs no atomics.
+// Exclusive scan of the cell counts into starts (and cursor).
+void launch_scan(const GridDesc& g, const uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* block_sums,
+                 cudaStream_t s);
+// The deposit of a step that ends with a sort, fused with the sort's scatter
+// of M (order of starts) into MQ (order of dst_starts, ranks in M.rank).
+void launch_deposit_sort(const StepConsts& c, MixParticles M, MixParticles MQ, const uint32_t* starts,
+                         const uint32_t* dst_starts, unsigned long long* acc, DevCounters* cnt, int sms,
+                         cudaStream_t s);
 void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, MixParticles M, MixParticles MQ,
                  uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* keys, uint32_t* block_sums,
                  bool have_hist, int sms, cudaStream_t s);
