@@ -651,7 +651,7 @@ static ch_status run_deposit_sort(ch_ctx* c) {
   StepConsts k = consts(c, 0);
   CH_CUDA_OK(cudaMemsetAsync(&c->cnt->range_error, 0, sizeof(int), c->stream));
   prof_begin(c);
-  launch_scan(c->g, c->counts, c->starts_next, c->cursor, c->block_sums, c->stream);
+  launch_scan(c->g.N, c->counts, c->starts_next, c->cursor, c->block_sums, c->stream);
   prof_end(c, &c->pr.sort_ms, &c->pr.sort_calls);
   prof_begin(c);
   launch_deposit_sort(k, c->M, c->MQ, c->starts, c->starts_next, c->acc, c->cnt, c->sms, c->stream);

@@ -80,6 +80,7 @@ struct ch_batch {
   int64_t* d_ion_off = nullptr;
   MixParticles M{}, MQ{};
   uint32_t *counts = nullptr, *starts = nullptr, *cursor = nullptr, *block_sums = nullptr, *dstep = nullptr;
+  uint32_t* starts_next = nullptr;  // the order a sort step's deposit writes (swaps with starts)
   double *phi = nullptr, *mom = nullptr, *b64 = nullptr, *r64 = nullptr;
   float4* E32 = nullptr;
   unsigned long long* acc = nullptr;
@@ -329,6 +330,7 @@ extern "C" ch_status ch_batch_create(const ch_params* runs, const int64_t* np, i
   b->M.rank = b->MQ.rank = P.get<uint32_t>(NP);
   b->counts = P.get<uint32_t>(N);
   b->starts = P.get<uint32_t>(N + 1);
+  b->starts_next = P.get<uint32_t>(N + 1);
   b->cursor = P.get<uint32_t>(N);
   b->block_sums = P.get<uint32_t>((N + 1023) / 1024 + 1);
   b->dstep = P.get<uint32_t>(1);
@@ -492,8 +494,11 @@ extern "C" ch_status ch_batch_download(ch_batch* b, int32_t run, ch_real_vector*
   return CH_OK;
 }
 
-// Full counting sort of every run's ions (counts are recounted).
+// Full counting sort of every run's ions (counts are recounted).  The step
+// graphs hold the ion and order buffers of their parity, which this swap does
+// not follow, so they are captured again.
 static void full_sort(ch_batch* b) {
+  drop_graphs(b);
   cudaMemsetAsync(b->counts, 0, sizeof(uint32_t) * b->Ntot, b->stream);
   launch_batch_hist(batch_dev(b), b->M, b->counts, b->sms, b->stream);
   launch_batch_sort(batch_dev(b), b->Ntot, b->M, b->MQ, b->counts, b->starts, b->cursor, b->block_sums, false,
@@ -569,18 +574,20 @@ static cudaError_t enqueue_step(ch_batch* b, bool sort_due) {
   const BatchDev B = batch_dev(b);
   if (b->prof) cudaEventRecord(b->ev[0], s);
   if (sort_due) cudaMemsetAsync(b->counts, 0, sizeof(uint32_t) * b->Ntot, s);
-  // push + collide + move, then the deposit (two launches, as the single-run step)
+  // push + collide + move, then the deposit (two launches, as the single-run step).
+  // Sort due: the push counts the new cells, the scan orders them, and the
+  // deposit writes every ion to its sorted slot of MQ.
   launch_batch_pass(PH_PUSH | PH_MOVE, B, b->dstep, b->M, b->E32, b->starts, b->acc, b->sbar, b->dep_log2,
                     sort_due ? b->counts : nullptr, b->tile_part, b->flags, b->tune.pass_ctas_per_sm, b->sms, s);
+  if (sort_due) launch_scan(b->Ntot, b->counts, b->starts_next, b->cursor, b->block_sums, s);
   launch_batch_pass(PH_DEPOSIT, B, b->dstep, b->M, b->E32, b->starts, b->acc, b->sbar, b->dep_log2, nullptr,
-                    b->tile_part + 4 * (size_t)b->total_tiles, b->flags, b->tune.pass_ctas_per_sm, b->sms, s);
+                    b->tile_part + 4 * (size_t)b->total_tiles, b->flags, b->tune.pass_ctas_per_sm, b->sms, s,
+                    b->MQ, sort_due ? b->starts_next : nullptr);
   launch_batch_runsum(B, b->tile_part, b->run_sums, b->sbar, b->flags, b->dstep, s);
   launch_batch_finalize(4 * b->Ntot, b->acc, 1.0 / b->dep_scale, b->mom, b->flags + b->nruns, b->sms, s);
   if (b->prof) cudaEventRecord(b->ev[1], s);
   cudaError_t e = solve_launch(b, b->tune.cluster, b->tune.cluster_big, s);
   if (b->prof) cudaEventRecord(b->ev[2], s);
-  if (sort_due)
-    launch_batch_sort(B, b->Ntot, b->M, b->MQ, b->counts, b->starts, b->cursor, b->block_sums, true, b->sms, s);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
@@ -633,6 +640,7 @@ extern "C" ch_status ch_batch_step(ch_batch* b, int64_t first_step, int32_t nste
     }
     if (sort_due) {
       std::swap(b->M, b->MQ);
+      std::swap(b->starts, b->starts_next);
       b->parity = !b->parity;
       b->since_sort = 0;
     } else {

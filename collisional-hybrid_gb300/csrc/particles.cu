@@ -1026,12 +1026,14 @@ __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH
 // run (its deferred ions finished inside the brick, as the next brick may
 // belong to another run).  Brick partials are written per brick, so the run
 // sums are formed in a fixed order afterwards.
-template <int PH>
+// SCAT: the deposit also writes the ions to Q in the order of dst_starts
+// (global slots, indexed by node_off[r] + cell), as the single-run pass.
+template <int PH, bool SCAT = false>
 __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH_CTAS)
     k_batch_pass(BatchDev B, const uint32_t* dstep, MixParticles P, const float4* __restrict__ E,
                  const uint32_t* __restrict__ starts, unsigned long long* __restrict__ acc,
                  const double* __restrict__ sbar, int shift_d, int shift_f, uint32_t* hist, double* tile_part,
-                 int* flags) {
+                 int* flags, MixParticles Q, const uint32_t* __restrict__ dst_starts) {
   extern __shared__ __align__(16) unsigned char smem_tiled[];
   TileShared& sh = tile_smem_base<PH>(smem_tiled);
   __shared__ StepConsts sc;
@@ -1068,8 +1070,9 @@ __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH
     unsigned qhead = 0, qtail = 0, ncol = 0, nref = 0;
     int bad = 0;
     // tile_pass starts with a barrier, after which sc.step is visible
-    tile_pass<PH, false>(sh, sc, P, E + no, starts + no, acc + 4 * no, pscale, shift_d, shift_f,
-                         hist ? hist + no : nullptr, t - R.tile_off, v2, gsum, qhead, qtail, ncol, nref, bad);
+    tile_pass<PH, false, SCAT>(sh, sc, P, E + no, starts + no, acc + 4 * no, pscale, shift_d, shift_f,
+                               hist ? hist + no : nullptr, t - R.tile_off, v2, gsum, qhead, qtail, ncol, nref, bad,
+                               Q, SCAT ? dst_starts + no : nullptr);
     if (bad) atomicOr(flags + r, 16);  // non-finite ion
     vsum[0] = v2[0]; vsum[1] = (double)gsum * CH_G_UNIT; vsum[2] = (double)ncol; vsum[3] = (double)nref;
     block_partials<4>(vsum, tile_part, t);
@@ -1688,9 +1691,8 @@ int launch_finalize(int64_t N, unsigned long long* acc, double inv_scale, int re
 
 // Exclusive scan of counts into starts (starts[N] = total); cursor gets a
 // copy of starts.
-void launch_scan(const GridDesc& g, const uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* block_sums,
+void launch_scan(int64_t N, const uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* block_sums,
                  cudaStream_t s) {
-  const int64_t N = g.N;
   const int nsb = (int)((N + 1023) / 1024);
   k_scan_blocks<<<nsb, 512, 0, s>>>(counts, starts, block_sums, N), ::ch::note_launch();
   k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nsb, starts + N), ::ch::note_launch();
@@ -1734,14 +1736,14 @@ void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, 
 }
 
 // ------------------------------------------------------------------ ensemble launchers
-template <int PH>
+template <int PH, bool SCAT = false>
 static void batch_smem_attr() {
   static std::atomic<uint32_t> done{0};
   int dev = 0;
   cudaGetDevice(&dev);
   const uint32_t bit = 1u << (dev & 31);
   if (done.load() & bit) return;
-  if (cudaFuncSetAttribute(k_batch_pass<PH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (cudaFuncSetAttribute(k_batch_pass<PH, SCAT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)tile_smem_bytes<PH>()) == cudaSuccess)
     done.fetch_or(bit);
 }
@@ -1749,23 +1751,31 @@ static void batch_smem_attr() {
 void batch_pass_prepare() {
   batch_smem_attr<PH_PUSH | PH_MOVE>();
   batch_smem_attr<PH_DEPOSIT>();
+  batch_smem_attr<PH_DEPOSIT, true>();
 }
 
 void launch_batch_pass(int phases, const BatchDev& B, const uint32_t* dstep, MixParticles P, const float4* E,
                        const uint32_t* starts, unsigned long long* acc, const double* sbar, int dep_log2,
-                       uint32_t* hist, double* tile_part, int* flags, int ctas_per_sm, int sms, cudaStream_t s) {
+                       uint32_t* hist, double* tile_part, int* flags, int ctas_per_sm, int sms, cudaStream_t s,
+                       MixParticles Q, const uint32_t* dst_starts) {
   const int sd = dep_log2 - CH_TILE_DLOG2, sf = dep_log2 - CH_TILE_FLOG2;
   auto grid = [&](int per_sm) { return B.total_tiles < per_sm * sms ? B.total_tiles : per_sm * sms; };
   // the deposit is a launch of its own
   if (phases & (PH_PUSH | PH_MOVE)) {
     k_batch_pass<PH_PUSH | PH_MOVE><<<grid(CH_PUSH_CTAS), 256, tile_smem_bytes<PH_PUSH | PH_MOVE>(), s>>>(
-        B, dstep, P, E, starts, acc, sbar, sd, sf, hist, tile_part, flags),
+        B, dstep, P, E, starts, acc, sbar, sd, sf, hist, tile_part, flags, MixParticles{}, nullptr),
         ::ch::note_launch();
   }
   if (phases & PH_DEPOSIT) {
-    k_batch_pass<PH_DEPOSIT><<<grid(ctas_per_sm < 1 ? 1 : ctas_per_sm), 256, tile_smem_bytes<PH_DEPOSIT>(), s>>>(
-        B, dstep, P, E, starts, acc, sbar, sd, sf, nullptr, tile_part, flags),
-        ::ch::note_launch();
+    const int nb = grid(ctas_per_sm < 1 ? 1 : ctas_per_sm);
+    if (dst_starts)
+      k_batch_pass<PH_DEPOSIT, true><<<nb, 256, tile_smem_bytes<PH_DEPOSIT>(), s>>>(
+          B, dstep, P, E, starts, acc, sbar, sd, sf, nullptr, tile_part, flags, Q, dst_starts),
+          ::ch::note_launch();
+    else
+      k_batch_pass<PH_DEPOSIT><<<nb, 256, tile_smem_bytes<PH_DEPOSIT>(), s>>>(
+          B, dstep, P, E, starts, acc, sbar, sd, sf, nullptr, tile_part, flags, MixParticles{}, nullptr),
+          ::ch::note_launch();
   }
 }
 

@@ -64,7 +64,7 @@ int launch_finalize(int64_t N, unsigned long long* acc, double inv_scale, int re
 // ion's rank in its new cell (mixed form, recorded by the preceding pass), so
 // the scatter needs no atomics.
 // Exclusive scan of the cell counts into starts (and cursor).
-void launch_scan(const GridDesc& g, const uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* block_sums,
+void launch_scan(int64_t N, const uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* block_sums,
                  cudaStream_t s);
 // The deposit of a step that ends with a sort, fused with the sort's scatter
 // of M (order of starts) into MQ (order of dst_starts, ranks in M.rank).
@@ -105,7 +105,8 @@ int tiles_of(const GridDesc& g);
 void batch_pass_prepare();  // once, before any capture
 void launch_batch_pass(int phases, const BatchDev& B, const uint32_t* dstep, MixParticles P, const float4* E,
                        const uint32_t* starts, unsigned long long* acc, const double* sbar, int dep_log2,
-                       uint32_t* hist, double* tile_part, int* flags, int ctas_per_sm, int sms, cudaStream_t s);
+                       uint32_t* hist, double* tile_part, int* flags, int ctas_per_sm, int sms, cudaStream_t s,
+                       MixParticles Q = MixParticles{}, const uint32_t* dst_starts = nullptr);
 // sums[4r + q] = the run's brick partials summed in a fixed order; sbar[r] =
 // S for the next step (runs with collisions); flags[r] |= 8 at the refusal
 // limit; *dstep advances by one.

@@ -87,6 +87,29 @@ def test_batch_graph_replay_equals_eager(chy):
 
 
 @pytest.mark.gpu
+def test_batch_reinitialize_between_sorts_equals_eager(chy):
+    """A second initialize swaps the ion buffers with a full sort after the
+    step graphs of both buffer parities exist: the replayed steps that follow
+    (two more sorts) must still read the current buffers."""
+    params, nions, loaders = _runs(chy)
+    out = []
+    for eager in (False, True):
+        with chy.Batch(params, nions) as b:
+            b.load(loaders)
+            b.initialize()
+            if eager:
+                b.set_profiling(True)
+            b.step(0, 9)
+            b.initialize()
+            info = b.step(9, 10)
+            assert all(i["status"] == 0 for i in info)
+            out.append([(b.moments(r), b.phi(r), b.download(r)) for r in range(len(params))])
+    for (ma, pa, (xa, va)), (mb, pb, (xb, vb)) in zip(*out):
+        assert np.array_equal(ma, mb) and np.array_equal(pa, pb)
+        assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+
+
+@pytest.mark.gpu
 def test_batch_autotune_restores_state(chy):
     params, nions, loaders = _runs(chy)
     with chy.Batch(params, nions) as b:
