@@ -90,8 +90,8 @@ __device__ __forceinline__ U4 ch_philox(uint32_t c0, uint32_t c1, uint32_t c2, u
   for (int r = 0; r < 10; ++r) {
     uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
     uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
-    uint32_t n0 = hi1 ^ c1 ^ k0;
-    uint32_t n2 = hi0 ^ c3 ^ k1;
+    const uint32_t n0 = hi1 ^ c1 ^ k0;
+    const uint32_t n2 = hi0 ^ c3 ^ k1;
     c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
     k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
   }
@@ -129,6 +129,8 @@ struct StepConsts {
     float t[3], s[3], pE0[3];   // pE0 = E0 tscale
     float vnT, vn0[3], mi, mn, viTr, m1;
     float nn_center, nn_sigma, nn_floor, dep_scale;
+    float wi, wn;   // mi / (mi + mn), mn / (mi + mn): centre-of-mass weights
+    float vlim2;    // (10 viTr)^2: the square of the refusal speed
   } f;
 };
 
@@ -152,6 +154,10 @@ inline void ch_consts_finish(StepConsts& k) {
   k.f.nn_sigma = (float)k.nn_sigma;
   k.f.nn_floor = (float)k.nn_floor;
   k.f.dep_scale = (float)k.dep_scale;
+  const double M = k.mi + k.mn;
+  k.f.wi = M > 0.0 ? (float)(k.mi / M) : 0.0f;
+  k.f.wn = M > 0.0 ? (float)(k.mn / M) : 0.0f;
+  k.f.vlim2 = (float)(100.0 * k.viTr * k.viTr);
 }
 
 // The constant in the kernel's precision: the FP64 field, or its FP32 copy.

@@ -687,7 +687,7 @@ __device__ __forceinline__ void tile_move_ion(const StepConsts& c, float4& p, co
 
 __device__ __forceinline__ float tile_gmean(const StepConsts& c, const float v[3]) {
   const float qx = v[0] - c.f.vn0[0], qy = v[1] - c.f.vn0[1], qz = v[2] - c.f.vn0[2];
-  return ch_gmean<float>(sqrtf(qx * qx + qy * qy + qz * qz), c.f.vnT);
+  return ch_gmean<float>(ch_qsqrt(qx * qx + qy * qy + qz * qz), c.f.vnT);
 }
 
 // One drain round of the calling warp's ring of deferred ions (warp-uniform
@@ -722,7 +722,8 @@ __device__ __forceinline__ void tile_queue_round(TileShared& sh, const StepConst
   const float qsc = q4.w;
   uint32_t qe = st & 0xFFu, qit = st >> 8;
   bool done = false;
-  if (act) done = ch_collide_round<float>(c, qid, qsc, qv, qtm, qe, qit, &ncol, &nref);
+  float gf = 0.0f;  // g of the final velocity of a finished ion
+  if (act) done = ch_collide_round<float>(c, qid, qsc, qv, qtm, qe, qit, &ncol, &nref, gf);
   const bool requeue = act && !done;
   const unsigned rm = __ballot_sync(0xffffffffu, requeue);
   if (requeue) {
@@ -740,7 +741,7 @@ __device__ __forceinline__ void tile_queue_round(TileShared& sh, const StepConst
   const bool fin = act && done;
   int qi = 0, qj = 0, qk = 0;
   if (fin) {
-    gsum += g_fixed(tile_gmean(c, qv));
+    gsum += g_fixed(gf);
     P.vel[qip] = make_float4(qv[0], qv[1], qv[2], __uint_as_float(qid));
     const uint32_t cell = __float_as_uint(qp.w);
     qi = cell & (CH_MAX_NX - 1); qj = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1);
@@ -925,7 +926,7 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
         // the queue keeps its waiting time
         const float u0 = ch_unitf(r0.x);
         if (lam > 0.0f && u0 > __expf(-lam)) {
-          qt0 = -ch_log(u0) / lam;
+          qt0 = ch_qdiv(-ch_log(u0), lam);
           defer = qt0 < 1.0f;
         }
         if (defer) qscale = lscale;
@@ -1133,7 +1134,7 @@ __global__ void k_sbar_mixed(MixParticles P, float vnT, float vn0x, float vn0y, 
   for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
     const float4 v = P.vel[ip];
     const float wx = v.x - vn0x, wy = v.y - vn0y, wz = v.z - vn0z;
-    s[0] += (double)g_fixed(ch_gmean<float>(sqrtf(wx * wx + wy * wy + wz * wz), vnT)) * CH_G_UNIT;
+    s[0] += (double)g_fixed(ch_gmean<float>(ch_qsqrt(wx * wx + wy * wy + wz * wz), vnT)) * CH_G_UNIT;
   }
   block_partials<1>(s, part);
 }

@@ -17,6 +17,18 @@ __device__ __forceinline__ float ch_log(float x) { return __logf(x); }
 __device__ __forceinline__ double ch_exp(double x) { return exp(x); }
 __device__ __forceinline__ float ch_exp(float x) { return expf(x); }
 __device__ __forceinline__ double ch_erf(double x) { return erf(x); }
+// Quick forms for the collision draws of the FP32 form: the hardware
+// approximate square root (PTX sqrt.approx.f32) and the full-range
+// approximate division (__fdividef, 2 ulp).  The draws are statistical and
+// their FP32 form is already rounded at 2^-24; the FP64 form stays exact.
+__device__ __forceinline__ double ch_qsqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float ch_qsqrt(float x) {
+  float y;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ double ch_qdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float ch_qdiv(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ float ch_erf(float x) { return erff(x); }
 __device__ __forceinline__ void ch_sincos2pi(double u, double* s, double* c) { sincos(2.0 * CH_PI * u, s, c); }
 // FP32 form, u in [0, 1): the hardware sine/cosine on the angle 2 pi (u -
@@ -191,41 +203,45 @@ __device__ __noinline__ int ch_collide(const StepConsts& c, uint32_t id, R lscal
 // already in t).  The round draws proposal it of event e from the same
 // Philox blocks as ch_collide; if it is accepted the scatter (or refusal) is
 // applied and the waiting time of event e + 1 is added.  Returns true when
-// the ion has no further event in this step.
+// the ion has no further event in this step; gfin is then the mean relative
+// speed g of its final velocity.  Quick square roots and divisions
+// (ch_qsqrt, ch_qdiv) and two identities of the scatter, |v - v_cm| =
+// mn / M |v - V| and the refusal |v'| > 10 viT compared in squares, keep
+// the FP32 rounds short.
 template <typename R>
 __device__ __forceinline__ bool ch_collide_round(const StepConsts& c, uint32_t id, R lscale, R v[3], R& t,
-                                                 uint32_t& e, uint32_t& it, unsigned* ncol, unsigned* refused) {
+                                                 uint32_t& e, uint32_t& it, unsigned* ncol, unsigned* refused,
+                                                 R& gfin) {
   const R sig = ch_pick<R>(c.vnT, c.f.vnT);
   const R vn0x = ch_pick<R>(c.vn0[0], c.f.vn0[0]), vn0y = ch_pick<R>(c.vn0[1], c.f.vn0[1]),
           vn0z = ch_pick<R>(c.vn0[2], c.f.vn0[2]);
   const R m1 = ch_pick<R>(c.m1, c.f.m1);
-  const R mi = ch_pick<R>(c.mi, c.f.mi), mn = ch_pick<R>(c.mn, c.f.mn), M = mn + mi;
   const R vix = v[0], viy = v[1], viz = v[2];
   const R wx = vix - vn0x, wy = viy - vn0y, wz = viz - vn0z;
-  const R w = ch_sqrt(wx * wx + wy * wy + wz * wz);
+  const R w = ch_qsqrt(wx * wx + wy * wy + wz * wz);
   const U4 a = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (e << 8) | (1 + 2 * it), c.run, c.seed_lo, c.seed_hi);
   const U4 b = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (e << 8) | (2 + 2 * it), c.run, c.seed_lo, c.seed_hi);
   R nx, ny, nz;
   if (unitR<R>(a.x) * (w + m1) < w) {
     R s1, c1, s2, c2;
-    const R r1 = ch_sqrt(R(-2) * ch_log(unitR<R>(a.y)));
+    const R r1 = ch_qsqrt(R(-2) * ch_log(unitR<R>(a.y)));
     ch_sincos2pi(unitR<R>(a.z), &s1, &c1);
-    const R r2 = ch_sqrt(R(-2) * ch_log(unitR<R>(a.w)));
+    const R r2 = ch_qsqrt(R(-2) * ch_log(unitR<R>(a.w)));
     ch_sincos2pi(unitR<R>(b.x), &s2, &c2);
     nx = sig * (r1 * c1); ny = sig * (r1 * s1); nz = sig * (r2 * c2);
   } else {
-    const R sp = sig * ch_sqrt(R(-2) * ch_log(unitR<R>(a.y) * unitR<R>(a.z)));
+    const R sp = sig * ch_qsqrt(R(-2) * ch_log(unitR<R>(a.y) * unitR<R>(a.z)));
     const R ct = R(2) * unitR<R>(a.w) - R(1);
     R st = R(1) - ct * ct;
-    st = ch_sqrt(st > R(0) ? st : R(0));
+    st = ch_qsqrt(st > R(0) ? st : R(0));
     R sph, cph;
     ch_sincos2pi(unitR<R>(b.x), &sph, &cph);
     nx = sp * st * cph; ny = sp * st * sph; nz = sp * ct;
   }
   const R Vx = vn0x + nx, Vy = vn0y + ny, Vz = vn0z + nz;
-  const R dV = ch_sqrt(nx * nx + ny * ny + nz * nz);
+  const R dV = ch_qsqrt(nx * nx + ny * ny + nz * nz);
   const R rx = vix - Vx, ry = viy - Vy, rz = viz - Vz;
-  const R D = ch_sqrt(rx * rx + ry * ry + rz * rz);
+  const R D = ch_qsqrt(rx * rx + ry * ry + rz * rz);
   const bool accept = unitR<R>(b.y) * (w + dV) < D;
   if (!accept && it + 1 < 64) {
     ++it;
@@ -235,27 +251,27 @@ __device__ __forceinline__ bool ch_collide_round(const StepConsts& c, uint32_t i
     // centre-of-mass scatter (src/particles.c:552-591)
     const R uz = R(2) * unitR<R>(b.z) - R(1);
     const R vrr = D;
-    const R vcx = (vix * mi + Vx * mn) / M, vcy = (viy * mi + Vy * mn) / M, vcz = (viz * mi + Vz * mn) / M;
-    const R ax = vix - vcx, ay = viy - vcy, az = viz - vcz;
-    const R vcr = ch_sqrt(ax * ax + ay * ay + az * az);
+    const R wi = ch_pick<R>(c.mi / (c.mi + c.mn), c.f.wi), wn = ch_pick<R>(c.mn / (c.mi + c.mn), c.f.wn);
+    const R vcx = vix * wi + Vx * wn, vcy = viy * wi + Vy * wn, vcz = viz * wi + Vz * wn;
+    const R vcr = wn * vrr;  // v - v_cm = wn (v - V)
     R up = R(1) - uz * uz;
-    const R uperp = ch_sqrt(up > R(0) ? up : R(0));
+    const R uperp = ch_qsqrt(up > R(0) ? up : R(0));
     R sph, cph;
     ch_sincos2pi(unitR<R>(b.w), &sph, &cph);
     const R ux = uperp * cph, uy = uperp * sph;
-    const R costht = vrr > R(0) ? rz / vrr : R(1);
+    const R costht = vrr > R(0) ? ch_qdiv(rz, vrr) : R(1);
     R st2 = R(1) - costht * costht;
-    const R sintht = ch_sqrt(st2 > R(0) ? st2 : R(0));
+    const R sintht = ch_qsqrt(st2 > R(0) ? st2 : R(0));
     R cosphi = R(1), sinphi = R(0);
     if (vrr * sintht > R(0)) {
-      cosphi = rx / (vrr * sintht);
-      sinphi = ry / (vrr * sintht);
+      const R inv = ch_qdiv(R(1), vrr * sintht);
+      cosphi = rx * inv;
+      sinphi = ry * inv;
     }
     const R ux1 = uz * sintht + ux * costht, uy1 = uy, uz1 = uz * costht - ux * sintht;
     const R ux2 = ux1 * cosphi - uy1 * sinphi, uy2 = ux1 * sinphi + uy1 * cosphi, uz2 = uz1;
     const R vfx = vcx + vcr * ux2, vfy = vcy + vcr * uy2, vfz = vcz + vcr * uz2;
-    const R vfr = ch_sqrt(vfx * vfx + vfy * vfy + vfz * vfz);
-    if (vfr / ch_pick<R>(c.viTr, c.f.viTr) > R(10)) {
+    if (vfx * vfx + vfy * vfy + vfz * vfz > ch_pick<R>(R(100) * c.viTr * c.viTr, c.f.vlim2)) {
       ++*refused;  // src/particles.c:597-606
     } else {
       v[0] = vfx; v[1] = vfy; v[2] = vfz;
@@ -267,12 +283,13 @@ __device__ __forceinline__ bool ch_collide_round(const StepConsts& c, uint32_t i
   // the next event's waiting time
   ++e;
   it = 0;
-  if (e >= CH_MAX_EVENTS) return true;
   const R qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
-  const R lam = lscale * ch_gmean<R>(ch_sqrt(qx * qx + qy * qy + qz * qz), sig);
+  gfin = ch_gmean<R>(ch_qsqrt(qx * qx + qy * qy + qz * qz), sig);
+  if (e >= CH_MAX_EVENTS) return true;
+  const R lam = lscale * gfin;
   if (!(lam > R(0))) return true;
   const U4 r0 = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (e << 8), c.run, c.seed_lo, c.seed_hi);
-  t += -ch_log(unitR<R>(r0.x)) / lam;
+  t += ch_qdiv(-ch_log(unitR<R>(r0.x)), lam);
   return !(t < R(1));
 }
 
