@@ -221,22 +221,29 @@ __device__ __forceinline__ bool ch_collide_round(const StepConsts& c, uint32_t i
   const R w = ch_qsqrt(wx * wx + wy * wy + wz * wz);
   const U4 a = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (e << 8) | (1 + 2 * it), c.run, c.seed_lo, c.seed_hi);
   const U4 b = ch_philox(id, c.step, (CH_PURPOSE_COLLIDE << 24) | (e << 8) | (2 + 2 * it), c.run, c.seed_lo, c.seed_hi);
+  // The two proposals of ch_collide, written so that the lanes of a warp
+  // that take different ones share a radius, one logarithm and the sine /
+  // cosine of b.x (the same draws, the same formulas):
+  //   Maxwellian: r = sig sqrt(-2 ln a.y), (cos, sin)(2 pi a.z) in x, y;
+  //               z = sig sqrt(-2 ln a.w) cos(2 pi b.x);
+  //   speed-weighted: r = sig sqrt(-2 ln(a.y a.z)), polar cosine 2 a.w - 1,
+  //               azimuth 2 pi b.x.
+  const bool maxw = unitR<R>(a.x) * (w + m1) < w;
+  const R ua = unitR<R>(a.y), ub = unitR<R>(a.z);
+  const R r = sig * ch_qsqrt(R(-2) * ch_log(maxw ? ua : ua * ub));
+  R sb, cb;
+  ch_sincos2pi(unitR<R>(b.x), &sb, &cb);
   R nx, ny, nz;
-  if (unitR<R>(a.x) * (w + m1) < w) {
-    R s1, c1, s2, c2;
-    const R r1 = ch_qsqrt(R(-2) * ch_log(unitR<R>(a.y)));
-    ch_sincos2pi(unitR<R>(a.z), &s1, &c1);
-    const R r2 = ch_qsqrt(R(-2) * ch_log(unitR<R>(a.w)));
-    ch_sincos2pi(unitR<R>(b.x), &s2, &c2);
-    nx = sig * (r1 * c1); ny = sig * (r1 * s1); nz = sig * (r2 * c2);
+  if (maxw) {
+    R s1, c1;
+    ch_sincos2pi(ub, &s1, &c1);
+    nx = r * c1; ny = r * s1;
+    nz = sig * ch_qsqrt(R(-2) * ch_log(unitR<R>(a.w))) * cb;
   } else {
-    const R sp = sig * ch_qsqrt(R(-2) * ch_log(unitR<R>(a.y) * unitR<R>(a.z)));
     const R ct = R(2) * unitR<R>(a.w) - R(1);
     R st = R(1) - ct * ct;
     st = ch_qsqrt(st > R(0) ? st : R(0));
-    R sph, cph;
-    ch_sincos2pi(unitR<R>(b.x), &sph, &cph);
-    nx = sp * st * cph; ny = sp * st * sph; nz = sp * ct;
+    nx = r * st * cb; ny = r * st * sb; nz = r * ct;
   }
   const R Vx = vn0x + nx, Vy = vn0y + ny, Vz = vn0z + nz;
   const R dV = ch_qsqrt(nx * nx + ny * ny + nz * nz);
