@@ -411,6 +411,7 @@ static_assert(CH_TILE_QW >= 64 && (CH_TILE_QW & (CH_TILE_QW - 1)) == 0,
 
 #define CH_TILE_K 4            // consecutive slots one thread deposits together
 #define CH_DEP_RW 256          // ring of displaced ions per warp (31 waiting + 128 of a chunk fit)
+#define CH_DEP_SEG 32768u      // ions of a brick deposited between two flushes of its tile
 
 // Shared memory of one CTA of the tiled pass: [push part][header][deposit
 // part].  A pass with the push allocates from the start; a deposit-only pass
@@ -439,8 +440,12 @@ struct TileShared {
   // ---- deposit part
   uint32_t d_ip[8 * CH_DEP_RW];  // per warp: ring of displaced ions (indices into the ion arrays)
   unsigned d_sum[8][32 * 33];    // per warp: lane l's 32 sums in row l (33 words: no bank conflicts)
-  unsigned acc_lo[4][BNODES];    // 64-bit fixed-point sums at the tile scale as
-  int acc_hi[4][BNODES];         // lo + hi * 2^32, carried exactly (order-free)
+  // Fixed-point sums at the tile scale, each value v added as its low 16
+  // bits to acc_lo and as v >> 16 to acc_hi: the sum is acc_hi 2^16 +
+  // acc_lo, exact in any order while a segment of the brick adds fewer than
+  // 2^16 values to a word (CH_DEP_SEG).
+  unsigned acc_lo[4][BNODES];
+  int acc_hi[4][BNODES];
 };
 
 template <int PH>
@@ -462,12 +467,13 @@ __device__ __forceinline__ TileShared& tile_smem_base(unsigned char* smem) {
 // value += v for a 64-bit integer kept as (hi, lo) 32-bit words in shared
 // memory; the carry out of lo is detected from the returned old value, so
 // the final (hi, lo) is the exact 64-bit sum whatever the order of adds.
+// Adds v (|v| < 2^31) to a tile sum: two 32-bit reductions that need no
+// returned value, so no carry round trip; neither word can overflow within
+// a segment of at most CH_DEP_SEG ions (below 2^16 adds of under 2^16 to
+// acc_lo, of under 2^15 in magnitude to acc_hi).
 __device__ __forceinline__ void shared_add64(unsigned* lo, int* hi, long long v) {
-  const unsigned vlo = (unsigned)(unsigned long long)v;
-  const int vhi = (int)(v >> 32);
-  const unsigned old = atomicAdd(lo, vlo);
-  const int carry = (old + vlo < old) ? 1 : 0;
-  if (vhi + carry != 0) atomicAdd(hi, vhi + carry);
+  atomicAdd(lo, (unsigned)(v & 0xFFFF));
+  atomicAdd(hi, (int)(v >> 16));
 }
 
 // One ion's 32 fixed-point contributions added lane by lane to the shared
@@ -520,9 +526,9 @@ __device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, i
 // its registers.
 template <bool SCAT>
 __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepConsts& c, MixParticles P,
-                                                    unsigned long long* __restrict__ acc, uint32_t total, int bi0,
-                                                    int bj0, int bk0, int& bad, MixParticles Q,
-                                                    const uint32_t* __restrict__ dst_starts) {
+                                                    unsigned long long* __restrict__ acc, uint32_t seg0,
+                                                    uint32_t total, int bi0, int bj0, int bk0, int& bad,
+                                                    MixParticles Q, const uint32_t* __restrict__ dst_starts) {
   const GridDesc& g = c.g;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t* ring = sh.d_ip + warp * CH_DEP_RW;
@@ -542,7 +548,7 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
     dh += n;
     __syncwarp();  // the entries are read before later appends reuse them
   };
-  for (uint32_t cb = (uint32_t)warp * 128u; cb < total; cb += (blockDim.x >> 5) * 128u) {
+  for (uint32_t cb = seg0 + (uint32_t)warp * 128u; cb < total; cb += (blockDim.x >> 5) * 128u) {
     const uint32_t s0 = cb + 4u * (uint32_t)lane;
     int r = 0;
 #pragma unroll
@@ -655,6 +661,25 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
     while (dt - dh >= 32u) drain(32u);
   }
   if (dt != dh) drain(dt - dh);
+}
+
+// Adds the brick's tile to the global accumulators (tile sums are at the
+// tile scale, 2^22 density and 2^19 flux, shifted to the accumulator scale
+// 2^s) and, with zero, clears it for the next segment.  Each thread flushes
+// and clears its own entries.
+__device__ __forceinline__ void tile_flush(TileShared& sh, const GridDesc& g, unsigned long long* __restrict__ acc,
+                                           int bi0, int bj0, int bk0, int shift_d, int shift_f, bool zero) {
+  for (int q = threadIdx.x; q < 4 * BNODES; q += blockDim.x) {
+    const int m = q / BNODES, nd = q % BNODES;
+    const long long a = ((long long)sh.acc_hi[m][nd] * 65536 + (long long)sh.acc_lo[m][nd])
+                        << (m == 0 ? shift_d : shift_f);
+    if (zero) { sh.acc_lo[m][nd] = 0u; sh.acc_hi[m][nd] = 0; }
+    if (a != 0) {
+      const int bi = nd % BX, bj = (nd / BX) % BY, bk = nd / (BX * BY);
+      const int gi = ch_wrap(bi0 + bi, g.Nx), gj = ch_wrap(bj0 + bj, g.Ny), gk = ch_wrap(bk0 + bk, g.Nz);
+      atomicAdd(acc + (int64_t)m * g.N + ((int64_t)gk * g.Ny + gj) * g.Nx + gi, (unsigned long long)a);
+    }
+  }
 }
 
 // 16-byte asynchronous copy global -> shared (L2 only), and its group fences.
@@ -824,7 +849,17 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
   // post-step mean relative speeds, which normalise the next step's rates,
   // go to gsum as integers of 2^-20 so that S is exact whatever the ion order.
   float tsum0 = 0.0f;
-  if (PH == PH_DEPOSIT) tile_deposit_direct<SCAT>(sh, c, P, acc, total, bi0, bj0, bk0, bad, Q, dst_starts);
+  if (PH == PH_DEPOSIT) {
+    // segments of at most CH_DEP_SEG ions, the tile flushed between them
+    for (uint32_t seg = 0; seg < total; seg += CH_DEP_SEG) {
+      if (seg > 0) {
+        __syncthreads();
+        tile_flush(sh, g, acc, bi0, bj0, bk0, shift_d, shift_f, true);
+        __syncthreads();
+      }
+      tile_deposit_direct<SCAT>(sh, c, P, acc, seg, min(total, seg + CH_DEP_SEG), bi0, bj0, bk0, bad, Q, dst_starts);
+    }
+  }
   const uint32_t ptotal = total * (PH == PH_DEPOSIT ? 0u : 1u);  // ions the push / move loop visits
   // index of slot idx in the ion arrays (rows of the brick are contiguous)
   auto slot_ip = [&](uint32_t idx) -> uint32_t {
@@ -973,19 +1008,7 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
   vsum[0] += (double)tsum0;
   if (PH & PH_DEPOSIT) {
     __syncthreads();
-    for (int q = threadIdx.x; q < 4 * BNODES; q += blockDim.x) {
-      const int m = q / BNODES, nd = q % BNODES;
-      // tile sums are at the tile scale (2^22 density, 2^19 flux): shift
-      // them to the accumulator scale 2^s
-      const long long a = (long long)(((unsigned long long)(unsigned)sh.acc_hi[m][nd] << 32) |
-                                      (unsigned long long)sh.acc_lo[m][nd])
-                          << (m == 0 ? shift_d : shift_f);
-      if (a != 0) {
-        const int bi = nd % BX, bj = (nd / BX) % BY, bk = nd / (BX * BY);
-        const int gi = ch_wrap(bi0 + bi, g.Nx), gj = ch_wrap(bj0 + bj, g.Ny), gk = ch_wrap(bk0 + bk, g.Nz);
-        atomicAdd(acc + (int64_t)m * g.N + ((int64_t)gk * g.Ny + gj) * g.Nx + gi, (unsigned long long)a);
-      }
-    }
+    tile_flush(sh, g, acc, bi0, bj0, bk0, shift_d, shift_f, false);
   }
 }
 

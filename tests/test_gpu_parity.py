@@ -100,6 +100,20 @@ def test_deposit_mixed_error(chy, po, golden):
     assert rel(nodes, golden["g8_collect1"].reshape(-1, 4)) < 1e-6
 
 
+def test_deposit_mixed_dense_bricks(chy):
+    """200 ions per cell put 51,200 ions in each 16x4x4-cell brick, so the
+    mixed deposit flushes its tile between segments of 32,768 ions: the
+    moments must still match the FP64 form of the same seeded ions."""
+    N, ppc = (16, 16, 16), 200
+    out = []
+    for prec in ("fp64", "mixed"):
+        p = chy.params_for(N, precision=chy.PRECISION[prec], E0=(1.0, 0.0, 0.0), mn=0.0, seed=5)
+        with chy.Hybrid(p) as h:
+            h.load(N[0] * N[1] * N[2] * ppc, chy.loader(amp=(0.2, 0.1, 0.05), phase=(0.3, 1.1, 2.0)))
+            out.append(h.CollectVlasovQuantities())
+    assert rel(out[1], out[0]) < 1e-6
+
+
 # ------------------------------------------------------------------ RHS and operator
 @pytest.mark.parametrize("tag", ["g8", "g15x10x8"])
 @pytest.mark.parametrize("ki,kappa", [(0, (0.0, 0.0, 0.0)), (1, (0.3, -0.2, 1.0))])
