@@ -826,22 +826,26 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
       for (int m = 0; m < 4; ++m) { sh.acc_lo[m][q] = 0u; sh.acc_hi[m][q] = 0; }
     }
   }
-  if (threadIdx.x == 0) {
-    uint32_t tot = 0;
-    int r = 0;
-    for (int tk = k0; tk < k0 + TZ; ++tk)
-      for (int tj = j0; tj < j0 + TY; ++tj, ++r) {
-        sh.pre[r] = tot;
-        if (tk < k1 && tj < j1) {
-          const int64_t cf = ((int64_t)tk * g.Ny + tj) * g.Nx + i0;
-          const uint32_t b = starts[cf], e = starts[cf + (i1 - i0)];
-          sh.rowbeg[r] = b;
-          tot += e - b;
-        } else {
-          sh.rowbeg[r] = 0;
-        }
-      }
-    sh.pre[TY * TZ] = tot;
+  if (threadIdx.x < 32) {  // lane r: row r (tk = k0 + r / TY, tj = j0 + r % TY); pre = scan of the counts
+    static_assert(TY * TZ <= 32, "one lane per row of the brick");
+    const int r = threadIdx.x, tk = k0 + r / TY, tj = j0 + r % TY;
+    uint32_t b = 0, n = 0;
+    if (r < TY * TZ && tk < k1 && tj < j1) {
+      const int64_t cf = ((int64_t)tk * g.Ny + tj) * g.Nx + i0;
+      b = starts[cf];
+      n = starts[cf + (i1 - i0)] - b;
+    }
+    uint32_t x = n;  // inclusive scan over the lanes
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+      if (r >= d) x += y;
+    }
+    if (r < TY * TZ) {
+      sh.rowbeg[r] = b;
+      sh.pre[r] = x - n;
+    }
+    if (r == TY * TZ - 1) sh.pre[TY * TZ] = x;
   }
   __syncthreads();
   const uint32_t total = sh.pre[TY * TZ];
