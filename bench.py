@@ -220,8 +220,10 @@ def run_gpu(args, w, rank, world, dist):
 
 
 def e2e(args, h, w, step):
-    """Per step: host->device copy of the ions (DMSwarm RealVector arrays,
-    pinned), the step, device->host copy of the ions and phi."""
+    """Per step, through ch_step_host: host->device copy of the ions (DMSwarm
+    RealVector arrays, pinned), the step, device->host copy of the ions (it
+    starts when the push has moved them and overlaps the deposit and the
+    potential solve), then phi."""
     m = chy()
     import torch
 
@@ -231,15 +233,11 @@ def e2e(args, h, w, step):
         m.host_register(a)
     K = max(1, min(args.steps, args.e2e_steps))
     try:
-        h.upload(pos, vel)
-        h.step(step, 1)
-        h.download(pos, vel)
+        h.step_host(pos, vel, step, 1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for s in range(K):
-            h.upload(pos, vel)
-            h.step(step + 1 + s, 1)
-            h.download(pos, vel)
+            h.step_host(pos, vel, step + 1 + s, 1)
             phi[:] = h.phi()
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0

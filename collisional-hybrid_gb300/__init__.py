@@ -158,6 +158,7 @@ def lib():
             "ch_collect_moments": [vp, vp, C.POINTER(StepInfo)],
             "ch_compute_potential": [vp, vp, C.POINTER(SolveInfo)],
             "ch_step": [vp, C.c_int64, C.c_int32, C.POINTER(StepInfo)],
+            "ch_step_host": [vp, C.c_int64, C.c_int32, vp, vp, C.POINTER(StepInfo)],
             "ch_set_moments": [vp, vp],
             "ch_get_phi": [vp, vp],
             "ch_set_phi": [vp, vp],
@@ -338,6 +339,18 @@ class Hybrid:
     def step(self, first_step: int, nsteps: int = 1) -> dict:
         info = StepInfo()
         _check(lib().ch_step(self._h, int(first_step), int(nsteps), C.byref(info)))
+        return info.as_dict()
+
+    def step_host(self, pos: np.ndarray, vel: np.ndarray, first_step: int, nsteps: int = 1) -> dict:
+        """Steps with the ions held by the host (ch_step_host): uploads pos /
+        vel (np x 4 FP64, C order), runs the steps and downloads the ions back
+        into them.  Registered arrays (host_register) let the download overlap
+        the last step's deposit and potential solve."""
+        assert pos.shape == vel.shape == (self.np, 4) and pos.dtype == vel.dtype == np.float64
+        assert pos.flags.c_contiguous and vel.flags.c_contiguous
+        info = StepInfo()
+        _check(lib().ch_step_host(self._h, int(first_step), int(nsteps), pos.ctypes.data, vel.ctypes.data,
+                                  C.byref(info)))
         return info.as_dict()
 
     # ---------------------------------------------------------------- grid access

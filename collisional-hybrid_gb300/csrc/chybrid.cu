@@ -98,9 +98,10 @@ struct ch_ctx {
   uint32_t* slot_of_id = nullptr;
   bool slot_map_valid = false;
   // download of registered arrays: conversion chunks on `stream`, their
-  // copies to the host on copy_stream
-  cudaStream_t copy_stream = nullptr;
-  cudaEvent_t copy_ev = nullptr;
+  // downloads: id-order conversion on conv_stream, copies to the host on
+  // copy_stream (chunk_ev[k]: chunk k converted)
+  cudaStream_t copy_stream = nullptr, conv_stream = nullptr;
+  cudaEvent_t chunk_ev[8] = {};
   // state
   double sbar = 0.0;
   double dep_scale = 0.0;
@@ -235,8 +236,10 @@ extern "C" ch_status ch_destroy(ch_ctx* c) {
   c->solver.release();
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
-  if (c->copy_ev) cudaEventDestroy(c->copy_ev);
+  for (cudaEvent_t e : c->chunk_ev)
+    if (e) cudaEventDestroy(e);
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  if (c->conv_stream) cudaStreamDestroy(c->conv_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return CH_OK;
@@ -448,6 +451,49 @@ extern "C" ch_status ch_particles_load(ch_ctx* c, int64_t np, const ch_loader* L
   return after_load(c);
 }
 
+// Registered host arrays, mixed form: the ions of src (the buffers of the
+// current order, or of the order a sort step's deposit has just written),
+// converted chunk by chunk into the staging arrays in id order on
+// conv_stream, each chunk copied out over the host link on copy_stream while
+// the next converts, so the link runs without gaps.  remap rebuilds the
+// id -> slot map from src first (after a sort; the map also lets the next
+// upload keep the order).  The map and the first chunk are converted on
+// c->stream itself, so the link starts at once even when the kernels that
+// follow there (a deposit's persistent CTAs) fill the GPU; the other chunks
+// convert on conv_stream.  Returns without waiting: the caller
+// synchronises copy_stream.
+static ch_status download_enqueue(ch_ctx* c, MixParticles src, bool remap, ch_real_vector* pos,
+                                  ch_real_vector* vel) {
+  if (!c->slot_of_id) {
+    CH_CUDA_OK(cudaMalloc(&c->slot_of_id, sizeof(uint32_t) * c->np));
+    remap = true;
+  }
+  ch_status rs = ensure_staging(c);
+  if (rs) return rs;
+  if (!c->copy_stream) {
+    CH_CUDA_OK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    CH_CUDA_OK(cudaStreamCreateWithFlags(&c->conv_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : c->chunk_ev) CH_CUDA_OK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  if (remap) launch_slot_map(src, c->slot_of_id, c->sms, c->stream);
+  const int64_t chunks = 8, per = ((c->np + chunks - 1) / chunks + 31) / 32 * 32;
+  int k = 0;
+  for (int64_t a = 0; a < c->np; a += per, ++k) {
+    const int64_t b = a + per < c->np ? a + per : c->np;
+    cudaStream_t cs = k == 0 ? c->stream : c->conv_stream;
+    launch_mixed_to_host(c->g, src, c->slot_of_id, c->stage_pos, c->stage_vel, a, b, c->sms, cs);
+    CH_CUDA_OK(cudaEventRecord(c->chunk_ev[k], cs));
+    if (k == 0) CH_CUDA_OK(cudaStreamWaitEvent(c->conv_stream, c->chunk_ev[0], 0));
+    CH_CUDA_OK(cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[k], 0));
+    const size_t off = sizeof(double4_32a) * (size_t)a, len = sizeof(double4_32a) * (size_t)(b - a);
+    CH_CUDA_OK(cudaMemcpyAsync(reinterpret_cast<char*>(pos) + off, reinterpret_cast<char*>(c->stage_pos) + off, len,
+                               cudaMemcpyDeviceToHost, c->copy_stream));
+    CH_CUDA_OK(cudaMemcpyAsync(reinterpret_cast<char*>(vel) + off, reinterpret_cast<char*>(c->stage_vel) + off, len,
+                               cudaMemcpyDeviceToHost, c->copy_stream));
+  }
+  return CH_OK;
+}
+
 extern "C" ch_status ch_particles_download(ch_ctx* c, ch_real_vector* pos, ch_real_vector* vel) {
   if (!c || !pos || !vel) return ch_fail(CH_ERR_ARG, "ch_particles_download: null argument");
   if (c->np == 0) return ch_fail(CH_ERR_STATE, "no ions");
@@ -455,30 +501,8 @@ extern "C" ch_status ch_particles_download(ch_ctx* c, ch_real_vector* pos, ch_re
   void* dp = device_view(pos, bytes, 16);
   void* dv = device_view(vel, bytes, 16);
   if (dp && dv && c->mixed) {
-    // registered host arrays: chunks of ids converted into the staging arrays
-    // in id order while the previous chunk is copied out over the host link,
-    // which then runs without gaps (the slot map also lets the next upload
-    // keep the order)
-    if (!c->slot_of_id) CH_CUDA_OK(cudaMalloc(&c->slot_of_id, sizeof(uint32_t) * c->np));
-    ch_status rs = ensure_staging(c);
+    ch_status rs = download_enqueue(c, c->M, !c->slot_map_valid, pos, vel);
     if (rs) return rs;
-    if (!c->copy_stream) {
-      CH_CUDA_OK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-      CH_CUDA_OK(cudaEventCreateWithFlags(&c->copy_ev, cudaEventDisableTiming));
-    }
-    launch_slot_map(c->M, c->slot_of_id, c->sms, c->stream);
-    const int64_t chunks = 8, per = ((c->np + chunks - 1) / chunks + 31) / 32 * 32;
-    for (int64_t a = 0; a < c->np; a += per) {
-      const int64_t b = a + per < c->np ? a + per : c->np;
-      launch_mixed_to_host(c->g, c->M, c->slot_of_id, c->stage_pos, c->stage_vel, a, b, c->sms, c->stream);
-      CH_CUDA_OK(cudaEventRecord(c->copy_ev, c->stream));
-      CH_CUDA_OK(cudaStreamWaitEvent(c->copy_stream, c->copy_ev, 0));
-      const size_t off = sizeof(double4_32a) * (size_t)a, len = sizeof(double4_32a) * (size_t)(b - a);
-      CH_CUDA_OK(cudaMemcpyAsync(reinterpret_cast<char*>(pos) + off, reinterpret_cast<char*>(c->stage_pos) + off, len,
-                                 cudaMemcpyDeviceToHost, c->copy_stream));
-      CH_CUDA_OK(cudaMemcpyAsync(reinterpret_cast<char*>(vel) + off, reinterpret_cast<char*>(c->stage_vel) + off, len,
-                                 cudaMemcpyDeviceToHost, c->copy_stream));
-    }
     CH_CUDA_OK(cudaStreamSynchronize(c->copy_stream));
     c->slot_map_valid = true;
     return CH_OK;
@@ -664,7 +688,13 @@ static ch_status run_deposit_sort(ch_ctx* c) {
   return CH_OK;
 }
 
-extern "C" ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_step_info* info) {
+// nsteps steps.  With dpos / dvel (registered host arrays, mixed form) the
+// last step also downloads its ions: they are final once the push has moved
+// them, so the download starts then and overlaps the deposit and the
+// potential solve; on a sort step it starts after the deposit, from the new
+// order, so the id -> slot map stays valid for the next upload.
+static ch_status run_steps(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_step_info* info,
+                           ch_real_vector* dpos = nullptr, ch_real_vector* dvel = nullptr) {
   if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
   if (c->np == 0) return ch_fail(CH_ERR_STATE, "no ions");
   if (!c->solved_once) return ch_fail(CH_ERR_STATE, "initial potential not computed");
@@ -673,18 +703,21 @@ extern "C" ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_s
   for (int32_t s = 0; s < nsteps; ++s) {
     memset(&local, 0, sizeof(local));
     const bool sort_due = c->p.sort_period > 0 && c->since_sort + 1 >= c->p.sort_period;
+    const bool download = dpos && s + 1 == nsteps;
     // Two launches: push + collide + move (with the new-cell histogram when
     // a sort is due) at 4 CTAs per SM in a small shared footprint, then the
     // deposit.  The pair is faster than one fused launch, whose shared
     // memory and registers allow only 2 CTAs per SM; the results are the
     // same bit for bit.
     ch_status rc = run_pass(c, PH_PUSH | PH_MOVE, first_step + s, &local, sort_due);
+    if (!rc && download && !sort_due) rc = download_enqueue(c, c->M, !c->slot_map_valid, dpos, dvel);
     // Mixed form, sort due: the push counted every ion's new cell and rank;
     // the scan gives the new order, and the deposit, which reads every ion
     // anyway, also writes it there (the counting sort's scatter).
     const bool fused_sort = sort_due && c->mixed;
     if (!rc && fused_sort) rc = run_deposit_sort(c);
     else if (!rc) rc = run_pass(c, PH_DEPOSIT, 0, nullptr);
+    if (!rc && download && fused_sort) rc = download_enqueue(c, c->MQ, true, dpos, dvel);
     if (rc) return rc;
     rc = finalize_moments(c, &local);
     if (rc) return rc;
@@ -700,8 +733,34 @@ extern "C" ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_s
     }
   }
   CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  if (dpos) {
+    CH_CUDA_OK(cudaStreamSynchronize(c->copy_stream));
+    c->slot_map_valid = true;  // rebuilt from the order the ions now have, or still valid
+  }
   if (info) *info = local;
   return CH_OK;
+}
+
+extern "C" ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_step_info* info) {
+  return run_steps(c, first_step, nsteps, info);
+}
+
+extern "C" ch_status ch_step_host(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_real_vector* pos,
+                                  ch_real_vector* vel, ch_step_info* info) {
+  if (!c || !pos || !vel) return ch_fail(CH_ERR_ARG, "ch_step_host: null argument");
+  if (c->np == 0) return ch_fail(CH_ERR_STATE, "no ions");
+  if (nsteps < 1) return ch_fail(CH_ERR_ARG, "nsteps < 1");
+  ch_status rc = ch_particles_upload(c, pos, vel, c->np);
+  if (rc) return rc;
+  const uint64_t bytes = sizeof(double4_32a) * (uint64_t)c->np;
+  const bool overlap = c->mixed && device_view(pos, bytes, 16) && device_view(vel, bytes, 16);
+  if (!overlap) {
+    rc = run_steps(c, first_step, nsteps, info);
+    return rc ? rc : ch_particles_download(c, pos, vel);
+  }
+  rc = run_steps(c, first_step, nsteps, info, pos, vel);
+  if (rc && c->copy_stream) cudaStreamSynchronize(c->copy_stream);  // no copy left running on failure
+  return rc;
 }
 
 extern "C" ch_status ch_set_moments(ch_ctx* c, const ch_grid_node* in) {

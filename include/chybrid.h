@@ -183,6 +183,15 @@ ch_status ch_compute_potential(ch_ctx* c, double* phi_out, ch_solve_info* info);
 /* The reference time-loop body (src/hybrid.c:101-123) without output,
  * nsteps times, steps numbered first_step, first_step+1, ... */
 ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_step_info* info);
+/* The same steps with the ions held by the host, as DMSwarm keeps them in
+ * the reference's loop (src/hybrid.c:101-123): uploads pos / vel (the ions
+ * last uploaded or downloaded, same count), runs nsteps >= 1 steps and
+ * downloads the ions into pos / vel in id order.  With registered arrays
+ * (ch_host_register) in the mixed form the download of the last step
+ * starts once its push has moved the ions and overlaps its deposit and
+ * potential solve; otherwise it follows the steps. */
+ch_status ch_step_host(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_real_vector* pos,
+                       ch_real_vector* vel, ch_step_info* info);
 
 /* Grid-vector access for hosts and tests (natural order, FP64). */
 ch_status ch_set_moments(ch_ctx* c, const ch_grid_node* host_in);  /* LoadVlasovQuantities, src/fileio.c:6-70 */

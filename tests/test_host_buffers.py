@@ -100,3 +100,44 @@ def test_round_trip_through_registered_arrays_keeps_the_run(chy, extra):
                     chy.host_unregister(vel)
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("extra", [0, 7])
+def test_step_host_equals_upload_step_download(chy, extra):
+    """ch_step_host, whose download overlaps the last step's deposit and
+    potential solve (started after the deposit, from the new order, on a sort
+    step), leaves the host arrays and the device state exactly as upload,
+    ch_step and download do: with plain and registered arrays, one or two
+    steps per call, sort steps (every 3rd) last in a call."""
+    p = chy.params_for((16, 12, 20), precision=chy.PRECISION["mixed"], nui=0.4, sort_period=3)
+    n = 16 * 12 * 20 * 8 + extra
+    outs = []
+    for mode in ("separate", "step_host", "step_host_registered"):
+        with chy.Hybrid(p) as h:
+            h.load(n, chy.loader(amp=(0.05, 0.02, 0.0)))
+            h.CollectVlasovQuantities(copy=False)
+            h.ComputePotential(copy=False)
+            h.step(0, 1)
+            pos, vel = h.download()
+            registered = mode == "step_host_registered"
+            if registered:
+                chy.host_register(pos)
+                chy.host_register(vel)
+            try:
+                s = 1
+                for nsteps in (1, 1, 2, 1, 1):  # the calls starting at steps 2 and 5 end with a sort
+                    if mode == "separate":
+                        h.upload(pos, vel)
+                        h.step(s, nsteps)
+                        h.download(pos, vel)
+                    else:
+                        h.step_host(pos, vel, s, nsteps)
+                    s += nsteps
+                outs.append((pos.copy(), vel.copy(), h.CollectVlasovQuantities(), h.phi()))
+            finally:
+                if registered:
+                    chy.host_unregister(pos)
+                    chy.host_unregister(vel)
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            assert np.array_equal(a, b)
