@@ -32,6 +32,7 @@ RHS = {"constant": 0, "sinusoidal": 1, "full": 2}
 KSP = {"cg": 0, "bcgs": 1}
 PC = {"none": 0, "jacobi": 1, "mg": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
+NN_PROFILE = {"uniform": 0, "gaussian_x": 1}  # CH_NN_*: neutral density n_n(x)
 FAITHFUL = {2: 1 << 2, 3: 1 << 3, 4: 1 << 4, 5: 1 << 5, 6: 1 << 6, 7: 1 << 7, 8: 1 << 8}
 
 _dp = C.POINTER(C.c_double)

@@ -333,6 +333,45 @@ def test_collisions_match_oracle_per_ion(chy, po, golden):
         assert abs(o["info"]["expected"] - o["rinfo"]["expected"]) < 1e-9 * o["rinfo"]["expected"]
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_collisions_with_gaussian_neutral_profile(chy, po, golden, precision):
+    """A neutral density n_n(x) = max(floor, exp(-(x - xc)^2 / (2 sigma^2)))
+    scales each ion's collision rate.  The FP64 form draws the oracle's
+    per-ion events, as with uniform neutrals.  The mixed form, whose rate is
+    evaluated in FP32, matches the oracle's expected event count and its
+    realised count within Poisson noise.  The profile must lower the
+    expected count below that of uniform neutrals."""
+    Lx = float(golden["g8_meta"][3])
+    kw = dict(nui=2.0, ksp_rtol=1e-12, nn_profile=chy.NN_PROFILE["gaussian_x"], nn_center=0.5 * Lx,
+              nn_sigma=Lx / 6.0, nn_floor=0.1)
+    p, q, ions = golden_case(chy, po, golden, "g8", precision=precision, **kw)
+    out, N = run_pair(chy, po, p, q, ions, 3)
+    for s, o in enumerate(out):
+        info, rinfo = o["info"], o["rinfo"]
+        assert info["Nc"] == rinfo["Nc"]
+        if precision == "fp64":
+            rp, rv = o["rions"]
+            dv = np.abs(o["vel"][:, :3] - rv[:, :3]).max(axis=1)
+            bad = (dv > 1e-10 * np.abs(rv).max()).sum()
+            assert bad <= max(1, ions.np // 10000), (s, bad)
+            assert abs(info["collisions"] - rinfo["collisions"]) <= bad
+            assert abs(info["expected"] - rinfo["expected"]) < 1e-9 * rinfo["expected"]
+        else:
+            # step 0 starts from the same ions; later steps from states that
+            # parted where an FP32 and an FP64 test fell on either side
+            tol = 1e-5 if s == 0 else 2e-2
+            assert abs(info["expected"] - rinfo["expected"]) < tol * rinfo["expected"], (s, info, rinfo)
+            assert abs(info["collisions"] - rinfo["collisions"]) < 4 * np.sqrt(rinfo["expected"]) + 2, (s, info,
+                                                                                                    rinfo)
+    p0, _, _ = golden_case(chy, po, golden, "g8", precision=precision, **dict(kw, nn_profile=0))
+    with chy.Hybrid(p0) as h:
+        upload(h, ions)
+        h.CollectVlasovQuantities()
+        h.ComputePotential()
+        uniform = h.step(0, 1)
+    assert out[0]["info"]["expected"] < 0.8 * uniform["expected"]
+
+
 @pytest.mark.parametrize("case", [0, 1])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_collision_statistics_vs_reference(chy, po, golden, case, precision):
