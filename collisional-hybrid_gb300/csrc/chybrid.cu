@@ -387,11 +387,11 @@ static ch_status ensure_staging(ch_ctx* c) {
   return CH_OK;
 }
 
-static void do_sort(ch_ctx* c, bool have_hist = false) {
+static void do_sort(ch_ctx* c) {
   c->slot_map_valid = false;
   prof_begin(c);
   launch_sort(c->mixed, c->g, c->P, c->Q, c->M, c->MQ, c->counts, c->starts, c->cursor, c->keys, c->block_sums,
-              have_hist, c->sms, c->stream);
+              c->sms, c->stream);
   prof_end(c, &c->pr.sort_ms, &c->pr.sort_calls);
   std::swap(c->P, c->Q);
   std::swap(c->M, c->MQ);
@@ -729,7 +729,7 @@ static ch_status run_steps(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_ste
       c->since_sort = 0;
       c->slot_map_valid = false;
     } else if (sort_due) {
-      do_sort(c, c->mixed);
+      do_sort(c);  // FP64 form (the mixed form sorts inside its deposit)
     }
   }
   CH_CUDA_OK(cudaStreamSynchronize(c->stream));

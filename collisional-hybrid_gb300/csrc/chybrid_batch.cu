@@ -501,8 +501,8 @@ static void full_sort(ch_batch* b) {
   drop_graphs(b);
   cudaMemsetAsync(b->counts, 0, sizeof(uint32_t) * b->Ntot, b->stream);
   launch_batch_hist(batch_dev(b), b->M, b->counts, b->sms, b->stream);
-  launch_batch_sort(batch_dev(b), b->Ntot, b->M, b->MQ, b->counts, b->starts, b->cursor, b->block_sums, false,
-                    b->sms, b->stream);
+  launch_batch_sort(batch_dev(b), b->Ntot, b->M, b->MQ, b->counts, b->starts, b->cursor, b->block_sums, b->sms,
+                    b->stream);
   std::swap(b->M, b->MQ);
   b->since_sort = 0;
 }

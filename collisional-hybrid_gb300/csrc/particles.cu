@@ -1283,41 +1283,6 @@ __global__ void k_scatter_mixed(GridDesc g, MixParticles P, MixParticles Q, uint
 }
 
 // Exclusive scan of counts[0..n) into starts[0..n] (three phases).
-// Scatter with the in-cell ranks the pass recorded: no atomics.
-// P and Q are different buffers.  A thread moves 4 ions per iteration (each
-// of the 4 a coalesced slot of its warp) and issues all their loads before
-// any store, so that 4 ions' memory latency overlaps.
-__global__ void k_scatter_ranked(GridDesc g, MixParticles P, MixParticles Q, const uint32_t* __restrict__ starts) {
-  const float4* __restrict__ ppos = P.pos;
-  const float4* __restrict__ pvel = P.vel;
-  const uint32_t* __restrict__ prank = P.rank;
-  float4* __restrict__ qpos = Q.pos;
-  float4* __restrict__ qvel = Q.vel;
-  const int64_t T = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < P.np; i0 += 4 * T) {
-    float4 p[4], v[4];
-    uint32_t rk[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int64_t ip = i0 + u * T;
-      if (ip < P.np) {
-        p[u] = ppos[ip];
-        v[u] = pvel[ip];
-        rk[u] = prank[ip];
-      }
-    }
-    uint32_t dst[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (i0 + u * T < P.np) dst[u] = starts[key_mixed(g, p[u].w)] + rk[u];
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (i0 + u * T < P.np) {
-        qpos[dst[u]] = p[u];
-        qvel[dst[u]] = v[u];
-      }
-  }
-}
 
 __global__ void k_scan_blocks(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint32_t* block_sums,
                               int64_t n) {
@@ -1406,22 +1371,6 @@ __global__ void k_batch_hist(BatchDev B, MixParticles P, uint32_t* counts) {
       key = (uint32_t)R.node_off + key_mixed(R.c.g, P.pos[ip].w);
     }
     agg_inc(counts, key, act);
-  }
-}
-
-__global__ void k_batch_scatter_ranked(BatchDev B, MixParticles P, MixParticles Q,
-                                       const uint32_t* __restrict__ starts) {
-  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
-    const float4 p = P.pos[ip];
-    int lo = 0, hi = B.nruns;  // run of slot ip
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (B.ion_off[mid] <= ip) lo = mid; else hi = mid;
-    }
-    const BatchRunDev& R = B.runs[lo];
-    const uint32_t dst = starts[(uint32_t)R.node_off + key_mixed(R.c.g, p.w)] + P.rank[ip];
-    Q.pos[dst] = p;
-    Q.vel[dst] = P.vel[ip];
   }
 }
 
@@ -1744,22 +1693,19 @@ void launch_deposit_sort(const StepConsts& c, MixParticles M, MixParticles MQ, c
 }
 
 void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, MixParticles M, MixParticles MQ,
-                 uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* keys, uint32_t* block_sums,
-                 bool have_hist, int sms, cudaStream_t s) {
+                 uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* keys, uint32_t* block_sums, int sms,
+                 cudaStream_t s) {
   const int64_t np = mixed ? M.np : P.np;
   const int64_t N = g.N;
   const int nb = grid_for(np, 256, sms, 8);
-  if (!(mixed && have_hist)) {
-    cudaMemsetAsync(counts, 0, sizeof(uint32_t) * N, s);
-    if (mixed) k_hist_mixed<<<nb, 256, 0, s>>>(g, M, counts, keys), ::ch::note_launch();
-    else k_hist_f64<<<nb, 256, 0, s>>>(g, P, counts, keys), ::ch::note_launch();
-  }
+  cudaMemsetAsync(counts, 0, sizeof(uint32_t) * N, s);
+  if (mixed) k_hist_mixed<<<nb, 256, 0, s>>>(g, M, counts, keys), ::ch::note_launch();
+  else k_hist_f64<<<nb, 256, 0, s>>>(g, P, counts, keys), ::ch::note_launch();
   const int nsb = (int)((N + 1023) / 1024);
   k_scan_blocks<<<nsb, 512, 0, s>>>(counts, starts, block_sums, N), ::ch::note_launch();
   k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nsb, starts + N), ::ch::note_launch();
   k_scan_add<<<(int)((N + 255) / 256), 256, 0, s>>>(starts, block_sums, N, cursor), ::ch::note_launch();
-  if (mixed && have_hist && M.rank) k_scatter_ranked<<<nb, 256, 0, s>>>(g, M, MQ, starts), ::ch::note_launch();
-  else if (mixed) k_scatter_mixed<<<nb, 256, 0, s>>>(g, M, MQ, cursor), ::ch::note_launch();
+  if (mixed) k_scatter_mixed<<<nb, 256, 0, s>>>(g, M, MQ, cursor), ::ch::note_launch();
   else k_scatter_f64<<<nb, 256, 0, s>>>(P, Q, keys, cursor), ::ch::note_launch();
 }
 
@@ -1822,16 +1768,12 @@ void launch_batch_finalize(int64_t n4, unsigned long long* acc, double inv_scale
 }
 
 void launch_batch_sort(const BatchDev& B, int64_t Ntot, MixParticles M, MixParticles MQ, uint32_t* counts,
-                       uint32_t* starts, uint32_t* cursor, uint32_t* block_sums, bool ranked, int sms,
-                       cudaStream_t s) {
+                       uint32_t* starts, uint32_t* cursor, uint32_t* block_sums, int sms, cudaStream_t s) {
   const int nsb = (int)((Ntot + 1023) / 1024);
   k_scan_blocks<<<nsb, 512, 0, s>>>(counts, starts, block_sums, Ntot), ::ch::note_launch();
   k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nsb, starts + Ntot), ::ch::note_launch();
   k_scan_add<<<(int)((Ntot + 255) / 256), 256, 0, s>>>(starts, block_sums, Ntot, cursor), ::ch::note_launch();
-  if (ranked && M.rank)
-    k_batch_scatter_ranked<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(B, M, MQ, starts), ::ch::note_launch();
-  else
-    k_batch_scatter<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(B, M, MQ, cursor), ::ch::note_launch();
+  k_batch_scatter<<<grid_for(M.np, 256, sms, 8), 256, 0, s>>>(B, M, MQ, cursor), ::ch::note_launch();
 }
 
 }  // namespace ch

@@ -59,10 +59,7 @@ void launch_reduce_partials(const double* part, int nblocks, int K, double* out,
 int launch_finalize(int64_t N, unsigned long long* acc, double inv_scale, int reset, double* mom, double* part,
                     DevCounters* cnt, int sms, cudaStream_t s);
 // Counting sort by cell: counts (N), starts (N+1), cursor (N), keys (np),
-// block_sums (ceil(N/1024)+1).  Results land in the Q buffers.
-// have_hist: counts already hold the per-cell ion counts and M.rank each
-// ion's rank in its new cell (mixed form, recorded by the preceding pass), so
-// the scatter needs no atomics.
+// block_sums (ceil(N/1024)+1).
 // Exclusive scan of the cell counts into starts (and cursor).
 void launch_scan(int64_t N, const uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* block_sums,
                  cudaStream_t s);
@@ -71,9 +68,12 @@ void launch_scan(int64_t N, const uint32_t* counts, uint32_t* starts, uint32_t* 
 void launch_deposit_sort(const StepConsts& c, MixParticles M, MixParticles MQ, const uint32_t* starts,
                          const uint32_t* dst_starts, unsigned long long* acc, DevCounters* cnt, int sms,
                          cudaStream_t s);
+// Counting sort of P (FP64 form) or M (mixed) into Q / MQ: cell count,
+// scan, scatter with atomic cursors.  The mixed step's own sort is the scan
+// plus launch_deposit_sort, whose push counted the cells and ranks.
 void launch_sort(bool mixed, const GridDesc& g, F64Particles P, F64Particles Q, MixParticles M, MixParticles MQ,
-                 uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* keys, uint32_t* block_sums,
-                 bool have_hist, int sms, cudaStream_t s);
+                 uint32_t* counts, uint32_t* starts, uint32_t* cursor, uint32_t* keys, uint32_t* block_sums, int sms,
+                 cudaStream_t s);
 
 // ------------------------------------------------------------------ ensembles
 // One run of a batch (independent runs of different grids and parameters
@@ -119,10 +119,8 @@ void launch_batch_hist(const BatchDev& B, MixParticles M, uint32_t* counts, int 
 void launch_batch_finalize(int64_t n4, unsigned long long* acc, double inv_scale, double* mom, int* flag, int sms,
                            cudaStream_t s);
 // Counting sort over the batch grid (keys node_off[r] + cell keep the runs
-// contiguous); counts hold the cell counts.  ranked: the preceding pass
-// counted them and stored each ion's in-cell rank in M.rank.
+// contiguous); counts hold the cell counts.
 void launch_batch_sort(const BatchDev& B, int64_t Ntot, MixParticles M, MixParticles MQ, uint32_t* counts,
-                       uint32_t* starts, uint32_t* cursor, uint32_t* block_sums, bool ranked, int sms,
-                       cudaStream_t s);
+                       uint32_t* starts, uint32_t* cursor, uint32_t* block_sums, int sms, cudaStream_t s);
 
 }  // namespace ch
