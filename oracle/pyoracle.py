@@ -132,8 +132,10 @@ CH_FAITHFUL = {2: 1 << 2, 3: 1 << 3, 4: 1 << 4, 5: 1 << 5, 6: 1 << 6, 7: 1 << 7,
 
 
 def default_params(N=(8, 8, 8), L=None, **kw) -> Params:
-    """Normalised-unit defaults (e = kB = 1); BASELINE configuration 0
-    physics unless overridden."""
+    """Normalised-unit defaults (e = kB = 1): unit spacing, Maxwellian ions
+    with vT = 1, Omega_i = 1 along z, E0 = (0.5, 0, 0), nu = 0.1 with
+    equal-mass neutrals (the 32^3 FP64 workload's physics) unless
+    overridden."""
     p = Params()
     p.Nx, p.Ny, p.Nz = N
     L = L if L is not None else tuple(float(n) for n in N)
