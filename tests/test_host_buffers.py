@@ -102,14 +102,15 @@ def test_round_trip_through_registered_arrays_keeps_the_run(chy, extra):
         assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("extra", [0, 7])
-def test_step_host_equals_upload_step_download(chy, extra):
+@pytest.mark.parametrize("precision,extra", [("mixed", 0), ("mixed", 7), ("fp64", 7)])
+def test_step_host_equals_upload_step_download(chy, precision, extra):
     """ch_step_host, whose download overlaps the last step's deposit and
     potential solve (started after the deposit, from the new order, on a sort
     step), leaves the host arrays and the device state exactly as upload,
     ch_step and download do: with plain and registered arrays, one or two
-    steps per call, sort steps (every 3rd) last in a call."""
-    p = chy.params_for((16, 12, 20), precision=chy.PRECISION["mixed"], nui=0.4, sort_period=3)
+    steps per call, sort steps (every 3rd) last in a call.  The FP64 form
+    downloads after the steps."""
+    p = chy.params_for((16, 12, 20), precision=chy.PRECISION[precision], nui=0.4, sort_period=3)
     n = 16 * 12 * 20 * 8 + extra
     outs = []
     for mode in ("separate", "step_host", "step_host_registered"):
@@ -141,3 +142,19 @@ def test_step_host_equals_upload_step_download(chy, extra):
     for o in outs[1:]:
         for a, b in zip(outs[0], o):
             assert np.array_equal(a, b)
+
+
+def test_step_host_rejects_bad_calls(chy):
+    """ch_step_host wants ions on the device (their count sizes the host
+    arrays) and at least one step."""
+    p = chy.params_for((8, 8, 8), precision=chy.PRECISION["mixed"])
+    with chy.Hybrid(p) as h:
+        pos = np.zeros((8, 4))
+        with pytest.raises(chy.HybridError):
+            chy._check(chy.lib().ch_step_host(h._h, 0, 1, pos.ctypes.data, pos.ctypes.data, None))
+        h.load(8 * 8 * 8 * 4, chy.loader())
+        h.CollectVlasovQuantities(copy=False)
+        h.ComputePotential(copy=False)
+        pos, vel = h.download()
+        with pytest.raises(chy.HybridError):
+            h.step_host(pos, vel, 0, 0)
