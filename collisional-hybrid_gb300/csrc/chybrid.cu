@@ -14,6 +14,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <vector>
 #include <thread>
 #include <vector>
 
@@ -109,24 +110,61 @@ struct ch_ctx {
   bool moments_valid = false;
   int64_t since_sort = 0;
   PotentialSolver solver;
-  // profiling
+  // profiling: each phase's pair of events is resolved when the profile is
+  // read or a step returns, so timing adds no host round trip inside a step
+  struct ProfPhase {
+    cudaEvent_t a, b;
+    double *ms, *ms2;
+  };
   bool prof = false;
-  cudaEvent_t ev[2] = {nullptr, nullptr};
+  std::vector<cudaEvent_t> ev_free;
+  std::vector<ProfPhase> ev_pending;
+  cudaEvent_t ev_open = nullptr;
   ch_profile pr{};
 };
 
 // Times [begin, end) of one phase on the context stream when profiling.
-static void prof_begin(ch_ctx* c) {
-  if (c->prof) cudaEventRecord(c->ev[0], c->stream);
+// The events are read later (prof_flush), so the stream keeps running; the
+// call counts are taken at once.
+static cudaEvent_t prof_event(ch_ctx* c) {
+  cudaEvent_t e = nullptr;
+  if (!c->ev_free.empty()) {
+    e = c->ev_free.back();
+    c->ev_free.pop_back();
+  } else if (cudaEventCreate(&e) != cudaSuccess) {
+    e = nullptr;
+  }
+  return e;
 }
-static void prof_end(ch_ctx* c, double* ms, int64_t* calls) {
+// Adds the elapsed times of the recorded phases (waiting for their ends).
+static void prof_flush(ch_ctx* c) {
+  for (const auto& q : c->ev_pending) {
+    float t = 0.0f;
+    if (cudaEventSynchronize(q.b) == cudaSuccess && cudaEventElapsedTime(&t, q.a, q.b) == cudaSuccess) {
+      *q.ms += t;
+      if (q.ms2) *q.ms2 += t;
+    }
+    c->ev_free.push_back(q.a);
+    c->ev_free.push_back(q.b);
+  }
+  c->ev_pending.clear();
+}
+static void prof_begin(ch_ctx* c) {
   if (!c->prof) return;
-  cudaEventRecord(c->ev[1], c->stream);
-  cudaEventSynchronize(c->ev[1]);
-  float t = 0.0f;
-  cudaEventElapsedTime(&t, c->ev[0], c->ev[1]);
-  *ms += t;
+  if (!c->ev_open) c->ev_open = prof_event(c);
+  if (c->ev_open) cudaEventRecord(c->ev_open, c->stream);
+}
+// ms2 / calls2 (nullable): a second tally the phase also counts towards.
+static void prof_end(ch_ctx* c, double* ms, int64_t* calls, double* ms2 = nullptr, int64_t* calls2 = nullptr) {
+  if (!c->prof) return;
   *calls += 1;
+  if (calls2) *calls2 += 1;
+  cudaEvent_t e = c->ev_open ? prof_event(c) : nullptr;
+  if (!e) return;
+  cudaEventRecord(e, c->stream);
+  c->ev_pending.push_back(ch_ctx::ProfPhase{c->ev_open, e, ms, ms2});
+  c->ev_open = nullptr;
+  if (c->ev_pending.size() >= 256) prof_flush(c);  // bounded
 }
 
 extern "C" const char* ch_last_error(void) { return g_err; }
@@ -234,8 +272,9 @@ extern "C" ch_status ch_destroy(ch_ctx* c) {
   if (c->hcnt) cudaFreeHost(c->hcnt);
   if (c->hred) cudaFreeHost(c->hred);
   c->solver.release();
-  for (auto& e : c->ev)
-    if (e) cudaEventDestroy(e);
+  prof_flush(c);
+  for (cudaEvent_t e : c->ev_free) cudaEventDestroy(e);
+  if (c->ev_open) cudaEventDestroy(c->ev_open);
   for (cudaEvent_t e : c->chunk_ev)
     if (e) cudaEventDestroy(e);
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
@@ -541,12 +580,10 @@ static ch_status run_pass(ch_ctx* c, int phases, int64_t step, ch_step_info* inf
   }
   const int nb = launch_pass(c->mixed, phases, k, c->P, c->M, c->E64, c->E32, c->phi, c->acc, (double)Nc, c->sbar,
                              c->cnt, c->part, c->starts, hist, c->sms, c->stream);
-  const double before = c->pr.pass_ms;
-  prof_end(c, &c->pr.pass_ms, &c->pr.pass_calls);
-  if (phases == PH_DEPOSIT && c->prof) {
-    c->pr.deposit_ms += c->pr.pass_ms - before;
-    c->pr.deposit_calls += 1;
-  }
+  if (phases == PH_DEPOSIT)
+    prof_end(c, &c->pr.pass_ms, &c->pr.pass_calls, &c->pr.deposit_ms, &c->pr.deposit_calls);
+  else
+    prof_end(c, &c->pr.pass_ms, &c->pr.pass_calls);
   if (push) {
     launch_reduce_partials(c->part, nb, 2, c->red, c->stream);
     CH_CUDA_OK(cudaMemcpyAsync(c->hred, c->red, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
@@ -679,12 +716,7 @@ static ch_status run_deposit_sort(ch_ctx* c) {
   prof_end(c, &c->pr.sort_ms, &c->pr.sort_calls);
   prof_begin(c);
   launch_deposit_sort(k, c->M, c->MQ, c->starts, c->starts_next, c->acc, c->cnt, c->sms, c->stream);
-  const double before = c->pr.pass_ms;
-  prof_end(c, &c->pr.pass_ms, &c->pr.pass_calls);
-  if (c->prof) {
-    c->pr.deposit_ms += c->pr.pass_ms - before;
-    c->pr.deposit_calls += 1;
-  }
+  prof_end(c, &c->pr.pass_ms, &c->pr.pass_calls, &c->pr.deposit_ms, &c->pr.deposit_calls);
   return CH_OK;
 }
 
@@ -733,6 +765,7 @@ static ch_status run_steps(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_ste
     }
   }
   CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  prof_flush(c);  // the events have completed
   if (dpos) {
     CH_CUDA_OK(cudaStreamSynchronize(c->copy_stream));
     c->slot_map_valid = true;  // rebuilt from the order the ions now have, or still valid
@@ -841,16 +874,14 @@ extern "C" ch_status ch_host_unregister(void* ptr) {
 
 extern "C" ch_status ch_set_profiling(ch_ctx* c, int32_t enable) {
   if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
-  if (enable && !c->ev[0]) {
-    CH_CUDA_OK(cudaEventCreate(&c->ev[0]));
-    CH_CUDA_OK(cudaEventCreate(&c->ev[1]));
-  }
+  if (!enable) prof_flush(c);
   c->prof = enable != 0;
   return CH_OK;
 }
 
 extern "C" ch_status ch_get_profile(ch_ctx* c, ch_profile* out) {
   if (!c || !out) return ch_fail(CH_ERR_ARG, "null argument");
+  prof_flush(c);
   *out = c->pr;
   out->launches = (int64_t)g_launches.load();
   return CH_OK;
@@ -858,6 +889,7 @@ extern "C" ch_status ch_get_profile(ch_ctx* c, ch_profile* out) {
 
 extern "C" ch_status ch_reset_profile(ch_ctx* c) {
   if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
+  prof_flush(c);
   c->pr = ch_profile{};
   return CH_OK;
 }
