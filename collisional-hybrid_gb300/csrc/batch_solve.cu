@@ -331,7 +331,9 @@ __global__ void __launch_bounds__(256) k_batch_solve(const BSolveRun* runs) {
   }
   if (!(rn <= tol * 1.01) && rn > 0.0) flags |= 2;
   if (!isfinite(rn)) flags |= 4;
-  // ---- node field of the next push, premultiplied by (q/m) dt/2
+  // ---- node field of the next push, premultiplied by (q/m) dt/2: one FP64
+  // difference and one product per component (as k_node_efield_mixed)
+  const double esx = -R.tscale / (2.0 * g.dx), esy = -R.tscale / (2.0 * g.dy), esz = -R.tscale / (2.0 * g.dz);
   OWN(ce, N) {
     const int64_t c = ce;
     int i, j, k;
@@ -340,12 +342,10 @@ __global__ void __launch_bounds__(256) k_batch_solve(const BSolveRun* runs) {
     const int jp = j + 1 == g.Ny ? 0 : j + 1, jm = j == 0 ? g.Ny - 1 : j - 1;
     const int kp = k + 1 == g.Nz ? 0 : k + 1, km = k == 0 ? g.Nz - 1 : k - 1;
     const int64_t row = ((int64_t)k * g.Ny + j) * g.Nx;
-    const double ex = -(R.phi[row + ip] - R.phi[row + im]) / (2.0 * g.dx);
-    const double ey = -(R.phi[((int64_t)k * g.Ny + jp) * g.Nx + i] - R.phi[((int64_t)k * g.Ny + jm) * g.Nx + i]) /
-                      (2.0 * g.dy);
-    const double ez = -(R.phi[((int64_t)kp * g.Ny + j) * g.Nx + i] - R.phi[((int64_t)km * g.Ny + j) * g.Nx + i]) /
-                      (2.0 * g.dz);
-    R.E32[c] = make_float4((float)(ex * R.tscale), (float)(ey * R.tscale), (float)(ez * R.tscale), 0.0f);
+    const double dx = R.phi[row + ip] - R.phi[row + im];
+    const double dy = R.phi[((int64_t)k * g.Ny + jp) * g.Nx + i] - R.phi[((int64_t)k * g.Ny + jm) * g.Nx + i];
+    const double dz = R.phi[((int64_t)kp * g.Ny + j) * g.Nx + i] - R.phi[((int64_t)km * g.Ny + j) * g.Nx + i];
+    R.E32[c] = make_float4((float)(dx * esx), (float)(dy * esy), (float)(dz * esz), 0.0f);
   }
   // ---- status (flags gathered from every CTA)
   double fl[1] = {(double)(flags & 1)};

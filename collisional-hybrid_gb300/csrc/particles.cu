@@ -232,7 +232,12 @@ __global__ void k_node_efield_f64(GridDesc g, const double* __restrict__ phi, do
   }
 }
 
-__global__ void k_node_efield_mixed(GridDesc g, float tscale, const double* __restrict__ phi, float4* __restrict__ E) {
+// -grad(phi) at the nodes by central differences, premultiplied by the push
+// scale (q/m) dt/2.  s[d] = -(q/m)(dt/2) / (2 h_d) comes from the host, so a
+// component is one FP64 difference and one product: FP64 division is slow
+// on this part.
+__global__ void k_node_efield_mixed(GridDesc g, double sx, double sy, double sz, const double* __restrict__ phi,
+                                    float4* __restrict__ E) {
   const int64_t N = g.N;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
     int i, j, k;
@@ -241,13 +246,10 @@ __global__ void k_node_efield_mixed(GridDesc g, float tscale, const double* __re
     const int jp = j + 1 == g.Ny ? 0 : j + 1, jm = j == 0 ? g.Ny - 1 : j - 1;
     const int kp = k + 1 == g.Nz ? 0 : k + 1, km = k == 0 ? g.Nz - 1 : k - 1;
     const int64_t row = ((int64_t)k * g.Ny + j) * g.Nx;
-    const double ex = -(phi[row + ip] - phi[row + im]) / (2.0 * g.dx);
-    const double ey =
-        -(phi[((int64_t)k * g.Ny + jp) * g.Nx + i] - phi[((int64_t)k * g.Ny + jm) * g.Nx + i]) / (2.0 * g.dy);
-    const double ez =
-        -(phi[((int64_t)kp * g.Ny + j) * g.Nx + i] - phi[((int64_t)km * g.Ny + j) * g.Nx + i]) / (2.0 * g.dz);
-    // stored premultiplied by the push scale (q/m) dt/2
-    E[c] = make_float4((float)(ex * tscale), (float)(ey * tscale), (float)(ez * tscale), 0.0f);
+    const double dx = phi[row + ip] - phi[row + im];
+    const double dy = phi[((int64_t)k * g.Ny + jp) * g.Nx + i] - phi[((int64_t)k * g.Ny + jm) * g.Nx + i];
+    const double dz = phi[((int64_t)kp * g.Ny + j) * g.Nx + i] - phi[((int64_t)km * g.Ny + j) * g.Nx + i];
+    E[c] = make_float4((float)(dx * sx), (float)(dy * sy), (float)(dz * sz), 0.0f);
   }
 }
 
@@ -1576,7 +1578,10 @@ void launch_aos_out(bool mixed, const GridDesc& g, F64Particles P, MixParticles 
 
 void launch_node_efield(bool mixed, const GridDesc& g, double tscale, const double* phi, double* E64, float4* E32,
                         int sms, cudaStream_t s) {
-  if (mixed) k_node_efield_mixed<<<grid_for(g.N, 256, sms, 8), 256, 0, s>>>(g, (float)tscale, phi, E32), ::ch::note_launch();
+  if (mixed)
+    k_node_efield_mixed<<<grid_for(g.N, 256, sms, 8), 256, 0, s>>>(g, -tscale / (2.0 * g.dx), -tscale / (2.0 * g.dy),
+                                                                   -tscale / (2.0 * g.dz), phi, E32),
+        ::ch::note_launch();
   else k_node_efield_f64<<<grid_for(g.N, 256, sms, 8), 256, 0, s>>>(g, phi, E64), ::ch::note_launch();
 }
 
