@@ -304,6 +304,29 @@ def test_fused_step_equals_separate_calls(chy, po, golden):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_sorting_does_not_change_the_run(chy, precision):
+    """The order of the ions enters no result: deposit sums are integers and
+    every collision draw is keyed by the ion's id.  So a run that sorts after
+    every step (in the mixed form: the scatter inside the step's deposit,
+    through the push's cell counts and ranks) must equal, bit for bit, a run
+    that never sorts: ions by id, moments and phi.  Any ion lost or doubled
+    by a sort would show."""
+    outs = []
+    for period in (1, 0):
+        p = chy.params_for((16, 12, 20), precision=chy.PRECISION[precision], nui=0.5, E0=(1.0, 0.2, 0.0),
+                           sort_period=period)
+        with chy.Hybrid(p) as h:
+            h.load(16 * 12 * 20 * 6 + 5, chy.loader(amp=(0.05, 0.02, 0.01)))
+            h.CollectVlasovQuantities(copy=False)
+            h.ComputePotential(copy=False)
+            h.step(0, 5)
+            pos, vel = h.download()
+            outs.append((pos, vel, h.CollectVlasovQuantities(), h.phi()))
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_deterministic_run_to_run(chy, po, golden, precision):
     p, q, ions = golden_case(chy, po, golden, "g8", precision=precision, sort_period=1)
     res = []
