@@ -12,6 +12,10 @@ prints one JSON line.
     --mode solve: --steps steps of the plasma of the pass mode; the solves
         inside them (warm start from the previous step's potential) are the
         ones a run makes; prints the solve time, iterations and refinements.
+    --mode e2e: the ions through registered host arrays every step, --steps
+        times: upload, ch_step and download as separate calls (wall time of
+        each, synchronised), then ch_step_host (the download overlapping the
+        deposit and solve).
 
     python collisional-hybrid_gb300/profile_pass.py --grid 128 --ppc 64 --nu 0.5
 """
@@ -34,7 +38,7 @@ def main(argv=None):
     ap.add_argument("--sort-period", type=int, default=4)
     ap.add_argument("--warm", type=int, default=3)
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
-    ap.add_argument("--mode", choices=["pass", "ensemble", "adjoint", "solve"], default="pass")
+    ap.add_argument("--mode", choices=["pass", "ensemble", "adjoint", "solve", "e2e"], default="pass")
     ap.add_argument("--runs", type=int, default=8)
     ap.add_argument("--steps", type=int, default=4)
     a = ap.parse_args(argv)
@@ -45,6 +49,8 @@ def main(argv=None):
         return adjoint(m, a)
     if a.mode == "solve":
         return solve(m, a)
+    if a.mode == "e2e":
+        return e2e(m, a)
     N = a.grid
     p = m.params_for((N, N, N), precision=m.PRECISION[a.precision], E0=(a.Ex, 0.0, 0.0), nui=a.nu, ksp_rtol=1e-10,
                      pc_type=m.PC["mg"], sort_period=a.sort_period, mn=(1.0 if a.nu > 0 else 0.0))
@@ -79,6 +85,54 @@ def solve(m, a):
             info = h.step(s, 1)
             rows.append([round(h.profile()["solve_ms"], 3), info["iterations"], info["refinements"]])
         print(json.dumps({"mode": "solve", "grid": N, "ppc": a.ppc, "steps[solve_ms, iterations, refinements]": rows}))
+
+
+def e2e(m, a):
+    import time
+
+    import torch
+
+    N = a.grid
+    p = m.params_for((N, N, N), precision=m.PRECISION[a.precision], E0=(a.Ex, 0.0, 0.0), nui=a.nu, ksp_rtol=1e-10,
+                     pc_type=m.PC["mg"], sort_period=a.sort_period, mn=(1.0 if a.nu > 0 else 0.0))
+    out = {"mode": "e2e", "grid": N, "ppc": a.ppc}
+    with m.Hybrid(p) as h:
+        h.load(N ** 3 * a.ppc, m.loader(amp=(0.02, 0.02, 0.02), phase=tuple(m.mode_phases(1))))
+        h.CollectVlasovQuantities(copy=False)
+        h.ComputePotential(copy=False)
+        for s in range(a.warm):
+            h.step(s, 1)
+        pos, vel = h.download()
+        out["bytes_each_way"] = int(pos.nbytes + vel.nbytes)
+        for x in (pos, vel):
+            m.host_register(x)
+        try:
+            step = a.warm
+            h.upload(pos, vel)
+            h.step(step, 1)
+            h.download(pos, vel)
+            step += 1
+            rows = []
+            for _ in range(a.steps):
+                t = [time.perf_counter()]
+                h.upload(pos, vel); torch.cuda.synchronize(); t.append(time.perf_counter())
+                h.step(step, 1); torch.cuda.synchronize(); t.append(time.perf_counter())
+                h.download(pos, vel); torch.cuda.synchronize(); t.append(time.perf_counter())
+                step += 1
+                rows.append([round(1e3 * (t[i + 1] - t[i]), 2) for i in range(3)])
+            out["separate[upload_ms, step_ms, download_ms]"] = rows
+            host = []
+            for _ in range(a.steps):
+                t0 = time.perf_counter()
+                h.step_host(pos, vel, step, 1)
+                torch.cuda.synchronize()
+                host.append(round(1e3 * (time.perf_counter() - t0), 2))
+                step += 1
+            out["step_host_ms"] = host
+        finally:
+            for x in (pos, vel):
+                m.host_unregister(x)
+    print(json.dumps(out))
 
 
 def ensemble(m, a):
