@@ -238,24 +238,30 @@ ch_status ch_output_wait(ch_ctx* c, int64_t* written);
 
 /* CollectVlasovQuantities for callers that cannot allocate device memory
  * (no counterpart in the reference).  Hosts whose device memory belongs to
- * their own pool allocator, code that records its launches into a CUDA graph
- * (cudaMalloc is not allowed while a stream is being captured), and
- * time-critical loops that cannot absorb the device-wide synchronisation of
- * cudaMalloc/cudaFree cannot create a ch_ctx; this call needs none.  It
- * allocates nothing: the caller passes device pointers to the ions (FP64 SoA
- * positions and velocities, np of each) and to the output `moments`
- * (4 * Nx*Ny*Nz doubles: n, then Gx, Gy, Gz, each in DMDA natural order),
- * and the deposit's fixed-point scratch lives in a static device array of
- * 4 * 2^18 * 8 bytes = 8 MiB, so grids of at most 2^18 nodes (64^3) are
- * accepted; larger grids return CH_ERR_ARG.  Every GPU that loads the
- * library holds that array until the process exits.  The work is queued on
- * `stream` (a cudaStream_t; NULL = the legacy default stream) and the call
- * returns without waiting.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress), so make that first call before any
- * stream capture.  All calls share the one array, and each call clears it
- * before depositing: calls that may overlap on the GPU (different streams,
- * or different host threads) race and must be serialised by the caller.
- * Results equal ch_collect_moments (same fixed-point sums). */
+ * their own pool allocator (a framework that reserves the GPU's memory up
+ * front and hands out sub-blocks) and time-critical loops that cannot absorb
+ * the device-wide synchronisation of cudaMalloc/cudaFree cannot create a
+ * ch_ctx; this call needs none.  It allocates nothing: the caller passes
+ * device pointers to the ions (FP64 SoA positions and velocities, np of
+ * each) and to the output `moments` (4 * Nx*Ny*Nz doubles: n, then Gx, Gy,
+ * Gz, each in DMDA natural order), and the deposit's fixed-point scratch
+ * lives in a static device array of 4 * 2^18 * 8 bytes = 8 MiB, so grids of
+ * at most 2^18 nodes (64^3) are accepted; larger grids return CH_ERR_ARG.
+ * Every GPU that loads the library holds that array until the process
+ * exits.  The work is queued on `stream` (a cudaStream_t; NULL = the legacy
+ * default stream) and the call returns without waiting.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) in that
+ * device's primary context, so make that first call before any stream
+ * capture; callers on a non-primary driver context, or that reset the device
+ * between calls, are not supported.  All calls share the one array, and each
+ * call clears it before depositing: calls that may overlap on the GPU
+ * (different streams, or different host threads) race and must be
+ * serialised by the caller.  For finite ions the moments equal those of
+ * ch_collect_moments in the FP64 form bit for bit (same fixed-point sums).
+ * An ion with a non-finite position or velocity, or one so far out that no
+ * cell index or fixed-point contribution fits, or a density sum beyond the
+ * fixed-point range, makes every output value NaN: the asynchronous form of
+ * the CH_ERR_NAN / CH_ERR_RANGE that ch_collect_moments returns. */
 ch_status ch_collect_moments_noalloc(const ch_params* p, const double* x, const double* y, const double* z,
                                      const double* vx, const double* vy, const double* vz, int64_t np,
                                      double* moments, void* stream);

@@ -78,3 +78,38 @@ def test_batch_rejects_unsupported_runs_before_touching_the_device(chy):
     rc = chy.lib().ch_batch_create(C.cast(arr, C.c_void_p), C.cast((C.c_int64 * 1)(0), C.c_void_p), 1, -1,
                                    C.byref(C.c_void_p()))
     assert rc == -1 and b"no ions" in chy.lib().ch_last_error()
+
+
+def test_noalloc_deposit_rejects_bad_arguments_before_touching_the_device(chy):
+    """ch_collect_moments_noalloc checks every argument on the host before its
+    first CUDA call: an axis so long that the node count would wrap int64
+    (2^22 per axis), a grid beyond its static scratch, a deposit scale outside
+    the FP64 form's [1, 62], an empty domain, np < 0 and null pointers."""
+    f = chy.lib().ch_collect_moments_noalloc
+    f.argtypes = [C.c_void_p] + [C.c_void_p] * 6 + [C.c_int64, C.c_void_p, C.c_void_p]
+    f.restype = C.c_int32
+    fake = C.c_void_p(256)  # never dereferenced: every case fails its checks first
+    ions = [fake] * 6
+
+    def call(p, np_=10, out=fake, ptrs=ions):
+        return f(C.byref(p), *ptrs, np_, out, None)
+
+    cases = []
+    p = chy.params_for((8, 8, 8))
+    p.Nx = p.Ny = p.Nz = 1 << 22  # 2^66 nodes: wraps to 0 in int64
+    cases.append((p, {}, b"exceeds the scratch"))
+    cases.append((chy.params_for((128, 64, 64)), {}, b"at most 262144 nodes"))
+    cases.append((chy.params_for((1 << 19, 3, 3)), {}, b"exceeds the scratch"))
+    for s in (0.5, 63.0, -1.0, float("nan")):
+        cases.append((chy.params_for((8, 8, 8), deposit_scale_log2=s), {}, b"deposit_scale_log2"))
+    p = chy.params_for((8, 8, 8))
+    p.x1 = p.x0
+    cases.append((p, {}, b"empty"))
+    cases.append((chy.params_for((2, 8, 8)), {}, b"at least 3"))
+    cases.append((chy.params_for((8, 8, 8)), dict(np_=-1), b"np < 0"))
+    cases.append((chy.params_for((8, 8, 8)), dict(out=None), b"null"))
+    cases.append((chy.params_for((8, 8, 8)), dict(ptrs=[fake] * 5 + [None]), b"null"))
+    for p, kw, msg in cases:
+        rc = call(p, **kw)
+        assert rc == -1, (msg, rc)
+        assert msg in chy.lib().ch_last_error(), (msg, chy.lib().ch_last_error())
