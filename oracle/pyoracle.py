@@ -15,6 +15,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 REFLIB = os.path.join(HERE, "_ref", "libref.so")
+# Where the reference's sources lie (the same REF variable as oracle/Makefile);
+# only the recipe that compiles them and the tests that read its headers use it.
+REF = os.environ.get("REF", "/root/reference")
+REF_SRC = os.path.join(REF, "src")
 
 _dp = C.POINTER(C.c_double)
 
@@ -62,8 +66,8 @@ class State(C.Structure):
 
 def build(ref: bool = False) -> None:
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True, stdout=subprocess.DEVNULL)
-    if ref and os.path.isdir("/root/reference/src"):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True, stdout=subprocess.DEVNULL)
+    if ref and os.path.isdir(REF_SRC):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF}"], check=True, stdout=subprocess.DEVNULL)
 
 
 _lib = None

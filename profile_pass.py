@@ -17,7 +17,7 @@ prints one JSON line.
         each, synchronised), then ch_step_host (the download overlapping the
         deposit and solve).
 
-    python collisional-hybrid_gb300/profile_pass.py --grid 128 --ppc 64 --nu 0.5
+    python profile_pass.py --grid 128 --ppc 64 --nu 0.5
 """
 import argparse
 import importlib
@@ -26,7 +26,7 @@ import os
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.dirname(HERE))
+sys.path.insert(0, HERE)
 
 
 def main(argv=None):

@@ -9,6 +9,7 @@ import tempfile
 import pytest
 
 from conftest import REPO
+from oracle.pyoracle import REF_SRC
 
 HOST = os.path.join(REPO, "collisional-hybrid_gb300", "host")
 PKG = os.path.join(REPO, "collisional-hybrid_gb300")
@@ -78,11 +79,11 @@ def test_rejects_unsupported_options(optlib, chy):
     assert rc == -1
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/src"), reason="reference headers not present")
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference headers not present")
 def test_petsc_dropin_compiles_against_reference_headers():
     with tempfile.TemporaryDirectory() as d:
         r = subprocess.run(["gcc", "-std=gnu11", "-Wall", "-Werror", "-Wno-unused-function", "-DCH_WITH_PETSC",
-                            "-I", os.path.join(REPO, "oracle", "ref", "shim"), "-I", "/root/reference/src",
+                            "-I", os.path.join(REPO, "oracle", "ref", "shim"), "-I", REF_SRC,
                             "-I", os.path.join(REPO, "include"), "-c", os.path.join(HOST, "petsc_dropin.c"),
                             "-o", os.path.join(d, "dropin.o")], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
