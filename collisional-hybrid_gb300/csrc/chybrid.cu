@@ -329,7 +329,12 @@ extern "C" ch_status ch_create(const ch_params* p, int32_t device, ch_ctx** out)
   rc = c->solver.init(*p, c->g, c->sms);
   if (rc) { ch_destroy(c); return rc; }
   // fixed-point deposit scale 2^s
-  c->dep_scale = ldexp(1.0, (int)(p->deposit_scale_log2 > 0.0 ? p->deposit_scale_log2 : 40.0));
+  // default fixed-point scale: 2^-48 per unit weight keeps the FP64 form's
+  // moments within 1e-15 of an FP64 sum (2^40 left 5e-13, which the RHS
+  // differences lift to 1.5e-12 in phi) while a node still holds 8192 ion
+  // weights and |sum v w| up to 32768; the mixed form's tiles flush at 2^40
+  const double s_default = p->precision == CH_MIXED ? 40.0 : 48.0;
+  c->dep_scale = ldexp(1.0, (int)(p->deposit_scale_log2 > 0.0 ? p->deposit_scale_log2 : s_default));
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) { ch_destroy(c); return ch_cuda_fail(e, "ch_create", __FILE__, __LINE__); }
   *out = c;

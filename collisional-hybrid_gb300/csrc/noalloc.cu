@@ -148,7 +148,7 @@ extern "C" ch_status ch_collect_moments_noalloc(const ch_params* p, const double
   g.x0 = p->x0; g.y0 = p->y0; g.z0 = p->z0;
   g.Lx = p->x1 - p->x0; g.Ly = p->y1 - p->y0; g.Lz = p->z1 - p->z0;
   g.dx = g.Lx / p->Nx; g.dy = g.Ly / p->Ny; g.dz = g.Lz / p->Nz;
-  const int s2 = (int)(p->deposit_scale_log2 > 0.0 ? p->deposit_scale_log2 : 40.0);
+  const int s2 = (int)(p->deposit_scale_log2 > 0.0 ? p->deposit_scale_log2 : 48.0);  // the FP64 form's default
   const double scale = ldexp(1.0, s2);
   // |v| w 2^s < 2^62 for every weight w <= 1
   const double vmax = ldexp(1.0, 62 - s2);

@@ -112,7 +112,8 @@ typedef struct ch_params {
   uint32_t faithful;         /* CH_FAITHFUL_* bits                            */
   int32_t push_E0;           /* -ch_push_E0: add E0 to the ion push           */
   int32_t sort_period;       /* steps between counting sorts (0 = never)      */
-  double deposit_scale_log2; /* fixed-point deposit scale 2^s (0 = default)   */
+  double deposit_scale_log2; /* fixed-point deposit scale 2^s (0 = default:  
+                                2^48 in the FP64 form, 2^40 in the mixed form) */
 } ch_params;
 
 /* Fills *p with the reference defaults (src/parameters.c:28-562) in
@@ -257,7 +258,8 @@ ch_status ch_output_wait(ch_ctx* c, int64_t* written);
  * call clears it before depositing: calls that may overlap on the GPU
  * (different streams, or different host threads) race and must be
  * serialised by the caller.  For finite ions the moments equal those of
- * ch_collect_moments in the FP64 form bit for bit (same fixed-point sums).
+ * ch_collect_moments in the FP64 form bit for bit (same fixed-point sums,
+ * default scale 2^48).
  * An ion with a non-finite position or velocity, or one so far out that no
  * cell index or fixed-point contribution fits, or a density sum beyond the
  * fixed-point range, makes every output value NaN: the asynchronous form of

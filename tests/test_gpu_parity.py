@@ -1,14 +1,21 @@
 """Parity of the CUDA path (through the C ABI) with the CPU oracle and with
 the reference's own outputs.  Tolerances are stated per check:
 
-* FP64 plain form, collisionless: 1e-12 relative (norm-wise, max over
-  entries / max magnitude) for positions, velocities, moments, RHS, A x.
-* potential: zero-mean phi within 1e-11 relative after both solve to rtol
-  1e-14 (the difference is bounded by cond(A) x rtol).
+* FP64 plain form, collisionless: 1e-12 relative (max over entries / max
+  magnitude) for positions, velocities, moments, RHS, A x and the zero-mean
+  potential, both sides solving to rtol 1e-14, per step and across 20 steps
+  of the 32^3 x 16 ions/cell plasma.  Measured: solves agree to <= 1e-13,
+  steps to <= 2e-13.
 * collisions: identical Philox streams, so per-ion results agree to 1e-12
   except for ions whose draw lies within rounding of the threshold; counts
   and velocity moments against the reference within 4 standard errors.
-* mixed form: errors against the FP64 oracle stated per output below.
+* mixed form against the FP64 oracle: potential <= 1e-6 relative (measured
+  2e-7 to 5e-7, rtol 1e-10 solves), including the 256 x 256 x 64 anisotropic
+  grid; moments <= 3e-6 (the fixed-point quanta of the tile deposit are
+  2^-22 per unit weight and 2^-19 per unit flux); velocities <= 1e-6;
+  positions <= 5e-7 cells per step.  With collisions the forms part where an
+  FP32 and an FP64 collision test fall on either side of a threshold, so
+  velocity moments are held to 4 standard errors over 4 seeds.
 """
 import numpy as np
 import pytest
@@ -47,6 +54,22 @@ def golden_case(chy, po, golden, tag, **kw):
 def upload(h, ions):
     pos, vel = ions.aos()
     h.upload(pos, vel)
+
+
+class oracle_threads:
+    """All host cores for the oracle inside a block (its large cases)."""
+
+    def __init__(self, po):
+        self.lib = po.lib()
+
+    def __enter__(self):
+        import os
+
+        self.old = self.lib.orc_get_threads()
+        self.lib.orc_set_threads(os.cpu_count() or 1)
+
+    def __exit__(self, *a):
+        self.lib.orc_set_threads(self.old)
 
 
 # ------------------------------------------------------------------ loader
@@ -159,19 +182,20 @@ def test_operator_matches_reference(chy, po, golden, tag, ki, kappa, lt):
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("pc", ["jacobi", "mg"])
 def test_solve_matches_oracle(chy, po, golden, ksp, kappa, precision, pc):
-    p, q, _ = golden_case(chy, po, golden, "g8", kappa_e=kappa, ksp_type=chy.KSP[ksp], ksp_rtol=1e-12,
+    p, q, _ = golden_case(chy, po, golden, "g8", kappa_e=kappa, ksp_type=chy.KSP[ksp], ksp_rtol=1e-14,
                           precision=precision, pc_type=chy.PC[pc])
     nodes = golden["g8_collect1"]
     with chy.Hybrid(p) as h:
         h.set_moments(nodes)
         phi = h.ComputePotential()
         info = h.last_solve
-    assert info["rnorm"] <= 1e-12 * info["bnorm"] * 1.01
+    assert info["rnorm"] <= 1e-14 * info["bnorm"] * 1.01
     b = po.rhs(q, nodes)
     ref, rinfo = po.solve(q, nodes[0::4], b, rtol=1e-14, maxit=20000)
     assert rinfo["rc"] == 0
     assert abs(phi.mean()) < 1e-12 * np.abs(phi).max()
-    assert rel(phi, ref) < 1e-9
+    # both residuals <= 1e-14 |b|: the solutions differ by <= cond(A) 2e-14
+    assert rel(phi, ref) < 1e-12, rel(phi, ref)
 
 
 @pytest.mark.parametrize("N", [(32, 32, 32), (48, 16, 24), (64, 64, 8)])
@@ -179,7 +203,7 @@ def test_solve_matches_oracle(chy, po, golden, ksp, kappa, precision, pc):
 def test_multigrid_solve_on_larger_grids(chy, po, N, precision):
     """MG-preconditioned CG against the oracle's Jacobi-CG on grids with
     full and semi coarsening; the preconditioner must cut the iterations."""
-    p, q = make(chy, po, N, precision=precision, ksp_rtol=1e-10, pc_type=chy.PC["mg"])
+    p, q = make(chy, po, N, precision=precision, ksp_rtol=1e-14, pc_type=chy.PC["mg"])
     ions = po.load(q, po.make_loader(amp=(0.05, 0.03, 0.02), phase=(0.1, 0.7, 2.0)), int(np.prod(N)) * 4)
     nodes = po.collect(q, ions)
     with chy.Hybrid(p) as h:
@@ -191,10 +215,13 @@ def test_multigrid_solve_on_larger_grids(chy, po, N, precision):
         h.set_moments(nodes)
         h.ComputePotential()
         jac_info = h.last_solve
-    assert mg_info["rnorm"] <= 1e-10 * mg_info["bnorm"] * 1.01
+    assert mg_info["rnorm"] <= 1e-14 * mg_info["bnorm"] * 1.01
     assert mg_info["iterations"] * 3 < jac_info["iterations"], (mg_info, jac_info)
-    ref, rinfo = po.solve(q, nodes[0::4], po.rhs(q, nodes), rtol=1e-12, maxit=50000)
-    assert rel(phi, ref) < 1e-7
+    with oracle_threads(po):
+        ref, rinfo = po.solve(q, nodes[0::4], po.rhs(q, nodes), rtol=1e-14, maxit=100000)
+    assert rinfo["rc"] == 0
+    # measured <= 9e-14 on these grids
+    assert rel(phi, ref) < 1e-12, rel(phi, ref)
 
 
 # ------------------------------------------------------------------ push and move
@@ -258,7 +285,10 @@ def test_download_returns_upload_order(chy, po, golden):
 
 
 # ------------------------------------------------------------------ whole steps
-def run_pair(chy, po, p, q, ions, nsteps, fused=True):
+def run_pair(chy, po, p, q, ions, nsteps, fused=True, moments=False, initial=None):
+    """The GPU run and the oracle's run from the same ions, step by step.
+    moments=True also reads the moments each step deposited; `initial`
+    (a dict, optional) receives the moments and phi before the first step."""
     N = p.Nx * p.Ny * p.Nz
     out = []
     ref = po.Run(q, ions.copy())
@@ -266,8 +296,10 @@ def run_pair(chy, po, p, q, ions, nsteps, fused=True):
     assert rc == 0
     with chy.Hybrid(p) as h:
         upload(h, ions)
-        h.CollectVlasovQuantities()
+        m0 = h.CollectVlasovQuantities()
         h.ComputePotential()
+        if initial is not None:
+            initial.update(mom=m0, phi=h.phi(), rnodes=ref.nodes.copy(), rphi=ref.phi.copy())
         for s in range(nsteps):
             if fused:
                 info = h.step(s, 1)
@@ -280,18 +312,44 @@ def run_pair(chy, po, p, q, ions, nsteps, fused=True):
             assert rc == 0
             pos, vel = h.download()
             out.append(dict(phi=h.phi(), pos=pos, vel=vel, info=info, rinfo=rinfo, rphi=ref.phi.copy(),
-                            rnodes=ref.nodes.copy(), rions=ref.ions.aos()))
+                            rnodes=ref.nodes.copy(), rions=ref.ions.aos(),
+                            mom=h.CollectVlasovQuantities() if moments else None))
     return out, N
 
 
 def test_steps_collisionless_fp64(chy, po, golden):
-    p, q, ions = golden_case(chy, po, golden, "g8", mn=0.0, ksp_rtol=1e-13)
-    out, N = run_pair(chy, po, p, q, ions, 4)
+    p, q, ions = golden_case(chy, po, golden, "g8", mn=0.0, ksp_rtol=1e-14)
+    out, N = run_pair(chy, po, p, q, ions, 4, moments=True)
     for s, o in enumerate(out):
         rp, rv = o["rions"]
         assert rel(o["pos"][:, :3], rp[:, :3]) < 1e-12, s
         assert rel(o["vel"][:, :3], rv[:, :3]) < 1e-12, s
-        assert rel(o["phi"], o["rphi"]) < 1e-8, s
+        assert rel(o["mom"], o["rnodes"].reshape(-1, 4)) < 1e-12, s
+        assert rel(o["phi"], o["rphi"]) < 1e-12, (s, rel(o["phi"], o["rphi"]))
+
+
+def test_config0_plasma_collisionless_fp64_for_20_steps(chy, po):
+    """The FP64 form on the 32^3 plasma of 16 ions/cell (524,288 ions; E0 =
+    (0.5, 0, 0), B along z, density 1 + 0.01 sin(2 pi x/Lx), seed 1), with
+    collisions off, against the oracle's run from the same ions for 20
+    steps: positions, velocities, moments and phi within 1e-12 at every
+    step, both solving to rtol 1e-14 (measured: phi <= 2e-13, positions and
+    velocities <= 2e-14)."""
+    p, q = make(chy, po, (32, 32, 32), E0=(0.5, 0.0, 0.0), mn=0.0, ksp_rtol=1e-14, pc_type=chy.PC["mg"],
+                seed=1)
+    ions = po.load(q, po.make_loader(amp=(0.01, 0.0, 0.0)), 32 ** 3 * 16)
+    first = {}
+    with oracle_threads(po):
+        out, N = run_pair(chy, po, p, q, ions, 20, moments=True, initial=first)
+    assert rel(first["mom"], first["rnodes"].reshape(-1, 4)) < 1e-12
+    assert rel(first["phi"], first["rphi"]) < 1e-12
+    for s, o in enumerate(out):
+        rp, rv = o["rions"]
+        assert o["info"]["rnorm"] <= 1e-14 * o["info"]["bnorm"] * 1.01, s
+        assert rel(o["pos"][:, :3], rp[:, :3]) < 1e-12, s
+        assert rel(o["vel"][:, :3], rv[:, :3]) < 1e-12, s
+        assert rel(o["mom"], o["rnodes"].reshape(-1, 4)) < 1e-12, s
+        assert rel(o["phi"], o["rphi"]) < 1e-12, (s, rel(o["phi"], o["rphi"]))
 
 
 def test_fused_step_equals_separate_calls(chy, po, golden):
@@ -447,13 +505,102 @@ def test_mixed_form_error_vs_fp64_oracle(chy, po, golden, rtol):
     """Mixed form (FP32 ions and inner solves, FP64 refinement and sums)
     against the FP64 oracle, 4 collisionless steps: stated errors."""
     p, q, ions = golden_case(chy, po, golden, "g8", precision="mixed", mn=0.0, ksp_rtol=rtol)
-    out, N = run_pair(chy, po, p, q, ions, 4)
+    out, N = run_pair(chy, po, p, q, ions, 4, moments=True)
     for s, o in enumerate(out):
         rp, rv = o["rions"]
-        assert np.abs(o["pos"][:, :3] - rp[:, :3]).max() < 1e-5 * (s + 1)
-        assert rel(o["vel"][:, :3], rv[:, :3]) < 1e-5 * (s + 1)
-        assert rel(o["phi"], o["rphi"]) < 1e-4
+        assert np.abs(o["pos"][:, :3] - rp[:, :3]).max() < 5e-7 * (s + 1)
+        assert rel(o["vel"][:, :3], rv[:, :3]) < 1e-6
+        assert rel(o["mom"], o["rnodes"].reshape(-1, 4)) < 3e-6
+        assert rel(o["phi"], o["rphi"]) < 1e-6, (s, rel(o["phi"], o["rphi"]))
         assert o["info"]["rnorm"] <= rtol * o["info"]["bnorm"] * 1.01
+
+
+def test_mixed_form_on_the_production_plasma_shape(chy, po):
+    """The production plasma's shape at 32^3 x 16 ions/cell: E_x = 1, three
+    random-phase density modes of amplitude 0.02, rtol 1e-10, collisions off;
+    the mixed form against the FP64 oracle over 10 steps."""
+    p, q = make(chy, po, (32, 32, 32), precision="mixed", E0=(1.0, 0.0, 0.0), mn=0.0, ksp_rtol=1e-10,
+                pc_type=chy.PC["mg"], seed=1)
+    q.precision = 0
+    ions = po.load(q, po.make_loader(amp=(0.02, 0.02, 0.02), phase=tuple(po.mode_phases(1))), 32 ** 3 * 16)
+    first = {}
+    with oracle_threads(po):
+        out, N = run_pair(chy, po, p, q, ions, 10, moments=True, initial=first)
+    assert rel(first["mom"], first["rnodes"].reshape(-1, 4)) < 3e-6
+    assert rel(first["phi"], first["rphi"]) < 1e-6
+    for s, o in enumerate(out):
+        rp, rv = o["rions"]
+        assert np.abs(o["pos"][:, :3] - rp[:, :3]).max() < 5e-7 * (s + 1), s
+        assert rel(o["vel"][:, :3], rv[:, :3]) < 1e-6, s
+        assert rel(o["mom"], o["rnodes"].reshape(-1, 4)) < 3e-6, s
+        assert rel(o["phi"], o["rphi"]) < 1e-6, (s, rel(o["phi"], o["rphi"]))
+        assert o["info"]["rnorm"] <= 1e-10 * o["info"]["bnorm"] * 1.01
+
+
+def test_mixed_form_on_the_anisotropic_grid(chy, po):
+    """The 256 x 256 x 64 grid of the anisotropic plasma (drift 0.3 along y,
+    Gaussian neutral profile, E0 = (0.8, 0, 0)) with 2 ions per cell instead
+    of 32 (8,388,608 ions): the mixed moments and the mixed potential (semi-
+    coarsened multigrid: x and y coarsen before z) against the oracle's FP64
+    deposit of the same ions and its Jacobi-CG solve at rtol 1e-12, then one
+    collisionless step of both."""
+    N = (256, 256, 64)
+    kw = dict(E0=(0.8, 0.0, 0.0), vi0=(0.0, 0.3, 0.0), mn=0.0, ksp_rtol=1e-10, pc_type=chy.PC["mg"], seed=1,
+              nn_profile=chy.NN_PROFILE["gaussian_x"], nn_center=N[0] / 2.0, nn_sigma=N[0] / 6.0, nn_floor=0.1)
+    p, q = make(chy, po, N, precision="mixed", **kw)
+    q.precision = 0
+    q.ksp_rtol = 1e-12
+    ions = po.load(q, po.make_loader(v0=(0.0, 0.3, 0.0), amp=(0.0, 0.0, 0.0)), int(np.prod(N)) * 2)
+    first = {}
+    with oracle_threads(po):
+        out, _ = run_pair(chy, po, p, q, ions, 1, moments=True, initial=first)
+    assert rel(first["mom"], first["rnodes"].reshape(-1, 4)) < 3e-6
+    assert rel(first["phi"], first["rphi"]) < 1e-6, rel(first["phi"], first["rphi"])
+    o = out[0]
+    assert o["info"]["rnorm"] <= 1e-10 * o["info"]["bnorm"] * 1.01
+    assert rel(o["vel"][:, :3], o["rions"][1][:, :3]) < 1e-6
+    assert rel(o["mom"], o["rnodes"].reshape(-1, 4)) < 3e-6
+    assert rel(o["phi"], o["rphi"]) < 1e-6, rel(o["phi"], o["rphi"])
+
+
+def test_mixed_form_collisional_statistics_over_four_seeds(chy, po):
+    """With collisions (nu = 0.5) the mixed and FP64 forms draw the same
+    Philox numbers but part where an FP32 and an FP64 collision test fall on
+    either side of a threshold (about 0.2% of ions in 5 steps).  Over 4
+    seeds, 16^3 x 32 ions/cell, 5 steps: the realised event count is within
+    4 sqrt(expected) of the oracle's each step, the expected count within
+    1e-5, and the mean, variance and kurtosis of each velocity component
+    within 4 standard errors of the oracle's, per seed and averaged over the
+    seeds (standard errors of the oracle's population: sqrt(var/n),
+    var sqrt(2/n), sqrt(24/n))."""
+    z_all = []
+    for seed in (1, 2, 3, 4):
+        p, q = make(chy, po, (16, 16, 16), precision="mixed", E0=(1.0, 0.0, 0.0), nui=0.5, ksp_rtol=1e-10,
+                    pc_type=chy.PC["mg"], seed=seed)
+        q.precision = 0
+        ions = po.load(q, po.make_loader(amp=(0.02, 0.0, 0.0)), 16 ** 3 * 32)
+        with oracle_threads(po):
+            out, _ = run_pair(chy, po, p, q, ions, 5)
+        for o in out:
+            i, r = o["info"], o["rinfo"]
+            assert i["Nc"] == r["Nc"]
+            assert abs(i["expected"] - r["expected"]) < 1e-5 * r["expected"]
+            assert abs(i["collisions"] - r["collisions"]) < 4 * np.sqrt(r["expected"])
+        a, b = out[-1]["vel"][:, :3], out[-1]["rions"][1][:, :3]
+        n = a.shape[0]
+
+        def moments(v):
+            m = v.mean(axis=0)
+            c = v - m
+            var = (c ** 2).mean(axis=0)
+            return m, var, (c ** 4).mean(axis=0) / var ** 2
+
+        (ma, va, ka), (mb, vb, kb) = moments(a), moments(b)
+        z = np.concatenate([(ma - mb) / np.sqrt(vb / n), (va - vb) / (vb * np.sqrt(2.0 / n)),
+                            (ka - kb) / np.sqrt(24.0 / n)])
+        assert np.all(np.abs(z) < 4), (seed, z)
+        z_all.append(z)
+    assert np.all(np.abs(np.mean(z_all, axis=0)) < 4 / np.sqrt(len(z_all)))
 
 
 # ------------------------------------------------------------------ failure reporting
