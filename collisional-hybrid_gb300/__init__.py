@@ -172,6 +172,7 @@ def lib():
             "ch_output_open": [vp, C.c_char_p],
             "ch_output": [vp, C.c_char_p],
             "ch_output_wait": [vp, C.POINTER(C.c_int64)],
+            "ch_set_solver": [vp, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32],
             "ch_host_register": [vp, C.c_uint64],
             "ch_host_unregister": [vp],
             "ch_batch_create": [vp, vp, C.c_int32, C.c_int32, C.POINTER(vp)],
@@ -355,6 +356,10 @@ class Hybrid:
         return info.as_dict()
 
     # ---------------------------------------------------------------- grid access
+    def set_solver(self, ksp: str = "cg", pc: str = "mg", rtol: float = 1e-8, atol: float = 0.0, max_it: int = 10000):
+        """KSPSetType / KSPSetTolerances for the following solves."""
+        _check(lib().ch_set_solver(self._h, KSP[ksp], PC[pc], float(rtol), float(atol), int(max_it)))
+
     def set_moments(self, nodes: np.ndarray):
         nodes = np.ascontiguousarray(nodes, dtype=np.float64).reshape(self.N, 4)
         _check(lib().ch_set_moments(self._h, nodes.ctypes.data))

@@ -670,8 +670,21 @@ extern "C" ch_status ch_collect_moments(ch_ctx* c, ch_grid_node* host_out, ch_st
   return CH_OK;
 }
 
+// CG needs a symmetric operator.  With kappa_e != 0 the full operator's
+// tensor R = I + kk^T + [k]x has an antisymmetric part (src/lhs.c:412-420),
+// so only BiCGStab applies.
+static bool cg_unsound(const ch_params& p) {
+  return p.ksp_type == CH_KSP_CG && p.lhs_type == CH_LHS_FULL &&
+         (p.kappa_e[0] != 0.0 || p.kappa_e[1] != 0.0 || p.kappa_e[2] != 0.0);
+}
+
 static ch_status potential(ch_ctx* c, ch_solve_info* info) {
   if (!c->moments_valid) return ch_fail(CH_ERR_STATE, "no moments: call ch_collect_moments first");
+  if (cg_unsound(c->p))
+    return ch_fail(CH_ERR_UNSUPPORTED,
+                   "-ksp_type cg with kappa_e = (%g, %g, %g): the full operator is not symmetric "
+                   "(src/lhs.c:412-420); use -ksp_type bcgs",
+                   c->p.kappa_e[0], c->p.kappa_e[1], c->p.kappa_e[2]);
   const int64_t N = c->g.N;
   prof_begin(c);
   c->solver.build_rhs(c->mom, c->rhs, c->stream);
@@ -697,6 +710,23 @@ static ch_status potential(ch_ctx* c, ch_solve_info* info) {
                    c->p.ksp_rtol * st.bnorm, st.iterations);
   if (rc) return rc;
   if (!isfinite(st.rnorm)) return ch_fail(CH_ERR_NAN, "non-finite potential residual");
+  return CH_OK;
+}
+
+extern "C" ch_status ch_set_solver(ch_ctx* c, int32_t ksp_type, int32_t pc_type, double rtol, double atol,
+                                   int32_t max_it) {
+  if (!c) return ch_fail(CH_ERR_ARG, "null ctx");
+  if (ksp_type != CH_KSP_CG && ksp_type != CH_KSP_BCGS) return ch_fail(CH_ERR_ARG, "unknown ksp_type %d", ksp_type);
+  if (pc_type != CH_PC_NONE && pc_type != CH_PC_JACOBI && pc_type != CH_PC_MG)
+    return ch_fail(CH_ERR_ARG, "unknown pc_type %d", pc_type);
+  if (!(rtol > 0.0) || !(atol >= 0.0) || max_it < 1)
+    return ch_fail(CH_ERR_ARG, "bad ksp tolerances: rtol %g, atol %g, max_it %d", rtol, atol, max_it);
+  c->p.ksp_type = ksp_type;
+  c->p.pc_type = pc_type;
+  c->p.ksp_rtol = rtol;
+  c->p.ksp_atol = atol;
+  c->p.ksp_max_it = max_it;
+  c->solver.set_options(ksp_type, pc_type, rtol, atol, max_it);
   return CH_OK;
 }
 

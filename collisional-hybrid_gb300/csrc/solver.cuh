@@ -71,6 +71,15 @@ class PotentialSolver {
   void set_E0(const double E0[3]) {
     for (int d = 0; d < 3; ++d) p_.E0[d] = E0[d];
   }
+  // Krylov method, preconditioner and tolerances for the following solves
+  // (the multigrid hierarchy is built on the first solve that needs it).
+  void set_options(int32_t ksp_type, int32_t pc_type, double rtol, double atol, int32_t max_it) {
+    p_.ksp_type = ksp_type;
+    p_.pc_type = pc_type;
+    p_.ksp_rtol = rtol;
+    p_.ksp_atol = atol;
+    p_.ksp_max_it = max_it;
+  }
 
  private:
   ch_status solve_fp64(const double* n, const double* b, double* phi, SolveStats* st, cudaStream_t s);

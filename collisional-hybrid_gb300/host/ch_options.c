@@ -16,7 +16,9 @@ static const char* const RHS_NAMES[] = {"constant", "sinusoidal", "full", NULL};
 static const char* const LHS_NAMES[] = {"identity", "laplacian", "full", NULL};
 static const char* const DENSITY_NAMES[] = {"flat-sobol", "flat-reverse", "flat-normal", "uniform",
                                             "sinusoidal", "gaussian", NULL};
-static const char* const KSP_NAMES[] = {"cg", "bcgs", NULL};
+/* -ksp_type: cg, bcgs, or PETSc's default gmres, which has no GPU form
+ * here and maps to CG for a symmetric operator, BiCGStab otherwise */
+static const char* const KSP_NAMES[] = {"cg", "bcgs", "gmres", NULL};
 static const char* const PC_NAMES[] = {"none", "jacobi", "mg", NULL};
 static const char* const PREC_NAMES[] = {"fp64", "mixed", NULL};
 
@@ -168,7 +170,14 @@ ch_status ch_parse_options(int argc, char** argv, ch_params* p, ch_run_options* 
   if (get_real(&a, "-ch_kappa_ey", &d) > 0) p->kappa_e[1] = d;
   if (get_real(&a, "-ch_kappa_ez", &d) > 0) p->kappa_e[2] = d;
   /* solver */
-  if (get_enum(&a, "-ksp_type", KSP_NAMES, &p->ksp_type) < 0) FAIL("-ksp_type: cg or bcgs");
+  int kt = 2;  /* absent: PETSc's default, gmres */
+  if (get_enum(&a, "-ksp_type", KSP_NAMES, &kt) < 0) FAIL("-ksp_type: cg, bcgs or gmres");
+  if (kt == 2) {
+    const int sym = p->lhs_type != CH_LHS_FULL ||
+                    (p->kappa_e[0] == 0.0 && p->kappa_e[1] == 0.0 && p->kappa_e[2] == 0.0);
+    kt = sym ? CH_KSP_CG : CH_KSP_BCGS;
+  }
+  p->ksp_type = kt;
   if (get_enum(&a, "-ch_pc", PC_NAMES, &p->pc_type) < 0) FAIL("-ch_pc: none, jacobi or mg");
   if (get_real(&a, "-ksp_rtol", &d) > 0) p->ksp_rtol = d;
   if (get_real(&a, "-ksp_atol", &d) > 0) p->ksp_atol = d;

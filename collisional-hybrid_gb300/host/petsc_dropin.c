@@ -14,12 +14,25 @@
  * and link libchybrid.so.  One MPI rank drives one GPU (the replacement
  * rejects more ranks: the GPU path does not decompose the grid).
  *
- * Data flow: the DMSwarm "position"/"velocity" fields (RealVector AoS) are
- * copied to the device at the start of each particle call and back at its
- * end, so every host routine between calls sees current ions; the vlasov
- * global Vec (GridNode, dof 4) receives the moments; ctx->phi receives the
- * potential.  Reference option names map to ch_params through the Context
- * that ProcessOptions filled (src/parameters.c:28-562).
+ * Data flow: the ions stay on the device between the particle calls of a
+ * step.  UpdateVelocities uploads the DMSwarm "position"/"velocity" fields
+ * (RealVector AoS) only when the host holds newer ions than the device: on
+ * the first call, when the fields' base address or local size changed (a
+ * DMSwarm reallocation or migration), or after the host called
+ * HybridGPUIonsChanged().  UpdatePositions downloads the step's ions once,
+ * so the DMSwarm holds them for DMSwarmMigrate and any host routine after
+ * it; CollectVlasovQuantities then deposits from the device copy.  One
+ * upload and one download per step instead of one of each per call.  The
+ * vlasov global Vec (GridNode, dof 4) receives the moments; ctx->phi
+ * receives the potential.
+ *
+ * Options: the Context fields that ProcessOptions filled
+ * (src/parameters.c:28-562) give the physics; the KSP gives the solver as
+ * KSPSetFromOptions set it (src/hybrid.c:75): -ksp_type cg | bcgs (PETSc's
+ * default gmres, which has no GPU form here, maps to CG for a symmetric
+ * operator and to BiCGStab otherwise), -ksp_rtol, -ksp_atol, -ksp_max_it;
+ * the options database gives -ch_precision fp64|mixed, -ch_pc
+ * none|jacobi|mg, -ch_sort_period n and -ch_faithful bits.
  */
 #ifdef CH_WITH_PETSC
 
@@ -31,10 +44,37 @@
 
 static ch_ctx* g_gpu = NULL;
 static long long g_step = 0;
+/* Which copy of the ions is current (see the data flow above). */
+static const void* g_pos_seen = NULL;
+static const void* g_vel_seen = NULL;
+static PetscInt g_np_seen = -1;
+static int g_host_newer = 1;
+static int g_device_newer = 0;
+
+#define CH_PETSC(call)                                                                           \
+  do {                                                                                           \
+    ch_status rc_ = (call);                                                                      \
+    if (rc_ == CH_ERR_COLLISION_LIMIT) SETERRQ(PETSC_COMM_WORLD, PETSC_ERR_SIG, "%s", ch_last_error()); \
+    if (rc_ != CH_OK) SETERRQ(PETSC_COMM_WORLD, PETSC_ERR_LIB, "%s", ch_last_error());           \
+  } while (0)
+
+/* -name value from the options database, as an index into names[] (-1 when
+ * the option is absent; -2 when its value is not one of names[]). */
+static int option_enum(const char* name, const char* const* names, int n) {
+  char buf[64];
+  PetscBool set = PETSC_FALSE;
+  if (PetscOptionsGetString(NULL, NULL, name, buf, sizeof buf, &set) || !set) return -1;
+  for (int i = 0; i < n; ++i)
+    if (!strcmp(buf, names[i])) return i;
+  return -2;
+}
 
 /* SI constants of the reference (src/constants.h) are folded into the
  * electron coefficients exactly as ComputeFullRHS forms them (src/rhs.c:190-191). */
-static void params_from_context(const Context* ctx, ch_params* p) {
+static PetscErrorCode params_from_context(const Context* ctx, ch_params* p) {
+  static const char* const prec_names[] = {"fp64", "mixed"};
+  static const char* const pc_names[] = {"none", "jacobi", "mg"};
+  PetscFunctionBeginUser;
   ch_params_default(p);
   p->Nx = ctx->grid.N.x;
   p->Ny = ctx->grid.N.y;
@@ -60,14 +100,46 @@ static void params_from_context(const Context* ctx, ch_params* p) {
   p->lhs_type = (int32_t)ctx->lhsType;
   p->rhs_type = (int32_t)ctx->rhsType;
   p->seed = (uint64_t)(ctx->seed < 0 ? -ctx->seed : ctx->seed);
+  int e = option_enum("-ch_precision", prec_names, 2);
+  if (e == -2) SETERRQ(PETSC_COMM_WORLD, PETSC_ERR_ARG_OUTOFRANGE, "-ch_precision: fp64 or mixed");
+  if (e >= 0) p->precision = e;
+  e = option_enum("-ch_pc", pc_names, 3);
+  if (e == -2) SETERRQ(PETSC_COMM_WORLD, PETSC_ERR_ARG_OUTOFRANGE, "-ch_pc: none, jacobi or mg");
+  if (e >= 0) p->pc_type = e;
+  PetscInt iv;
+  PetscBool set = PETSC_FALSE;
+  PetscCall(PetscOptionsGetInt(NULL, NULL, "-ch_sort_period", &iv, &set));
+  if (set) p->sort_period = (int32_t)iv;
+  set = PETSC_FALSE;
+  PetscCall(PetscOptionsGetInt(NULL, NULL, "-ch_faithful", &iv, &set));
+  if (set) p->faithful = (uint32_t)iv;
+  PetscFunctionReturn(PETSC_SUCCESS);
 }
 
-#define CH_PETSC(call)                                                                           \
-  do {                                                                                           \
-    ch_status rc_ = (call);                                                                      \
-    if (rc_ == CH_ERR_COLLISION_LIMIT) SETERRQ(PETSC_COMM_WORLD, PETSC_ERR_SIG, "%s", ch_last_error()); \
-    if (rc_ != CH_OK) SETERRQ(PETSC_COMM_WORLD, PETSC_ERR_LIB, "%s", ch_last_error());           \
-  } while (0)
+/* The KSP's method and tolerances, as KSPSetFromOptions left them. */
+static PetscErrorCode solver_from_ksp(KSP ksp, const Context* ctx) {
+  PetscReal rtol, atol, dtol;
+  PetscInt maxits;
+  KSPType type;
+  ch_params p;
+  PetscFunctionBeginUser;
+  PetscCall(KSPGetTolerances(ksp, &rtol, &atol, &dtol, &maxits));
+  PetscCall(KSPGetType(ksp, &type));
+  PetscCall(params_from_context(ctx, &p));
+  const int symmetric = p.lhs_type != CH_LHS_FULL ||
+                        (p.kappa_e[0] == 0.0 && p.kappa_e[1] == 0.0 && p.kappa_e[2] == 0.0);
+  int32_t kt;
+  if (type && !strcmp(type, "cg"))
+    kt = CH_KSP_CG;  /* the library refuses it for a non-symmetric operator */
+  else if (type && !strcmp(type, "bcgs"))
+    kt = CH_KSP_BCGS;
+  else if (!type || !strcmp(type, "gmres") || !strcmp(type, "fgmres") || !strcmp(type, "lgmres"))
+    kt = symmetric ? CH_KSP_CG : CH_KSP_BCGS;
+  else
+    SETERRQ(PETSC_COMM_WORLD, PETSC_ERR_SUP, "-ksp_type %s: the GPU solve offers cg and bcgs", type);
+  CH_PETSC(ch_set_solver(g_gpu, kt, p.pc_type, rtol, atol, (int32_t)maxits));
+  PetscFunctionReturn(PETSC_SUCCESS);
+}
 
 static PetscErrorCode ensure_gpu(Context* ctx) {
   PetscMPIInt size;
@@ -76,36 +148,74 @@ static PetscErrorCode ensure_gpu(Context* ctx) {
   PetscCallMPI(MPI_Comm_size(PETSC_COMM_WORLD, &size));
   if (size != 1) SETERRQ(PETSC_COMM_WORLD, PETSC_ERR_SUP, "the GPU hot path runs on one rank (got %d)", size);
   ch_params p;
-  params_from_context(ctx, &p);
+  PetscCall(params_from_context(ctx, &p));
   CH_PETSC(ch_create(&p, -1, &g_gpu));
+  g_host_newer = 1;
+  g_device_newer = 0;
   PetscFunctionReturn(PETSC_SUCCESS);
 }
 
-/* DMSwarm fields -> device */
-static PetscErrorCode push_ions(Context* ctx) {
+/* DMSwarm fields -> device, when the host holds the newer ions */
+static PetscErrorCode sync_to_device(Context* ctx) {
   PetscInt np;
   RealVector *pos, *vel;
   PetscFunctionBeginUser;
   PetscCall(DMSwarmGetLocalSize(ctx->ionsDM, &np));
   PetscCall(DMSwarmGetField(ctx->ionsDM, "position", NULL, NULL, (void**)&pos));
   PetscCall(DMSwarmGetField(ctx->ionsDM, "velocity", NULL, NULL, (void**)&vel));
-  ch_status rc = ch_particles_upload(g_gpu, (const ch_real_vector*)pos, (const ch_real_vector*)vel, np);
+  ch_status rc = CH_OK;
+  const int moved = (const void*)pos != g_pos_seen || (const void*)vel != g_vel_seen || np != g_np_seen;
+  if (g_host_newer || moved) {
+    if (g_device_newer && !g_host_newer && moved)
+      rc = CH_ERR_STATE;  /* the fields moved while the device held newer ions */
+    else
+      rc = ch_particles_upload(g_gpu, (const ch_real_vector*)pos, (const ch_real_vector*)vel, np);
+    if (rc == CH_OK) {
+      g_pos_seen = pos;
+      g_vel_seen = vel;
+      g_np_seen = np;
+      g_host_newer = 0;
+      g_device_newer = 0;
+    }
+  }
+  PetscCall(DMSwarmRestoreField(ctx->ionsDM, "velocity", NULL, NULL, (void**)&vel));
+  PetscCall(DMSwarmRestoreField(ctx->ionsDM, "position", NULL, NULL, (void**)&pos));
+  if (rc == CH_ERR_STATE)
+    SETERRQ(PETSC_COMM_WORLD, PETSC_ERR_ORDER, "the DMSwarm fields changed while the device held newer ions");
+  CH_PETSC(rc);
+  PetscFunctionReturn(PETSC_SUCCESS);
+}
+
+/* device -> DMSwarm fields, when the device holds the newer ions */
+static PetscErrorCode sync_to_host(Context* ctx) {
+  RealVector *pos, *vel;
+  PetscFunctionBeginUser;
+  if (!g_device_newer) PetscFunctionReturn(PETSC_SUCCESS);
+  PetscCall(DMSwarmGetField(ctx->ionsDM, "position", NULL, NULL, (void**)&pos));
+  PetscCall(DMSwarmGetField(ctx->ionsDM, "velocity", NULL, NULL, (void**)&vel));
+  ch_status rc = ch_particles_download(g_gpu, (ch_real_vector*)pos, (ch_real_vector*)vel);
+  if (rc == CH_OK) {
+    g_pos_seen = pos;
+    g_vel_seen = vel;
+    g_device_newer = 0;
+  }
   PetscCall(DMSwarmRestoreField(ctx->ionsDM, "velocity", NULL, NULL, (void**)&vel));
   PetscCall(DMSwarmRestoreField(ctx->ionsDM, "position", NULL, NULL, (void**)&pos));
   CH_PETSC(rc);
   PetscFunctionReturn(PETSC_SUCCESS);
 }
 
-/* device -> DMSwarm fields */
-static PetscErrorCode pull_ions(Context* ctx) {
-  RealVector *pos, *vel;
+PetscErrorCode HybridGPUIonsChanged(void) {
   PetscFunctionBeginUser;
-  PetscCall(DMSwarmGetField(ctx->ionsDM, "position", NULL, NULL, (void**)&pos));
-  PetscCall(DMSwarmGetField(ctx->ionsDM, "velocity", NULL, NULL, (void**)&vel));
-  ch_status rc = ch_particles_download(g_gpu, (ch_real_vector*)pos, (ch_real_vector*)vel);
-  PetscCall(DMSwarmRestoreField(ctx->ionsDM, "velocity", NULL, NULL, (void**)&vel));
-  PetscCall(DMSwarmRestoreField(ctx->ionsDM, "position", NULL, NULL, (void**)&pos));
-  CH_PETSC(rc);
+  if (g_device_newer)
+    SETERRQ(PETSC_COMM_WORLD, PETSC_ERR_ORDER, "the device holds newer ions: call HybridGPUSyncIons first");
+  g_host_newer = 1;
+  PetscFunctionReturn(PETSC_SUCCESS);
+}
+
+PetscErrorCode HybridGPUSyncIons(Context* ctx) {
+  PetscFunctionBeginUser;
+  if (g_gpu) PetscCall(sync_to_host(ctx));
   PetscFunctionReturn(PETSC_SUCCESS);
 }
 
@@ -113,19 +223,20 @@ PetscErrorCode UpdateVelocities(KSP ksp, Context* ctx) {
   PetscFunctionBeginUser;
   (void)ksp;  /* phi stays on the device from the last ComputePotential */
   PetscCall(ensure_gpu(ctx));
-  PetscCall(push_ions(ctx));
+  PetscCall(sync_to_device(ctx));
   ch_step_info info;
   CH_PETSC(ch_update_velocities(g_gpu, g_step, &info));
-  PetscCall(pull_ions(ctx));
+  g_device_newer = 1;
   PetscFunctionReturn(PETSC_SUCCESS);
 }
 
 PetscErrorCode UpdatePositions(Context* ctx) {
   PetscFunctionBeginUser;
   PetscCall(ensure_gpu(ctx));
-  PetscCall(push_ions(ctx));
+  PetscCall(sync_to_device(ctx));
   CH_PETSC(ch_update_positions(g_gpu));
-  PetscCall(pull_ions(ctx));
+  g_device_newer = 1;
+  PetscCall(sync_to_host(ctx));                       /* the step's ions, once */
   PetscCall(DMSwarmMigrate(ctx->ionsDM, PETSC_TRUE)); /* src/particles.c:714 */
   g_step++;
   PetscFunctionReturn(PETSC_SUCCESS);
@@ -135,7 +246,7 @@ PetscErrorCode CollectVlasovQuantities(Context* ctx) {
   PetscScalar* a;
   PetscFunctionBeginUser;
   PetscCall(ensure_gpu(ctx));
-  PetscCall(push_ions(ctx));
+  PetscCall(sync_to_device(ctx));
   PetscCall(VecGetArray(ctx->vlasov, &a)); /* GridNode, natural order on one rank */
   ch_status rc = ch_collect_moments(g_gpu, (ch_grid_node*)a, NULL);
   PetscCall(VecRestoreArray(ctx->vlasov, &a));
@@ -148,6 +259,7 @@ PetscErrorCode ComputePotential(KSP ksp, Context* ctx) {
   DM dm;
   PetscFunctionBeginUser;
   PetscCall(ensure_gpu(ctx));
+  PetscCall(solver_from_ksp(ksp, ctx));
   /* the host may have replaced the moments (LoadVlasovQuantities, src/fileio.c:6-70) */
   PetscCall(VecGetArray(ctx->vlasov, &a));
   ch_status rc = ch_set_moments(g_gpu, (const ch_grid_node*)a);

@@ -181,6 +181,12 @@ ch_status ch_collect_moments(ch_ctx* c, ch_grid_node* host_out, ch_step_info* in
 /* ComputePotential (src/potential.c:6-15): RHS (rhs.c), operator (lhs.c),
  * Krylov solve warm-started from the previous phi.  phi_out nullable. */
 ch_status ch_compute_potential(ch_ctx* c, double* phi_out, ch_solve_info* info);
+/* KSPSetType / KSPSetTolerances as KSPSetFromOptions applies them
+ * (src/hybrid.c:75): the Krylov method (CH_KSP_CG | CH_KSP_BCGS), the
+ * preconditioner (CH_PC_*), rtol, atol and max_it of the following solves.
+ * A solve with CG while kappa_e != 0 and the full LHS returns
+ * CH_ERR_UNSUPPORTED: that operator is not symmetric (src/lhs.c:412-420). */
+ch_status ch_set_solver(ch_ctx* c, int32_t ksp_type, int32_t pc_type, double rtol, double atol, int32_t max_it);
 /* The reference time-loop body (src/hybrid.c:101-123) without output,
  * nsteps times, steps numbered first_step, first_step+1, ... */
 ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_step_info* info);

@@ -44,6 +44,8 @@ typedef int MPI_Comm;
 #define PETSC_ERR_SIG 59
 #define PETSC_ERR_SUP 56
 #define PETSC_ERR_LIB 76
+#define PETSC_ERR_ARG_OUTOFRANGE 63
+#define PETSC_ERR_ORDER 73
 
 typedef enum { INSERT_VALUES = 1, ADD_VALUES = 2 } InsertMode;
 typedef enum { MAT_FLUSH_ASSEMBLY = 1, MAT_FINAL_ASSEMBLY = 0 } MatAssemblyType;
@@ -61,6 +63,11 @@ typedef struct _p_KSP* KSP;
 typedef struct _p_MatNullSpace* MatNullSpace;
 typedef struct _p_PetscViewer* PetscViewer;
 typedef struct _p_PetscObject* PetscObject;
+typedef struct _p_PetscOptions* PetscOptions;
+typedef const char* KSPType;
+#define KSPCG "cg"
+#define KSPBCGS "bcgs"
+#define KSPGMRES "gmres"
 
 extern int ch_standin_verbose;
 int ch_standin_error(int code, const char* func, const char* fmt, ...);
@@ -148,6 +155,15 @@ PetscErrorCode MatNullSpaceRemove(MatNullSpace sp, Vec v);
 PetscErrorCode KSPGetDM(KSP ksp, DM* dm);
 PetscErrorCode KSPGetSolution(KSP ksp, Vec* v);
 PetscErrorCode KSPGetOperators(KSP ksp, Mat* A, Mat* P);
+PetscErrorCode KSPGetTolerances(KSP ksp, PetscReal* rtol, PetscReal* abstol, PetscReal* dtol, PetscInt* maxits);
+PetscErrorCode KSPGetType(KSP ksp, KSPType* type);
+/* Options database (PetscOptionsGet*; NULL database = the global one) */
+PetscErrorCode PetscOptionsGetString(PetscOptions o, const char pre[], const char name[], char str[], size_t len,
+                                     PetscBool* set);
+PetscErrorCode PetscOptionsGetInt(PetscOptions o, const char pre[], const char name[], PetscInt* v, PetscBool* set);
+PetscErrorCode PetscOptionsGetReal(PetscOptions o, const char pre[], const char name[], PetscReal* v,
+                                   PetscBool* set);
+PetscErrorCode PetscOptionsHasName(PetscOptions o, const char pre[], const char name[], PetscBool* set);
 PetscErrorCode PetscViewerBinaryOpen(MPI_Comm c, const char* name, PetscFileMode m, PetscViewer* v);
 PetscErrorCode PetscViewerDestroy(PetscViewer* v);
 

@@ -304,6 +304,89 @@ PetscErrorCode MatNullSpaceRemove(MatNullSpace sp, Vec v) {
 PetscErrorCode KSPGetDM(KSP ksp, DM* dm) { *dm = ksp->dm; return 0; }
 PetscErrorCode KSPGetSolution(KSP ksp, Vec* v) { *v = ksp->sol; return 0; }
 PetscErrorCode KSPGetOperators(KSP ksp, Mat* A, Mat* P) { if (A) *A = ksp->A; if (P) *P = ksp->A; return 0; }
+/* ---------------- options database and KSP settings ---------------- */
+#define CH_STANDIN_MAXOPT 64
+static char* g_opt_name[CH_STANDIN_MAXOPT];
+static char* g_opt_val[CH_STANDIN_MAXOPT];
+static int g_nopt = 0;
+
+void ch_standin_options(int argc, const char* const* argv) {
+  for (int i = 0; i < g_nopt; ++i) { free(g_opt_name[i]); free(g_opt_val[i]); }
+  g_nopt = 0;
+  for (int i = 0; i < argc && g_nopt < CH_STANDIN_MAXOPT; ++i) {
+    if (argv[i][0] != '-') continue;
+    const int has_val = i + 1 < argc && argv[i + 1][0] != '-';
+    g_opt_name[g_nopt] = strdup(argv[i]);
+    g_opt_val[g_nopt] = has_val ? strdup(argv[i + 1]) : NULL;
+    ++g_nopt;
+    if (has_val) ++i;
+  }
+}
+
+static const char* opt_find(const char* name, int* found) {
+  *found = 0;
+  for (int i = g_nopt - 1; i >= 0; --i)
+    if (!strcmp(g_opt_name[i], name)) { *found = 1; return g_opt_val[i]; }
+  return NULL;
+}
+
+PetscErrorCode PetscOptionsGetString(PetscOptions o, const char pre[], const char name[], char str[], size_t len,
+                                     PetscBool* set) {
+  (void)o; (void)pre;
+  int f;
+  const char* v = opt_find(name, &f);
+  *set = (f && v) ? PETSC_TRUE : PETSC_FALSE;
+  if (*set && len) { strncpy(str, v, len - 1); str[len - 1] = 0; }
+  return 0;
+}
+PetscErrorCode PetscOptionsGetInt(PetscOptions o, const char pre[], const char name[], PetscInt* v, PetscBool* set) {
+  (void)o; (void)pre;
+  int f;
+  const char* s = opt_find(name, &f);
+  *set = (f && s) ? PETSC_TRUE : PETSC_FALSE;
+  if (*set) *v = (PetscInt)strtol(s, NULL, 10);
+  return 0;
+}
+PetscErrorCode PetscOptionsGetReal(PetscOptions o, const char pre[], const char name[], PetscReal* v,
+                                   PetscBool* set) {
+  (void)o; (void)pre;
+  int f;
+  const char* s = opt_find(name, &f);
+  *set = (f && s) ? PETSC_TRUE : PETSC_FALSE;
+  if (*set) *v = strtod(s, NULL);
+  return 0;
+}
+PetscErrorCode PetscOptionsHasName(PetscOptions o, const char pre[], const char name[], PetscBool* set) {
+  (void)o; (void)pre;
+  int f;
+  (void)opt_find(name, &f);
+  *set = f ? PETSC_TRUE : PETSC_FALSE;
+  return 0;
+}
+
+KSP ch_standin_ksp(DM dm) {
+  KSP k = (KSP)calloc(1, sizeof(*k));
+  k->dm = dm;
+  strcpy(k->type, KSPGMRES);
+  k->rtol = 1e-5; k->abstol = 1e-50; k->dtol = 1e4; k->maxits = 10000;
+  PetscBool set;
+  char buf[32];
+  PetscOptionsGetString(NULL, NULL, "-ksp_type", buf, sizeof buf, &set);
+  if (set) strcpy(k->type, buf);
+  PetscOptionsGetReal(NULL, NULL, "-ksp_rtol", &k->rtol, &set);
+  PetscOptionsGetReal(NULL, NULL, "-ksp_atol", &k->abstol, &set);
+  PetscOptionsGetInt(NULL, NULL, "-ksp_max_it", &k->maxits, &set);
+  return k;
+}
+PetscErrorCode KSPGetTolerances(KSP ksp, PetscReal* rtol, PetscReal* abstol, PetscReal* dtol, PetscInt* maxits) {
+  if (rtol) *rtol = ksp->rtol;
+  if (abstol) *abstol = ksp->abstol;
+  if (dtol) *dtol = ksp->dtol;
+  if (maxits) *maxits = ksp->maxits;
+  return 0;
+}
+PetscErrorCode KSPGetType(KSP ksp, KSPType* type) { *type = ksp->type; return 0; }
+
 PetscErrorCode PetscViewerBinaryOpen(MPI_Comm c, const char* n, PetscFileMode m, PetscViewer* v) {
   (void)c; (void)n; (void)m; *v = NULL;
   return PETSC_ERR_ARG_WRONG;

@@ -36,6 +36,9 @@ struct _p_KSP {
   DM dm;
   Vec sol;
   Mat A;
+  char type[32];          /* KSPSetType / -ksp_type (PETSc's default: gmres) */
+  double rtol, abstol, dtol;
+  int maxits;
 };
 
 DM ch_standin_dmda(int Nx, int Ny, int Nz, int dof, const char* const* names);
@@ -43,4 +46,11 @@ DM ch_standin_swarm(DM celldm, int np);
 Mat ch_standin_mat(int N);
 void ch_standin_mat_free(Mat A);
 Vec ch_standin_global(DM dm);
+/* A KSP whose type and tolerances are those KSPSetFromOptions would set
+ * from the options database (-ksp_type, -ksp_rtol, -ksp_atol, -ksp_max_it),
+ * on PETSc's defaults (gmres, 1e-5, 1e-50, 1e4, 10000). */
+KSP ch_standin_ksp(DM dm);
+/* Replaces the options database with argv[0..argc) ("-name value" pairs,
+ * or a lone "-name"). */
+void ch_standin_options(int argc, const char* const* argv);
 #endif

@@ -198,6 +198,31 @@ def test_solve_matches_oracle(chy, po, golden, ksp, kappa, precision, pc):
     assert rel(phi, ref) < 1e-12, rel(phi, ref)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solver_options_set_after_create(chy, po, golden, precision):
+    """ch_set_solver (KSPSetFromOptions' settings, as the PETSc drop-in passes
+    them): with kappa_e != 0 the full operator is not symmetric, so a CG
+    solve is refused (CH_ERR_UNSUPPORTED) and BiCGStab with multigrid meets
+    -ksp_rtol 1e-10 and agrees with the oracle's BiCGStab solve."""
+    kappa = (0.0, 0.0, 1.5)
+    p, q, _ = golden_case(chy, po, golden, "g8", kappa_e=kappa, precision=precision)
+    nodes = golden["g8_collect1"]
+    with chy.Hybrid(p) as h:
+        h.set_moments(nodes)
+        h.set_solver("cg", "mg", 1e-10)
+        with pytest.raises(chy.HybridError) as e:
+            h.ComputePotential()
+        assert e.value.status == -10
+        h.set_solver("bcgs", "mg", 1e-10, 0.0, 500)
+        phi = h.ComputePotential()
+        info = h.last_solve
+    assert info["rnorm"] <= 1e-10 * info["bnorm"] * 1.01
+    q.ksp_type = 1
+    ref, rinfo = po.solve(q, nodes[0::4], po.rhs(q, nodes), rtol=1e-14, maxit=20000)
+    assert rinfo["rc"] == 0
+    assert rel(phi, ref) < 1e-7
+
+
 @pytest.mark.parametrize("N", [(32, 32, 32), (48, 16, 24), (64, 64, 8)])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_multigrid_solve_on_larger_grids(chy, po, N, precision):

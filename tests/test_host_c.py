@@ -92,6 +92,51 @@ def test_petsc_dropin_compiles_against_reference_headers():
             assert f" T {f}" in syms
 
 
+def _dropin_loop(args):
+    """Builds the drop-in with the PETSc stand-in and a recording test double
+    of the C ABI (tests/dropin/), runs the reference's loop order through it
+    with the given options, and returns what reached the C ABI."""
+    d = tempfile.mkdtemp()
+    exe = os.path.join(d, "loop")
+    dd = os.path.join(REPO, "tests", "dropin")
+    r = subprocess.run(["gcc", "-std=gnu11", "-Wall", "-Werror", "-Wno-unused-function", "-DCH_WITH_PETSC",
+                        "-I", os.path.join(REPO, "oracle", "ref", "shim"), "-I", os.path.join(REPO, "oracle", "ref"),
+                        "-I", REF_SRC, "-I", os.path.join(REPO, "include"), "-I", HOST,
+                        os.path.join(REPO, "oracle", "ref", "standin.c"), os.path.join(HOST, "petsc_dropin.c"),
+                        os.path.join(dd, "fake_chybrid.c"), os.path.join(dd, "dropin_loop.c"), "-o", exe, "-lm"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([exe] + args, capture_output=True, text=True).stdout
+    rec = {}
+    for ln in out.splitlines():
+        k, _, v = ln.partition(" ")
+        rec[k] = v
+    return rec
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference headers not present")
+def test_petsc_dropin_passes_the_ksp_and_ch_options_down():
+    """KSPSetFromOptions' settings (-ksp_type, -ksp_rtol, -ksp_max_it, read
+    back with KSPGetTolerances / KSPGetType) and the -ch_ options reach the C
+    ABI; kappa_e comes from the Context.  Over the reference's loop order
+    (initial deposit and solve, then 3 steps) the ions go up once and come
+    back once per step."""
+    rec = _dropin_loop(["-ksp_type", "bcgs", "-ksp_rtol", "1e-10", "-ksp_max_it", "500", "-ch_precision", "mixed",
+                        "-ch_pc", "mg", "-ch_sort_period", "2", "-test_kappa_z", "1.5"])
+    assert rec["status"] == "0"
+    assert rec["ksp"] == "1" and float(rec["rtol"]) == 1e-10 and rec["maxit"] == "500" and rec["pc"] == "2"
+    assert rec["precision"] == "1" and rec["create_pc"] == "2" and rec["sort_period"] == "2"
+    assert [float(x) for x in rec["kappa"].split()] == [0.0, 0.0, 1.5]
+    assert rec["uploads"] == "1" and rec["downloads"] == "3" and rec["solves"] == "4"
+    # PETSc's default gmres: BiCGStab for the non-symmetric operator, CG otherwise
+    assert _dropin_loop(["-test_kappa_z", "1.5"])["ksp"] == "1"
+    rec = _dropin_loop([])
+    assert rec["ksp"] == "0" and float(rec["rtol"]) == 1e-5 and rec["maxit"] == "10000"
+    # a value the drop-in does not know is an error before anything is created
+    rec = _dropin_loop(["-ch_precision", "bogus"])
+    assert rec["status"] != "0" and rec["creates"] == "0"
+
+
 @pytest.mark.gpu
 def test_c_driver_runs_reference_loop(chy):
     exe = os.path.join(PKG, "hybrid_gpu")
