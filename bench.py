@@ -166,6 +166,51 @@ class DeviceTimer:
         return e
 
 
+def pass_roofline(w, r, prof, N, K, peak, peak_kind):
+    """The ion pass's two launches against HBM: the push launch (push,
+    collisions, move; reads and writes the ion state, reads the node field;
+    on a step before a sort it also stores each ion's rank in its new cell)
+    and the deposit launch (reads the ion state, writes the moment
+    accumulators; on a sort step it also reads the ranks and writes every
+    ion to its sorted slot).  Algorithmic bytes per launch are averaged over
+    the timed steps; the headline kernel is the one with the larger time."""
+    np_ = r["np"]
+    sorts = prof["sort_calls"]
+    dep_calls = max(1, prof["deposit_calls"])
+    push_calls = max(1, prof["pass_calls"] - prof["deposit_calls"])
+    push_ms = (prof["pass_ms"] - prof["deposit_ms"]) / push_calls
+    dep_ms = prof["deposit_ms"] / dep_calls
+    if w["precision"] == "mixed":
+        push_b = np_ * 64 + N * 16 + np_ * 4 * sorts / push_calls
+        dep_b = np_ * 32 + N * 32 + np_ * 36 * sorts / dep_calls
+        names = ("k_pass_tiled<PUSH|MOVE>", "k_pass_tiled<DEPOSIT>")
+    else:
+        push_b = np_ * 104 + N * 24
+        dep_b = np_ * 52 + N * 32
+        names = ("k_pass_f64<PUSH|MOVE>", "k_pass_f64<DEPOSIT>")
+    launches = {}
+    for key, name, b, ms in (("push", names[0], push_b, push_ms), ("deposit", names[1], dep_b, dep_ms)):
+        tr = committed_traffic(name)
+        launches[key] = {"kernel": name, "algorithmic_bytes_per_launch": b, "avg_launch_ms": ms,
+                         "achieved": b / (ms / 1e3) / 1e9 if ms > 0 else None,
+                         "frac": b / (ms / 1e3) / 1e9 / peak if ms > 0 else None,
+                         "traffic": (tr["dram_bytes_per_launch"] * np_ / tr["ions"]
+                                     if isinstance(tr, dict) and "dram_bytes_per_launch" in tr else None),
+                         "calls": push_calls if key == "push" else dep_calls}
+    top = max(launches, key=lambda k: launches[k]["avg_launch_ms"] * launches[k]["calls"])
+    L = launches[top]
+    both_b = push_b * push_calls + dep_b * dep_calls
+    both_ms = push_ms * push_calls + dep_ms * dep_calls
+    return {"bound": "hbm", "achieved": L["achieved"], "peak": peak, "unit": "GB/s", "frac": L["frac"],
+            "peak_kind": peak_kind, "kernel": L["kernel"],
+            "algorithmic_bytes_per_launch": L["algorithmic_bytes_per_launch"], "avg_launch_ms": L["avg_launch_ms"],
+            "traffic": L["traffic"],
+            "traffic_source": "dram bytes of the committed ncu capture (profiles/traffic.json) scaled by the ion count",
+            "launches": launches, "sorts_in_timed_steps": sorts,
+            "ion_pass": {"achieved": both_b / (both_ms / 1e3) / 1e9, "frac": both_b / (both_ms / 1e3) / 1e9 / peak,
+                         "ms_per_step": both_ms / K}}
+
+
 def ions_for(w):
     return w["N"][0] * w["N"][1] * w["N"][2] * w["ppc"]
 
@@ -219,35 +264,106 @@ def run_gpu(args, w, rank, world, dist):
     return res
 
 
+def host_link():
+    """The host link as the bench sees it: pinned 1 GiB copies each way and
+    both ways at once (CUDA events / host clock, best of 3), and the host
+    NUMA node nearest the GPU (cudaDevAttrHostNumaId) beside the NUMA nodes
+    this process may allocate on."""
+    import ctypes as C
+
+    import torch
+
+    out = {}
+    n = 1 << 30
+    h = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(n, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream()
+    for name, dst, src in (("h2d_GBps", d, h), ("d2h_GBps", h, d)):
+        best = 1e30
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            dst.copy_(src, non_blocking=True)
+            e1.record(st)
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        out[name] = n / (best / 1e3) / 1e9
+    # both directions at once (two streams): the host link is nearly duplex
+    h2 = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    d2 = torch.empty(n, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    best = 1e30
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.cuda.stream(s1):
+            d.copy_(h, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+        torch.cuda.synchronize()
+        best = min(best, time.perf_counter() - t0)
+    out["duplex_GBps"] = 2 * n / best / 1e9
+    del h, d, h2, d2
+    try:
+        rt = C.CDLL("libcudart.so")
+    except OSError:
+        try:
+            rt = C.CDLL("/usr/local/cuda/lib64/libcudart.so")
+        except OSError:
+            rt = None
+    if rt is not None:
+        v = C.c_int(-1)
+        if rt.cudaDeviceGetAttribute(C.byref(v), 134, torch.cuda.current_device()) == 0:  # cudaDevAttrHostNumaId
+            out["host_numa_node_of_gpu"] = v.value
+    try:
+        with open("/proc/self/status") as f:
+            for ln in f:
+                if ln.startswith("Mems_allowed_list"):
+                    out["process_numa_nodes"] = ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return out
+
+
 def e2e(args, h, w, step):
-    """Per step, through ch_step_host: host->device copy of the ions (DMSwarm
-    RealVector arrays, pinned), the step, device->host copy of the ions (it
-    starts when the push has moved them and overlaps the deposit and the
-    potential solve), then phi."""
+    """Per step, through ch_step_host: the ions from the host's RealVector
+    arrays (page-locked, from ch_host_alloc) to the device, the step, the
+    ions back into the arrays, then phi into a host array; K >= 10 steps,
+    timed by the host clock around synchronised calls.  The link's own copy
+    rates are measured beside it, so the transfer floor of a step is known."""
     m = chy()
     import torch
 
-    pos, vel = h.download()
-    phi = np.empty(h.N)
-    for a in (pos, vel, phi):
-        m.host_register(a)
-    K = max(1, min(args.steps, args.e2e_steps))
+    HP, HV, HF = m.HostArray((h.np, 4)), m.HostArray((h.np, 4)), m.HostArray((h.N,))
+    pos, vel, phi = HP.a, HV.a, HF.a
+    K = max(1, args.e2e_steps)
     try:
+        h.download(pos, vel)
         h.step_host(pos, vel, step, 1)
         torch.cuda.synchronize()
+        h.reset_profile()
+        h.set_profiling(True)
         t0 = time.perf_counter()
         for s in range(K):
             h.step_host(pos, vel, step + 1 + s, 1)
-            phi[:] = h.phi()
+            h.phi(out=phi)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
+        prof = h.profile()
+        h.set_profiling(False)
+        Bi = pos.nbytes + vel.nbytes
+        Bo = pos.nbytes + vel.nbytes + phi.nbytes
     finally:
-        for a in (pos, vel, phi):
-            m.host_unregister(a)
-    Bi = pos.nbytes + vel.nbytes
-    Bo = pos.nbytes + vel.nbytes + phi.nbytes
+        del pos, vel, phi
+        for a in (HP, HV, HF):
+            a.free()
+    link = host_link()
+    link["sequential_floor_ms_per_step"] = 1e3 * (Bi / (link["h2d_GBps"] * 1e9) + Bo / (link["d2h_GBps"] * 1e9))
+    link["duplex_floor_ms_per_step"] = 1e3 * (Bi + Bo) / (link["duplex_GBps"] * 1e9)
     return {"value": h.np * K / dt, "unit": UNIT, "h2d_bytes_per_step": int(Bi), "d2h_bytes_per_step": int(Bo),
-            "steps": K, "ms_per_step": 1e3 * dt / K}
+            "steps": K, "ms_per_step": 1e3 * dt / K, "link": link,
+            "host_streamed_pushes": prof["host_push_calls"], "reruns": prof["host_push_reruns"],
+            "host_arrays": "ch_host_alloc (page-locked, transparent huge pages)"}
 
 
 # ------------------------------------------------------------------ forms beside the step
@@ -407,53 +523,107 @@ def run_adjoint(fd=True):
 
 
 # ------------------------------------------------------------------ CPU arm
-def cpu_sample(w, threads, np_sample, steps, warmup):
-    """FP64 CPU restatement of the step on the host cores: particle phases
-    timed on np_sample ions, the potential solve on the full grid;
-    particle-steps/s of the full workload = Np / (t_ion * Np / np_sample +
-    t_solve)."""
+# The CPU legs (the reference arm and cpu_baseline) run the FP64 CPU
+# restatement of the step, built from the oracle alone: nothing of the product
+# package is imported or loaded on these legs.
+def oracle_params(w, N, seed=1, run=0):
+    """The workload's plasma on grid N for the FP64 CPU restatement (Jacobi-CG
+    at the workload's rtol; the CPU has no multigrid)."""
+    from oracle import pyoracle as po
+
+    kw = dict(E0=w["E0"], nui=w["nu"], ksp_rtol=w["rtol"], seed=seed, run=run, vi0=w["drift"], pc_type=1,
+              precision=0)
+    if w["nn"]:
+        kw.update(nn_profile=1, nn_center=N[0] / 2.0, nn_sigma=N[0] / 6.0, nn_floor=0.1)
+    return po.default_params(tuple(N), **kw)
+
+
+def oracle_loader(w, seed=1, run=0):
+    from oracle import pyoracle as po
+
+    amp, ph = [0.0, 0.0, 0.0], [0.0, 0.0, 0.0]
+    if w["modes"] == 1:
+        amp[0] = w["amp"]
+    elif w["modes"] == 3:
+        amp = [w["amp"]] * 3
+        ph = po.mode_phases(seed, run)
+    return po.make_loader(amp=tuple(amp), phase=tuple(ph), v0=w["drift"], vT=(1.0, 1.0, 1.0))
+
+
+def sample_grid(w, div):
+    """A sub-box of the workload's grid, 1/div per axis, with the same ions per
+    cell: the same plasma at 1/div^3 of the ions and nodes."""
+    return tuple(max(8, n // div) for n in w["N"])
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith("model name"):
+                    return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+
+    return platform.machine()
+
+
+def cpu_run(w, div, threads, steps, warmup):
+    """The FP64 CPU restatement of the step (push with collisions, move,
+    deposit, RHS and Jacobi-CG solve), run for warmup + steps steps on the
+    sub-box sample_grid(w, div) with `threads` OpenMP threads; every timed
+    step is executed, none is extrapolated."""
     from oracle import pyoracle as po
 
     po.build()
     po.lib().orc_set_threads(threads)
-    p = make_params(w)
-    q = po.params_from(p)
-    q.precision = 0
-    L = make_loader(w)
-    ions = po.load(q, po.make_loader(amp=tuple(L.amp), phase=tuple(L.phase), v0=tuple(L.v0), vT=tuple(L.vT)),
-                   np_sample)
+    N = sample_grid(w, div)
+    q = oracle_params(w, N)
+    nions = N[0] * N[1] * N[2] * w["ppc"]
+    ions = po.load(q, oracle_loader(w), nions)
     run = po.Run(q, ions)
     rc, _ = run.initialize()
-    N = q.Nx * q.Ny * q.Nz
-    t_ion, t_solve = [], []
+    if rc:
+        raise RuntimeError(f"oracle initial solve: status {rc}")
+    times = []
     for s in range(warmup + steps):
         t0 = time.perf_counter()
-        rc, snext, _ = po.update_velocities(q, run.phi, ions, s, run.s.sbar)
-        run.s.sbar = snext
-        po.update_positions(q, ions)
-        po.collect(q, ions, nodes=run.nodes)
+        rc, _ = run.step(s)
         t1 = time.perf_counter()
-        b = po.rhs(q, run.nodes)
-        phi, info = po.solve(q, run.nodes[0::4].copy(), b, phi0=run.phi)
-        run.phi[:] = phi
-        t2 = time.perf_counter()
+        if rc:
+            raise RuntimeError(f"oracle step {s}: status {rc}")
         if s >= warmup:
-            t_ion.append(t1 - t0)
-            t_solve.append(t2 - t1)
-    Np = ions_for(w)
-    per_ion = statistics.mean(t_ion) / np_sample
-    ts = statistics.mean(t_solve)
-    value = Np / (per_ion * Np + ts)
-    return dict(value=value, per_ion_s=per_ion, solve_s=ts, threads=threads, np_sample=np_sample, N=N)
+            times.append(t1 - t0)
+    ms = 1e3 * statistics.mean(times)
+    return dict(value=nions / (ms / 1e3), ms_per_step=ms, ions=nions, grid=N, threads=threads, steps=steps,
+                warmup=warmup, total_s=sum(times))
 
 
-def cpu_desc(c, w):
-    return (f"FP64 CPU restatement (OpenMP, {c['threads']} threads): ion phases timed on {c['np_sample']:,} ions "
-            f"of the {w['N'][0]}x{w['N'][1]}x{w['N'][2]} grid, full-grid potential solve; scaled to "
-            f"{ions_for(w):,} ions as Np/(t_ion*Np + t_solve)")
+def cpu_desc(c, w, kind="all host cores"):
+    g = c["grid"]
+    return (f"FP64 CPU restatement of the step (push with collisions, move, deposit, RHS, Jacobi-CG to rtol "
+            f"{w['rtol']:g}; OpenMP, {c['threads']} thread{'s' if c['threads'] > 1 else ''}, {kind}) on a "
+            f"{g[0]}x{g[1]}x{g[2]} sub-box of the {w['N'][0]}x{w['N'][1]}x{w['N'][2]} workload at the same "
+            f"{w['ppc']} ions/cell ({c['ions']:,} ions): {c['steps']} timed steps after {c['warmup']} warm-up, "
+            f"{c['ms_per_step']:.0f} ms per step, all executed")
 
 
 # ------------------------------------------------------------------ main
+def config_of(args, w, world):
+    """The workload's config, identical in both arms."""
+    return {"workload": args.workload, "grid": list(w["N"]), "ions": ions_for(w), "ions_per_cell": w["ppc"],
+            "precision": w["precision"], "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+            "l2": "inputs larger than L2 (ion state 4.3 GB)", "ksp_rtol": w["rtol"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -462,9 +632,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-ions", type=int, default=1 << 22)
+    ap.add_argument("--cpu-div", type=int, default=2,
+                    help="CPU legs run a sub-box of 1/div of the grid per axis at the same ions per cell")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form comparison line")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble (ch_batch) measurement")
     ap.add_argument("--ensemble-steps", type=int, default=10)
@@ -474,30 +645,31 @@ def main():
     w = WORKLOADS[args.workload]
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+
+    if args.impl == "reference":
+        # the reference's PETSc build is unavailable (no PETSc, MPI or HDF5);
+        # its CPU algorithm is the FP64 restatement, timed on the host cores
+        # by rank 0 alone, every step executed
+        if rank != 0:
+            return
+        threads = os.cpu_count() or 1
+        c = cpu_run(w, args.cpu_div, threads, max(1, args.steps), max(0, args.warmup))
+        line = {"metric": METRIC, "value": c["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": c["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+                "config": config_of(args, w, world),
+                "cpu_baseline": {"value": c["value"], "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": cpu_desc(c, w), "cpu_model": cpu_model(),
+                                 "timed_s": c["total_s"]},
+                "e2e": {"value": c["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
     dist = None
     if world > 1:
         import torch.distributed as dist  # noqa: F811
 
         dist.init_process_group("gloo")
-    threads = os.cpu_count() or 1
-
-    if args.impl == "reference":
-        if rank == 0:
-            c = cpu_sample(w, threads, args.cpu_ions, max(1, args.steps), max(0, min(args.warmup, 1)))
-            line = {"metric": METRIC, "value": c["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-                    "warmup": args.warmup, "ms_per_step": 1e3 * ions_for(w) / c["value"],
-                    "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                    "data": "synthetic", "impl": "reference",
-                    "config": {"workload": args.workload, "grid": list(w["N"]), "ions": ions_for(w),
-                               "precision": "fp64"},
-                    "cpu_baseline": {"value": c["value"], "unit": UNIT, "cores": threads, "kind": "port",
-                                     "sample": cpu_desc(c, w)},
-                    "e2e": {"value": c["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-            print(json.dumps(line), flush=True)
-        if dist:
-            dist.destroy_process_group()
-        return
-
     r = run_gpu(args, w, rank, world, dist)
     fp64 = None
     if not args.no_fp64 and w["precision"] == "mixed" and rank == 0:
@@ -517,41 +689,13 @@ def main():
     prof = r["prof"]
     peak, peak_kind = measured_peak()
     N = w["N"][0] * w["N"][1] * w["N"][2]
-    # A step's pass is two launches: push + collisions + move (the dominant
-    # kernel: reads and writes the ion state, reads the node field), then
-    # the deposit (reads the ion state, writes the moment accumulators).
-    steps_timed = max(1, prof["pass_calls"] - prof["deposit_calls"])
-    push_ms = (prof["pass_ms"] - prof["deposit_ms"]) / steps_timed
-    dep_ms = prof["deposit_ms"] / max(1, prof["deposit_calls"])
-    if w["precision"] == "mixed":
-        alg = r["np"] * 64 + N * 16
-        alg_dep = r["np"] * 32 + N * 32
-        kname = "k_pass_tiled<PUSH|MOVE>"
-    else:
-        alg = r["np"] * 104 + N * 24
-        alg_dep = r["np"] * 52 + N * 32
-        kname = "k_pass_f64<PUSH|MOVE>"
-    achieved = alg / (push_ms / 1e3) / 1e9
-    tr = committed_traffic(kname)
-    tr_dep = committed_traffic("k_pass_tiled<DEPOSIT>") if w["precision"] == "mixed" else None
+    roof = pass_roofline(w, r, prof, N, K, peak, peak_kind)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if w["precision"] == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "grid": list(w["N"]), "ions": r["np"], "ions_per_cell": w["ppc"],
-                   "precision": w["precision"], "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
-                   "l2": "inputs larger than L2 (ion state 4.3 GB)", "ksp_rtol": w["rtol"]},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "kernel": kname, "algorithmic_bytes_per_launch": alg,
-                     "avg_launch_ms": push_ms,
-                     "deposit_kernel": {"algorithmic_bytes_per_launch": alg_dep, "avg_launch_ms": dep_ms,
-                                        "achieved": alg_dep / (dep_ms / 1e3) / 1e9 if dep_ms > 0 else None,
-                                        "traffic": (tr_dep["dram_bytes_per_launch"] * r["np"] / tr_dep["ions"]
-                                                    if isinstance(tr_dep, dict) else None)},
-                     "traffic": (tr["dram_bytes_per_launch"] * r["np"] / tr["ions"]
-                                 if isinstance(tr, dict) and "dram_bytes_per_launch" in tr else None),
-                     "traffic_source": (f"ncu capture of {tr['ions']:,} ions scaled by the ion count"
-                                        if isinstance(tr, dict) else None)},
+        "config": config_of(args, w, world),
+        "roofline": roof,
         "phase_ms_per_step": {k.replace("_ms", ""): prof[k] / K for k in ("pass_ms", "solve_ms", "sort_ms",
                                                                           "moments_ms")},
         "solve": {"iterations_last": r["infos"][-1]["iterations"], "refinements_last": r["infos"][-1]["refinements"],
@@ -568,6 +712,8 @@ def main():
         line["e2e"] = {k: e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")}
         line["e2e"]["value"] *= world
         line["e2e"]["ms_per_step"] = e["ms_per_step"]
+        for k in ("steps", "link", "host_streamed_pushes", "reruns", "host_arrays"):
+            line["e2e"][k] = e[k]
     if not args.no_fp64 and w["precision"] == "mixed":
         line["errors_vs_fp64"] = errors_vs_fp64(w)
     if not args.no_ensemble:
@@ -575,9 +721,14 @@ def main():
     if not args.no_adjoint:
         line["adjoint"] = run_adjoint(fd=not args.no_adjoint_fd)
     if not args.no_cpu:
-        c = cpu_sample(w, os.cpu_count() or 1, args.cpu_ions, 1, 0)
+        # all host cores (the reference arm's leg, 3 timed steps), and one
+        # core on a sub-box of 1/4 per axis (the reference's serial loops)
+        c = cpu_run(w, args.cpu_div, os.cpu_count() or 1, 3, 1)
+        c1 = cpu_run(w, 2 * args.cpu_div, 1, 2, 1)
         line["cpu_baseline"] = {"value": c["value"], "unit": UNIT, "cores": c["threads"], "kind": "port",
-                                "sample": cpu_desc(c, w)}
+                                "sample": cpu_desc(c, w), "cpu_model": cpu_model(),
+                                "single_thread": {"value": c1["value"], "unit": UNIT, "cores": 1,
+                                                  "sample": cpu_desc(c1, w, "one core")}}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -128,7 +128,8 @@ class Profile(C.Structure):
     _fields_ = [("pass_ms", C.c_double), ("pass_calls", C.c_int64), ("solve_ms", C.c_double),
                 ("solve_calls", C.c_int64), ("sort_ms", C.c_double), ("sort_calls", C.c_int64),
                 ("moments_ms", C.c_double), ("moments_calls", C.c_int64), ("launches", C.c_int64),
-                ("deposit_ms", C.c_double), ("deposit_calls", C.c_int64)]
+                ("deposit_ms", C.c_double), ("deposit_calls", C.c_int64), ("host_push_calls", C.c_int64),
+                ("host_push_reruns", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -174,6 +175,8 @@ def lib():
             "ch_output_wait": [vp, C.POINTER(C.c_int64)],
             "ch_set_solver": [vp, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32],
             "ch_host_register": [vp, C.c_uint64],
+            "ch_host_alloc": [C.c_uint64, C.POINTER(vp)],
+            "ch_host_free": [vp],
             "ch_host_unregister": [vp],
             "ch_batch_create": [vp, vp, C.c_int32, C.c_int32, C.POINTER(vp)],
             "ch_batch_destroy": [vp],
@@ -364,8 +367,10 @@ class Hybrid:
         nodes = np.ascontiguousarray(nodes, dtype=np.float64).reshape(self.N, 4)
         _check(lib().ch_set_moments(self._h, nodes.ctypes.data))
 
-    def phi(self):
-        out = np.empty(self.N)
+    def phi(self, out: np.ndarray | None = None):
+        if out is None:
+            out = np.empty(self.N)
+        assert out.dtype == np.float64 and out.size == self.N and out.flags.c_contiguous
         _check(lib().ch_get_phi(self._h, out.ctypes.data))
         return out
 
@@ -609,3 +614,30 @@ def host_register(a: np.ndarray):
 
 def host_unregister(a: np.ndarray):
     _check(lib().ch_host_unregister(a.ctypes.data))
+
+
+class HostArray:
+    """A numpy array in page-locked host memory from ch_host_alloc (the
+    memory the GPU streams at the full host-link rate); free() or leaving
+    the with-block releases it, after which the array must not be used."""
+
+    def __init__(self, shape, dtype=np.float64):
+        dt = np.dtype(dtype)
+        n = int(np.prod(shape)) * dt.itemsize
+        p = C.c_void_p()
+        _check(lib().ch_host_alloc(n, C.byref(p)))
+        self._p = p
+        buf = (C.c_char * n).from_address(p.value)
+        self.a = np.frombuffer(buf, dtype=dt).reshape(shape)
+
+    def free(self):
+        if self._p is not None and self._p.value:
+            self.a = None
+            _check(lib().ch_host_free(self._p))
+            self._p = None
+
+    def __enter__(self):
+        return self.a
+
+    def __exit__(self, *exc):
+        self.free()

@@ -12,6 +12,8 @@
 #include <condition_variable>
 #include <deque>
 #include <mutex>
+#include <sys/mman.h>
+#include <unistd.h>
 #include <new>
 #include <string>
 #include <vector>
@@ -98,6 +100,9 @@ struct ch_ctx {
   // into mapped host arrays; valid until the order changes (sort, load)
   uint32_t* slot_of_id = nullptr;
   bool slot_map_valid = false;
+  // the ions as a host-streaming push read them (k_host_push), kept so that
+  // the step can be run again the ordinary way if their S differs
+  MixParticles HB{};
   // download of registered arrays: conversion chunks on `stream`, their
   // downloads: id-order conversion on conv_stream, copies to the host on
   // copy_stream (chunk_ev[k]: chunk k converted)
@@ -242,9 +247,10 @@ static GridDesc make_grid(const ch_params& p) {
 static void free_particles(ch_ctx* c) {
   void* v[] = {c->P.x, c->P.y, c->P.z, c->P.vx, c->P.vy, c->P.vz, c->P.id, c->Q.x, c->Q.y, c->Q.z, c->Q.vx,
                c->Q.vy, c->Q.vz, c->Q.id, c->M.pos, c->M.vel, c->MQ.pos, c->MQ.vel, c->keys, c->stage_pos,
-               c->stage_vel, c->part, c->slot_of_id};
+               c->stage_vel, c->part, c->slot_of_id, c->HB.pos, c->HB.vel};
   for (void* q : v)
     if (q) cudaFree(q);
+  c->HB = MixParticles{};
   c->slot_of_id = nullptr;
   c->slot_map_valid = false;
   c->P = F64Particles{};
@@ -809,6 +815,122 @@ static ch_status run_steps(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_ste
   return CH_OK;
 }
 
+// The push launch of a step of ch_step_host whose ions the host holds
+// (registered arrays, mixed form, ions in the id order of the last
+// transfer): k_host_push reads them (read) and/or writes the step's result
+// back (write) over the host link while it pushes, both directions at once.
+// It uses S of the previous step.  When the ions it read give another S (the
+// host changed velocities since the last transfer), it puts the uploaded ions
+// back into M, takes their S and sets *redo: the caller then runs the push
+// the ordinary way.
+static ch_status run_host_push(ch_ctx* c, int64_t step, ch_step_info* info, bool count_cells, bool read, bool write,
+                               void* dp, void* dv, bool* redo) {
+  *redo = false;
+  StepConsts k = consts(c, step);
+  launch_node_efield(true, c->g, k.tscale, c->phi, c->E64, c->E32, c->sms, c->stream);
+  CH_CUDA_OK(cudaMemsetAsync(c->cnt, 0, sizeof(DevCounters), c->stream));
+  const int64_t Nc = k.collide ? collision_count(c->p, c->np) : 0;
+  if (read && !c->HB.pos) {
+    CH_CUDA_OK(cudaMalloc(&c->HB.pos, sizeof(float4) * c->np));
+    CH_CUDA_OK(cudaMalloc(&c->HB.vel, sizeof(float4) * c->np));
+    c->HB.np = c->np;
+  }
+  if (!read && !c->slot_map_valid) {  // a sort earlier in the call changed the order
+    launch_slot_map(c->M, c->slot_of_id, c->sms, c->stream);
+    c->slot_map_valid = true;
+  }
+  uint32_t* hist = nullptr;
+  if (count_cells) {
+    CH_CUDA_OK(cudaMemsetAsync(c->counts, 0, sizeof(uint32_t) * c->g.N, c->stream));
+    hist = c->counts;
+  }
+  prof_begin(c);
+  const int nb = launch_host_push(k, dp, dv, c->slot_of_id, c->M, c->HB, c->E32, (double)Nc, c->sbar, hist, read,
+                                  write, c->cnt, c->part, c->sms, c->stream);
+  prof_end(c, &c->pr.pass_ms, &c->pr.pass_calls);
+  launch_reduce_partials(c->part, nb, 3, c->red, c->stream);
+  CH_CUDA_OK(cudaMemcpyAsync(c->hred, c->red, sizeof(double) * 3, cudaMemcpyDeviceToHost, c->stream));
+  CH_CUDA_OK(cudaMemcpyAsync(c->hcnt, c->cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, c->stream));
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  c->pr.host_push_calls++;
+  if (read && k.collide && c->hred[2] != c->sbar) {
+    c->pr.host_push_reruns++;
+    CH_CUDA_OK(cudaMemcpyAsync(c->M.pos, c->HB.pos, sizeof(float4) * c->np, cudaMemcpyDeviceToDevice, c->stream));
+    CH_CUDA_OK(cudaMemcpyAsync(c->M.vel, c->HB.vel, sizeof(float4) * c->np, cudaMemcpyDeviceToDevice, c->stream));
+    c->sbar = c->hred[2];
+    *redo = true;
+    return CH_OK;
+  }
+  if (k.collide) c->sbar = c->hred[1];
+  if (info) {
+    info->Nc = Nc;
+    info->collisions = (int64_t)c->hcnt->collisions;
+    info->refused = (int64_t)c->hcnt->refused;
+    info->expected = c->hred[0];
+  }
+  if (k.collide && c->hcnt->refused >= 10)
+    return ch_fail(CH_ERR_COLLISION_LIMIT, "%llu collisions refused in step %lld (src/particles.c:603-605)",
+                   (unsigned long long)c->hcnt->refused, (long long)step);
+  c->since_sort++;
+  return CH_OK;
+}
+
+// ch_step_host's steps when the ions the host holds are in the id order of
+// the last transfer through registered arrays (mixed form): the first step's
+// push reads them straight from the host arrays and the last step's push
+// writes the result back, so the upload and the download share the link
+// instead of following each other.
+static ch_status run_steps_host(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_step_info* info, void* dp,
+                                void* dv, ch_real_vector* pos, ch_real_vector* vel) {
+  ch_step_info local;
+  bool enqueued = false;
+  for (int32_t s = 0; s < nsteps; ++s) {
+    memset(&local, 0, sizeof(local));
+    const bool sort_due = c->p.sort_period > 0 && c->since_sort + 1 >= c->p.sort_period;
+    const bool read = s == 0, write = s + 1 == nsteps;
+    bool redo = false, written = false;
+    ch_status rc = CH_OK;
+    if (read || write) {
+      rc = run_host_push(c, first_step + s, &local, sort_due, read, write, dp, dv, &redo);
+      written = write && !redo;
+    }
+    if (!rc && ((!read && !write) || redo)) rc = run_pass(c, PH_PUSH | PH_MOVE, first_step + s, &local, sort_due);
+    const bool download = write && !written;
+    if (!rc && download && !sort_due) {
+      rc = download_enqueue(c, c->M, !c->slot_map_valid, pos, vel);
+      enqueued = true;
+    }
+    if (!rc && sort_due) rc = run_deposit_sort(c);
+    else if (!rc) rc = run_pass(c, PH_DEPOSIT, 0, nullptr);
+    if (!rc && download && sort_due) {
+      rc = download_enqueue(c, c->MQ, true, pos, vel);
+      enqueued = true;
+    }
+    if (rc) return rc;
+    rc = finalize_moments(c, &local);
+    if (rc) return rc;
+    rc = potential(c, &local.solve);
+    if (rc) return rc;
+    if (sort_due) {
+      std::swap(c->M, c->MQ);
+      std::swap(c->starts, c->starts_next);
+      c->since_sort = 0;
+      c->slot_map_valid = false;
+    }
+  }
+  if (enqueued) {
+    CH_CUDA_OK(cudaStreamSynchronize(c->copy_stream));
+    c->slot_map_valid = true;  // download_enqueue rebuilt it from the current order
+  } else if (!c->slot_map_valid) {
+    launch_slot_map(c->M, c->slot_of_id, c->sms, c->stream);
+    c->slot_map_valid = true;
+  }
+  CH_CUDA_OK(cudaStreamSynchronize(c->stream));
+  prof_flush(c);
+  if (info) *info = local;
+  return CH_OK;
+}
+
 extern "C" ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_step_info* info) {
   return run_steps(c, first_step, nsteps, info);
 }
@@ -818,9 +940,18 @@ extern "C" ch_status ch_step_host(ch_ctx* c, int64_t first_step, int32_t nsteps,
   if (!c || !pos || !vel) return ch_fail(CH_ERR_ARG, "ch_step_host: null argument");
   if (c->np == 0) return ch_fail(CH_ERR_STATE, "no ions");
   if (nsteps < 1) return ch_fail(CH_ERR_ARG, "nsteps < 1");
+  const uint64_t bytes = sizeof(double4_32a) * (uint64_t)c->np;
+  if (c->mixed && c->slot_map_valid && c->solved_once) {
+    void* dp = device_view(pos, bytes, 16);
+    void* dv = device_view(vel, bytes, 16);
+    if (dp && dv) {
+      ch_status rh = run_steps_host(c, first_step, nsteps, info, dp, dv, pos, vel);
+      if (rh && c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+      return rh;
+    }
+  }
   ch_status rc = ch_particles_upload(c, pos, vel, c->np);
   if (rc) return rc;
-  const uint64_t bytes = sizeof(double4_32a) * (uint64_t)c->np;
   const bool overlap = c->mixed && device_view(pos, bytes, 16) && device_view(vel, bytes, 16);
   if (!overlap) {
     rc = run_steps(c, first_step, nsteps, info);
@@ -904,6 +1035,70 @@ extern "C" ch_status ch_host_unregister(void* ptr) {
       }
   }
   CH_CUDA_OK(cudaHostUnregister(ptr));
+  return CH_OK;
+}
+
+// Allocations of ch_host_alloc: anonymous mappings backed by transparent
+// huge pages where the kernel offers them, page-locked and mapped for the
+// GPU.  The GPU reads and writes host memory through its own page tables;
+// a range of huge pages keeps them few and contiguous, so the link runs at
+// its full rate however fragmented free memory has become (registered base
+// pages of an ordinary allocation, scattered after heavy allocation churn,
+// were measured 10 to 30 times slower).
+struct HostAlloc {
+  char* p;
+  uint64_t n;
+};
+static std::vector<HostAlloc> g_ha;
+
+extern "C" ch_status ch_host_alloc(uint64_t bytes, void** out) {
+  if (!out || !bytes) return ch_fail(CH_ERR_ARG, "null argument");
+  *out = nullptr;
+  void* p = mmap(nullptr, bytes, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+  if (p == MAP_FAILED)
+    return ch_fail(CH_ERR_NOMEM, "ch_host_alloc: mmap of %llu bytes failed", (unsigned long long)bytes);
+#ifdef MADV_HUGEPAGE
+  madvise(p, bytes, MADV_HUGEPAGE);  // advisory: base pages where huge ones are not offered
+#endif
+  // touch every page now, so that the pinning below finds them in place
+  const long pg = sysconf(_SC_PAGESIZE) > 0 ? sysconf(_SC_PAGESIZE) : 4096;
+  for (uint64_t o = 0; o < bytes; o += (uint64_t)pg) static_cast<volatile char*>(p)[o] = 0;
+  cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
+  void* d = nullptr;
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer(&d, p, 0);
+  if (e != cudaSuccess) {
+    cudaHostUnregister(p);
+    cudaGetLastError();
+    munmap(p, bytes);
+    return ch_cuda_fail(e, "ch_host_alloc: cudaHostRegister", __FILE__, __LINE__);
+  }
+  std::lock_guard<std::mutex> lk(g_hr_mu);
+  g_hr.push_back(HostRange{static_cast<char*>(p), bytes, static_cast<char*>(d)});
+  g_ha.push_back(HostAlloc{static_cast<char*>(p), bytes});
+  *out = p;
+  return CH_OK;
+}
+
+extern "C" ch_status ch_host_free(void* ptr) {
+  if (!ptr) return CH_OK;
+  uint64_t n = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_hr_mu);
+    for (size_t i = 0; i < g_ha.size(); ++i)
+      if (g_ha[i].p == ptr) {
+        n = g_ha[i].n;
+        g_ha.erase(g_ha.begin() + (long)i);
+        break;
+      }
+    if (!n) return ch_fail(CH_ERR_ARG, "ch_host_free: not an allocation of ch_host_alloc");
+    for (size_t i = 0; i < g_hr.size(); ++i)
+      if (g_hr[i].p == ptr) {
+        g_hr.erase(g_hr.begin() + (long)i);
+        break;
+      }
+  }
+  CH_CUDA_OK(cudaHostUnregister(ptr));
+  munmap(ptr, n);
   return CH_OK;
 }
 

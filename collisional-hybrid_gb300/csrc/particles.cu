@@ -712,9 +712,58 @@ __device__ __forceinline__ void tile_move_ion(const StepConsts& c, float4& p, co
   p = make_float4(ox, oy, oz, __uint_as_float(cell));
 }
 
+// The 8 node-field values around cell (i, j, k) from global memory.
+__device__ __forceinline__ void tile_gather_global(const GridDesc& g, const float4* __restrict__ E, int i, int j, int k,
+                                                   float4& e000, float4& e100, float4& e010, float4& e110,
+                                                   float4& e001, float4& e101, float4& e011, float4& e111) {
+  const int ii1 = i + 1 == g.Nx ? 0 : i + 1, jj1 = j + 1 == g.Ny ? 0 : j + 1, kk1 = k + 1 == g.Nz ? 0 : k + 1;
+  const int64_t r00 = ((int64_t)k * g.Ny + j) * g.Nx, r10 = ((int64_t)k * g.Ny + jj1) * g.Nx,
+                r01 = ((int64_t)kk1 * g.Ny + j) * g.Nx, r11 = ((int64_t)kk1 * g.Ny + jj1) * g.Nx;
+  e000 = __ldg(E + r00 + i); e100 = __ldg(E + r00 + ii1); e010 = __ldg(E + r10 + i);
+  e110 = __ldg(E + r10 + ii1); e001 = __ldg(E + r01 + i); e101 = __ldg(E + r01 + ii1);
+  e011 = __ldg(E + r11 + i); e111 = __ldg(E + r11 + ii1);
+}
+
+// Trilinear gather of the node field (premultiplied by (q/m) dt/2) at the
+// in-cell offsets of p, then the Boris push of v (src/particles.c:374-447);
+// every kernel of the mixed form that pushes an ion calls this, so they
+// agree bit for bit.
+__device__ __forceinline__ void tile_boris(const StepConsts& c, const float4& e000, const float4& e100,
+                                           const float4& e010, const float4& e110, const float4& e001,
+                                           const float4& e101, const float4& e011, const float4& e111,
+                                           const float4& p, bool cross, float v[3]) {
+  const float t0 = c.f.t[0], t1 = c.f.t[1], t2 = c.f.t[2];
+  const float s0 = c.f.s[0], s1 = c.f.s[1], s2 = c.f.s[2];
+  const float wx = p.x, wy = p.y, wz = p.z;
+  float Ef[3];
+#define LERP3(f, d)                                                                \
+{                                                                                \
+  const float wll = e000.f + wy * (e010.f - e000.f);                             \
+  const float wlh = e100.f + wy * (e110.f - e100.f);                             \
+  const float whl = e001.f + wy * (e011.f - e001.f);                             \
+  const float whh = e101.f + wy * (e111.f - e101.f);                             \
+  const float ezl = wll + wx * (wlh - wll), ezh = whl + wx * (whh - whl);        \
+  Ef[d] = ezl + wz * (ezh - ezl);                                                \
+}
+  LERP3(x, 0) LERP3(y, 1) LERP3(z, 2)
+#undef LERP3
+  if (c.push_E0) { Ef[0] += c.f.pE0[0]; Ef[1] += c.f.pE0[1]; Ef[2] += c.f.pE0[2]; }
+  // Boris with E premultiplied by (q/m) dt/2
+  const float vm0 = v[0] + Ef[0], vm1 = v[1] + Ef[1], vm2 = v[2] + Ef[2];
+  float vp0 = vm0, vp1 = vm1, vp2 = vm2;
+  if (cross) {
+    const float q0 = vm0 + (vm1 * t2 - vm2 * t1);
+    const float q1 = vm1 + (vm2 * t0 - vm0 * t2);
+    const float q2 = vm2 + (vm0 * t1 - vm1 * t0);
+    vp0 = vm0 + (q1 * s2 - q2 * s1);
+    vp1 = vm1 + (q2 * s0 - q0 * s2);
+    vp2 = vm2 + (q0 * s1 - q1 * s0);
+  }
+  v[0] = vp0 + Ef[0]; v[1] = vp1 + Ef[1]; v[2] = vp2 + Ef[2];
+}
+
 __device__ __forceinline__ float tile_gmean(const StepConsts& c, const float v[3]) {
-  const float qx = v[0] - c.f.vn0[0], qy = v[1] - c.f.vn0[1], qz = v[2] - c.f.vn0[2];
-  return ch_gmean<float>(ch_qsqrt(qx * qx + qy * qy + qz * qz), c.f.vnT);
+  return ch_gmean<float>(ch_relspeed_rn(v[0], v[1], v[2], c.f.vn0[0], c.f.vn0[1], c.f.vn0[2]), c.f.vnT);
 }
 
 // One drain round of the calling warp's ring of deferred ions (warp-uniform
@@ -805,8 +854,6 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
   const GridDesc& g = c.g;
   const int lane = threadIdx.x & 31;
   const unsigned wbase = (threadIdx.x >> 5) * CH_TILE_QW;
-  const float t0 = c.f.t[0], t1 = c.f.t[1], t2 = c.f.t[2];
-  const float s0 = c.f.s[0], s1 = c.f.s[1], s2 = c.f.s[2];
   const bool cross = !(c.faithful & CH_FAITHFUL_D2);
   const bool move = (PH & PH_MOVE) && !(c.faithful & CH_FAITHFUL_D5);
   const bool collide = (PH & PH_PUSH) && c.collide;
@@ -920,39 +967,9 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
         e001 = sh.E[q + BX * BY]; e101 = sh.E[q + BX * BY + 1]; e011 = sh.E[q + BX * BY + BX];
         e111 = sh.E[q + BX * BY + BX + 1];
       } else {
-        const int ii1 = i + 1 == g.Nx ? 0 : i + 1, jj1 = j + 1 == g.Ny ? 0 : j + 1, kk1 = k + 1 == g.Nz ? 0 : k + 1;
-        const int64_t r00 = ((int64_t)k * g.Ny + j) * g.Nx, r10 = ((int64_t)k * g.Ny + jj1) * g.Nx,
-                      r01 = ((int64_t)kk1 * g.Ny + j) * g.Nx, r11 = ((int64_t)kk1 * g.Ny + jj1) * g.Nx;
-        e000 = __ldg(E + r00 + i); e100 = __ldg(E + r00 + ii1); e010 = __ldg(E + r10 + i);
-        e110 = __ldg(E + r10 + ii1); e001 = __ldg(E + r01 + i); e101 = __ldg(E + r01 + ii1);
-        e011 = __ldg(E + r11 + i); e111 = __ldg(E + r11 + ii1);
+        tile_gather_global(g, E, i, j, k, e000, e100, e010, e110, e001, e101, e011, e111);
       }
-      const float wx = p.x, wy = p.y, wz = p.z;
-      float Ef[3];
-#define LERP3(f, d)                                                                \
-{                                                                                \
-  const float wll = e000.f + wy * (e010.f - e000.f);                             \
-  const float wlh = e100.f + wy * (e110.f - e100.f);                             \
-  const float whl = e001.f + wy * (e011.f - e001.f);                             \
-  const float whh = e101.f + wy * (e111.f - e101.f);                             \
-  const float ezl = wll + wx * (wlh - wll), ezh = whl + wx * (whh - whl);        \
-  Ef[d] = ezl + wz * (ezh - ezl);                                                \
-}
-      LERP3(x, 0) LERP3(y, 1) LERP3(z, 2)
-#undef LERP3
-      if (c.push_E0) { Ef[0] += c.f.pE0[0]; Ef[1] += c.f.pE0[1]; Ef[2] += c.f.pE0[2]; }
-      // Boris (src/particles.c:374-447) with E premultiplied by (q/m) dt/2
-      const float vm0 = v[0] + Ef[0], vm1 = v[1] + Ef[1], vm2 = v[2] + Ef[2];
-      float vp0 = vm0, vp1 = vm1, vp2 = vm2;
-      if (cross) {
-        const float q0 = vm0 + (vm1 * t2 - vm2 * t1);
-        const float q1 = vm1 + (vm2 * t0 - vm0 * t2);
-        const float q2 = vm2 + (vm0 * t1 - vm1 * t0);
-        vp0 = vm0 + (q1 * s2 - q2 * s1);
-        vp1 = vm1 + (q2 * s0 - q0 * s2);
-        vp2 = vm2 + (q0 * s1 - q1 * s0);
-      }
-      v[0] = vp0 + Ef[0]; v[1] = vp1 + Ef[1]; v[2] = vp2 + Ef[2];
+      tile_boris(c, e000, e100, e010, e110, e001, e101, e011, e111, p, cross, v);
       if (collide) {
         const float gi = tile_gmean(c, v);
         float nd = 1.0f;
@@ -1162,8 +1179,7 @@ __global__ void k_sbar_mixed(MixParticles P, float vnT, float vn0x, float vn0y, 
   double s[1] = {0.0};
   for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
     const float4 v = P.vel[ip];
-    const float wx = v.x - vn0x, wy = v.y - vn0y, wz = v.z - vn0z;
-    s[0] += (double)g_fixed(ch_gmean<float>(ch_qsqrt(wx * wx + wy * wy + wz * wz), vnT)) * CH_G_UNIT;
+    s[0] += (double)g_fixed(ch_gmean<float>(ch_relspeed_rn(v.x, v.y, v.z, vn0x, vn0y, vn0z), vnT)) * CH_G_UNIT;
   }
   block_partials<1>(s, part);
 }
@@ -1532,6 +1548,156 @@ __global__ void __launch_bounds__(256) k_host_to_mixed(GridDesc g, const double2
     }
     __syncwarp();
   }
+}
+
+// One step's push, collisions and move of ions held by the host in id order
+// (registered RealVector arrays, read and written in place over the host
+// link).  Warp w takes ions i0 .. i0+31: with `read` its lanes load the
+// chunk's 1 KB of positions and velocities one chunk ahead (in registers,
+// so the next chunk travels over the link while this one is pushed), put it
+// in shared memory, pack each ion into the mixed form and keep a copy in B
+// (the ions as uploaded); otherwise they take the ions from their slots in
+// P.  Each lane then pushes its ion with the arithmetic of the tiled pass
+// (tile_gather_global, tile_boris, the same collision draws and rounds,
+// tile_move_ion), stores it back into its slot of P for the deposit and,
+// with `write`, puts the FP64 result into shared memory, which the warp
+// writes out over the link 512 contiguous bytes per instruction.  The link
+// carries the upload and the download at once (about 1.6x the rate of one
+// direction).  Block partials: the expected events, S of the pushed
+// velocities (for the next step) and S of the velocities read, integer sums
+// of 2^-20 units, exact in any order.
+__global__ void __launch_bounds__(256, 2) k_host_push(StepConsts c, double2* pos, double2* vel,
+                                                      const uint32_t* __restrict__ slot_of_id, MixParticles P,
+                                                      MixParticles B, const float4* __restrict__ E, float pscale,
+                                                      uint32_t* hist, int read, int write, DevCounters* cnt,
+                                                      double* part) {
+  __shared__ double2 bp[8][64], bv[8][64];
+  const GridDesc& g = c.g;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const bool cross = !(c.faithful & CH_FAITHFUL_D2);
+  const bool move = !(c.faithful & CH_FAITHFUL_D5);
+  float tsum = 0.0f;
+  unsigned long long gsum = 0ull, ssum = 0ull;
+  unsigned ncol = 0, nref = 0;
+  double2 rp0 = make_double2(0.0, 0.0), rp1 = rp0, rv0 = rp0, rv1 = rp0;
+  auto fetch = [&](int64_t c0) {
+    if (read && c0 < P.np) {
+      const int64_t m2 = 2 * (P.np - c0 < 32 ? P.np - c0 : 32);
+      if (lane < m2) { rp0 = pos[2 * c0 + lane]; rv0 = vel[2 * c0 + lane]; }
+      if (lane + 32 < m2) { rp1 = pos[2 * c0 + lane + 32]; rv1 = vel[2 * c0 + lane + 32]; }
+    }
+  };
+  int64_t i0 = (blockIdx.x * (int64_t)(blockDim.x >> 5) + w) * 32;
+  fetch(i0);
+  for (; i0 < P.np; i0 += nw * 32) {
+    const int64_t n2 = 2 * (P.np - i0 < 32 ? P.np - i0 : 32);  // 16-byte words of this chunk
+    if (read) {
+      if (lane < n2) { bp[w][lane] = rp0; bv[w][lane] = rv0; }
+      if (lane + 32 < n2) { bp[w][lane + 32] = rp1; bv[w][lane + 32] = rv1; }
+      fetch(i0 + nw * 32);
+    }
+    __syncwarp();
+    const int64_t ia = i0 + lane;
+    const bool active = ia < P.np;
+    uint32_t slot = 0;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f), vv = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) {
+      slot = slot_of_id[ia];
+      if (read) {
+        const double2 p0 = bp[w][2 * lane], p1 = bp[w][2 * lane + 1], v0 = bv[w][2 * lane], v1 = bv[w][2 * lane + 1];
+        const double sx[3] = {p0.x, p0.y, p1.x};
+        p = pack_mixed(g, sx);
+        vv = make_float4((float)v0.x, (float)v0.y, (float)v1.x, __uint_as_float((uint32_t)ia));
+        B.pos[slot] = p;
+        B.vel[slot] = vv;
+      } else {
+        p = P.pos[slot];
+        vv = P.vel[slot];
+      }
+    }
+    const uint32_t cell = __float_as_uint(p.w);
+    int i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1), k = cell >> (CH_PACK_BX + CH_PACK_BY);
+    float v[3] = {vv.x, vv.y, vv.z};
+    if (active) {
+      if (read && c.collide) ssum += g_fixed(tile_gmean(c, v));
+      float4 e000, e100, e010, e110, e001, e101, e011, e111;
+      tile_gather_global(g, E, i, j, k, e000, e100, e010, e110, e001, e101, e011, e111);
+      tile_boris(c, e000, e100, e010, e110, e001, e101, e011, e111, p, cross, v);
+      if (c.collide) {
+        const float gi = tile_gmean(c, v);
+        float nd = 1.0f;
+        if (c.nn_profile == CH_NN_GAUSSIAN_X)
+          nd = ch_neutral_density<float>(c, (float)(g.x0 + ((double)i + (double)p.x) * g.dx));
+        const float lscale = pscale * nd;
+        const float lam = lscale * gi;
+        tsum += lam;
+        const uint32_t id = __float_as_uint(vv.w);
+        const U4 r0 = ch_philox(id, c.step, CH_PURPOSE_COLLIDE << 24, c.run, c.seed_lo, c.seed_hi);
+        const float u0 = ch_unitf(r0.x);
+        bool defer = false;
+        float qt = 0.0f;
+        if (lam > 0.0f && u0 > __expf(-lam)) {
+          qt = ch_qdiv(-ch_log(u0), lam);
+          defer = qt < 1.0f;
+        }
+        if (defer) {
+          // the event process of the tiled pass's rings, run to its end here
+          uint32_t qe = 0, qit = 0;
+          float gf = 0.0f;
+          while (!ch_collide_round<float>(c, id, lscale, v, qt, qe, qit, &ncol, &nref, gf)) {
+          }
+          gsum += g_fixed(gf);
+        } else {
+          gsum += g_fixed(gi);
+        }
+      }
+      vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
+      if (move) tile_move_ion(c, p, v, i, j, k);
+      P.pos[slot] = p;
+      P.vel[slot] = vv;
+    }
+    if (hist) {
+      const uint32_t rk = agg_inc(hist, (uint32_t)(((int64_t)k * g.Ny + j) * g.Nx + i), active);
+      if (active && P.rank) P.rank[slot] = rk;
+    }
+    __syncwarp();  // every lane has read its ion from the buffers before they are refilled
+    if (write) {
+      if (active) {
+        const uint32_t cw = __float_as_uint(p.w);
+        const int ci = cw & (CH_MAX_NX - 1), cj = (cw >> CH_PACK_BX) & (CH_MAX_NY - 1),
+                  ck = cw >> (CH_PACK_BX + CH_PACK_BY);
+        bp[w][2 * lane] = make_double2(g.x0 + ((double)ci + (double)p.x) * g.dx, g.y0 + ((double)cj + (double)p.y) * g.dy);
+        bp[w][2 * lane + 1] = make_double2(g.z0 + ((double)ck + (double)p.z) * g.dz, 0.0);
+        bv[w][2 * lane] = make_double2((double)vv.x, (double)vv.y);
+        bv[w][2 * lane + 1] = make_double2((double)vv.z, 0.0);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = lane + 32 * h;
+        if (q < n2) {
+          pos[2 * i0 + q] = bp[w][q];
+          vel[2 * i0 + q] = bv[w][q];
+        }
+      }
+    }
+    __syncwarp();  // the buffers are written out before the next chunk refills them
+  }
+  double vs[3] = {(double)tsum, (double)gsum * CH_G_UNIT, (double)ssum * CH_G_UNIT};
+  count_add(cnt, ncol, nref);
+  block_partials<3>(vs, part);
+}
+
+int launch_host_push(const StepConsts& c, void* pos, void* vel, const uint32_t* slot_of_id, MixParticles M,
+                     MixParticles B, const float4* E32, double Nc, double sbar, uint32_t* hist, bool read, bool write,
+                     DevCounters* cnt, double* part, int sms, cudaStream_t s) {
+  const float pscale = sbar > 0.0 ? (float)(Nc / sbar) : 0.0f;
+  const int nb = grid_for(M.np, 256, sms, 4);
+  k_host_push<<<nb, 256, 0, s>>>(c, (double2*)pos, (double2*)vel, slot_of_id, M, B, E32, pscale, hist, read ? 1 : 0,
+                                 write ? 1 : 0, cnt, part),
+      ::ch::note_launch();
+  return nb;
 }
 
 void launch_slot_map(MixParticles M, uint32_t* slot_of_id, int sms, cudaStream_t s) {

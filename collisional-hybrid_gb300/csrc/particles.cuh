@@ -33,6 +33,13 @@ void launch_aos_in(bool mixed, const GridDesc& g, const double4_32a* pos, const 
 // order: the slot map of the current order, the conversion of an id range,
 // and the upload that puts every ion back into its slot.
 void launch_slot_map(MixParticles M, uint32_t* slot_of_id, int sms, cudaStream_t s);
+// One step's push / collisions / move of ions held in registered host arrays
+// (id order, read and written in place through their device addresses);
+// returns the number of blocks, whose 3 partials (expected events, S after
+// the push, S of the ions read) are in part.
+int launch_host_push(const StepConsts& c, void* pos, void* vel, const uint32_t* slot_of_id, MixParticles M,
+                     MixParticles B, const float4* E32, double Nc, double sbar, uint32_t* hist, bool read, bool write,
+                     DevCounters* cnt, double* part, int sms, cudaStream_t s);
 void launch_mixed_to_host(const GridDesc& g, MixParticles M, const uint32_t* slot_of_id, void* pos, void* vel,
                           int64_t i_begin, int64_t i_end, int sms, cudaStream_t s);
 void launch_host_to_mixed(const GridDesc& g, const void* pos, const void* vel, const uint32_t* slot_of_id,

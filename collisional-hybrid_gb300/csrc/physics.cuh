@@ -58,17 +58,42 @@ __device__ __forceinline__ R ch_gmean(R w, R sigma) {
 // the first term; below a = 0.3 the series 2 sigma sqrt(2/pi)(1 + a^2/3 -
 // a^4/30 + a^6/210) avoids the cancellation in 1 - P e^{-a^2}.  Relative
 // error below 1e-6 against the FP64 form.
+// Every operation is rounded as written (the _rn intrinsics are neither
+// contracted nor reordered by the compiler), so each kernel that evaluates
+// g of the same velocity gets the same bits: the collision-rate sum S formed
+// by one step and the S formed from the ions it wrote agree exactly.
 template <>
 __device__ __forceinline__ float ch_gmean<float>(float w, float sigma) {
   if (!(sigma > 0.0f)) return w;
-  const float a = __fdividef(w, sigma * 1.41421356f);
-  const float c = sigma * 0.797884561f;
-  const float a2 = a * a;
-  if (a < 0.3f) return 2.0f * c * (1.0f + a2 * (0.333333333f + a2 * (-0.0333333333f + a2 * 0.00476190476f)));
+  const float a = __fdividef(w, __fmul_rn(sigma, 1.41421356f));
+  const float c = __fmul_rn(sigma, 0.797884561f);
+  const float a2 = __fmul_rn(a, a);
+  if (a < 0.3f)
+    return __fmul_rn(__fmul_rn(2.0f, c),
+                     __fmaf_rn(a2, __fmaf_rn(a2, __fmaf_rn(a2, 0.00476190476f, -0.0333333333f), 0.333333333f), 1.0f));
   const float e = __expf(-a2);
-  const float t = __fdividef(1.0f, 1.0f + 0.3275911f * a);
-  const float P = t * (0.254829592f + t * (-0.284496736f + t * (1.421413741f + t * (-1.453152027f + t * 1.061405429f))));
-  return c * e + (w + __fdividef(sigma * sigma, w)) * (1.0f - P * e);
+  const float t = __fdividef(1.0f, __fmaf_rn(0.3275911f, a, 1.0f));
+  float h = __fmaf_rn(t, 1.061405429f, -1.453152027f);
+  h = __fmaf_rn(t, h, 1.421413741f);
+  h = __fmaf_rn(t, h, -0.284496736f);
+  h = __fmaf_rn(t, h, 0.254829592f);
+  const float P = __fmul_rn(t, h);
+  return __fmaf_rn(c, e, __fmul_rn(__fadd_rn(w, __fdividef(__fmul_rn(sigma, sigma), w)), __fmaf_rn(-P, e, 1.0f)));
+}
+
+// |v - vn0| of the FP32 form, rounded as written (see ch_gmean<float>).
+__device__ __forceinline__ float ch_relspeed_rn(float vx, float vy, float vz, float ux, float uy, float uz) {
+  const float qx = __fsub_rn(vx, ux), qy = __fsub_rn(vy, uy), qz = __fsub_rn(vz, uz);
+  return ch_qsqrt(__fmaf_rn(qz, qz, __fmaf_rn(qy, qy, __fmul_rn(qx, qx))));
+}
+template <typename R>
+__device__ __forceinline__ R ch_relspeed(R vx, R vy, R vz, R ux, R uy, R uz) {
+  const R qx = vx - ux, qy = vy - uy, qz = vz - uz;
+  return ch_qsqrt(qx * qx + qy * qy + qz * qz);
+}
+template <>
+__device__ __forceinline__ float ch_relspeed<float>(float vx, float vy, float vz, float ux, float uy, float uz) {
+  return ch_relspeed_rn(vx, vy, vz, ux, uy, uz);
 }
 
 template <typename R>
@@ -290,8 +315,7 @@ __device__ __forceinline__ bool ch_collide_round(const StepConsts& c, uint32_t i
   // the next event's waiting time
   ++e;
   it = 0;
-  const R qx = v[0] - vn0x, qy = v[1] - vn0y, qz = v[2] - vn0z;
-  gfin = ch_gmean<R>(ch_qsqrt(qx * qx + qy * qy + qz * qz), sig);
+  gfin = ch_gmean<R>(ch_relspeed<R>(v[0], v[1], v[2], vn0x, vn0y, vn0z), sig);
   if (e >= CH_MAX_EVENTS) return true;
   const R lam = lscale * gfin;
   if (!(lam > R(0))) return true;

@@ -194,9 +194,15 @@ ch_status ch_step(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_step_info* i
  * the reference's loop (src/hybrid.c:101-123): uploads pos / vel (the ions
  * last uploaded or downloaded, same count), runs nsteps >= 1 steps and
  * downloads the ions into pos / vel in id order.  With registered arrays
- * (ch_host_register) in the mixed form the download of the last step
- * starts once its push has moved the ions and overlaps its deposit and
- * potential solve; otherwise it follows the steps. */
+ * (ch_host_register, ch_host_alloc) in the mixed form, once the arrays hold
+ * the ions in the id order of a previous transfer, the first step's push
+ * reads them straight from the host arrays and the last step's push writes
+ * its result back in the same launch, so the upload and the download share
+ * the host link (nearly duplex); it uses the collision-rate sum S of the
+ * previous step and runs the step again the ordinary way if the host
+ * changed velocities since (the result is the same either way).  Otherwise
+ * the download of the last step starts once its push has moved the ions and
+ * overlaps its deposit and potential solve, or follows the steps. */
 ch_status ch_step_host(ch_ctx* c, int64_t first_step, int32_t nsteps, ch_real_vector* pos,
                        ch_real_vector* vel, ch_step_info* info);
 
@@ -223,6 +229,9 @@ typedef struct ch_profile {
   int64_t launches;    /* kernels launched by this library, all contexts */
   double deposit_ms;   /* the deposit-only passes among pass_ms */
   int64_t deposit_calls;
+  int64_t host_push_calls;   /* ch_step_host pushes that streamed the host arrays */
+  int64_t host_push_reruns;  /* of those, steps run again because the host had
+                                changed velocities since the last transfer */
 } ch_profile;
 ch_status ch_set_profiling(ch_ctx* c, int32_t enable);
 ch_status ch_get_profile(ch_ctx* c, ch_profile* out);
@@ -392,6 +401,14 @@ ch_status ch_adjoint_get_timing(ch_adjoint* a, ch_adjoint_timing* out);
  * the host). */
 ch_status ch_host_register(void* ptr, uint64_t bytes);
 ch_status ch_host_unregister(void* ptr);
+/* Page-locked host memory for hosts that own their particle arrays: an
+ * anonymous mapping backed by transparent huge pages where the kernel offers
+ * them, touched, page-locked and mapped for the GPU.  The GPU streams it at
+ * the full host-link rate however fragmented free memory has become, where
+ * registered base pages of an ordinary allocation can come many times
+ * slower.  Free with ch_host_free.  (No counterpart in the reference.) */
+ch_status ch_host_alloc(uint64_t bytes, void** out);
+ch_status ch_host_free(void* ptr);
 
 #ifdef __cplusplus
 }

@@ -158,3 +158,67 @@ def test_step_host_rejects_bad_calls(chy):
         pos, vel = h.download()
         with pytest.raises(chy.HybridError):
             h.step_host(pos, vel, 0, 0)
+
+
+@pytest.mark.parametrize("nu", [0.4, 0.0])
+def test_step_host_after_the_host_changed_the_ions(chy, nu):
+    """Once the host arrays hold the ions in id order, ch_step_host pushes
+    them straight from the host arrays and writes the result back in the
+    same launch, using the collision-rate normaliser S of the previous step.
+    A host that changes velocities between calls changes S: the call then
+    runs the step again the ordinary way.  Changed positions need no rerun.
+    Either way the host arrays, moments and phi equal those of upload,
+    ch_step and download, bit for bit, with sort steps inside the calls;
+    arrays from ch_host_alloc and registered numpy arrays give the same."""
+    p = chy.params_for((16, 12, 20), precision=chy.PRECISION["mixed"], nui=nu, mn=1.0 if nu > 0 else 0.0,
+                       sort_period=3)
+    n = 16 * 12 * 20 * 8 + 5
+    outs = []
+    for mode in ("separate", "registered", "host_alloc"):
+        with chy.Hybrid(p) as h:
+            h.load(n, chy.loader(amp=(0.05, 0.02, 0.0)))
+            h.CollectVlasovQuantities(copy=False)
+            h.ComputePotential(copy=False)
+            h.step(0, 1)
+            held = []
+            if mode == "host_alloc":
+                held = [chy.HostArray((n, 4)), chy.HostArray((n, 4))]
+                pos, vel = held[0].a, held[1].a
+                h.download(pos, vel)
+            else:
+                pos, vel = h.download()
+            if mode == "registered":
+                chy.host_register(pos)
+                chy.host_register(vel)
+            h.set_profiling(True)
+            try:
+                s = 1
+                for call, nsteps in enumerate((1, 1, 2, 1, 1, 3)):
+                    if call == 2:
+                        vel[::97, 0] *= 1.01   # the host edits some velocities
+                    if call == 4:
+                        pos[::89, 1] += 0.25    # and later some positions
+                    if mode == "separate":
+                        h.upload(pos, vel)
+                        h.step(s, nsteps)
+                        h.download(pos, vel)
+                    else:
+                        h.step_host(pos, vel, s, nsteps)
+                    s += nsteps
+                prof = h.profile()
+                outs.append((pos.copy(), vel.copy(), h.CollectVlasovQuantities(), h.phi()))
+            finally:
+                if mode == "registered":
+                    chy.host_unregister(pos)
+                    chy.host_unregister(vel)
+                del pos, vel
+                for a in held:
+                    a.free()
+            if mode != "separate" and nu > 0:
+                # every call after the first streams the host arrays; only
+                # the call after the velocity edit runs its step again
+                assert prof["host_push_calls"] >= 5, prof
+                assert prof["host_push_reruns"] == 1, prof
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            assert np.array_equal(a, b)
