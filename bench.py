@@ -522,6 +522,48 @@ def run_adjoint(fd=True):
     return out
 
 
+def run_solves(reps=10):
+    """The stand-alone solve (src/solver.c's work) on the two production
+    grids: a loaded density (n = 1 + 0.02 sum_m sin(2 pi m x/Lx + phase_m),
+    flux = the workload's drift times n), then `reps` solves, each from
+    phi = 0 (ComputeInitialPhi) to rtol 1e-10 with the workload's solver
+    (mixed form: multigrid-preconditioned CG in FP32 inside FP64 refinement),
+    timed with the library's CUDA events on its stream."""
+    m = chy()
+    out = {}
+    for name in ("128cubed-64ppc-mixed", "256x256x64-32ppc-mixed"):
+        w = WORKLOADS[name]
+        N = w["N"]
+        p = make_params(w)
+        x = (np.arange(N[0]) / N[0])[None, None, :]
+        ph = m.mode_phases(1)
+        n = 1.0 + 0.02 * sum(np.sin(2 * np.pi * k * x + ph[k - 1]) for k in (1, 2, 3))
+        n = np.broadcast_to(n, (N[2], N[1], N[0])).ravel()
+        nodes = np.zeros((n.size, 4))
+        nodes[:, 0] = n
+        for d in range(3):
+            nodes[:, 1 + d] = w["drift"][d] * n
+        zeros = np.zeros(n.size)
+        with m.Hybrid(p) as h:
+            h.set_moments(nodes)
+            its = []
+            for k in range(reps + 2):
+                if k == 2:
+                    h.set_profiling(True)
+                    h.reset_profile()
+                h.set_phi(zeros)
+                h.ComputePotential(copy=False)
+                its.append((h.last_solve["iterations"], h.last_solve["refinements"],
+                            h.last_solve["rnorm"] / h.last_solve["bnorm"]))
+            prof = h.profile()
+            h.set_profiling(False)
+        ms = prof["solve_ms"] / max(1, prof["solve_calls"])
+        out[name] = {"grid": list(N), "solves_per_s": 1e3 / ms, "ms_per_solve": ms, "solves": reps,
+                     "iterations": its[-1][0], "refinements": its[-1][1], "rel_residual": its[-1][2],
+                     "start": "phi = 0", "ksp_rtol": w["rtol"]}
+    return out
+
+
 # ------------------------------------------------------------------ CPU arm
 # The CPU legs (the reference arm and cpu_baseline) run the FP64 CPU
 # restatement of the step, built from the oracle alone: nothing of the product
@@ -641,6 +683,7 @@ def main():
     ap.add_argument("--ensemble-steps", type=int, default=10)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (ch_adjoint) measurement")
     ap.add_argument("--no-adjoint-fd", action="store_true", help="skip its finite-difference check")
+    ap.add_argument("--no-solve", action="store_true", help="skip the stand-alone solves (solves/s)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     rank = int(os.environ.get("RANK", "0"))
@@ -718,6 +761,8 @@ def main():
         line["errors_vs_fp64"] = errors_vs_fp64(w)
     if not args.no_ensemble:
         line["ensemble"] = run_ensemble(args.ensemble_steps)
+    if not args.no_solve:
+        line["solves"] = run_solves()
     if not args.no_adjoint:
         line["adjoint"] = run_adjoint(fd=not args.no_adjoint_fd)
     if not args.no_cpu:

@@ -33,6 +33,8 @@ KSP = {"cg": 0, "bcgs": 1}
 PC = {"none": 0, "jacobi": 1, "mg": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
 NN_PROFILE = {"uniform": 0, "gaussian_x": 1}  # CH_NN_*: neutral density n_n(x)
+# --density-type (CH_DENSITY_*), the reference's DensityTypes order
+DENSITY = {"flat-sobol": 0, "flat-reverse": 1, "flat-normal": 2, "uniform": 3, "sinusoidal": 4, "gaussian": 5}
 FAITHFUL = {2: 1 << 2, 3: 1 << 3, 4: 1 << 4, 5: 1 << 5, 6: 1 << 6, 7: 1 << 7, 8: 1 << 8}
 
 _dp = C.POINTER(C.c_double)
@@ -174,6 +176,7 @@ def lib():
             "ch_output": [vp, C.c_char_p],
             "ch_output_wait": [vp, C.POINTER(C.c_int64)],
             "ch_set_solver": [vp, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32],
+            "ch_particles_load_placed": [vp, C.c_int64, vp, C.c_int32],
             "ch_host_register": [vp, C.c_uint64],
             "ch_host_alloc": [C.c_uint64, C.POINTER(vp)],
             "ch_host_free": [vp],
@@ -305,6 +308,12 @@ class Hybrid:
 
     def load(self, np_: int, L: Loader):
         _check(lib().ch_particles_load(self._h, int(np_), C.byref(L)))
+        self.np = int(np_)
+
+    def load_placed(self, np_: int, L: Loader, density_type: str = "flat-sobol"):
+        """InitializePositions with the reference's --density-type placement
+        and Maxwellian velocities from L (ch_particles_load_placed)."""
+        _check(lib().ch_particles_load_placed(self._h, int(np_), C.byref(L), DENSITY[density_type]))
         self.np = int(np_)
 
     def download(self, pos=None, vel=None):

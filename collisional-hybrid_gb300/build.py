@@ -73,18 +73,23 @@ HOST = os.path.join(HERE, "host")
 DRIVER = os.path.join(HERE, "hybrid_gpu")
 
 
+SOLVER = os.path.join(HERE, "solver_gpu")
+
+
 def build_host() -> str:
-    """The C driver mirroring src/hybrid.c over the C ABI (plain C, gcc)."""
-    srcs = [os.path.join(HOST, "hybrid_gpu.c"), os.path.join(HOST, "ch_options.c")]
-    if not _stale(DRIVER, srcs + [os.path.join(HOST, "ch_options.h"), OUT]):
-        return DRIVER
+    """The C drivers over the C ABI (plain C, gcc): hybrid_gpu mirrors
+    src/hybrid.c, solver_gpu mirrors src/solver.c."""
     cc = shutil.which("gcc") or shutil.which("cc")
-    cmd = [cc, "-O2", "-std=c11", "-Wall", "-I", os.path.join(REPO, "include"), "-I", HOST, *srcs, "-o", DRIVER,
-           "-L", HERE, "-lchybrid", f"-Wl,-rpath,{HERE}", "-lm"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode:
-        sys.stderr.write(r.stdout + r.stderr)
-        raise RuntimeError("host driver build failed")
+    for exe, main in ((DRIVER, "hybrid_gpu.c"), (SOLVER, "solver_gpu.c")):
+        srcs = [os.path.join(HOST, main), os.path.join(HOST, "ch_options.c")]
+        if not _stale(exe, srcs + [os.path.join(HOST, "ch_options.h"), OUT]):
+            continue
+        cmd = [cc, "-O2", "-std=gnu11", "-Wall", "-I", os.path.join(REPO, "include"), "-I", HOST, *srcs, "-o", exe,
+               "-L", HERE, "-lchybrid", f"-Wl,-rpath,{HERE}", "-lm"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            sys.stderr.write(r.stdout + r.stderr)
+            raise RuntimeError(f"host driver build failed: {main}")
     return DRIVER
 
 

@@ -501,6 +501,28 @@ extern "C" ch_status ch_particles_load(ch_ctx* c, int64_t np, const ch_loader* L
   return after_load(c);
 }
 
+extern "C" ch_status ch_particles_load_placed(ch_ctx* c, int64_t np, const ch_loader* L, int32_t density_type) {
+  static const char* const names[] = {"flat-sobol", "flat-reverse", "flat-normal", "uniform", "sinusoidal",
+                                      "gaussian"};
+  if (!c || !L) return ch_fail(CH_ERR_ARG, "ch_particles_load_placed: null argument");
+  if (density_type < 0 || density_type > CH_DENSITY_GAUSSIAN)
+    return ch_fail(CH_ERR_ARG, "unknown --density-type %d", density_type);
+  if (density_type == CH_DENSITY_FLAT_REVERSE || density_type == CH_DENSITY_FLAT_NORMAL ||
+      density_type == CH_DENSITY_GAUSSIAN)
+    return ch_fail(CH_ERR_UNSUPPORTED, "Not implemented: %s density (src/particles.c:28-45)", names[density_type]);
+  if (np < 1) return ch_fail(CH_ERR_ARG, "np < 1");
+  if (density_type == CH_DENSITY_UNIFORM && np % c->g.N != 0)
+    return ch_fail(CH_ERR_ARG,
+                   "uniform placement puts the same number of ions in every cell: np = %lld is not a multiple of "
+                   "%lld cells",
+                   (long long)np, (long long)c->g.N);
+  if (np > (int64_t)UINT32_MAX) return ch_fail(CH_ERR_ARG, "np beyond 32-bit ion ids");
+  ch_status rc = ensure_particles(c, np);
+  if (rc) return rc;
+  launch_load_placed(c->mixed, c->g, *L, density_type, c->p.seed, c->p.run, c->P, c->M, c->sms, c->stream);
+  return after_load(c);
+}
+
 // Registered host arrays, mixed form: the ions of src (the buffers of the
 // current order, or of the order a sort step's deposit has just written),
 // converted chunk by chunk into the staging arrays in id order on

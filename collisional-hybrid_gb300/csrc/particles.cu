@@ -171,6 +171,127 @@ __global__ void k_load_mixed(GridDesc g, ch_loader L, uint32_t slo, uint32_t shi
   }
 }
 
+// ------------------------------------------------------------------ placement loaders
+// InitializePositions (src/particles.c:9-132) with the reference's
+// --density-type choices; velocities Maxwellian as in load_one.  Positions
+// use explicitly rounded arithmetic (no contraction) so that the CPU
+// restatement of each placement gives the same bits.
+struct SobolDirs {
+  uint32_t v[3][32];
+};
+
+// Point n of the 3-D Sobol sequence in Gray-code order (Antonov & Saleev):
+// the XOR of the direction numbers of the set bits of n ^ (n >> 1).
+__device__ __forceinline__ void sobol_point(const SobolDirs& D, uint32_t n, double r[3]) {
+  const uint32_t gc = n ^ (n >> 1);
+  uint32_t x[3] = {0u, 0u, 0u};
+  for (int k = 0; k < 32; ++k)
+    if (gc & (1u << k)) {
+      x[0] ^= D.v[0][k];
+      x[1] ^= D.v[1][k];
+      x[2] ^= D.v[2][k];
+    }
+  for (int d = 0; d < 3; ++d) r[d] = (double)x[d] * 2.3283064365386962890625e-10;  // 2^-32, exact
+}
+
+// SobolDistribution (src/distributions.c:96-128): v = r (L + d) - d/2,
+// clamped to [p0 + 0.01 d, p1 - 0.01 d] as the reference does.
+__device__ __forceinline__ double sobol_coord(double r, double L, double d, double p0, double p1) {
+  const double v = __dsub_rn(__dmul_rn(r, __dadd_rn(L, d)), __dmul_rn(0.5, d));
+  if (v < p0) return __dadd_rn(p0, __dmul_rn(0.01, d));
+  if (v > p1) return __dsub_rn(p1, __dmul_rn(0.01, d));
+  return v;
+}
+
+__device__ __forceinline__ void load_placed_one(const GridDesc& g, const ch_loader& L, const SobolDirs& D, int type,
+                                                int64_t per_cell, uint32_t slo, uint32_t shi, uint32_t run,
+                                                uint32_t id, double out[6]) {
+  if (type == CH_DENSITY_FLAT_SOBOL) {
+    double r[3];
+    sobol_point(D, id + 1u, r);  // point 0 is the origin; the reference's first call initialises
+    out[0] = sobol_coord(r[0], g.Lx, g.dx, g.x0, g.x0 + g.Lx);
+    out[1] = sobol_coord(r[1], g.Ly, g.dy, g.y0, g.y0 + g.Ly);
+    out[2] = sobol_coord(r[2], g.Lz, g.dz, g.z0, g.z0 + g.Lz);
+  } else if (type == CH_DENSITY_UNIFORM) {
+    // UniformDistribution (src/distributions.c:33-94): per_cell ions at the
+    // centre of every cell, ion id in cell id mod N
+    const int64_t c = (int64_t)id % g.N;
+    const int i = (int)(c % g.Nx), j = (int)((c / g.Nx) % g.Ny), k = (int)(c / ((int64_t)g.Nx * g.Ny));
+    out[0] = __dadd_rn(g.x0, __dmul_rn(g.dx, __dadd_rn((double)i, 0.5)));
+    out[1] = __dadd_rn(g.y0, __dmul_rn(g.dy, __dadd_rn((double)j, 0.5)));
+    out[2] = __dadd_rn(g.z0, __dmul_rn(g.dz, __dadd_rn((double)k, 0.5)));
+    (void)per_cell;
+  } else {
+    // Rejection (src/distributions.c:143-232) of SinusoidalDistribution
+    // (:131-141), n(x) = 1 + 0.25 sin(2 pi x) at the proposal's x = r L,
+    // accepted when n > v max n with the bound max n = 1.25 (the reference
+    // takes the maximum over integer points, where the sine vanishes)
+    for (uint32_t a = 0; a < 256u; ++a) {
+      const U4 q = ch_philox(id, CH_STEP_LOADER, (CH_PURPOSE_LOAD << 24) | (2u + a), run, slo, shi);
+      const double x = __dmul_rn(ch_unit(q.x), g.Lx), y = __dmul_rn(ch_unit(q.y), g.Ly),
+                   z = __dmul_rn(ch_unit(q.z), g.Lz);
+      const double w = 1.0 + 0.25 * sin(2.0 * CH_PI * x);
+      out[0] = g.x0 + x;
+      out[1] = g.y0 + y;
+      out[2] = g.z0 + z;
+      if (w > __dmul_rn(ch_unit(q.w), 1.25)) break;
+    }
+  }
+  const U4 b = ch_philox(id, CH_STEP_LOADER, (CH_PURPOSE_LOAD << 24) | 1u, run, slo, shi);
+  const double r1 = sqrt(-2.0 * log(ch_unit(b.x))), t1 = 2.0 * CH_PI * ch_unit(b.y);
+  const double r2 = sqrt(-2.0 * log(ch_unit(b.z))), t2 = 2.0 * CH_PI * ch_unit(b.w);
+  out[3] = L.v0[0] + L.vT[0] * (r1 * cos(t1));
+  out[4] = L.v0[1] + L.vT[1] * (r1 * sin(t1));
+  out[5] = L.v0[2] + L.vT[2] * (r2 * cos(t2));
+}
+
+template <bool MIXED>
+__global__ void k_load_placed(GridDesc g, ch_loader L, SobolDirs D, int type, int64_t per_cell, uint32_t slo,
+                              uint32_t shi, uint32_t run, F64Particles P, MixParticles M) {
+  const int64_t np = MIXED ? M.np : P.np;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np; i += (int64_t)gridDim.x * blockDim.x) {
+    double s[6];
+    load_placed_one(g, L, D, type, per_cell, slo, shi, run, (uint32_t)i, s);
+    if (MIXED) {
+      M.pos[i] = pack_mixed(g, s);
+      M.vel[i] = make_float4((float)s[3], (float)s[4], (float)s[5], __uint_as_float((uint32_t)i));
+    } else {
+      P.x[i] = s[0]; P.y[i] = s[1]; P.z[i] = s[2];
+      P.vx[i] = s[3]; P.vy[i] = s[4]; P.vz[i] = s[5];
+      P.id[i] = (uint32_t)i;
+    }
+  }
+}
+
+// Direction numbers of the first three Sobol dimensions (Joe & Kuo's table):
+// dimension 1 the van der Corput sequence; dimension 2 the polynomial x + 1
+// with m1 = 1; dimension 3 x^2 + x + 1 with m1 = 1, m2 = 3.  Bratley & Fox's
+// recursion v_k = a1 v_{k-1} ^ ... ^ v_{k-s} ^ (v_{k-s} >> s).
+static SobolDirs sobol_dirs() {
+  SobolDirs D;
+  for (int k = 0; k < 32; ++k) D.v[0][k] = 1u << (31 - k);
+  D.v[1][0] = 1u << 31;
+  for (int k = 1; k < 32; ++k) D.v[1][k] = D.v[1][k - 1] ^ (D.v[1][k - 1] >> 1);
+  D.v[2][0] = 1u << 31;
+  D.v[2][1] = 3u << 30;
+  for (int k = 2; k < 32; ++k) D.v[2][k] = D.v[2][k - 1] ^ D.v[2][k - 2] ^ (D.v[2][k - 2] >> 2);
+  return D;
+}
+
+void launch_load_placed(bool mixed, const GridDesc& g, const ch_loader& L, int type, uint64_t seed, uint32_t run,
+                        F64Particles P, MixParticles M, int sms, cudaStream_t s) {
+  const uint32_t lo = (uint32_t)seed, hi = (uint32_t)(seed >> 32);
+  const SobolDirs D = sobol_dirs();
+  const int64_t np = mixed ? M.np : P.np;
+  const int64_t per_cell = np / (g.N > 0 ? g.N : 1);
+  if (mixed)
+    k_load_placed<true><<<grid_for(np, 256, sms, 8), 256, 0, s>>>(g, L, D, type, per_cell, lo, hi, run, P, M),
+        ::ch::note_launch();
+  else
+    k_load_placed<false><<<grid_for(np, 256, sms, 8), 256, 0, s>>>(g, L, D, type, per_cell, lo, hi, run, P, M),
+        ::ch::note_launch();
+}
+
 // AoS RealVector (x, y, z, r) staging -> state, id = index.
 __global__ void k_aos_to_f64(const double4_32a* __restrict__ pos, const double4_32a* __restrict__ vel, F64Particles P) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.np; i += (int64_t)gridDim.x * blockDim.x) {

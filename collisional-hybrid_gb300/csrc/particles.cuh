@@ -33,6 +33,10 @@ void launch_aos_in(bool mixed, const GridDesc& g, const double4_32a* pos, const 
 // order: the slot map of the current order, the conversion of an id range,
 // and the upload that puts every ion back into its slot.
 void launch_slot_map(MixParticles M, uint32_t* slot_of_id, int sms, cudaStream_t s);
+// The reference's --density-type placements (CH_DENSITY_FLAT_SOBOL,
+// CH_DENSITY_UNIFORM, CH_DENSITY_SINUSOIDAL) with Maxwellian velocities.
+void launch_load_placed(bool mixed, const GridDesc& g, const ch_loader& L, int type, uint64_t seed, uint32_t run,
+                        F64Particles P, MixParticles M, int sms, cudaStream_t s);
 // One step's push / collisions / move of ions held in registered host arrays
 // (id order, read and written in place through their device addresses);
 // returns the number of blocks, whose 3 partials (expected events, S after

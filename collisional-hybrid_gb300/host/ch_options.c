@@ -195,14 +195,15 @@ ch_status ch_parse_options(int argc, char** argv, ch_params* p, ch_run_options* 
     p->nn_floor = 0.1;
     if (get_real(&a, "-ch_nn_floor", &d) > 0) p->nn_floor = d;
   }
-  r->amp[0] = r->density_type == 4 ? 0.25 : 0.0; /* SinusoidalDistribution: 1 + 0.25 sin (src/distributions.c:149) */
-  if (get_real(&a, "-ch_amp1", &d) > 0) r->amp[0] = d;
-  if (get_real(&a, "-ch_amp2", &d) > 0) r->amp[1] = d;
-  if (get_real(&a, "-ch_amp3", &d) > 0) r->amp[2] = d;
-  if (get_real(&a, "-ch_phase1", &d) > 0) r->phase[0] = d;
-  if (get_real(&a, "-ch_phase2", &d) > 0) r->phase[1] = d;
-  if (get_real(&a, "-ch_phase3", &d) > 0) r->phase[2] = d;
+  r->use_modes = 0;
+  if (get_real(&a, "-ch_amp1", &d) > 0) { r->amp[0] = d; r->use_modes = 1; }
+  if (get_real(&a, "-ch_amp2", &d) > 0) { r->amp[1] = d; r->use_modes = 1; }
+  if (get_real(&a, "-ch_amp3", &d) > 0) { r->amp[2] = d; r->use_modes = 1; }
+  if (get_real(&a, "-ch_phase1", &d) > 0) { r->phase[0] = d; r->use_modes = 1; }
+  if (get_real(&a, "-ch_phase2", &d) > 0) { r->phase[1] = d; r->use_modes = 1; }
+  if (get_real(&a, "-ch_phase3", &d) > 0) { r->phase[2] = d; r->use_modes = 1; }
   r->random_phases = has(&a, "-ch_random_phases");
+  if (r->random_phases) r->use_modes = 1;
   r->verbose = has(&a, "-ch_verbose");
   if (r->Np < 0) r->Np = (int64_t)p->Nx * p->Ny * p->Nz; /* src/setup.c:44-46 */
   (void)e;

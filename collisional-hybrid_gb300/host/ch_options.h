@@ -24,6 +24,9 @@ typedef struct ch_run_options {
   double phase[3];       /* -ch_phase1..3 (-ch_random_phases draws them)       */
   int32_t random_phases; /* -ch_random_phases                                  */
   int32_t verbose;       /* -ch_verbose                                        */
+  int32_t use_modes;     /* a -ch_amp / -ch_phase option was given: load by the
+                            inverse CDF of the density modes (ch_particles_load)
+                            instead of the --density-type placement          */
 } ch_run_options;
 
 /* Parses argv (unknown options are ignored, like PETSc's options database)

@@ -3,8 +3,9 @@
  * GPU through the C ABI, without PETSc: same option names, same step order
  *   UpdateVelocities -> UpdatePositions -> CollectVlasovQuantities ->
  *   ComputePotential
- * for Nt steps, printing one summary line per step.  Ions are a seeded
- * synthetic plasma generated on the device (-ch_amp*, -ch_phase*).
+ * for Nt steps, printing one summary line per step.  Ions are placed on the
+ * device by the reference's --density-type (default flat-sobol), or, with
+ * -ch_amp* / -ch_phase*, by the inverse CDF of those density modes.
  *
  *   hybrid_gpu -Nx 32 -Ny 32 -Nz 32 -x1 32 -y1 32 -z1 32 -Np 524288 -viT 1
  *              -B0z 1 -E0x 0.5 -nui 0.1 -dt 0.05 -Nt 100 -ch_vnT 1 ...
@@ -46,7 +47,10 @@ int main(int argc, char** argv) {
     L.v0[m] = p.vi0[m];
     L.vT[m] = p.viT[m];
   }
-  CHECK(ch_particles_load(ctx, r.Np, &L));
+  if (r.use_modes)
+    CHECK(ch_particles_load(ctx, r.Np, &L));
+  else
+    CHECK(ch_particles_load_placed(ctx, r.Np, &L, r.density_type)); /* InitializePositions, src/hybrid.c:57 */
   ch_step_info info;
   ch_solve_info sinfo;
   CHECK(ch_collect_moments(ctx, NULL, &info));         /* src/hybrid.c:67 */

@@ -169,6 +169,33 @@ typedef struct ch_loader {
 } ch_loader;
 ch_status ch_particles_load(ch_ctx* c, int64_t np, const ch_loader* L);
 
+/* --density-type (DensityTypes, src/parameters.c:18-20, default flat-sobol) */
+enum {
+  CH_DENSITY_FLAT_SOBOL = 0,   /* SobolDistribution (src/distributions.c:96-128) */
+  CH_DENSITY_FLAT_REVERSE = 1, /* not implemented in the reference either      */
+  CH_DENSITY_FLAT_NORMAL = 2,  /* not implemented in the reference either      */
+  CH_DENSITY_UNIFORM = 3,      /* UniformDistribution (src/distributions.c:33-94) */
+  CH_DENSITY_SINUSOIDAL = 4,   /* Rejection of SinusoidalDistribution (:131-232) */
+  CH_DENSITY_GAUSSIAN = 5      /* not implemented in the reference either      */
+};
+/* InitializePositions (src/particles.c:9-132) with the reference's
+ * --density-type placements, and Maxwellian velocities v0 + vT N(0,1) from
+ * L (InitializeVelocities, :136-165; Philox-keyed by ion id and seed; L's
+ * density modes are not used):
+ *   flat-sobol  point id + 1 of a 3-D Sobol sequence in Gray-code order
+ *               (direction numbers of Joe & Kuo for the first three
+ *               dimensions), v = r (L + d) - d/2 per axis, clamped to
+ *               [p0 + 0.01 d, p1 - 0.01 d] as the reference clamps;
+ *   uniform     np / (Nx Ny Nz) ions at the centre of every cell (np must be
+ *               a multiple of the cell count; the reference fills all but
+ *               the last cell of each axis and leaves the rest at the origin);
+ *   sinusoidal  rejection sampling of n = 1 + 0.25 sin(2 pi x) over the box,
+ *               with the bound 1.25 (the reference evaluates its bound at
+ *               integer points, where the sine vanishes).
+ * flat-reverse, flat-normal and gaussian return CH_ERR_UNSUPPORTED, as the
+ * reference's InitializePositions does (src/particles.c:28-45). */
+ch_status ch_particles_load_placed(ch_ctx* c, int64_t np, const ch_loader* L, int32_t density_type);
+
 /* UpdateVelocities (src/particles.c:628-643): BorisMover (:348-464) with E
  * gathered from the current phi, then ComputeCollisions (:471-624) if mn > 0.
  * `step` keys the Philox streams of this step. */

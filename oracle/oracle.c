@@ -125,6 +125,82 @@ int orc_load(const ch_params* p, const ch_loader* L, orc_particles* P) {
   return 0;
 }
 
+/* The reference's --density-type placements (src/particles.c:9-132,
+ * src/distributions.c:33-232), restated for the device loader
+ * ch_particles_load_placed: flat-sobol (0), uniform (3), sinusoidal (4).
+ * Velocities as orc_load. */
+static void sobol_directions(uint32_t v[3][32]) {
+  /* first three Sobol dimensions (Joe & Kuo): van der Corput; x + 1 with
+   * m1 = 1; x^2 + x + 1 with m1 = 1, m2 = 3; v_k by Bratley & Fox's
+   * recursion, as 32-bit fractions */
+  for (int k = 0; k < 32; ++k) v[0][k] = 1u << (31 - k);
+  v[1][0] = 1u << 31;
+  for (int k = 1; k < 32; ++k) v[1][k] = v[1][k - 1] ^ (v[1][k - 1] >> 1);
+  v[2][0] = 1u << 31;
+  v[2][1] = 3u << 30;
+  for (int k = 2; k < 32; ++k) v[2][k] = v[2][k - 1] ^ v[2][k - 2] ^ (v[2][k - 2] >> 2);
+}
+
+/* SobolDistribution (src/distributions.c:96-128): v = r (L + d) - d/2,
+ * clamped to [p0 + 0.01 d, p1 - 0.01 d]. */
+static double sobol_coord(double r, double L, double d, double p0, double p1) {
+  double v = r * (L + d) - 0.5 * d;
+  if (v < p0) return p0 + 0.01 * d;
+  if (v > p1) return p1 - 0.01 * d;
+  return v;
+}
+
+int orc_load_placed(const ch_params* p, const ch_loader* L, int type, orc_particles* P) {
+  grid g = mkgrid(p);
+  if (type != 0 && type != 3 && type != 4) return CH_ERR_UNSUPPORTED;
+  if (type == 3 && P->np % g.N != 0) return CH_ERR_ARG;
+  uint32_t dirs[3][32];
+  sobol_directions(dirs);
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int64_t i = 0; i < P->np; ++i) {
+    const uint32_t id = (uint32_t)i;
+    if (type == 0) {
+      /* point id + 1 in Gray-code order (Antonov & Saleev) */
+      const uint32_t n = id + 1u, gc = n ^ (n >> 1);
+      uint32_t x[3] = {0u, 0u, 0u};
+      for (int k = 0; k < 32; ++k)
+        if (gc & (1u << k))
+          for (int d = 0; d < 3; ++d) x[d] ^= dirs[d][k];
+      P->x[i] = sobol_coord((double)x[0] * 2.3283064365386962890625e-10, g.Lx, g.dx, g.x0, g.x0 + g.Lx);
+      P->y[i] = sobol_coord((double)x[1] * 2.3283064365386962890625e-10, g.Ly, g.dy, g.y0, g.y0 + g.Ly);
+      P->z[i] = sobol_coord((double)x[2] * 2.3283064365386962890625e-10, g.Lz, g.dz, g.z0, g.z0 + g.Lz);
+    } else if (type == 3) {
+      /* UniformDistribution (src/distributions.c:33-94), every cell */
+      const int64_t c = (int64_t)id % g.N;
+      const int ci = (int)(c % g.Nx), cj = (int)((c / g.Nx) % g.Ny), ck = (int)(c / ((int64_t)g.Nx * g.Ny));
+      P->x[i] = g.x0 + g.dx * ((double)ci + 0.5);
+      P->y[i] = g.y0 + g.dy * ((double)cj + 0.5);
+      P->z[i] = g.z0 + g.dz * ((double)ck + 0.5);
+    } else {
+      /* Rejection (src/distributions.c:143-232) of 1 + 0.25 sin(2 pi x)
+       * (:131-141) with the bound 1.25 */
+      for (uint32_t a = 0; a < 256u; ++a) {
+        uint32_t q[4];
+        draw(p, id, STEP_LOADER, PURPOSE_LOAD, 2u + a, q);
+        const double x = unit(q[0]) * g.Lx, y = unit(q[1]) * g.Ly, z = unit(q[2]) * g.Lz;
+        const double w = 1.0 + 0.25 * sin(2.0 * PI * x);
+        P->x[i] = g.x0 + x;
+        P->y[i] = g.y0 + y;
+        P->z[i] = g.z0 + z;
+        if (w > unit(q[3]) * 1.25) break;
+      }
+    }
+    uint32_t b[4];
+    draw(p, id, STEP_LOADER, PURPOSE_LOAD, 1, b);
+    double r1 = sqrt(-2.0 * log(unit(b[0]))), t1 = 2.0 * PI * unit(b[1]);
+    double r2 = sqrt(-2.0 * log(unit(b[2]))), t2 = 2.0 * PI * unit(b[3]);
+    P->vx[i] = L->v0[0] + L->vT[0] * (r1 * cos(t1));
+    P->vy[i] = L->v0[1] + L->vT[1] * (r1 * sin(t1));
+    P->vz[i] = L->v0[2] + L->vT[2] * (r2 * cos(t2));
+  }
+  return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* DifferenceVector (src/vectors.c:12-138).  Values are read through a
  * periodic wrap, which equals the ghost-width-1 local array of the

@@ -32,6 +32,9 @@ typedef struct orc_particles {
 
 /* Seeded loader shared with the GPU loader (same Philox counters). */
 int orc_load(const ch_params* p, const ch_loader* L, orc_particles* P);
+/* the reference's --density-type placements 0 (flat-sobol), 3 (uniform),
+ * 4 (sinusoidal rejection), as ch_particles_load_placed places them */
+int orc_load_placed(const ch_params* p, const ch_loader* L, int type, orc_particles* P);
 
 /* DifferenceVector (src/vectors.c:12-138): numerators of the central
  * differences of phi interpolated to the cell-unit point (X, Y, Z).

@@ -82,6 +82,7 @@ def lib():
         L = C.CDLL(LIB)
         L.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.orc_load.argtypes = [C.POINTER(Params), C.POINTER(Loader), C.POINTER(Particles)]
+        L.orc_load_placed.argtypes = [C.POINTER(Params), C.POINTER(Loader), C.c_int, C.POINTER(Particles)]
         L.orc_difference_vector.argtypes = [C.POINTER(Params), _dp, C.c_double, C.c_double, C.c_double,
                                             C.c_uint32, _dp]
         L.orc_node_efield.argtypes = [C.POINTER(Params), _dp, _dp, _dp, _dp]
@@ -234,6 +235,17 @@ def load(p: Params, L: Loader, np_: int) -> Ions:
     s = Ions(np_)
     P = s.struct()
     lib().orc_load(C.byref(p), C.byref(L), C.byref(P))
+    return s
+
+
+def load_placed(p: Params, L: Loader, np_: int, density_type: int) -> Ions:
+    """The reference's --density-type placements (0 flat-sobol, 3 uniform,
+    4 sinusoidal rejection) with Maxwellian velocities."""
+    s = Ions(np_)
+    P = s.struct()
+    rc = lib().orc_load_placed(C.byref(p), C.byref(L), int(density_type), C.byref(P))
+    if rc:
+        raise ValueError(f"orc_load_placed: status {rc}")
     return s
 
 

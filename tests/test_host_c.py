@@ -6,6 +6,7 @@ import os
 import subprocess
 import tempfile
 
+import numpy as np
 import pytest
 
 from conftest import REPO
@@ -30,7 +31,8 @@ def optlib(chy):
 
 class RunOpts(C.Structure):
     _fields_ = [("Nt", C.c_int32), ("Np", C.c_int64), ("density_type", C.c_int32), ("amp", C.c_double * 3),
-                ("phase", C.c_double * 3), ("random_phases", C.c_int32), ("verbose", C.c_int32)]
+                ("phase", C.c_double * 3), ("random_phases", C.c_int32), ("verbose", C.c_int32),
+                ("use_modes", C.c_int32)]
 
 
 def parse(optlib, chy, args):
@@ -148,3 +150,53 @@ def test_c_driver_runs_reference_loop(chy):
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("Time step")]
     assert len(lines) == 5
     assert "Elapsed time" in r.stdout
+    # the reference's own placements: flat-sobol (its default) and the sinusoid
+    for dens in ("flat-sobol", "sinusoidal"):
+        r = subprocess.run([exe, "-Nx", "16", "-Ny", "16", "-Nz", "16", "-x1", "16", "-y1", "16", "-z1", "16",
+                            "-Np", "65536", "-viT", "1", "-B0z", "1", "-E0x", "0.5", "-nui", "0.1", "-dt", "0.05",
+                            "-Nt", "2", "-ch_vnT", "1", "-ch_cth", "1", "-ch_cG", "0.1", "-ch_kappa_ez", "0",
+                            "--density-type", dens, "-ksp_rtol", "1e-8"], capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, (dens, r.stderr)
+        assert len([ln for ln in r.stdout.splitlines() if ln.startswith("Time step")]) == 2
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solver_driver_solves_a_loaded_density(chy, po, precision):
+    """solver_gpu (src/solver.c's work: load a density, form the fluxes as
+    --x/y/z-flux-scale times it, one solve from phi = 0, write the datasets)
+    on an analytic density of the kind the reference's write_hdf5 script
+    makes (n0 + dn times a sinusoid times a Gaussian): the residual meets
+    -ksp_rtol, and phi agrees with the oracle's solve of the same system
+    (1e-12 in the FP64 form, 1e-6 in the mixed form)."""
+    N, L = (32, 16, 24), (1.0, 1.0, 1.0)
+    x = (np.arange(N[0]) / N[0])[None, None, :]
+    y = (np.arange(N[1]) / N[1])[None, :, None]
+    z = (np.arange(N[2]) / N[2])[:, None, None]
+    n = 1.0 + 0.4 * np.sin(2 * np.pi * (2 * x + y)) * np.exp(-((z - 0.5) ** 2) / (2 * 0.2 ** 2))
+    n = np.ascontiguousarray(n.ravel())
+    d = tempfile.mkdtemp()
+    src = os.path.join(d, "vlasov.density.f64")
+    n.tofile(src)
+    exe = os.path.join(PKG, "solver_gpu")
+    args = [exe, "-Nx", "32", "-Ny", "16", "-Nz", "24", "-x1", "1", "-y1", "1", "-z1", "1", "--input", src,
+            "--x-flux-scale", "0.2", "--output", os.path.join(d, "res"), "-ksp_rtol", "1e-13", "-ch_pc", "mg",
+            "-ch_precision", precision, "-ch_cth", "1", "-ch_cG", "0.1", "-ch_kappa_ez", "0", "-E0x", "0.5",
+            "-ch_repeat", "3"]
+    r = subprocess.run(args, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("KSP iterations")][0]
+    rr = float(line.split("|r|/|b|")[1].split()[0])
+    assert rr <= 1e-13 * 1.01, line
+    assert "solves/s" in r.stdout
+    phi = np.fromfile(os.path.join(d, "res.potential.f64"))
+    p = chy.params_for(N, L, precision=chy.PRECISION[precision], E0=(0.5, 0.0, 0.0), cth=1.0, cG=0.1,
+                       ksp_rtol=1e-13)
+    q = po.params_from(p)
+    nodes = np.zeros((n.size, 4))
+    nodes[:, 0], nodes[:, 1], nodes[:, 2], nodes[:, 3] = n, 0.2 * n, n, n
+    nodes = nodes.ravel()
+    ref, info = po.solve(q, nodes[0::4].copy(), po.rhs(q, nodes), rtol=1e-14, maxit=50000)
+    assert info["rc"] == 0
+    err = np.abs(phi - ref).max() / np.abs(ref).max()
+    assert err < (1e-12 if precision == "fp64" else 1e-6), err
