@@ -473,7 +473,7 @@ def run_adjoint(fd=True):
     """Differentiation workload: 64^3 grid, 32 ions/cell, E0 = (0.5, 0.1, 0),
     nu = 0.3, 50 steps, checkpoints every 10, objective over the final 10
     steps (mean x flux + 0.1 mean square potential); gradient w.r.t. E0,
-    vn0, amp against central differences (eps 1e-6) of the frozen-event
+    vn0, amp against central differences of the frozen-event
     forward."""
     m = chy()
     N = (64, 64, 64)
@@ -495,9 +495,14 @@ def run_adjoint(fd=True):
                "events": tim["events"], "ions": np_, "steps": 50, "checkpoint_every": 10,
                "wall_s": {"forward": t1 - t0, "gradient": t2 - t1}}
         if fd:
-            # eps = 1e-6 for every parameter; for amp also 3e-7: its
-            # perturbation moves every ion by ~eps Lx/pi cells and ions that
-            # cross a cell face pass a kink of the CIC weights
+            # every parameter at eps = 1e-6; the amplitude also down to
+            # 3e-9.  Its perturbation moves every ion's start by up to
+            # eps 2 Lx / (2 pi) / 0.99 cells, and an ion that comes that
+            # close to a cell face in some step passes a kink of the CIC
+            # weights and biases its difference quotient; the expected number
+            # of such ion-steps is 2 x that distance x ions x steps.  J's
+            # noise (solves to rtol 1e-13) is about 1e-15, so the smallest
+            # step still resolves the quotient to a few 1e-6.
             def central(k, eps):
                 e = np.zeros_like(th)
                 e[k] = eps
@@ -508,16 +513,14 @@ def run_adjoint(fd=True):
             err = np.abs(g - fdv) / scale
             out["central_fd_eps1e-6"] = [float(x) for x in fdv]
             out["rel_err_vs_fd_eps1e-6"] = [float(x) for x in err]
-            # the kink error of amp is linear in eps: smaller steps and the
-            # linear extrapolation of the two smallest to eps = 0
-            amp = {eps: central(6, eps) for eps in (3e-7, 1e-7)}
-            e1, e2 = 3e-7, 1e-7
-            amp0 = (e1 * amp[e2] - e2 * amp[e1]) / (e1 - e2)
-            out["amp_central_fd"] = {"1e-6": float(fdv[6]), "3e-7": float(amp[e1]), "1e-7": float(amp[e2]),
-                                     "extrapolated_to_0": float(amp0)}
-            out["amp_rel_err"] = {"1e-6": float(err[6]), "3e-7": float(abs(g[6] - amp[e1]) / scale[6]),
-                                  "1e-7": float(abs(g[6] - amp[e2]) / scale[6]),
-                                  "extrapolated_to_0": float(abs(g[6] - amp0) / scale[6])}
+            sweep = {}
+            for eps in (1e-6, 1e-7, 1e-8, 3e-9):
+                v = float(fdv[6]) if eps == 1e-6 else central(6, eps)
+                reach = eps * 2.0 * N[0] / (2.0 * np.pi) / 0.99
+                sweep[f"{eps:g}"] = {"fd": v, "rel_err": float(abs(g[6] - v) / abs(v)),
+                                     "kink_ion_steps_expected": 2.0 * reach * np_ * 50}
+            out["amp_fd_sweep"] = sweep
+            out["amp_rel_err_at_smallest_eps"] = sweep["3e-09"]["rel_err"]
             out["max_rel_err_vs_fd_E0_vn0"] = float(err[:6].max())
     return out
 

@@ -69,6 +69,7 @@ int main(int argc, char** argv) {
   const double fs = arg_real(argc, argv, "--flux-scale", 1.0);  /* src/parameters.c:419-439 */
   const double fsc[3] = {arg_real(argc, argv, "--x-flux-scale", fs), arg_real(argc, argv, "--y-flux-scale", fs),
                          arg_real(argc, argv, "--z-flux-scale", fs)};
+  p.mn = 0.0;  /* a solve has no ions: no neutrals, no collision setup */
   const int64_t N = (int64_t)p.Nx * p.Ny * p.Nz;
   nodes = (ch_grid_node*)calloc((size_t)N, sizeof(ch_grid_node));
   phi = (double*)calloc((size_t)N, sizeof(double));

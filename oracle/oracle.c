@@ -792,7 +792,17 @@ int orc_solve(const ch_params* p, const double* n, const double* b, double* phi,
     for (int64_t i_ = 0; i_ < N; ++i_) (dst)[i_] = jac ? (src)[i_] * dinv[i_] : (src)[i_]; \
     if (singular) remove_mean((dst), N);                          \
   } while (0)
-  if (rn > tol) {
+  /* Krylov iterations; when the recurrence says converged but the true
+   * residual b - A phi (checked below) is still above tol -- the recurrence
+   * drifts near FP64's floor at tight rtol -- restart from the true residual */
+  for (int restart = 0; restart < 8 && rn > tol && it < maxit; ++restart) {
+    if (restart > 0) {
+      orc_apply(p, n, phi, q);
+      #pragma omp parallel for num_threads(g_threads) schedule(static)
+      for (int64_t i = 0; i < N; ++i) r[i] = b[i] - q[i];
+      rn = sqrt(dot(r, r, N));
+      if (rn <= tol) break;
+    }
     if (p->ksp_type == CH_KSP_CG) {
       PREC(z, r);
       #pragma omp parallel for num_threads(g_threads) schedule(static)
@@ -861,6 +871,11 @@ int orc_solve(const ch_params* p, const double* n, const double* b, double* phi,
       }
       free(sh);
     }
+    /* true residual of this pass */
+    orc_apply(p, n, phi, q);
+    #pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t i = 0; i < N; ++i) r[i] = b[i] - q[i];
+    rn = sqrt(dot(r, r, N));
   }
 #undef PREC
   if (singular) remove_mean(phi, N);
