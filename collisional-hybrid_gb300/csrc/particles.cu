@@ -412,6 +412,42 @@ __device__ void diffvec_faithful(const GridDesc& g, const double* __restrict__ p
 
 // ------------------------------------------------------------------ FP64 pass
 // Block partials: 0 expected, 1 S(next).
+// Colliding ions of the FP64 pass wait in a per-warp ring and run their
+// event process 32 at a time, so the FP64 pipe (the bound of this form on
+// GB300) is not spent on lanes idling through another lane's rejection loop.
+#define CH_F64_QW 64
+struct F64Queue {
+  uint32_t ip[8][CH_F64_QW];
+  double v[8][CH_F64_QW][3];
+  double ls[8][CH_F64_QW];
+};
+
+// Finishes n <= 32 queued ions of the calling warp (warp-uniform head/n):
+// the event process, the step's S term, the velocity and, with the move,
+// the new position.
+template <int PH>
+__device__ __forceinline__ void f64_queue_round(F64Queue& Q, const StepConsts& c, F64Particles P, unsigned& head,
+                                                unsigned n, double& gsum, unsigned& ncol, unsigned& nref) {
+  const GridDesc& g = c.g;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if ((unsigned)lane < n) {
+    const unsigned e = (head + lane) & (CH_F64_QW - 1);
+    const int64_t ip = Q.ip[w][e];
+    double v[3] = {Q.v[w][e][0], Q.v[w][e][1], Q.v[w][e][2]};
+    ncol += ch_collide<double>(c, P.id[ip], Q.ls[w][e], v, &nref);
+    const double qx = v[0] - c.vn0[0], qy = v[1] - c.vn0[1], qz = v[2] - c.vn0[2];
+    gsum += ch_gmean<double>(sqrt(qx * qx + qy * qy + qz * qz), c.vnT);
+    P.vx[ip] = v[0]; P.vy[ip] = v[1]; P.vz[ip] = v[2];
+    if ((PH & PH_MOVE) && !(c.faithful & CH_FAITHFUL_D5)) {
+      P.x[ip] = wrap_pos(P.x[ip] + v[0] * c.dt, g.x0, g.Lx);
+      P.y[ip] = wrap_pos(P.y[ip] + v[1] * c.dt, g.y0, g.Ly);
+      P.z[ip] = wrap_pos(P.z[ip] + v[2] * c.dt, g.z0, g.Lz);
+    }
+  }
+  head += n;
+  __syncwarp();  // the entries are read before later appends reuse them
+}
+
 template <int PH>
 __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, const double* __restrict__ E,
                                                   const double* __restrict__ phi, unsigned long long* __restrict__ acc,
@@ -421,11 +457,26 @@ __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, 
   double vsum[2] = {0.0, 0.0};
   unsigned ncol = 0, nref = 0;
   int bad = 0;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const bool gather_faithful = (c.faithful & (CH_FAITHFUL_D3 | CH_FAITHFUL_D4)) != 0;
-  for (int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ip < P.np; ip += (int64_t)gridDim.x * blockDim.x) {
-    double x = P.x[ip], y = P.y[ip], z = P.z[ip];
-    double v[3] = {P.vx[ip], P.vy[ip], P.vz[ip]};
-    if (PH & PH_PUSH) {
+  constexpr bool QUEUE = (PH & PH_PUSH) != 0;
+  extern __shared__ __align__(16) unsigned char smem_f64[];
+  F64Queue& Q = *reinterpret_cast<F64Queue*>(smem_f64);
+  unsigned qhead = 0, qtail = 0;  // warp-uniform
+  // block-uniform iterations: the deposit's warp reduction and the queue
+  // need every lane
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < P.np; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ip = base + threadIdx.x;
+    const bool act = ip < P.np;
+    double x = 0.0, y = 0.0, z = 0.0;
+    double v[3] = {0.0, 0.0, 0.0};
+    if (act) {
+      x = P.x[ip]; y = P.y[ip]; z = P.z[ip];
+      v[0] = P.vx[ip]; v[1] = P.vy[ip]; v[2] = P.vz[ip];
+    }
+    bool defer = false;
+    double lscale = 0.0;
+    if ((PH & PH_PUSH) && act) {
       const double X = (x - g.x0) / g.dx, Y = (y - g.y0) / g.dy, Z = (z - g.z0) / g.dz;
       double Ef[3];
       if (gather_faithful) {
@@ -458,33 +509,56 @@ __global__ void __launch_bounds__(256) k_pass_f64(StepConsts c, F64Particles P, 
       if (c.collide) {
         const double wx = v[0] - c.vn0[0], wy = v[1] - c.vn0[1], wz = v[2] - c.vn0[2];
         const double gi = ch_gmean<double>(sqrt(wx * wx + wy * wy + wz * wz), c.vnT);
-        const double lscale = sbar > 0.0 ? (Nc * ch_neutral_density<double>(c, x)) / sbar : 0.0;
+        lscale = sbar > 0.0 ? (Nc * ch_neutral_density<double>(c, x)) / sbar : 0.0;
         const double lam = lscale * gi;
         vsum[0] += lam;
-        // first waiting time inline; the event loop runs only for colliding ions
+        // the first waiting time here; ions with an event inside the step
+        // join the warp's queue, the others keep g of their velocity for S
         const U4 r0 = ch_philox(P.id[ip], c.step, CH_PURPOSE_COLLIDE << 24, c.run, c.seed_lo, c.seed_hi);
-        if (lam > 0.0 && -log(ch_unit(r0.x)) / lam < 1.0) ncol += ch_collide<double>(c, P.id[ip], lscale, v, &nref);
-        const double qx = v[0] - c.vn0[0], qy = v[1] - c.vn0[1], qz = v[2] - c.vn0[2];
-        vsum[1] += ch_gmean<double>(sqrt(qx * qx + qy * qy + qz * qz), c.vnT);
+        defer = lam > 0.0 && -log(ch_unit(r0.x)) / lam < 1.0;
+        if (!defer) vsum[1] += gi;
       }
-      P.vx[ip] = v[0]; P.vy[ip] = v[1]; P.vz[ip] = v[2];
+      if (!defer) { P.vx[ip] = v[0]; P.vy[ip] = v[1]; P.vz[ip] = v[2]; }
     }
-    if ((PH & PH_MOVE) && !(c.faithful & CH_FAITHFUL_D5)) {
+    if ((PH & PH_MOVE) && !(c.faithful & CH_FAITHFUL_D5) && act && !defer) {
       x = wrap_pos(x + v[0] * c.dt, g.x0, g.Lx);
       y = wrap_pos(y + v[1] * c.dt, g.y0, g.Ly);
       z = wrap_pos(z + v[2] * c.dt, g.z0, g.Lz);
       P.x[ip] = x; P.y[ip] = y; P.z[ip] = z;
     }
-    if (PH & PH_DEPOSIT) {
-      if (!(isfinite(x) && isfinite(y) && isfinite(z) && isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) {
-        bad = 1;  // a non-finite ion is reported, never deposited
-        continue;
+    if (QUEUE) {
+      // append (at most 31 wait between iterations, so 32 more fit), then
+      // full rounds
+      const unsigned dm = __ballot_sync(0xffffffffu, defer);
+      if (defer) {
+        const unsigned e = (qtail + __popc(dm & ((1u << lane) - 1u))) & (CH_F64_QW - 1);
+        Q.ip[w][e] = (uint32_t)ip;
+        Q.v[w][e][0] = v[0]; Q.v[w][e][1] = v[1]; Q.v[w][e][2] = v[2];
+        Q.ls[w][e] = lscale;
       }
-      const double X = (x - g.x0) / g.dx, Y = (y - g.y0) / g.dy, Z = (z - g.z0) / g.dz;
-      const double fi = floor(X), fj = floor(Y), fk = floor(Z);
-      deposit_cic<double>(g, acc, ch_wrap((int)fi, g.Nx), ch_wrap((int)fj, g.Ny), ch_wrap((int)fk, g.Nz), X - fi,
-                          Y - fj, Z - fk, v[0], v[1], v[2], c.dep_scale);
+      qtail += (unsigned)__popc(dm);
+      __syncwarp();
+      while (qtail - qhead >= 32u) f64_queue_round<PH>(Q, c, P, qhead, 32u, vsum[1], ncol, nref);
     }
+    if (PH & PH_DEPOSIT) {
+      bool ok = act;
+      if (act && !(isfinite(x) && isfinite(y) && isfinite(z) && isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) {
+        bad = 1;  // a non-finite ion is reported, never deposited
+        ok = false;
+      }
+      int di = 0, dj = 0, dk = 0;
+      double wx = 0.0, wy = 0.0, wz = 0.0;
+      if (ok) {
+        const double X = (x - g.x0) / g.dx, Y = (y - g.y0) / g.dy, Z = (z - g.z0) / g.dz;
+        const double fi = floor(X), fj = floor(Y), fk = floor(Z);
+        di = ch_wrap((int)fi, g.Nx); dj = ch_wrap((int)fj, g.Ny); dk = ch_wrap((int)fk, g.Nz);
+        wx = X - fi; wy = Y - fj; wz = Z - fk;
+      }
+      deposit_cic_warp(g, acc, ok, di, dj, dk, wx, wy, wz, v[0], v[1], v[2], c.dep_scale);
+    }
+  }
+  if (QUEUE) {
+    while (qtail != qhead) f64_queue_round<PH>(Q, c, P, qhead, min(qtail - qhead, 32u), vsum[1], ncol, nref);
   }
   if (bad) atomicOr(&cnt->range_error, 2);
   if (PH & PH_PUSH) {
@@ -1908,7 +1982,16 @@ static int pass_one(bool mixed, const StepConsts& c, F64Particles P, MixParticle
         ::ch::note_launch();
     }
   } else {
-    k_pass_f64<PH><<<nb, 256, 0, s>>>(c, P, E64, phi, acc, Nc, sbar, cnt, part), ::ch::note_launch();
+    // the queue of colliding ions (18 KB of shared memory) only with the push
+    const size_t smem = (PH & PH_PUSH) ? sizeof(F64Queue) : 0;
+    if (smem) {
+      static bool attr = false;
+      if (!attr) {
+        cudaFuncSetAttribute(k_pass_f64<PH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+      }
+    }
+    k_pass_f64<PH><<<nb, 256, smem, s>>>(c, P, E64, phi, acc, Nc, sbar, cnt, part), ::ch::note_launch();
   }
   return nb;
 }

@@ -12,10 +12,10 @@ prints one JSON line.
     --mode solve: --steps steps of the plasma of the pass mode; the solves
         inside them (warm start from the previous step's potential) are the
         ones a run makes; prints the solve time, iterations and refinements.
-    --mode e2e: the ions through registered host arrays every step, --steps
-        times: upload, ch_step and download as separate calls (wall time of
-        each, synchronised), then ch_step_host (the download overlapping the
-        deposit and solve).
+    --mode e2e: the ions through host arrays from ch_host_alloc every step,
+        --steps times: upload, ch_step and download as separate calls (wall
+        time of each, synchronised), then ch_step_host (the push streams the
+        host arrays in and out, k_host_push).
 
     python profile_pass.py --grid 128 --ppc 64 --nu 0.5
 """
@@ -102,16 +102,12 @@ def e2e(m, a):
         h.ComputePotential(copy=False)
         for s in range(a.warm):
             h.step(s, 1)
-        pos, vel = h.download()
+        HP, HV = m.HostArray((h.np, 4)), m.HostArray((h.np, 4))  # ch_host_alloc: page-locked, huge pages
+        pos, vel = HP.a, HV.a
+        h.download(pos, vel)
         out["bytes_each_way"] = int(pos.nbytes + vel.nbytes)
-        for x in (pos, vel):
-            m.host_register(x)
         try:
             step = a.warm
-            h.upload(pos, vel)
-            h.step(step, 1)
-            h.download(pos, vel)
-            step += 1
             rows = []
             for _ in range(a.steps):
                 t = [time.perf_counter()]
@@ -122,16 +118,22 @@ def e2e(m, a):
                 rows.append([round(1e3 * (t[i + 1] - t[i]), 2) for i in range(3)])
             out["separate[upload_ms, step_ms, download_ms]"] = rows
             host = []
+            h.set_profiling(True)
+            h.reset_profile()
             for _ in range(a.steps):
                 t0 = time.perf_counter()
                 h.step_host(pos, vel, step, 1)
                 torch.cuda.synchronize()
                 host.append(round(1e3 * (time.perf_counter() - t0), 2))
                 step += 1
+            prof = h.profile()
             out["step_host_ms"] = host
+            out["step_host_pass_ms"] = prof["pass_ms"] / max(1, a.steps)
+            out["host_push_calls"], out["host_push_reruns"] = prof["host_push_calls"], prof["host_push_reruns"]
         finally:
-            for x in (pos, vel):
-                m.host_unregister(x)
+            del pos, vel
+            HP.free()
+            HV.free()
     print(json.dumps(out))
 
 
