@@ -192,6 +192,7 @@ def lib():
             "ch_batch_set_phi": [vp, C.c_int32, vp],
             "ch_batch_get_moments": [vp, C.c_int32, vp],
             "ch_batch_autotune": [vp, C.POINTER(Tuning)],
+            "ch_batch_autotune_cached": [vp, C.c_char_p, C.POINTER(Tuning), C.POINTER(C.c_int32)],
             "ch_batch_set_tuning": [vp, C.POINTER(Tuning)],
             "ch_batch_get_tuning": [vp, C.POINTER(Tuning)],
             "ch_batch_set_profiling": [vp, C.c_int32],
@@ -508,10 +509,17 @@ class Batch:
         _check(lib().ch_batch_get_moments(self._h, int(r), out.ctypes.data))
         return out
 
-    def autotune(self) -> dict:
+    def autotune(self, cache: str | None = None) -> dict:
+        """Times the launch shapes and keeps the fastest; with `cache` (a
+        file of JSON lines) a batch of the same class takes the stored shape
+        instead, and the result says whether it was cached."""
         t = Tuning()
-        _check(lib().ch_batch_autotune(self._h, C.byref(t)))
-        return t.as_dict()
+        if cache is None:
+            _check(lib().ch_batch_autotune(self._h, C.byref(t)))
+            return t.as_dict()
+        hit = C.c_int32(0)
+        _check(lib().ch_batch_autotune_cached(self._h, os.fsencode(cache), C.byref(t), C.byref(hit)))
+        return dict(t.as_dict(), cached=bool(hit.value))
 
     def tuning(self) -> dict:
         t = Tuning()

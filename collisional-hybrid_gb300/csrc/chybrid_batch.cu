@@ -10,6 +10,7 @@
 // keep the runs contiguous).  The step number lives on the device, so a step
 // is captured once as a CUDA graph and replayed.
 #include <math.h>
+#include <stdio.h>
 #include <string.h>
 
 #include <new>
@@ -812,5 +813,77 @@ extern "C" ch_status ch_batch_get_profile(ch_batch* b, ch_profile* out) {
 extern "C" ch_status ch_batch_get_stream(ch_batch* b, void** stream) {
   if (!b || !stream) return ch_fail(CH_ERR_ARG, "null argument");
   *stream = (void*)b->stream;
+  return CH_OK;
+}
+
+// ------------------------------------------------------------------ tuning cache
+// The launch shape ch_batch_autotune picks depends on the device and on the
+// batch's shape: the run count and how the nodes and ions are spread over
+// the runs.  A batch whose class (device name and SM count, run count, and
+// the power-of-two buckets of its total nodes, total ions and largest run)
+// matches a line of the cache file takes that line's shape without timing.
+static int log2_bucket(int64_t v) {
+  int b = 0;
+  while (b < 62 && (int64_t(1) << (b + 1)) <= v) ++b;
+  return b;
+}
+
+static void tuning_key(const ch_batch* b, char* key, size_t n) {
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, b->device) != cudaSuccess) {
+    cudaGetLastError();
+    snprintf(prop.name, sizeof(prop.name), "unknown");
+  }
+  for (char* q = prop.name; *q; ++q)
+    if (*q == ' ' || *q == '"' || *q == '|') *q = '_';
+  int64_t maxrun = 0;
+  for (const GridDesc& g : b->g) maxrun = g.N > maxrun ? g.N : maxrun;
+  snprintf(key, n, "%s|sm%d|runs%d|nodes2^%d|ions2^%d|maxrun2^%d", prop.name, b->sms, b->nruns,
+           log2_bucket(b->Ntot), log2_bucket(b->NPtot), log2_bucket(maxrun));
+}
+
+extern "C" ch_status ch_batch_autotune_cached(ch_batch* b, const char* path, ch_batch_tuning* out, int32_t* hit) {
+  if (!b || !path) return ch_fail(CH_ERR_ARG, "null argument");
+  if (hit) *hit = 0;
+  char key[256];
+  tuning_key(b, key, sizeof(key));
+  FILE* f = fopen(path, "r");
+  if (f) {
+    char line[512];
+    ch_batch_tuning t, r;
+    bool found = false;
+    while (fgets(line, sizeof(line), f)) {
+      char k[256];
+      memset(&r, 0, sizeof(r));
+      if (sscanf(line,
+                 "{\"key\": \"%255[^\"]\", \"cluster\": %d, \"pass_ctas_per_sm\": %d, \"cluster_big\": %d, "
+                 "\"pass_ms\": %lf, \"solve_ms\": %lf}",
+                 k, &r.cluster, &r.pass_ctas_per_sm, &r.cluster_big, &r.pass_ms, &r.solve_ms) == 6 &&
+          !strcmp(k, key)) {
+        t = r;  // the last matching line wins
+        found = true;
+      }
+    }
+    fclose(f);
+    if (found) {
+      ch_status rc = ch_batch_set_tuning(b, &t);
+      if (rc) return rc;
+      b->tune.pass_ms = t.pass_ms;
+      b->tune.solve_ms = t.solve_ms;
+      if (hit) *hit = 1;
+      if (out) *out = b->tune;
+      return CH_OK;
+    }
+  }
+  ch_batch_tuning t;
+  ch_status rc = ch_batch_autotune(b, &t);
+  if (rc) return rc;
+  f = fopen(path, "a");
+  if (!f) return ch_fail(CH_ERR_ARG, "ch_batch_autotune_cached: cannot append to %s", path);
+  fprintf(f, "{\"key\": \"%s\", \"cluster\": %d, \"pass_ctas_per_sm\": %d, \"cluster_big\": %d, "
+             "\"pass_ms\": %.6f, \"solve_ms\": %.6f}\n",
+          key, t.cluster, t.pass_ctas_per_sm, t.cluster_big, t.pass_ms, t.solve_ms);
+  fclose(f);
+  if (out) *out = t;
   return CH_OK;
 }

@@ -661,9 +661,8 @@ __device__ __forceinline__ TileShared& tile_smem_base(unsigned char* smem) {
   return *reinterpret_cast<TileShared*>(smem - tile_smem_skip<PH>());
 }
 
-// value += v for a 64-bit integer kept as (hi, lo) 32-bit words in shared
-// memory; the carry out of lo is detected from the returned old value, so
-// the final (hi, lo) is the exact 64-bit sum whatever the order of adds.
+// value += v for a 64-bit integer kept in shared memory as two 32-bit words
+// whose sum lo + 2^16 hi is the exact value whatever the order of adds.
 // Adds v (|v| < 2^31) to a tile sum: two 32-bit reductions that need no
 // returned value, so no carry round trip; neither word can overflow within
 // a segment of at most CH_DEP_SEG ions (below 2^16 adds of under 2^16 to

@@ -372,6 +372,12 @@ ch_status ch_batch_set_phi(ch_batch* b, int32_t run, const double* in);
  * keeps the fastest; out (nullable) receives the choice. */
 ch_status ch_batch_autotune(ch_batch* b, ch_batch_tuning* out);
 ch_status ch_batch_set_tuning(ch_batch* b, const ch_batch_tuning* t);
+/* ch_batch_autotune with a cache file of JSON lines, kept across processes:
+ * a batch of the same class (device name and SM count, run count, and the
+ * power-of-two buckets of its total nodes, total ions and largest run)
+ * takes the stored launch shape without timing (*hit = 1); otherwise it is
+ * tuned and a line is appended (*hit = 0).  hit and out are nullable. */
+ch_status ch_batch_autotune_cached(ch_batch* b, const char* path, ch_batch_tuning* out, int32_t* hit);
 ch_status ch_batch_get_tuning(ch_batch* b, ch_batch_tuning* out);
 /* Per-phase timing of ch_batch_step (events; graphs are not used while
  * profiling is on) and the stream of the batch. */

@@ -200,3 +200,32 @@ def test_batch_sorting_does_not_change_the_runs(chy):
     for ra, rb in zip(*out):
         for a, c in zip(ra, rb):
             assert np.array_equal(a, c)
+
+
+@pytest.mark.gpu
+def test_batch_autotune_cache_across_batches(chy, tmp_path):
+    """ch_batch_autotune_cached: the first batch of a class is timed and its
+    launch shape appended to the cache file; a second batch of the same class
+    (another process would read the same file) takes the stored shape without
+    timing; a batch of another class is timed again."""
+    cache = str(tmp_path / "tuning.jsonl")
+    params, nions, loaders = _runs(chy)
+    shapes = []
+    for k in range(2):
+        with chy.Batch(params, nions) as b:
+            b.load(loaders)
+            b.initialize()
+            t = b.autotune(cache=cache)
+            assert t["cached"] == (k == 1), t
+            assert b.tuning()["cluster"] == t["cluster"]
+            b.step(0, 1)
+            shapes.append((t["cluster"], t["pass_ctas_per_sm"], t["cluster_big"]))
+    assert shapes[0] == shapes[1]
+    lines = open(cache).read().splitlines()
+    assert len(lines) == 1 and '"key": "' in lines[0]
+    # three runs instead of four: another class
+    with chy.Batch(params[:3], nions[:3]) as b:
+        b.load(loaders[:3])
+        b.initialize()
+        assert not b.autotune(cache=cache)["cached"]
+    assert len(open(cache).read().splitlines()) == 2
