@@ -710,9 +710,14 @@ __device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, i
 // contributions of its slots in the cell most of them share in registers;
 // the sums of lanes whose cells agree are then added up through a matrix in
 // shared memory (lane q sums entry q of each run of equal cells) and added to
-// the brick once per run.  Slots in another cell ("displaced": they moved
-// since the last sort) go to the warp's ring and are added lane by lane, 32
-// at a time.
+// the brick once per run.  The other slots go to the warp's ring and are
+// added lane by lane, 32 at a time: ions in another cell ("displaced": they
+// moved since the last sort) to the brick's tile, ions outside the brick's
+// halo or faster than CH_TILE_VMAX straight to the global accumulators.
+// The chunk itself runs without divergent branches: a slot the lane does not
+// sum enters the same arithmetic with zero weights and zero velocity
+// (selected, so that a non-finite ion adds nothing), and the accumulators
+// start at minus the four biases of rni_fma.
 // Every contribution is rounded to an integer before any addition, so the
 // result does not depend on the order; no block barrier is needed.
 // SCAT (a step that ends with a sort): every ion read is also written to
@@ -730,62 +735,76 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
   uint32_t* ring = sh.d_ip + warp * CH_DEP_RW;
   const unsigned lt = (1u << lane) - 1u;
   unsigned dh = 0, dt = 0;  // warp-uniform ring head / tail
-  // lanes l < n add the ring's next n displaced ions
+  // lanes l < n add the ring's next n ions
   auto drain = [&](unsigned n) {
     if ((unsigned)lane < n) {
       const uint32_t ip = ring[(dh + lane) & (CH_DEP_RW - 1)];
       const float4 p = P.pos[ip], v = P.vel[ip];
       const uint32_t cell = __float_as_uint(p.w);
-      bool inbox;  // checked when the ion was put in the ring
-      const int key = box_key(g, cell & (CH_MAX_NX - 1), (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
-                              cell >> (CH_PACK_BX + CH_PACK_BY), bi0, bj0, bk0, &inbox);
-      tile_deposit_lane(sh, key, p.x, p.y, p.z, v.x, v.y, v.z);
+      const int i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
+                kz = cell >> (CH_PACK_BX + CH_PACK_BY);
+      bool inbox;
+      const int key = box_key(g, i, j, kz, bi0, bj0, bk0, &inbox);
+      const bool slow = fabsf(v.x) >= CH_TILE_VMAX || fabsf(v.y) >= CH_TILE_VMAX || fabsf(v.z) >= CH_TILE_VMAX;
+      if (inbox && !slow) tile_deposit_lane(sh, key, p.x, p.y, p.z, v.x, v.y, v.z);
+      else deposit_cic<float>(g, acc, i, j, kz, p.x, p.y, p.z, v.x, v.y, v.z, c.f.dep_scale);
     }
     dh += n;
     __syncwarp();  // the entries are read before later appends reuse them
   };
   for (uint32_t cb = seg0 + (uint32_t)warp * 128u; cb < total; cb += (blockDim.x >> 5) * 128u) {
     const uint32_t s0 = cb + 4u * (uint32_t)lane;
-    int r = 0;
+    const uint32_t cend = min(cb + 128u, total);
+    // the row of the chunk's first slot (warp-uniform: the last row starting
+    // at or before it, so empty rows are skipped)
+    int rc = 0;
 #pragma unroll
     for (int st = 8; st > 0; st >>= 1)
-      if (r + st < TY * TZ && sh.pre[r + st] <= s0) r += st;
-    int keys[CH_TILE_K];
+      if (rc + st < TY * TZ && sh.pre[rc + st] <= cb) rc += st;
+    // slot -> index in the ion arrays; slots past the chunk's end read its
+    // last ion and are masked below
     uint32_t ips[CH_TILE_K];
-    float ox[CH_TILE_K], oy[CH_TILE_K], oz[CH_TILE_K], vx[CH_TILE_K], vy[CH_TILE_K], vz[CH_TILE_K];
+    if (cend <= sh.pre[rc + 1]) {  // the chunk lies in one row (warp-uniform)
+      const uint32_t base = sh.rowbeg[rc] - sh.pre[rc];
+#pragma unroll
+      for (int k = 0; k < CH_TILE_K; ++k) ips[k] = min(s0 + k, cend - 1u) + base;
+    } else {
+#pragma unroll
+      for (int k = 0; k < CH_TILE_K; ++k) {
+        const uint32_t s = min(s0 + k, cend - 1u);
+        int r = 0;
+#pragma unroll
+        for (int st = 8; st > 0; st >>= 1)
+          if (r + st < TY * TZ && sh.pre[r + st] <= s) r += st;
+        ips[k] = sh.rowbeg[r] + (s - sh.pre[r]);
+      }
+    }
+    float4 pk[CH_TILE_K], vk[CH_TILE_K];
+#pragma unroll
+    for (int k = 0; k < CH_TILE_K; ++k) { pk[k] = P.pos[ips[k]]; vk[k] = P.vel[ips[k]]; }
+    int keys[CH_TILE_K];
+    bool other[CH_TILE_K];  // to the ring whatever the lane's cell
 #pragma unroll
     for (int k = 0; k < CH_TILE_K; ++k) {
-      const uint32_t idx = s0 + k;
-      keys[k] = -1;
-      ips[k] = 0;
-      ox[k] = oy[k] = oz[k] = vx[k] = vy[k] = vz[k] = 0.0f;
-      if (idx < total) {
-        while (r + 1 < TY * TZ && sh.pre[r + 1] <= idx) ++r;  // rows may be empty
-        const uint32_t ip = sh.rowbeg[r] + (idx - sh.pre[r]);
-        const float4 p = P.pos[ip], v = P.vel[ip];
-        const uint32_t cell = __float_as_uint(p.w);
-        const int i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
-                  kz = cell >> (CH_PACK_BX + CH_PACK_BY);
-        if constexpr (SCAT) {  // every ion, whether or not it is deposited here
-          const uint32_t d = dst_starts[(kz * g.Ny + j) * g.Nx + i] + P.rank[ip];
-          Q.pos[d] = p;
-          Q.vel[d] = v;
-        }
-        const bool finite =
-            isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
-        bool inbox;
-        const int key = box_key(g, i, j, kz, bi0, bj0, bk0, &inbox);
-        const bool slow = fabsf(v.x) >= CH_TILE_VMAX || fabsf(v.y) >= CH_TILE_VMAX || fabsf(v.z) >= CH_TILE_VMAX;
-        if (!finite) {
-          bad = 1;
-        } else if (inbox && !slow) {
-          keys[k] = key;
-          ips[k] = ip;
-          ox[k] = p.x; oy[k] = p.y; oz[k] = p.z; vx[k] = v.x; vy[k] = v.y; vz[k] = v.z;
-        } else {
-          deposit_cic<float>(g, acc, i, j, kz, p.x, p.y, p.z, v.x, v.y, v.z, c.f.dep_scale);
-        }
+      const float4 p = pk[k], v = vk[k];
+      const bool valid = s0 + k < cend;
+      const uint32_t cell = __float_as_uint(p.w);
+      const int i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
+                kz = cell >> (CH_PACK_BX + CH_PACK_BY);
+      if (SCAT && valid) {  // every ion, whether or not it is deposited here
+        const uint32_t d = dst_starts[(kz * g.Ny + j) * g.Nx + i] + P.rank[ips[k]];
+        Q.pos[d] = p;
+        Q.vel[d] = v;
       }
+      const bool finite =
+          isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
+      bool inbox;
+      const int key = box_key(g, i, j, kz, bi0, bj0, bk0, &inbox);
+      const bool slow = fabsf(v.x) >= CH_TILE_VMAX || fabsf(v.y) >= CH_TILE_VMAX || fabsf(v.z) >= CH_TILE_VMAX;
+      if (valid && !finite) bad = 1;
+      const bool take = valid && finite && inbox && !slow;
+      keys[k] = take ? key : -1;
+      other[k] = valid && finite && !take;
     }
     // the cell most of the lane's slots share (ties: the earliest)
     int akey = -1, best = 0;
@@ -796,28 +815,31 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
       for (int q = 0; q < CH_TILE_K; ++q) n += (keys[q] == keys[k]) ? 1 : 0;
       if (keys[k] >= 0 && n > best) { best = n; akey = keys[k]; }
     }
-    // displaced slots to the ring (at most 31 wait there, so 128 more fit)
+    // displaced, outside and fast slots to the ring (at most 31 wait there,
+    // so 128 more fit)
 #pragma unroll
     for (int k = 0; k < CH_TILE_K; ++k) {
-      const bool dsp = keys[k] >= 0 && keys[k] != akey;
+      const bool dsp = other[k] || (keys[k] >= 0 && keys[k] != akey);
       const unsigned m = __ballot_sync(0xffffffffu, dsp);
       if (dsp) ring[(dt + __popc(m & lt)) & (CH_DEP_RW - 1)] = ips[k];
       dt += (unsigned)__popc(m);
     }
+    // each slot adds rint(x) + CH_RNI_BIAS per entry; starting from minus
+    // four biases leaves the exact sums, |sum| < 2^25
     unsigned a[32];
 #pragma unroll
-    for (int q = 0; q < 32; ++q) a[q] = 0u;
-    unsigned cnt = 0;
+    for (int q = 0; q < 32; ++q) a[q] = 0u - (unsigned)CH_TILE_K * (unsigned)CH_RNI_BIAS;
 #pragma unroll
     for (int k = 0; k < CH_TILE_K; ++k) {
-      if (keys[k] < 0 || keys[k] != akey) continue;
-      ++cnt;
-      const float wxh = ox[k], wyh = oy[k], wzh = oz[k];
-      const float wxl = 1.0f - wxh, wyl = 1.0f - wyh, wzl = 1.0f - wzh;
+      const bool use = keys[k] >= 0 && keys[k] == akey;
+      const float wxh = use ? pk[k].x : 0.0f, wyh = use ? pk[k].y : 0.0f, oz = use ? pk[k].z : 0.0f;
+      const float wxl = 1.0f - wxh, wyl = 1.0f - wyh;
+      const float wzh = use ? oz : 0.0f, wzl = use ? 1.0f - oz : 0.0f;
       const float w[8] = {wzl * wyl * wxl, wzl * wyl * wxh, wzl * wyh * wxl, wzl * wyh * wxh,
                           wzh * wyl * wxl, wzh * wyl * wxh, wzh * wyh * wxl, wzh * wyh * wxh};
       // (v 2^19) w is v (w 2^19) exactly: the scale is a power of two
-      const float fx = vx[k] * CH_TILE_FSCALE, fy = vy[k] * CH_TILE_FSCALE, fz = vz[k] * CH_TILE_FSCALE;
+      const float fx = use ? vk[k].x * CH_TILE_FSCALE : 0.0f, fy = use ? vk[k].y * CH_TILE_FSCALE : 0.0f,
+                  fz = use ? vk[k].z * CH_TILE_FSCALE : 0.0f;
 #pragma unroll
       for (int cn = 0; cn < 8; ++cn) {
         a[cn] += (unsigned)rni_fma(w[cn], CH_TILE_DSCALE);
@@ -826,9 +848,6 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
         a[24 + cn] += (unsigned)rni_fma(fz, w[cn]);
       }
     }
-    const unsigned unbias = cnt * (unsigned)CH_RNI_BIAS;
-#pragma unroll
-    for (int q = 0; q < 32; ++q) a[q] -= unbias;  // exact sums, |sum| < 2^25
     // Sums of lanes whose cells agree: lane l's 32 sums become row l of the
     // warp's matrix, and lane q walks column q down the rows, adding one sum
     // per run of equal cells (consecutive in sorted order) to node q & 7 of
