@@ -826,9 +826,8 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
     }
     // each slot adds rint(x) + CH_RNI_BIAS per entry; starting from minus
     // four biases leaves the exact sums, |sum| < 2^25
+    constexpr unsigned a0 = 0u - (unsigned)CH_TILE_K * (unsigned)CH_RNI_BIAS;
     unsigned a[32];
-#pragma unroll
-    for (int q = 0; q < 32; ++q) a[q] = 0u - (unsigned)CH_TILE_K * (unsigned)CH_RNI_BIAS;
 #pragma unroll
     for (int k = 0; k < CH_TILE_K; ++k) {
       const bool use = keys[k] >= 0 && keys[k] == akey;
@@ -842,35 +841,36 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
                   fz = use ? vk[k].z * CH_TILE_FSCALE : 0.0f;
 #pragma unroll
       for (int cn = 0; cn < 8; ++cn) {
-        a[cn] += (unsigned)rni_fma(w[cn], CH_TILE_DSCALE);
-        a[8 + cn] += (unsigned)rni_fma(fx, w[cn]);
-        a[16 + cn] += (unsigned)rni_fma(fy, w[cn]);
-        a[24 + cn] += (unsigned)rni_fma(fz, w[cn]);
+        a[cn] = (k == 0 ? a0 : a[cn]) + (unsigned)rni_fma(w[cn], CH_TILE_DSCALE);
+        a[8 + cn] = (k == 0 ? a0 : a[8 + cn]) + (unsigned)rni_fma(fx, w[cn]);
+        a[16 + cn] = (k == 0 ? a0 : a[16 + cn]) + (unsigned)rni_fma(fy, w[cn]);
+        a[24 + cn] = (k == 0 ? a0 : a[24 + cn]) + (unsigned)rni_fma(fz, w[cn]);
       }
     }
     // Sums of lanes whose cells agree: lane l's 32 sums become row l of the
     // warp's matrix, and lane q walks column q down the rows, adding one sum
     // per run of equal cells (consecutive in sorted order) to node q & 7 of
-    // that cell, moment q >> 3.
+    // that cell, moment q >> 3.  The run ends come from one ballot, so the
+    // walk tests a bit of a warp-wide word per row instead of comparing cells.
     unsigned* M = sh.d_sum[warp];
 #pragma unroll
     for (int q = 0; q < 32; ++q) M[lane * 33 + q] = a[q];
+    const int up = __shfl_down_sync(0xffffffffu, akey, 1);
+    const unsigned ends = __ballot_sync(0xffffffffu, lane == 31 || akey != up);  // row l ends a run
     __syncwarp();
     {
       const int cn = lane & 7, m = lane >> 3;
       const int off = (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
-      int cur = -1, sum = 0;  // |sum| < 32 x 2^25
-#pragma unroll 8
+      int sum = 0;  // |sum| < 32 x 2^25
+#pragma unroll
       for (int l = 0; l < 32; ++l) {
-        const int kl = __shfl_sync(0xffffffffu, akey, l);
-        if (kl != cur) {  // warp-uniform
-          if (cur >= 0 && sum != 0) shared_add64(&sh.acc_lo[m][cur + off], &sh.acc_hi[m][cur + off], sum);
-          cur = kl;
+        sum += (int)M[l * 33 + lane];  // a lane without a cell holds zeros
+        if ((ends >> l) & 1u) {
+          const int kl = __shfl_sync(0xffffffffu, akey, l);
+          if (kl >= 0 && sum != 0) shared_add64(&sh.acc_lo[m][kl + off], &sh.acc_hi[m][kl + off], sum);
           sum = 0;
         }
-        sum += (int)M[l * 33 + lane];  // a lane without a cell holds zeros
       }
-      if (cur >= 0 && sum != 0) shared_add64(&sh.acc_lo[m][cur + off], &sh.acc_hi[m][cur + off], sum);
     }
     __syncwarp();  // ring entries visible, matrix read before the next chunk rewrites it
     while (dt - dh >= 32u) drain(32u);
