@@ -672,6 +672,14 @@ __device__ __forceinline__ void shared_add64(unsigned* lo, int* hi, long long v)
   atomicAdd(hi, (int)(v >> 16));
 }
 
+// Adds x to a tile sum from r = rni_fma(...) = rint(x) + CH_RNI_BIAS: the
+// bias has zero low 16 bits, so r's low half is x's and r's high half
+// exceeds x >> 16 by the bias's (r is positive: no sign to carry).
+__device__ __forceinline__ void shared_add_rni(unsigned* lo, int* hi, int r) {
+  atomicAdd(lo, (unsigned)r & 0xFFFFu);
+  atomicAdd(hi, (int)((unsigned)r >> 16) - (CH_RNI_BIAS >> 16));
+}
+
 // One ion's 32 fixed-point contributions added lane by lane to the shared
 // tile (node = the ion's cell within the box).
 __device__ __forceinline__ void tile_deposit_lane(TileShared& sh, int node, float wxh, float wyh, float wzh,
@@ -684,20 +692,22 @@ __device__ __forceinline__ void tile_deposit_lane(TileShared& sh, int node, floa
     const int nd = node + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
     // (v 2^19) w is v (w 2^19) exactly: the scale is a power of two
     const float wf = w[cn] * CH_TILE_FSCALE;
-    shared_add64(&sh.acc_lo[0][nd], &sh.acc_hi[0][nd], rni_fma(w[cn], CH_TILE_DSCALE) - CH_RNI_BIAS);
-    shared_add64(&sh.acc_lo[1][nd], &sh.acc_hi[1][nd], rni_fma(vx, wf) - CH_RNI_BIAS);
-    shared_add64(&sh.acc_lo[2][nd], &sh.acc_hi[2][nd], rni_fma(vy, wf) - CH_RNI_BIAS);
-    shared_add64(&sh.acc_lo[3][nd], &sh.acc_hi[3][nd], rni_fma(vz, wf) - CH_RNI_BIAS);
+    shared_add_rni(&sh.acc_lo[0][nd], &sh.acc_hi[0][nd], rni_fma(w[cn], CH_TILE_DSCALE));
+    shared_add_rni(&sh.acc_lo[1][nd], &sh.acc_hi[1][nd], rni_fma(vx, wf));
+    shared_add_rni(&sh.acc_lo[2][nd], &sh.acc_hi[2][nd], rni_fma(vy, wf));
+    shared_add_rni(&sh.acc_lo[3][nd], &sh.acc_hi[3][nd], rni_fma(vz, wf));
   }
 }
 
-// Box-relative cell offset of (i, j, k) from the box origin, periodic.
-__device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, int bi0, int bj0, int bk0,
+// Box-relative cell offset of (i, j, k) from the box origin, periodic; the
+// origin (wi0, wj0, wk0) is given wrapped into the grid, so one correction
+// per axis brings the difference into [0, N).
+__device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, int wi0, int wj0, int wk0,
                                        bool* inbox) {
-  int di = i - bi0, dj = j - bj0, dk = k - bk0;
-  di += di < 0 ? g.Nx : 0; di -= di >= g.Nx ? g.Nx : 0;
-  dj += dj < 0 ? g.Ny : 0; dj -= dj >= g.Ny ? g.Ny : 0;
-  dk += dk < 0 ? g.Nz : 0; dk -= dk >= g.Nz ? g.Nz : 0;
+  int di = i - wi0, dj = j - wj0, dk = k - wk0;
+  di += di < 0 ? g.Nx : 0;
+  dj += dj < 0 ? g.Ny : 0;
+  dk += dk < 0 ? g.Nz : 0;
   *inbox = di <= BX - 2 && dj <= BY - 2 && dk <= BZ - 2;
   return (dk * BY + dj) * BX + di;
 }
@@ -728,7 +738,7 @@ __device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, i
 template <bool SCAT>
 __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepConsts& c, MixParticles P,
                                                     unsigned long long* __restrict__ acc, uint32_t seg0,
-                                                    uint32_t total, int bi0, int bj0, int bk0, int& bad,
+                                                    uint32_t total, int wi0, int wj0, int wk0, int& bad,
                                                     MixParticles Q, const uint32_t* __restrict__ dst_starts) {
   const GridDesc& g = c.g;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -744,7 +754,7 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
       const int i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
                 kz = cell >> (CH_PACK_BX + CH_PACK_BY);
       bool inbox;
-      const int key = box_key(g, i, j, kz, bi0, bj0, bk0, &inbox);
+      const int key = box_key(g, i, j, kz, wi0, wj0, wk0, &inbox);
       const bool slow = fabsf(v.x) >= CH_TILE_VMAX || fabsf(v.y) >= CH_TILE_VMAX || fabsf(v.z) >= CH_TILE_VMAX;
       if (inbox && !slow) tile_deposit_lane(sh, key, p.x, p.y, p.z, v.x, v.y, v.z);
       else deposit_cic<float>(g, acc, i, j, kz, p.x, p.y, p.z, v.x, v.y, v.z, c.f.dep_scale);
@@ -752,130 +762,137 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
     dh += n;
     __syncwarp();  // the entries are read before later appends reuse them
   };
-  for (uint32_t cb = seg0 + (uint32_t)warp * 128u; cb < total; cb += (blockDim.x >> 5) * 128u) {
-    const uint32_t s0 = cb + 4u * (uint32_t)lane;
-    const uint32_t cend = min(cb + 128u, total);
-    // the row of the chunk's first slot (warp-uniform: the last row starting
-    // at or before it, so empty rows are skipped)
-    int rc = 0;
+  // one pass more than there are chunks: the last one only drains the ring
+  // (a single inlined copy of the drain)
+  for (uint32_t cb = seg0 + (uint32_t)warp * 128u;; cb += (blockDim.x >> 5) * 128u) {
+    const bool more = cb < total;  // warp-uniform
+    if (more) {
+      const uint32_t s0 = cb + 4u * (uint32_t)lane;
+      const uint32_t cend = min(cb + 128u, total);
+      // the row of the chunk's first slot (warp-uniform: the last row starting
+      // at or before it, so empty rows are skipped)
+      int rc = 0;
 #pragma unroll
-    for (int st = 8; st > 0; st >>= 1)
-      if (rc + st < TY * TZ && sh.pre[rc + st] <= cb) rc += st;
-    // slot -> index in the ion arrays; slots past the chunk's end read its
-    // last ion and are masked below
-    uint32_t ips[CH_TILE_K];
-    if (cend <= sh.pre[rc + 1]) {  // the chunk lies in one row (warp-uniform)
-      const uint32_t base = sh.rowbeg[rc] - sh.pre[rc];
+      for (int st = 8; st > 0; st >>= 1)
+        if (rc + st < TY * TZ && sh.pre[rc + st] <= cb) rc += st;
+      // slot -> index in the ion arrays; slots past the chunk's end read its
+      // last ion and are masked below
+      uint32_t ips[CH_TILE_K];
+      if (cend <= sh.pre[rc + 1]) {  // the chunk lies in one row (warp-uniform)
+        const uint32_t base = sh.rowbeg[rc] - sh.pre[rc];
 #pragma unroll
-      for (int k = 0; k < CH_TILE_K; ++k) ips[k] = min(s0 + k, cend - 1u) + base;
-    } else {
+        for (int k = 0; k < CH_TILE_K; ++k) ips[k] = min(s0 + k, cend - 1u) + base;
+      } else {
 #pragma unroll
-      for (int k = 0; k < CH_TILE_K; ++k) {
-        const uint32_t s = min(s0 + k, cend - 1u);
-        int r = 0;
+        for (int k = 0; k < CH_TILE_K; ++k) {
+          const uint32_t s = min(s0 + k, cend - 1u);
+          int r = 0;
 #pragma unroll
-        for (int st = 8; st > 0; st >>= 1)
-          if (r + st < TY * TZ && sh.pre[r + st] <= s) r += st;
-        ips[k] = sh.rowbeg[r] + (s - sh.pre[r]);
-      }
-    }
-    float4 pk[CH_TILE_K], vk[CH_TILE_K];
-#pragma unroll
-    for (int k = 0; k < CH_TILE_K; ++k) { pk[k] = P.pos[ips[k]]; vk[k] = P.vel[ips[k]]; }
-    int keys[CH_TILE_K];
-    bool other[CH_TILE_K];  // to the ring whatever the lane's cell
-#pragma unroll
-    for (int k = 0; k < CH_TILE_K; ++k) {
-      const float4 p = pk[k], v = vk[k];
-      const bool valid = s0 + k < cend;
-      const uint32_t cell = __float_as_uint(p.w);
-      const int i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
-                kz = cell >> (CH_PACK_BX + CH_PACK_BY);
-      if (SCAT && valid) {  // every ion, whether or not it is deposited here
-        const uint32_t d = dst_starts[(kz * g.Ny + j) * g.Nx + i] + P.rank[ips[k]];
-        Q.pos[d] = p;
-        Q.vel[d] = v;
-      }
-      const bool finite =
-          isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
-      bool inbox;
-      const int key = box_key(g, i, j, kz, bi0, bj0, bk0, &inbox);
-      const bool slow = fabsf(v.x) >= CH_TILE_VMAX || fabsf(v.y) >= CH_TILE_VMAX || fabsf(v.z) >= CH_TILE_VMAX;
-      if (valid && !finite) bad = 1;
-      const bool take = valid && finite && inbox && !slow;
-      keys[k] = take ? key : -1;
-      other[k] = valid && finite && !take;
-    }
-    // the cell most of the lane's slots share (ties: the earliest)
-    int akey = -1, best = 0;
-#pragma unroll
-    for (int k = 0; k < CH_TILE_K; ++k) {
-      int n = 0;
-#pragma unroll
-      for (int q = 0; q < CH_TILE_K; ++q) n += (keys[q] == keys[k]) ? 1 : 0;
-      if (keys[k] >= 0 && n > best) { best = n; akey = keys[k]; }
-    }
-    // displaced, outside and fast slots to the ring (at most 31 wait there,
-    // so 128 more fit)
-#pragma unroll
-    for (int k = 0; k < CH_TILE_K; ++k) {
-      const bool dsp = other[k] || (keys[k] >= 0 && keys[k] != akey);
-      const unsigned m = __ballot_sync(0xffffffffu, dsp);
-      if (dsp) ring[(dt + __popc(m & lt)) & (CH_DEP_RW - 1)] = ips[k];
-      dt += (unsigned)__popc(m);
-    }
-    // each slot adds rint(x) + CH_RNI_BIAS per entry; starting from minus
-    // four biases leaves the exact sums, |sum| < 2^25
-    constexpr unsigned a0 = 0u - (unsigned)CH_TILE_K * (unsigned)CH_RNI_BIAS;
-    unsigned a[32];
-#pragma unroll
-    for (int k = 0; k < CH_TILE_K; ++k) {
-      const bool use = keys[k] >= 0 && keys[k] == akey;
-      const float wxh = use ? pk[k].x : 0.0f, wyh = use ? pk[k].y : 0.0f, oz = use ? pk[k].z : 0.0f;
-      const float wxl = 1.0f - wxh, wyl = 1.0f - wyh;
-      const float wzh = use ? oz : 0.0f, wzl = use ? 1.0f - oz : 0.0f;
-      const float w[8] = {wzl * wyl * wxl, wzl * wyl * wxh, wzl * wyh * wxl, wzl * wyh * wxh,
-                          wzh * wyl * wxl, wzh * wyl * wxh, wzh * wyh * wxl, wzh * wyh * wxh};
-      // (v 2^19) w is v (w 2^19) exactly: the scale is a power of two
-      const float fx = use ? vk[k].x * CH_TILE_FSCALE : 0.0f, fy = use ? vk[k].y * CH_TILE_FSCALE : 0.0f,
-                  fz = use ? vk[k].z * CH_TILE_FSCALE : 0.0f;
-#pragma unroll
-      for (int cn = 0; cn < 8; ++cn) {
-        a[cn] = (k == 0 ? a0 : a[cn]) + (unsigned)rni_fma(w[cn], CH_TILE_DSCALE);
-        a[8 + cn] = (k == 0 ? a0 : a[8 + cn]) + (unsigned)rni_fma(fx, w[cn]);
-        a[16 + cn] = (k == 0 ? a0 : a[16 + cn]) + (unsigned)rni_fma(fy, w[cn]);
-        a[24 + cn] = (k == 0 ? a0 : a[24 + cn]) + (unsigned)rni_fma(fz, w[cn]);
-      }
-    }
-    // Sums of lanes whose cells agree: lane l's 32 sums become row l of the
-    // warp's matrix, and lane q walks column q down the rows, adding one sum
-    // per run of equal cells (consecutive in sorted order) to node q & 7 of
-    // that cell, moment q >> 3.  The run ends come from one ballot, so the
-    // walk tests a bit of a warp-wide word per row instead of comparing cells.
-    unsigned* M = sh.d_sum[warp];
-#pragma unroll
-    for (int q = 0; q < 32; ++q) M[lane * 33 + q] = a[q];
-    const int up = __shfl_down_sync(0xffffffffu, akey, 1);
-    const unsigned ends = __ballot_sync(0xffffffffu, lane == 31 || akey != up);  // row l ends a run
-    __syncwarp();
-    {
-      const int cn = lane & 7, m = lane >> 3;
-      const int off = (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
-      int sum = 0;  // |sum| < 32 x 2^25
-#pragma unroll
-      for (int l = 0; l < 32; ++l) {
-        sum += (int)M[l * 33 + lane];  // a lane without a cell holds zeros
-        if ((ends >> l) & 1u) {
-          const int kl = __shfl_sync(0xffffffffu, akey, l);
-          if (kl >= 0 && sum != 0) shared_add64(&sh.acc_lo[m][kl + off], &sh.acc_hi[m][kl + off], sum);
-          sum = 0;
+          for (int st = 8; st > 0; st >>= 1)
+            if (r + st < TY * TZ && sh.pre[r + st] <= s) r += st;
+          ips[k] = sh.rowbeg[r] + (s - sh.pre[r]);
         }
       }
+      float4 pk[CH_TILE_K], vk[CH_TILE_K];
+#pragma unroll
+      for (int k = 0; k < CH_TILE_K; ++k) { pk[k] = P.pos[ips[k]]; vk[k] = P.vel[ips[k]]; }
+      int keys[CH_TILE_K];
+      bool other[CH_TILE_K];  // to the ring whatever the lane's cell
+#pragma unroll
+      for (int k = 0; k < CH_TILE_K; ++k) {
+        const float4 p = pk[k], v = vk[k];
+        const bool valid = s0 + k < cend;
+        const uint32_t cell = __float_as_uint(p.w);
+        const int i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
+                  kz = cell >> (CH_PACK_BX + CH_PACK_BY);
+        if (SCAT && valid) {  // every ion, whether or not it is deposited here
+          const uint32_t d = dst_starts[(kz * g.Ny + j) * g.Nx + i] + P.rank[ips[k]];
+          Q.pos[d] = p;
+          Q.vel[d] = v;
+        }
+        const bool finite =
+            isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
+        bool inbox;
+        const int key = box_key(g, i, j, kz, wi0, wj0, wk0, &inbox);
+        const bool slow = fabsf(v.x) >= CH_TILE_VMAX || fabsf(v.y) >= CH_TILE_VMAX || fabsf(v.z) >= CH_TILE_VMAX;
+        if (valid && !finite) bad = 1;
+        const bool take = valid && finite && inbox && !slow;
+        keys[k] = take ? key : -1;
+        other[k] = valid && finite && !take;
+      }
+      // the cell most of the lane's slots share (ties: the earliest)
+      int akey = -1, best = 0;
+#pragma unroll
+      for (int k = 0; k < CH_TILE_K; ++k) {
+        int n = 0;
+#pragma unroll
+        for (int q = 0; q < CH_TILE_K; ++q) n += (keys[q] == keys[k]) ? 1 : 0;
+        if (keys[k] >= 0 && n > best) { best = n; akey = keys[k]; }
+      }
+      // displaced, outside and fast slots to the ring (at most 31 wait there,
+      // so 128 more fit)
+#pragma unroll
+      for (int k = 0; k < CH_TILE_K; ++k) {
+        const bool dsp = other[k] || (keys[k] >= 0 && keys[k] != akey);
+        const unsigned m = __ballot_sync(0xffffffffu, dsp);
+        if (dsp) ring[(dt + __popc(m & lt)) & (CH_DEP_RW - 1)] = ips[k];
+        dt += (unsigned)__popc(m);
+      }
+      // each slot adds rint(x) + CH_RNI_BIAS per entry; starting from minus
+      // four biases leaves the exact sums, |sum| < 2^25
+      constexpr unsigned a0 = 0u - (unsigned)CH_TILE_K * (unsigned)CH_RNI_BIAS;
+      unsigned a[32];
+#pragma unroll
+      for (int k = 0; k < CH_TILE_K; ++k) {
+        const bool use = keys[k] >= 0 && keys[k] == akey;
+        const float wxh = use ? pk[k].x : 0.0f, wyh = use ? pk[k].y : 0.0f, oz = use ? pk[k].z : 0.0f;
+        const float wxl = 1.0f - wxh, wyl = 1.0f - wyh;
+        const float wzh = use ? oz : 0.0f, wzl = use ? 1.0f - oz : 0.0f;
+        const float w[8] = {wzl * wyl * wxl, wzl * wyl * wxh, wzl * wyh * wxl, wzl * wyh * wxh,
+                            wzh * wyl * wxl, wzh * wyl * wxh, wzh * wyh * wxl, wzh * wyh * wxh};
+        // (v 2^19) w is v (w 2^19) exactly: the scale is a power of two
+        const float fx = use ? vk[k].x * CH_TILE_FSCALE : 0.0f, fy = use ? vk[k].y * CH_TILE_FSCALE : 0.0f,
+                    fz = use ? vk[k].z * CH_TILE_FSCALE : 0.0f;
+#pragma unroll
+        for (int cn = 0; cn < 8; ++cn) {
+          a[cn] = (k == 0 ? a0 : a[cn]) + (unsigned)rni_fma(w[cn], CH_TILE_DSCALE);
+          a[8 + cn] = (k == 0 ? a0 : a[8 + cn]) + (unsigned)rni_fma(fx, w[cn]);
+          a[16 + cn] = (k == 0 ? a0 : a[16 + cn]) + (unsigned)rni_fma(fy, w[cn]);
+          a[24 + cn] = (k == 0 ? a0 : a[24 + cn]) + (unsigned)rni_fma(fz, w[cn]);
+        }
+      }
+      // Sums of lanes whose cells agree: lane l's 32 sums become row l of the
+      // warp's matrix, and lane q walks column q down the rows, adding one sum
+      // per run of equal cells (consecutive in sorted order) to node q & 7 of
+      // that cell, moment q >> 3.  The run ends come from one ballot, so the
+      // walk tests a bit of a warp-wide word per row instead of comparing cells.
+      unsigned* M = sh.d_sum[warp];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) M[lane * 33 + q] = a[q];
+      const int up = __shfl_down_sync(0xffffffffu, akey, 1);
+      const unsigned ends = __ballot_sync(0xffffffffu, lane == 31 || akey != up);  // row l ends a run
+      __syncwarp();
+      {
+        const int cn = lane & 7, m = lane >> 3;
+        const int off = (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
+        int s2[2] = {0, 0};  // even and odd rows (two add chains); |sum| < 32 x 2^25
+#pragma unroll
+        for (int l = 0; l < 32; ++l) {
+          s2[l & 1] += (int)M[l * 33 + lane];  // a lane without a cell holds zeros
+          if ((ends >> l) & 1u) {
+            const int kl = __shfl_sync(0xffffffffu, akey, l);
+            const int sum = s2[0] + s2[1];
+            if (kl >= 0 && sum != 0) shared_add64(&sh.acc_lo[m][kl + off], &sh.acc_hi[m][kl + off], sum);
+            s2[0] = s2[1] = 0;
+          }
+        }
+      }
+      __syncwarp();  // ring entries visible, matrix read before the next chunk rewrites it
     }
-    __syncwarp();  // ring entries visible, matrix read before the next chunk rewrites it
-    while (dt - dh >= 32u) drain(32u);
+    // full rounds of 32; after the last chunk, the rest
+    while (dt - dh >= 32u || (!more && dt != dh)) drain(min(dt - dh, 32u));
+    if (!more) break;
   }
-  if (dt != dh) drain(dt - dh);
 }
 
 // Adds the brick's tile to the global accumulators (tile sums are at the
@@ -1075,17 +1092,15 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
   const int i0 = (tile % ntx) * TX, j0 = ((tile / ntx) % nty) * TY, k0 = (tile / (ntx * nty)) * TZ;
   const int i1 = min(i0 + TX, g.Nx), j1 = min(j0 + TY, g.Ny), k1 = min(k0 + TZ, g.Nz);
   const int bi0 = i0 - 1, bj0 = j0 - 1, bk0 = k0 - 1;  // box origin (node)
+  const int wi0 = ch_wrap(bi0, g.Nx), wj0 = ch_wrap(bj0, g.Ny), wk0 = ch_wrap(bk0, g.Nz);  // wrapped into the grid
   __syncthreads();  // previous brick's flush is done
-  // stage the node field, clear the deposit tile, row ranges
-  for (int q = threadIdx.x; q < BNODES; q += blockDim.x) {
-    const int bi = q % BX, bj = (q / BX) % BY, bk = q / (BX * BY);
-    if (PH & PH_PUSH) {
+  // stage the node field and the row ranges (the deposit tile is clear: the
+  // kernel clears it before its first brick, each flush after it)
+  if (PH & PH_PUSH) {
+    for (int q = threadIdx.x; q < BNODES; q += blockDim.x) {
+      const int bi = q % BX, bj = (q / BX) % BY, bk = q / (BX * BY);
       const int gi = ch_wrap(bi0 + bi, g.Nx), gj = ch_wrap(bj0 + bj, g.Ny), gk = ch_wrap(bk0 + bk, g.Nz);
       sh.E[q] = __ldg(E + ((int64_t)gk * g.Ny + gj) * g.Nx + gi);
-    }
-    if (PH & PH_DEPOSIT) {
-#pragma unroll
-      for (int m = 0; m < 4; ++m) { sh.acc_lo[m][q] = 0u; sh.acc_hi[m][q] = 0; }
     }
   }
   if (threadIdx.x < 32) {  // lane r: row r (tk = k0 + r / TY, tj = j0 + r % TY); pre = scan of the counts
@@ -1123,7 +1138,7 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
         tile_flush(sh, g, acc, bi0, bj0, bk0, shift_d, shift_f, true);
         __syncthreads();
       }
-      tile_deposit_direct<SCAT>(sh, c, P, acc, seg, min(total, seg + CH_DEP_SEG), bi0, bj0, bk0, bad, Q, dst_starts);
+      tile_deposit_direct<SCAT>(sh, c, P, acc, seg, min(total, seg + CH_DEP_SEG), wi0, wj0, wk0, bad, Q, dst_starts);
     }
   }
   const uint32_t ptotal = total * (PH == PH_DEPOSIT ? 0u : 1u);  // ions the push / move loop visits
@@ -1173,7 +1188,7 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
     float qscale = 0.0f, qt0 = 0.0f;  // rate scale and first waiting time of a deferred ion
     if ((PH & PH_PUSH) && active) {
       bool near;
-      const int q = box_key(g, i, j, k, bi0, bj0, bk0, &near);
+      const int q = box_key(g, i, j, k, wi0, wj0, wk0, &near);
       float4 e000, e100, e010, e110, e001, e101, e011, e111;
       if (near) {
         e000 = sh.E[q]; e100 = sh.E[q + 1]; e010 = sh.E[q + BX]; e110 = sh.E[q + BX + 1];
@@ -1244,7 +1259,19 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
   vsum[0] += (double)tsum0;
   if (PH & PH_DEPOSIT) {
     __syncthreads();
-    tile_flush(sh, g, acc, bi0, bj0, bk0, shift_d, shift_f, false);
+    tile_flush(sh, g, acc, bi0, bj0, bk0, shift_d, shift_f, true);
+  }
+}
+
+// Clears a deposit launch's tile before its first brick (tile_pass leaves it
+// clear after each brick); the first tile_pass starts with a block barrier.
+template <int PH>
+__device__ __forceinline__ void tile_clear(TileShared& sh) {
+  if (PH & PH_DEPOSIT) {
+    for (int q = threadIdx.x; q < BNODES; q += blockDim.x) {
+#pragma unroll
+      for (int m = 0; m < 4; ++m) { sh.acc_lo[m][q] = 0u; sh.acc_hi[m][q] = 0; }
+    }
   }
 }
 
@@ -1265,6 +1292,7 @@ __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH
   int bad = 0;
   const GridDesc& g = c.g;
   const int ntiles = ((g.Nx + TX - 1) / TX) * ((g.Ny + TY - 1) / TY) * ((g.Nz + TZ - 1) / TZ);
+  tile_clear<PH>(sh);
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
     tile_pass<PH, CARRY, SCAT>(sh, c, P, E, starts, acc, pscale, shift_d, shift_f, hist, tile, vsum, gsum, qhead,
                                qtail, ncol, nref, bad, Q, dst_starts);
@@ -1301,6 +1329,7 @@ __global__ void __launch_bounds__(256, (PH & PH_DEPOSIT) ? CH_DEP_CTAS : CH_PUSH
   __shared__ float s_pscale;
   constexpr int W = (int)(sizeof(StepConsts) / sizeof(uint32_t));
   static_assert(sizeof(StepConsts) % sizeof(uint32_t) == 0, "StepConsts is copied as words");
+  tile_clear<PH>(sh);
   for (int t = blockIdx.x; t < B.total_tiles; t += gridDim.x) {
     __syncthreads();  // the previous brick is done with sc
     if (threadIdx.x == 0) {
