@@ -699,6 +699,36 @@ __device__ __forceinline__ void tile_deposit_lane(TileShared& sh, int node, floa
   }
 }
 
+// An ion the tile does not take (outside the brick's halo, or a component of
+// v at or above CH_TILE_VMAX) goes straight to the global accumulators with
+// the tile's rounding: each contribution is the integer the tile would add,
+// rint(w 2^22) and rint((v 2^19) w) of the same FP32 weights (products exact
+// in FP64, ties to even as rni_fma), scaled by 2^shift to the accumulator
+// scale.  So the moments do not depend on which path an ion takes, which
+// depends on the order of the ions (their distance from the brick their slot
+// belongs to).  Out-of-range values saturate in the conversion.
+__device__ __forceinline__ void deposit_cic_tile_rounding(const GridDesc& g, unsigned long long* __restrict__ acc,
+                                                          int i, int j, int k, float wxh, float wyh, float wzh,
+                                                          float vx, float vy, float vz, int shift_d, int shift_f) {
+  const float wxl = 1.0f - wxh, wyl = 1.0f - wyh, wzl = 1.0f - wzh;
+  const float w[8] = {wzl * wyl * wxl, wzl * wyl * wxh, wzl * wyh * wxl, wzl * wyh * wxh,
+                      wzh * wyl * wxl, wzh * wyl * wxh, wzh * wyh * wxl, wzh * wyh * wxh};
+  const double fx = (double)(vx * CH_TILE_FSCALE), fy = (double)(vy * CH_TILE_FSCALE),
+               fz = (double)(vz * CH_TILE_FSCALE);
+  const double sd = ldexp(1.0, shift_d), sf = ldexp(1.0, shift_f);
+  const int i1 = i + 1 == g.Nx ? 0 : i + 1, j1 = j + 1 == g.Ny ? 0 : j + 1, k1 = k + 1 == g.Nz ? 0 : k + 1;
+  const int64_t N = g.N;
+#pragma unroll
+  for (int cn = 0; cn < 8; ++cn) {
+    const int64_t nd = ((int64_t)((cn >> 2) ? k1 : k) * g.Ny + ((cn >> 1) & 1 ? j1 : j)) * g.Nx + ((cn & 1) ? i1 : i);
+    const double wd = (double)w[cn];
+    red_add(acc + nd, __double2ll_rn(rint(wd * (double)CH_TILE_DSCALE) * sd));
+    red_add(acc + N + nd, __double2ll_rn(rint(fx * wd) * sf));
+    red_add(acc + 2 * N + nd, __double2ll_rn(rint(fy * wd) * sf));
+    red_add(acc + 3 * N + nd, __double2ll_rn(rint(fz * wd) * sf));
+  }
+}
+
 // Box-relative cell offset of (i, j, k) from the box origin, periodic; the
 // origin (wi0, wj0, wk0) is given wrapped into the grid, so one correction
 // per axis brings the difference into [0, N).
@@ -738,7 +768,8 @@ __device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, i
 template <bool SCAT>
 __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepConsts& c, MixParticles P,
                                                     unsigned long long* __restrict__ acc, uint32_t seg0,
-                                                    uint32_t total, int wi0, int wj0, int wk0, int& bad,
+                                                    uint32_t total, int wi0, int wj0, int wk0, int shift_d,
+                                                    int shift_f, int& bad,
                                                     MixParticles Q, const uint32_t* __restrict__ dst_starts) {
   const GridDesc& g = c.g;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -757,7 +788,7 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
       const int key = box_key(g, i, j, kz, wi0, wj0, wk0, &inbox);
       const bool slow = fabsf(v.x) >= CH_TILE_VMAX || fabsf(v.y) >= CH_TILE_VMAX || fabsf(v.z) >= CH_TILE_VMAX;
       if (inbox && !slow) tile_deposit_lane(sh, key, p.x, p.y, p.z, v.x, v.y, v.z);
-      else deposit_cic<float>(g, acc, i, j, kz, p.x, p.y, p.z, v.x, v.y, v.z, c.f.dep_scale);
+      else deposit_cic_tile_rounding(g, acc, i, j, kz, p.x, p.y, p.z, v.x, v.y, v.z, shift_d, shift_f);
     }
     dh += n;
     __syncwarp();  // the entries are read before later appends reuse them
@@ -1138,7 +1169,8 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
         tile_flush(sh, g, acc, bi0, bj0, bk0, shift_d, shift_f, true);
         __syncthreads();
       }
-      tile_deposit_direct<SCAT>(sh, c, P, acc, seg, min(total, seg + CH_DEP_SEG), wi0, wj0, wk0, bad, Q, dst_starts);
+      tile_deposit_direct<SCAT>(sh, c, P, acc, seg, min(total, seg + CH_DEP_SEG), wi0, wj0, wk0, shift_d, shift_f,
+                                bad, Q, dst_starts);
     }
   }
   const uint32_t ptotal = total * (PH == PH_DEPOSIT ? 0u : 1u);  // ions the push / move loop visits

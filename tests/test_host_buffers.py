@@ -68,13 +68,14 @@ def test_misaligned_view_of_a_registered_range_is_staged(chy):
         chy.host_unregister(big)
 
 
-@pytest.mark.parametrize("extra", [0, 7])  # 7: a last warp chunk and copy chunk that are partial
-def test_round_trip_through_registered_arrays_keeps_the_run(chy, extra):
+@pytest.mark.parametrize("extra,period", [(0, 3), (7, 3), (7, 1)])  # 7: partial last warp and copy chunks
+def test_round_trip_through_registered_arrays_keeps_the_run(chy, extra, period):
     """A download into registered arrays followed by an upload of the same
     arrays puts every ion back into its slot (no sort); a plain round trip
     re-sorts.  The order of the ions does not enter any result (integer
-    deposit sums, per-ion draws), so both runs stay identical bit for bit."""
-    p = chy.params_for((16, 12, 20), precision=chy.PRECISION["mixed"], nui=0.4, sort_period=3)
+    deposit sums, per-ion draws), so both runs stay identical bit for bit.
+    Sort period 1: every step ends with a sort."""
+    p = chy.params_for((16, 12, 20), precision=chy.PRECISION["mixed"], nui=0.4, sort_period=period)
     n = 16 * 12 * 20 * 8 + extra
     outs = []
     for registered in (False, True):
@@ -102,15 +103,16 @@ def test_round_trip_through_registered_arrays_keeps_the_run(chy, extra):
         assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("precision,extra", [("mixed", 0), ("mixed", 7), ("fp64", 7)])
-def test_step_host_equals_upload_step_download(chy, precision, extra):
+@pytest.mark.parametrize("precision,extra,period", [("mixed", 0, 3), ("mixed", 7, 3), ("fp64", 7, 3), ("mixed", 7, 1)])
+def test_step_host_equals_upload_step_download(chy, precision, extra, period):
     """ch_step_host, whose download overlaps the last step's deposit and
     potential solve (started after the deposit, from the new order, on a sort
     step), leaves the host arrays and the device state exactly as upload,
     ch_step and download do: with plain and registered arrays, one or two
     steps per call, sort steps (every 3rd) last in a call.  The FP64 form
-    downloads after the steps."""
-    p = chy.params_for((16, 12, 20), precision=chy.PRECISION[precision], nui=0.4, sort_period=3)
+    downloads after the steps.  Sort period 1 (mixed): every step ends with a
+    sort, so every call's download starts from the new order."""
+    p = chy.params_for((16, 12, 20), precision=chy.PRECISION[precision], nui=0.4, sort_period=period)
     n = 16 * 12 * 20 * 8 + extra
     outs = []
     for mode in ("separate", "step_host", "step_host_registered"):
