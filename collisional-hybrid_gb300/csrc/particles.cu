@@ -1175,12 +1175,12 @@ __device__ __forceinline__ void tile_pass(TileShared& sh, const StepConsts& c, M
   }
   const uint32_t ptotal = total * (PH == PH_DEPOSIT ? 0u : 1u);  // ions the push / move loop visits
   // index of slot idx in the ion arrays (rows of the brick are contiguous)
+  // (a thread's slots only increase, so its row is kept and advanced: the
+  // last row that starts at or before the slot, past empty rows)
+  int srow = 0;
   auto slot_ip = [&](uint32_t idx) -> uint32_t {
-    int r = 0;
-#pragma unroll
-    for (int st = 8; st > 0; st >>= 1)
-      if (r + st < TY * TZ && sh.pre[r + st] <= idx) r += st;
-    return sh.rowbeg[r] + (idx - sh.pre[r]);
+    while (srow + 1 < TY * TZ && sh.pre[srow + 1] <= idx) ++srow;
+    return sh.rowbeg[srow] + (idx - sh.pre[srow]);
   };
   // Thread t's ions are slots t, t + 256, ...; the next one is copied into
   // the thread's own prefetch slot by cp.async while this one is pushed (only
