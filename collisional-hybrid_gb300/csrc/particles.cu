@@ -682,20 +682,33 @@ __device__ __forceinline__ void shared_add_rni(unsigned* lo, int* hi, int r) {
 
 // One ion's 32 fixed-point contributions added lane by lane to the shared
 // tile (node = the ion's cell within the box).
+// The four moments are taken in an order rotated by lane & 3: lanes whose
+// ions landed in the same cell (displaced together) then add to different
+// words in each instruction instead of queueing on one.
 __device__ __forceinline__ void tile_deposit_lane(TileShared& sh, int node, float wxh, float wyh, float wzh,
                                                   float vx, float vy, float vz) {
   const float wxl = 1.0f - wxh, wyl = 1.0f - wyh, wzl = 1.0f - wzh;
   const float w[8] = {wzl * wyl * wxl, wzl * wyl * wxh, wzl * wyh * wxl, wzl * wyh * wxh,
                       wzh * wyl * wxl, wzh * wyl * wxh, wzh * wyh * wxl, wzh * wyh * wxh};
+  // moment m adds rint(a_m w): a = 2^22 (density), v 2^19 (fluxes), exact
+  // products inside the FMA
+  const float a0 = CH_TILE_DSCALE, a1 = vx * CH_TILE_FSCALE, a2 = vy * CH_TILE_FSCALE, a3 = vz * CH_TILE_FSCALE;
+  const int s = threadIdx.x & 3;
+  float ar[4];
+  unsigned* lo[4];
+  int* hi[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int m = (t + s) & 3;
+    ar[t] = m == 0 ? a0 : m == 1 ? a1 : m == 2 ? a2 : a3;
+    lo[t] = &sh.acc_lo[0][0] + m * BNODES + node;
+    hi[t] = &sh.acc_hi[0][0] + m * BNODES + node;
+  }
 #pragma unroll
   for (int cn = 0; cn < 8; ++cn) {
-    const int nd = node + (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
-    // (v 2^19) w is v (w 2^19) exactly: the scale is a power of two
-    const float wf = w[cn] * CH_TILE_FSCALE;
-    shared_add_rni(&sh.acc_lo[0][nd], &sh.acc_hi[0][nd], rni_fma(w[cn], CH_TILE_DSCALE));
-    shared_add_rni(&sh.acc_lo[1][nd], &sh.acc_hi[1][nd], rni_fma(vx, wf));
-    shared_add_rni(&sh.acc_lo[2][nd], &sh.acc_hi[2][nd], rni_fma(vy, wf));
-    shared_add_rni(&sh.acc_lo[3][nd], &sh.acc_hi[3][nd], rni_fma(vz, wf));
+    const int off = (cn & 1) + ((cn >> 1) & 1) * BX + (cn >> 2) * BX * BY;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) shared_add_rni(lo[t] + off, hi[t] + off, rni_fma(ar[t], w[cn]));
   }
 }
 
