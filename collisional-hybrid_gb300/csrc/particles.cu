@@ -636,7 +636,7 @@ struct TileShared {
   uint32_t pre[TY * TZ + 1];
   // ---- deposit part
   uint32_t d_ip[8 * CH_DEP_RW];  // per warp: ring of displaced ions (indices into the ion arrays)
-  unsigned d_sum[8][32 * 33];    // per warp: lane l's 32 sums in row l (33 words: no bank conflicts)
+  alignas(16) unsigned d_sum[8][32 * 33];    // per warp: lane l's 32 sums in row l (33 words: no bank conflicts)
   // Fixed-point sums at the tile scale, each value v added as its low 16
   // bits to acc_lo and as v >> 16 to acc_hi: the sum is acc_hi 2^16 +
   // acc_lo, exact in any order while a segment of the brick adds fewer than
@@ -822,8 +822,9 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
       // slot -> index in the ion arrays; slots past the chunk's end read its
       // last ion and are masked below
       uint32_t ips[CH_TILE_K];
-      if (cend <= sh.pre[rc + 1]) {  // the chunk lies in one row (warp-uniform)
-        const uint32_t base = sh.rowbeg[rc] - sh.pre[rc];
+      const bool onerow = cend <= sh.pre[rc + 1];  // the chunk lies in one row (warp-uniform)
+      const uint32_t base = sh.rowbeg[rc] - sh.pre[rc];
+      if (onerow) {
 #pragma unroll
         for (int k = 0; k < CH_TILE_K; ++k) ips[k] = min(s0 + k, cend - 1u) + base;
       } else {
@@ -838,8 +839,44 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
         }
       }
       float4 pk[CH_TILE_K], vk[CH_TILE_K];
+      if (onerow) {
+        // Coalesced: lane l loads slots cb + 32 i + l and parks them in the
+        // warp's matrix area (float4 q at q ^ ((q >> 3) & 7): neither the
+        // stores nor the reads below conflict); it then reads its own four.
+        // SCAT: the ions are scattered from here, where neighbouring lanes
+        // hold neighbouring slots, which the push ranked in this lane order,
+        // so a cell's ions leave for consecutive slots (full sectors).
+        static_assert(CH_TILE_K == 4 && 8 * sizeof(float4) * 32 <= sizeof(sh.d_sum[0]), "a chunk fits the matrix area");
+        float4* X = reinterpret_cast<float4*>(sh.d_sum[warp]);
 #pragma unroll
-      for (int k = 0; k < CH_TILE_K; ++k) { pk[k] = P.pos[ips[k]]; vk[k] = P.vel[ips[k]]; }
+        for (int i = 0; i < CH_TILE_K; ++i) {
+          const uint32_t sl = cb + 32u * (uint32_t)i + (uint32_t)lane;
+          const uint32_t ipc = min(sl, cend - 1u) + base;
+          const float4 p = P.pos[ipc], v = P.vel[ipc];
+          const int q = 32 * i + lane, qs = q ^ ((q >> 3) & 7);
+          X[qs] = p;
+          X[128 + qs] = v;
+          if (SCAT && sl < cend) {
+            const uint32_t cell = __float_as_uint(p.w);
+            const uint32_t ci = cell & (CH_MAX_NX - 1), cj = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
+                           ck = cell >> (CH_PACK_BX + CH_PACK_BY);
+            const uint32_t d = dst_starts[(ck * (uint32_t)g.Ny + cj) * (uint32_t)g.Nx + ci] + P.rank[ipc];
+            Q.pos[d] = p;
+            Q.vel[d] = v;
+          }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < CH_TILE_K; ++k) {
+          const int q = CH_TILE_K * lane + k, qs = q ^ ((q >> 3) & 7);
+          pk[k] = X[qs];
+          vk[k] = X[128 + qs];
+        }
+        __syncwarp();  // read before the lanes' sums overwrite the area
+      } else {
+#pragma unroll
+        for (int k = 0; k < CH_TILE_K; ++k) { pk[k] = P.pos[ips[k]]; vk[k] = P.vel[ips[k]]; }
+      }
       int keys[CH_TILE_K];
       bool other[CH_TILE_K];  // to the ring whatever the lane's cell
 #pragma unroll
@@ -849,7 +886,7 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
         const uint32_t cell = __float_as_uint(p.w);
         const int i = cell & (CH_MAX_NX - 1), j = (cell >> CH_PACK_BX) & (CH_MAX_NY - 1),
                   kz = cell >> (CH_PACK_BX + CH_PACK_BY);
-        if (SCAT && valid) {  // every ion, whether or not it is deposited here
+        if (SCAT && valid && !onerow) {  // every ion, whether or not it is deposited here
           const uint32_t d = dst_starts[(kz * g.Ny + j) * g.Nx + i] + P.rank[ips[k]];
           Q.pos[d] = p;
           Q.vel[d] = v;
