@@ -766,7 +766,8 @@ __device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, i
 // the brick once per run.  The other slots go to the warp's ring and are
 // added lane by lane, 32 at a time: ions in another cell ("displaced": they
 // moved since the last sort) to the brick's tile, ions outside the brick's
-// halo or faster than CH_TILE_VMAX straight to the global accumulators.
+// halo or faster than CH_TILE_VMAX straight to the global accumulators, and
+// non-finite ions are flagged (bad) and not deposited.
 // The chunk itself runs without divergent branches: a slot the lane does not
 // sum enters the same arithmetic with zero weights and zero velocity
 // (selected, so that a non-finite ion adds nothing), and the accumulators
@@ -799,8 +800,11 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
                 kz = cell >> (CH_PACK_BX + CH_PACK_BY);
       bool inbox;
       const int key = box_key(g, i, j, kz, wi0, wj0, wk0, &inbox);
+      const bool finite =
+          isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
       const bool slow = fabsf(v.x) >= CH_TILE_VMAX || fabsf(v.y) >= CH_TILE_VMAX || fabsf(v.z) >= CH_TILE_VMAX;
-      if (inbox && !slow) tile_deposit_lane(sh, key, p.x, p.y, p.z, v.x, v.y, v.z);
+      if (!finite) bad = 1;  // not deposited
+      else if (inbox && !slow) tile_deposit_lane(sh, key, p.x, p.y, p.z, v.x, v.y, v.z);
       else deposit_cic_tile_rounding(g, acc, i, j, kz, p.x, p.y, p.z, v.x, v.y, v.z, shift_d, shift_f);
     }
     dh += n;
@@ -891,15 +895,16 @@ __device__ __forceinline__ void tile_deposit_direct(TileShared& sh, const StepCo
           Q.pos[d] = p;
           Q.vel[d] = v;
         }
-        const bool finite =
-            isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
         bool inbox;
         const int key = box_key(g, i, j, kz, wi0, wj0, wk0, &inbox);
-        const bool slow = fabsf(v.x) >= CH_TILE_VMAX || fabsf(v.y) >= CH_TILE_VMAX || fabsf(v.z) >= CH_TILE_VMAX;
-        if (valid && !finite) bad = 1;
-        const bool take = valid && finite && inbox && !slow;
+        // |v| below the tile's bound and in-cell offsets (each in [0, 1))
+        // summing below 3: both comparisons fail for NaN and infinities, so
+        // a non-finite ion goes to the ring, where the drain flags it
+        const bool fits = fabsf(v.x) < CH_TILE_VMAX && fabsf(v.y) < CH_TILE_VMAX && fabsf(v.z) < CH_TILE_VMAX &&
+                          p.x + p.y + p.z < 3.0f;
+        const bool take = valid && inbox && fits;
         keys[k] = take ? key : -1;
-        other[k] = valid && finite && !take;
+        other[k] = valid && !take;
       }
       // the cell most of the lane's slots share (ties: the earliest)
       int akey = -1, best = 0;
