@@ -757,11 +757,13 @@ __device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, i
 
 // Deposit of one brick whose ions' cells are current (a deposit-only pass).
 // Warp w takes the chunks of 128 consecutive slots w, w + 8, ...; lane l the
-// 4 slots 4l .. 4l+3 of a chunk, read straight from global memory (the ions
-// of a cell are contiguous after a sort and mostly stay together between
-// sorts, so the 4 usually share a cell).  A lane sums the 32 fixed-point
-// contributions of its slots in the cell most of them share in registers;
-// the sums of lanes whose cells agree are then added up through a matrix in
+// 4 slots 4l .. 4l+3 of a chunk (the ions of a cell are contiguous after a
+// sort and mostly stay together between sorts, so the 4 usually share a
+// cell), loaded coalesced through the warp's matrix area when the chunk lies
+// in one brick row and straight from global memory otherwise.  A lane sums
+// the 32 fixed-point contributions of its slots in the cell most of them
+// share in registers; the sums of lanes whose cells agree are then added up
+// through a matrix in
 // shared memory (lane q sums entry q of each run of equal cells) and added to
 // the brick once per run.  The other slots go to the warp's ring and are
 // added lane by lane, 32 at a time: ions in another cell ("displaced": they
