@@ -137,6 +137,31 @@ def test_deposit_mixed_dense_bricks(chy):
     assert rel(out[1], out[0]) < 1e-6
 
 
+def test_deposit_mixed_fast_ions(chy, po):
+    """Ions with a velocity component at or above the tile's bound (8 cells
+    per unit time) bypass the mixed deposit's shared tile and are added to
+    the global accumulators with the tile's own integers.  With vT = 3 about
+    2% of the ions are that fast, and a few are set to 20 and -35: the
+    moments match the FP64 oracle within the mixed tolerance, and uploading
+    the same ions in reverse order gives the same moments bit for bit."""
+    N = (16, 12, 20)
+    p, q = make(chy, po, N, precision="mixed", mn=0.0)
+    ions = po.load(q, po.make_loader(amp=(0.05, 0.02, 0.0), vT=(3.0, 3.0, 3.0)), N[0] * N[1] * N[2] * 12)
+    ions.a[3, 5:9] = (20.0, -35.0, 8.0, -8.0)
+    ions.a[5, 11] = 27.5
+    fast = np.any(np.abs(ions.a[3:6]) >= 8.0, axis=0).mean()
+    assert 0.01 < fast < 0.05, fast
+    pos, vel = ions.aos()
+    out = []
+    for order in (slice(None), slice(None, None, -1)):
+        with chy.Hybrid(p) as h:
+            h.upload(np.ascontiguousarray(pos[order]), np.ascontiguousarray(vel[order]))
+            out.append(h.CollectVlasovQuantities())
+    assert np.array_equal(out[0], out[1])
+    orc = po.collect(q, ions).reshape(-1, 4)
+    assert rel(out[0], orc) < 1e-6
+
+
 # ------------------------------------------------------------------ RHS and operator
 @pytest.mark.parametrize("tag", ["g8", "g15x10x8"])
 @pytest.mark.parametrize("ki,kappa", [(0, (0.0, 0.0, 0.0)), (1, (0.3, -0.2, 1.0))])
