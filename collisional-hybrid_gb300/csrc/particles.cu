@@ -636,7 +636,9 @@ struct TileShared {
   uint32_t pre[TY * TZ + 1];
   // ---- deposit part
   uint32_t d_ip[8 * CH_DEP_RW];  // per warp: ring of displaced ions (indices into the ion arrays)
-  alignas(16) unsigned d_sum[8][32 * 33];    // per warp: lane l's 32 sums in row l (33 words: no bank conflicts)
+  // per warp: a chunk's ions while they are loaded, then lane l's 32 sums in
+  // row l (33 words: no bank conflicts)
+  alignas(16) unsigned d_sum[8][32 * 33];
   // Fixed-point sums at the tile scale, each value v added as its low 16
   // bits to acc_lo and as v >> 16 to acc_hi: the sum is acc_hi 2^16 +
   // acc_lo, exact in any order while a segment of the brick adds fewer than
@@ -763,9 +765,8 @@ __device__ __forceinline__ int box_key(const GridDesc& g, int i, int j, int k, i
 // in one brick row and straight from global memory otherwise.  A lane sums
 // the 32 fixed-point contributions of its slots in the cell most of them
 // share in registers; the sums of lanes whose cells agree are then added up
-// through a matrix in
-// shared memory (lane q sums entry q of each run of equal cells) and added to
-// the brick once per run.  The other slots go to the warp's ring and are
+// through a matrix in shared memory (lane q sums entry q of each run of equal
+// cells) and added to the brick once per run.  The other slots go to the warp's ring and are
 // added lane by lane, 32 at a time: ions in another cell ("displaced": they
 // moved since the last sort) to the brick's tile, ions outside the brick's
 // halo or faster than CH_TILE_VMAX straight to the global accumulators, and
